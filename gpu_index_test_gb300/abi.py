@@ -1,0 +1,112 @@
+"""ctypes mirrors of the records declared in include/gbsa.h.
+
+The layouts are byte-identical to the reference structs (RefRandstrobe,
+step2/randstrobes.hpp:65-94; QueryRandstrobe, step2/randstrobes.hpp:96-101; Nam,
+step2/my_struct.hpp:48-62) so numpy views of these arrays can be handed to either
+side without conversion.
+"""
+import ctypes as C
+
+import numpy as np
+
+GBSA_OK = 0
+GBSA_ERR_PARAM = 1
+GBSA_ERR_CUDA = 2
+GBSA_ERR_NOMEM = 3
+GBSA_ERR_INDEX_FILE = 4
+GBSA_ERR_CAPACITY = 5
+GBSA_ERR_READ_TOO_LONG = 6
+GBSA_ERR_NO_DEVICE = 7
+GBSA_ERR_DEVICE_STATUS = 8
+
+GBSA_DEFAULT = -2147483648
+GBSA_MAX_READ_LEN = 4096
+
+GBSA_SORT_SCORE = 0
+GBSA_SORT_REF_MATE2 = 1
+GBSA_SORT_REF_MATE1 = 2
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("canonical_read_length", C.c_int32),
+        ("k", C.c_int32),
+        ("s", C.c_int32),
+        ("t_syncmer", C.c_int32),
+        ("l", C.c_int32),
+        ("u", C.c_int32),
+        ("q", C.c_uint64),
+        ("max_dist", C.c_int32),
+        ("w_min", C.c_uint32),
+        ("w_max", C.c_uint32),
+        ("_pad", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("_")}
+
+
+class IndexInfo(C.Structure):
+    _fields_ = [
+        ("size", C.c_uint64),
+        ("bits", C.c_int32),
+        ("filter_cutoff", C.c_uint32),
+        ("tot_strobemer_count", C.c_uint64),
+        ("tot_occur_once", C.c_uint64),
+        ("tot_high_ab", C.c_uint64),
+        ("tot_mid_ab", C.c_uint64),
+        ("index_cutoff", C.c_uint64),
+        ("distinct_strobemers", C.c_uint64),
+    ]
+
+
+class MapOptions(C.Structure):
+    _fields_ = [
+        ("rescue_level", C.c_int32),
+        ("rescue_count_cap", C.c_uint32),
+        ("sort_mode", C.c_int32),
+        ("_pad", C.c_int32),
+    ]
+
+
+REF_RANDSTROBE = np.dtype([("hash", "<u8"), ("position", "<u4"), ("packed", "<u4")])
+QUERY_RANDSTROBE = np.dtype(
+    [("hash", "<u8"), ("start", "<u4"), ("end", "<u4"), ("is_reverse", "u1"), ("_pad", "u1", (7,))]
+)
+NAM = np.dtype(
+    [
+        ("nam_id", "<i4"),
+        ("query_start", "<i4"),
+        ("query_end", "<i4"),
+        ("query_prev_hit_startpos", "<i4"),
+        ("ref_start", "<i4"),
+        ("ref_end", "<i4"),
+        ("ref_prev_hit_startpos", "<i4"),
+        ("n_hits", "<i4"),
+        ("ref_id", "<i4"),
+        ("score", "<f4"),
+        ("is_rc", "u1"),
+        ("_pad", "u1", (3,)),
+    ]
+)
+assert REF_RANDSTROBE.itemsize == 16 and QUERY_RANDSTROBE.itemsize == 24 and NAM.itemsize == 44
+
+# Fields of a NAM that results are compared on (nam_id and the two prev-hit
+# positions are internal to the merge).
+NAM_COMPARED = ("ref_id", "query_start", "query_end", "ref_start", "ref_end", "n_hits", "score", "is_rc")
+
+
+def ptr(a, ctype=C.c_void_p):
+    """Pointer to a contiguous numpy array (or None)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return C.cast(a.ctypes.data, ctype)
+
+
+def map_options(rescue_level=2, rescue_count_cap=1000, sort_mode=GBSA_SORT_SCORE):
+    o = MapOptions()
+    o.rescue_level = rescue_level
+    o.rescue_count_cap = rescue_count_cap
+    o.sort_mode = sort_mode
+    return o

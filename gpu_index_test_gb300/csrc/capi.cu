@@ -1,0 +1,736 @@
+// capi.cu — the C-ABI (include/gbsa.h): parameters, index handle, mapper and the
+// host <-> device plumbing around the kernels.
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "index.h"
+#include "map.cuh"
+#include "prims.cuh"
+#include "runtime.h"
+
+namespace gbsa {
+
+std::atomic<uint64_t> g_launches{0};
+static thread_local std::string t_last_error;
+
+void set_last_error(const std::string& msg) { t_last_error = msg; }
+
+int device_sm_count() {
+    static std::mutex mu;
+    static std::vector<int> cache;
+    int dev = 0;
+    GBSA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+    if (!cache[dev]) GBSA_CUDA(cudaDeviceGetAttribute(&cache[dev], cudaDevAttrMultiProcessorCount, dev));
+    return cache[dev];
+}
+
+template <class F>
+static int guarded(F&& f) {
+    try {
+        f();
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return GBSA_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}
+
+static void require_device() {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        throw Error(GBSA_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+}
+
+// ---- IndexParameters (step2/indexparameters.{hpp,cpp}) -------------------------------
+bool params_valid(const gbsa_params& p) {
+    if (p.k <= 7 || p.k > 32) return false;                 // indexparameters.hpp:25-27
+    if (p.s > p.k || p.s < 1) return false;                 // :28-30
+    if ((p.k - p.s) % 2 != 0) return false;                 // :31-33
+    if (p.max_dist > 255 || p.max_dist < 0) return false;   // :62-64 (negative: no seed fits)
+    if (p.w_min > p.w_max) return false;                    // :65-67
+    return true;
+}
+
+static void make_params(uint64_t r, int k, int s, int l, int u, int q, int max_dist, gbsa_params* out) {
+    gbsa_params p{};
+    p.canonical_read_length = (int32_t)r;
+    p.k = k;
+    p.s = s;
+    p.t_syncmer = (k - s) / 2 + 1;
+    p.l = l;
+    p.u = u;
+    p.q = (uint64_t)(int64_t)q;
+    p.max_dist = max_dist;
+    if (k - s + 1 <= 0) throw Error(GBSA_ERR_PARAM, "s is larger than k");
+    p.w_min = (uint32_t)std::max(0, k / (k - s + 1) + l);   // indexparameters.hpp:83
+    p.w_max = (uint32_t)(k / (k - s + 1) + u);
+    if (!params_valid(p)) throw Error(GBSA_ERR_PARAM, "invalid index parameters (k in [8,32], s <= k, k-s even, "
+                                                      "max_dist <= 255, w_min <= w_max)");
+    *out = p;
+}
+
+int pick_bits_host(const gbsa_params& p, uint64_t size) {   // step2/index.cu:137-141
+    const uint64_t est = size / (uint64_t)(p.k - p.s + 1);
+    if (est == 0) return 8;
+    return std::clamp((int)std::log2((double)est) - 1, 8, 31);
+}
+
+void build_index(gbsa_index& ix, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+                 uint32_t n_contigs, float f);
+
+// ---- .sti format version 2 (step2/index.cu:73-134, step2/io.hpp:11-26) --------------
+static void write_sti(const gbsa_index& ix, const std::vector<gbsa_ref_randstrobe>& rs,
+                      const std::vector<uint64_t>& starts, const char* path) {
+    std::ofstream os(path, std::ios::binary);
+    if (!os) throw Error(GBSA_ERR_INDEX_FILE, std::string(path) + ": cannot open for writing");
+    auto w32 = [&](int32_t v) { os.write(reinterpret_cast<const char*>(&v), 4); };
+    auto w64 = [&](uint64_t v) { os.write(reinterpret_cast<const char*>(&v), 8); };
+    os.write("STI\1", 4);
+    w32(2);
+    w64(8);
+    const char reserved[8] = {0};
+    os.write(reserved, 8);
+    w32((int32_t)ix.filter_cutoff);
+    w32(ix.bits);
+    const gbsa_params& p = ix.params;
+    for (int32_t v : {p.canonical_read_length, p.k, p.s, p.l, p.u, (int32_t)p.q, p.max_dist}) w32(v);
+    w64(rs.size());
+    os.write(reinterpret_cast<const char*>(rs.data()), (std::streamsize)(rs.size() * sizeof(gbsa_ref_randstrobe)));
+    w64(starts.size());
+    os.write(reinterpret_cast<const char*>(starts.data()), (std::streamsize)(starts.size() * 8));
+    if (!os) throw Error(GBSA_ERR_INDEX_FILE, std::string(path) + ": write failed");
+}
+
+// ---- mapper --------------------------------------------------------------------------
+
+}  // namespace gbsa
+
+struct gbsa_mapper {
+    const gbsa_index* idx = nullptr;
+    gbsa_map_options opt{};
+    gbsa::MapConfig cfg{};
+    cudaStream_t st = nullptr;
+    uint32_t max_reads = 0;
+    uint64_t max_bases = 0;
+    gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
+        out_off, out_nams, out_frac, out_resc;
+    uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
+    uint32_t long_warps = 0;
+    gbsa::PinnedBuffer h_seqs, h_meta, h_out;
+    uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
+    int count_bytes = 0;
+};
+
+namespace gbsa {
+
+static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
+    m.seqs.resize(bases + 64);
+    m.offs.resize(8ull * (n + 1));
+    m.lens.resize(4ull * (n + 1));
+    m.rec.resize(sizeof(ReadRec) * (n + 1));
+    m.lists.resize(8ull * (n + 1));
+    m.ctr.resize(sizeof(Counters));
+    m.cnt.resize(8ull * (n + 1));
+    m.out_off.resize(8ull * (n + 1));
+    m.out_frac.resize(4ull * (n + 1));
+    m.out_resc.resize(n + 1);
+    // query randstrobes: ~2 per 5 bases plus slack
+    const uint64_t q_need = std::max<uint64_t>(4096, bases / 2 + 64ull * n / 8);
+    if (m.q_cap < q_need) {
+        m.q_cap = q_need;
+        m.q.resize(sizeof(Query) * m.q_cap);
+        m.qaux.resize(4 * m.q_cap);
+        m.qpos.resize(8 * m.q_cap);
+    }
+    if (m.hit_cap < 2 * q_need) {
+        m.hit_cap = 2 * q_need;
+        m.hits.resize(sizeof(HitRec) * m.hit_cap);
+    }
+    if (m.nam_cap < q_need) {
+        m.nam_cap = q_need;
+        m.nams.resize(sizeof(gbsa_nam) * m.nam_cap);
+    }
+    const uint32_t warps = nam_kernel_warps(std::max<uint32_t>(n, 1));
+    if (m.slot_bytes == 0) m.slot_bytes = 32 * 1024;
+    m.slots.resize((uint64_t)warps * m.slot_bytes);
+    if (m.ovf_cap == 0) {
+        m.ovf_cap = 64ull << 20;
+        m.ovf.resize(m.ovf_cap);
+    }
+    if (m.long_warps == 0) {
+        m.long_warps = (uint32_t)std::max(8, device_sm_count()) * 2;
+        m.long_scratch.resize((uint64_t)m.long_warps * kLongSlotBytes);
+    }
+}
+
+static Arenas arenas_of(gbsa_mapper& m) {
+    Arenas A;
+    A.q = m.q.as<Query>();
+    A.q_cap = m.q_cap;
+    A.q_aux = m.qaux.as<uint32_t>();
+    A.q_pos = m.qpos.as<uint64_t>();
+    A.hits = m.hits.as<HitRec>();
+    A.hit_cap = m.hit_cap;
+    A.nams = m.nams.as<gbsa_nam>();
+    A.nam_cap = m.nam_cap;
+    A.slots = m.slots.as<uint8_t>();
+    A.slot_bytes = m.slot_bytes;
+    A.ovf = m.ovf.as<uint8_t>();
+    A.ovf_cap = m.ovf_cap;
+    A.rescue_list = m.lists.as<uint32_t>();
+    A.long_list = m.lists.as<uint32_t>() + (m.lists.size() / 8);
+    return A;
+}
+
+static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
+    const uint64_t want = std::max<uint64_t>(cap * 2, used + used / 4 + 1024);
+    cap = want;
+    b.release();
+    b.resize(elem * cap);
+}
+
+// Runs seeding (unless the queries are already in place) → lookup → NAMs → rescue
+// for n reads whose bases/offsets/lengths are on the device; retries with larger
+// work areas when a bump allocator overflowed.  Leaves per-read NAM offsets in
+// m.out_off[0..n] and returns the NAM total.
+static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
+                             uint32_t n, bool seeded, cudaStream_t st) {
+    const IndexView I = view_of(*m.idx);
+    Workspace ws;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        Counters* ctr = m.ctr.as<Counters>();
+        GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
+        if (!seeded) {
+            GBSA_CUDA(cudaMemsetAsync(m.rec.as<void>(), 0, sizeof(ReadRec) * n, st));
+        } else {
+            // keep q_off / nq / nq2 written by the caller; clear the rest
+            launch_reset_recs(n, m.rec.as<ReadRec>(), st);
+        }
+        Arenas A = arenas_of(m);
+        MapConfig C = m.cfg;
+        C.count_bytes = m.count_bytes;
+        if (!seeded) {
+            launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+            launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr,
+                             m.long_scratch.as<uint8_t>(), m.long_warps, st);
+        }
+        launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        launch_rescue(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        Counters h{};
+        GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        if (h.status & kStatusReadTooLong)
+            throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
+        if (h.status & kStatusSyncmerOverflow)
+            throw Error(GBSA_ERR_DEVICE_STATUS, "syncmer buffer overflow");
+        bool retry = false;
+        if (h.status & kStatusQueryOverflow) {
+            if (seeded) throw Error(GBSA_ERR_DEVICE_STATUS, "query arena overflow");
+            grow(m.q, m.q_cap, h.q_used, sizeof(Query));
+            m.qaux.release();
+            m.qaux.resize(4 * m.q_cap);
+            m.qpos.release();
+            m.qpos.resize(8 * m.q_cap);
+            retry = true;
+        }
+        if (h.status & kStatusHitOverflow) {
+            grow(m.hits, m.hit_cap, h.hit_used, sizeof(HitRec));
+            retry = true;
+        }
+        if (h.status & kStatusNamOverflow) {
+            grow(m.nams, m.nam_cap, h.nam_used, sizeof(gbsa_nam));
+            retry = true;
+        }
+        if (h.status & kStatusScratchOverflow) {
+            grow(m.ovf, m.ovf_cap, h.scratch_used, 1);
+            retry = true;
+        }
+        if (retry) continue;
+        m.alg_bytes = h.alg_bytes;
+        // per-read NAM counts → offsets
+        uint64_t* cnt = m.cnt.as<uint64_t>();
+        uint64_t* off = m.out_off.as<uint64_t>();
+        launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st);
+        scan_exclusive_u64(cnt, off, n, off + n, ws, st);
+        uint64_t total = 0;
+        GBSA_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        return total;
+    }
+    throw Error(GBSA_ERR_DEVICE_STATUS, "work areas kept overflowing");
+}
+
+}  // namespace gbsa
+
+using namespace gbsa;
+
+extern "C" {
+
+const char* gbsa_last_error(void) { return t_last_error.c_str(); }
+int gbsa_version(void) { return 1; }
+uint64_t gbsa_launch_count(void) { return g_launches.load(); }
+
+int gbsa_params_from_read_length(int read_length, int k, int s, int l, int u, int c, int max_seed_len,
+                                 gbsa_params* out) {
+    return guarded([&] {
+        // profiles of step2/indexparameters.cpp:136-144
+        struct Profile { int r, thr, k, s_off, l, u; };
+        static const Profile profiles[] = {
+            {50, 90, 20, -4, -3, 2},  {100, 110, 20, -4, -2, 2}, {125, 135, 20, -4, -1, 4},
+            {150, 175, 20, -4, 1, 7}, {250, 275, 20, -4, 4, 13}, {300, 375, 22, -4, 2, 12},
+            {400, INT_MAX, 23, -6, 2, 12},
+        };
+        uint64_t canonical = 50;
+        for (const auto& p : profiles) {
+            if (read_length <= p.thr) {
+                if (k == GBSA_DEFAULT) k = p.k;
+                if (s == GBSA_DEFAULT) s = k + p.s_off;
+                if (l == GBSA_DEFAULT) l = p.l;
+                if (u == GBSA_DEFAULT) u = p.u;
+                canonical = (uint64_t)p.r;
+                break;
+            }
+        }
+        int max_dist;
+        if (max_seed_len == GBSA_DEFAULT) {
+            max_dist = std::min(255, std::max((int)canonical - 70, k));
+        } else {
+            max_dist = max_seed_len - k;
+        }
+        const int q = (int)(std::pow(2, c == GBSA_DEFAULT ? 8 : c) - 1);
+        make_params(canonical, k, s, l, u, q, max_dist, out);
+    });
+}
+
+int gbsa_params_make(uint64_t canonical_read_length, int k, int s, int l, int u, int q, int max_dist,
+                     gbsa_params* out) {
+    return guarded([&] { make_params(canonical_read_length, k, s, l, u, q, max_dist, out); });
+}
+
+int gbsa_pick_bits(const gbsa_params* p, uint64_t total_length) { return pick_bits_host(*p, total_length); }
+
+int gbsa_index_build(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+                     uint32_t n_contigs, int bits, float f, gbsa_index** out) {
+    return guarded([&] {
+        *out = nullptr;
+        if (!params_valid(*p)) throw Error(GBSA_ERR_PARAM, "invalid index parameters");
+        require_device();
+        uint64_t total = 0;
+        for (uint32_t c = 0; c < n_contigs; ++c) total += lengths[c];
+        const int b = bits == -1 ? pick_bits_host(*p, total) : bits;
+        if (b < 8 || b > 31) throw Error(GBSA_ERR_PARAM, "Bits must be between 8 and 31");   // index.hpp:45-47
+        std::unique_ptr<gbsa_index> ix(new gbsa_index());
+        ix->params = *p;
+        ix->dp = make_dev_params(*p);
+        ix->bits = b;
+        GBSA_CUDA(cudaGetDevice(&ix->device));
+        build_index(*ix, seqs, offsets, lengths, n_contigs, f);
+        *out = ix.release();
+    });
+}
+
+int gbsa_index_load(const gbsa_params* p, const gbsa_ref_randstrobe* randstrobes, uint64_t n,
+                    const uint64_t* start_indices, int bits, uint32_t filter_cutoff, gbsa_index** out) {
+    return guarded([&] {
+        *out = nullptr;
+        if (!params_valid(*p)) throw Error(GBSA_ERR_PARAM, "invalid index parameters");
+        if (bits < 8 || bits > 31) throw Error(GBSA_ERR_PARAM, "Bits must be between 8 and 31");
+        require_device();
+        std::unique_ptr<gbsa_index> ix(new gbsa_index());
+        ix->params = *p;
+        ix->dp = make_dev_params(*p);
+        ix->bits = bits;
+        ix->filter_cutoff = filter_cutoff;
+        ix->n = n;
+        GBSA_CUDA(cudaGetDevice(&ix->device));
+        ix->rs.resize(16 * (n + 1));
+        const uint64_t nb = (1ULL << bits) + 1;
+        ix->starts.resize(8 * nb);
+        if (n) GBSA_CUDA(cudaMemcpy(ix->rs.as<void>(), randstrobes, 16 * n, cudaMemcpyHostToDevice));
+        GBSA_CUDA(cudaMemcpy(ix->starts.as<void>(), start_indices, 8 * nb, cudaMemcpyHostToDevice));
+        ix->info.size = n;
+        ix->info.bits = bits;
+        ix->info.filter_cutoff = filter_cutoff;
+        ix->info.tot_strobemer_count = n;
+        *out = ix.release();
+    });
+}
+
+int gbsa_index_read_sti(const char* path, const gbsa_params* p, gbsa_index** out) {
+    return guarded([&] {
+        *out = nullptr;
+        std::ifstream is(path, std::ios::binary);
+        if (!is) throw Error(GBSA_ERR_INDEX_FILE, std::string(path) + ": cannot open");
+        char magic[4];
+        is.read(magic, 4);
+        if (!is || std::memcmp(magic, "STI\1", 4) != 0)
+            throw Error(GBSA_ERR_INDEX_FILE, "Index file has incorrect format (magic number mismatch)");
+        auto r32 = [&]() {
+            int32_t v = 0;
+            is.read(reinterpret_cast<char*>(&v), 4);
+            return v;
+        };
+        auto r64 = [&]() {
+            uint64_t v = 0;
+            is.read(reinterpret_cast<char*>(&v), 8);
+            return v;
+        };
+        const int32_t ver = r32();
+        if (ver != 2)
+            throw Error(GBSA_ERR_INDEX_FILE, "Can only read index file format version 2, but found version " +
+                                                 std::to_string(ver));
+        const uint64_t reserved = r64();
+        is.seekg((std::streamoff)reserved, std::ios_base::cur);
+        const uint32_t fc = (uint32_t)r32();
+        const int32_t bits = r32();
+        int32_t v[7];
+        for (auto& x : v) x = r32();
+        gbsa_params fp{};
+        make_params((uint64_t)v[0], v[1], v[2], v[3], v[4], v[5], v[6], &fp);
+        if (fp.canonical_read_length != p->canonical_read_length || fp.k != p->k || fp.s != p->s || fp.l != p->l ||
+            fp.u != p->u || fp.q != p->q || fp.max_dist != p->max_dist)
+            throw Error(GBSA_ERR_INDEX_FILE, "Index parameters in .sti file and those specified on command line differ");
+        const uint64_t n = r64();
+        std::vector<gbsa_ref_randstrobe> rs(n);
+        is.read(reinterpret_cast<char*>(rs.data()), (std::streamsize)(16 * n));
+        const uint64_t ns = r64();
+        if (bits < 8 || bits > 31 || ns != (1ULL << bits) + 1)
+            throw Error(GBSA_ERR_INDEX_FILE, "randstrobe_start_indices vector is of the wrong size");
+        std::vector<uint64_t> starts(ns);
+        is.read(reinterpret_cast<char*>(starts.data()), (std::streamsize)(8 * ns));
+        if (!is) throw Error(GBSA_ERR_INDEX_FILE, std::string(path) + ": truncated");
+        const int rc = gbsa_index_load(p, rs.data(), n, starts.data(), bits, fc, out);
+        if (rc != GBSA_OK) throw Error(rc, t_last_error);
+    });
+}
+
+int gbsa_index_write_sti(const gbsa_index* idx, const char* path) {
+    return guarded([&] {
+        std::vector<gbsa_ref_randstrobe> rs(idx->n);
+        std::vector<uint64_t> starts((1ULL << idx->bits) + 1);
+        if (idx->n) GBSA_CUDA(cudaMemcpy(rs.data(), idx->rs.as<void>(), 16 * idx->n, cudaMemcpyDeviceToHost));
+        GBSA_CUDA(cudaMemcpy(starts.data(), idx->starts.as<void>(), 8 * starts.size(), cudaMemcpyDeviceToHost));
+        write_sti(*idx, rs, starts, path);
+    });
+}
+
+int gbsa_index_get_info(const gbsa_index* idx, gbsa_index_info* out) {
+    *out = idx->info;
+    return GBSA_OK;
+}
+
+int gbsa_index_get_params(const gbsa_index* idx, gbsa_params* out) {
+    *out = idx->params;
+    return GBSA_OK;
+}
+
+int gbsa_index_export(const gbsa_index* idx, gbsa_ref_randstrobe* randstrobes, uint64_t* start_indices) {
+    return guarded([&] {
+        if (idx->n && randstrobes)
+            GBSA_CUDA(cudaMemcpy(randstrobes, idx->rs.as<void>(), 16 * idx->n, cudaMemcpyDeviceToHost));
+        if (start_indices)
+            GBSA_CUDA(cudaMemcpy(start_indices, idx->starts.as<void>(), 8 * ((1ULL << idx->bits) + 1),
+                                 cudaMemcpyDeviceToHost));
+    });
+}
+
+void gbsa_index_free(gbsa_index* idx) { delete idx; }
+
+int gbsa_find(const gbsa_index* idx, const uint64_t* hashes, uint64_t n, uint64_t* positions) {
+    return guarded([&] {
+        if (!n) return;
+        DeviceBuffer dh(8 * n), dp(8 * n);
+        GBSA_CUDA(cudaMemcpy(dh.as<void>(), hashes, 8 * n, cudaMemcpyHostToDevice));
+        launch_find(view_of(*idx), dh.as<uint64_t>(), n, dp.as<uint64_t>(), 0);
+        GBSA_CUDA(cudaMemcpy(positions, dp.as<void>(), 8 * n, cudaMemcpyDeviceToHost));
+    });
+}
+
+int gbsa_get_count(const gbsa_index* idx, const uint64_t* positions, uint64_t n, uint32_t* counts) {
+    return guarded([&] {
+        if (!n) return;
+        DeviceBuffer dp(8 * n), dc(4 * n);
+        GBSA_CUDA(cudaMemcpy(dp.as<void>(), positions, 8 * n, cudaMemcpyHostToDevice));
+        launch_get_count(view_of(*idx), dp.as<uint64_t>(), n, dc.as<uint32_t>(), 0);
+        GBSA_CUDA(cudaMemcpy(counts, dc.as<void>(), 4 * n, cudaMemcpyDeviceToHost));
+    });
+}
+
+// Copies n reads (host) into one contiguous pinned staging area and then to the device.
+static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
+                            uint32_t n, cudaStream_t st) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; ++i) total += lengths[i];
+    mapper_reserve(m, n, total);
+    m.h_meta.resize(12ull * (n + 1));
+    uint64_t* ho = m.h_meta.as<uint64_t>();
+    uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
+    bool contiguous = true;
+    uint64_t acc = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        ho[i] = acc;
+        hl[i] = lengths[i];
+        contiguous &= offsets[i] == offsets[0] + acc;
+        acc += lengths[i];
+    }
+    if (contiguous && total) {
+        GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), seqs + offsets[0], total, cudaMemcpyHostToDevice, st));
+    } else if (total) {
+        m.h_seqs.resize(total);
+        char* hs = m.h_seqs.as<char>();
+        for (uint32_t i = 0; i < n; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
+        GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), hs, total, cudaMemcpyHostToDevice, st));
+    }
+    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
+    return total;
+}
+
+int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
+                           uint32_t n_reads, gbsa_query_randstrobe* out, uint64_t out_capacity, uint64_t* out_offsets,
+                           uint64_t* out_total) {
+    return guarded([&] {
+        if (!params_valid(*p)) throw Error(GBSA_ERR_PARAM, "invalid index parameters");
+        require_device();
+        gbsa_index dummy;
+        dummy.params = *p;
+        dummy.dp = make_dev_params(*p);
+        gbsa_mapper m;
+        m.idx = &dummy;
+        GBSA_CUDA(cudaStreamCreateWithFlags(&m.st, cudaStreamNonBlocking));
+        struct G {
+            cudaStream_t s;
+            ~G() { cudaStreamDestroy(s); }
+        } g{m.st};
+        Workspace ws;
+        const uint32_t n = n_reads;
+        stage_reads(m, seqs, offsets, lengths, n, m.st);
+        for (int attempt = 0; attempt < 8; ++attempt) {
+            Counters* ctr = m.ctr.as<Counters>();
+            GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), m.st));
+            GBSA_CUDA(cudaMemsetAsync(m.rec.as<void>(), 0, sizeof(ReadRec) * (n + 1), m.st));
+            Arenas A = arenas_of(m);
+            launch_seed(dummy.dp, m.seqs.as<uint8_t>(), m.offs.as<uint64_t>(), m.lens.as<uint32_t>(), n,
+                        m.rec.as<ReadRec>(), A, ctr, m.st);
+            launch_seed_long(dummy.dp, m.seqs.as<uint8_t>(), m.offs.as<uint64_t>(), m.lens.as<uint32_t>(),
+                             m.rec.as<ReadRec>(), A, ctr, m.long_scratch.as<uint8_t>(), m.long_warps, m.st);
+            Counters h{};
+            GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, m.st));
+            GBSA_CUDA(cudaStreamSynchronize(m.st));
+            if (h.status & kStatusReadTooLong)
+                throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
+            if (h.status & kStatusSyncmerOverflow) throw Error(GBSA_ERR_DEVICE_STATUS, "syncmer buffer overflow");
+            if (h.status & kStatusQueryOverflow) {
+                grow(m.q, m.q_cap, h.q_used, sizeof(Query));
+                m.qaux.release();
+                m.qaux.resize(4 * m.q_cap);
+                m.qpos.release();
+                m.qpos.resize(8 * m.q_cap);
+                continue;
+            }
+            uint64_t* cnt = m.cnt.as<uint64_t>();
+            uint64_t* off = m.out_off.as<uint64_t>();
+            launch_read_counts(n, m.rec.as<ReadRec>(), 1, cnt, m.st);
+            scan_exclusive_u64(cnt, off, n, off + n, ws, m.st);
+            GBSA_CUDA(cudaMemcpyAsync(out_offsets, off, 8ull * (n + 1), cudaMemcpyDeviceToHost, m.st));
+            GBSA_CUDA(cudaStreamSynchronize(m.st));
+            const uint64_t total = out_offsets[n];
+            if (out_total) *out_total = total;
+            if (total > out_capacity) throw Error(GBSA_ERR_CAPACITY, "output capacity too small");
+            if (total) {
+                DeviceBuffer dout(sizeof(gbsa_query_randstrobe) * total);
+                launch_gather_queries(n, m.rec.as<ReadRec>(), m.q.as<Query>(), off,
+                                      dout.as<gbsa_query_randstrobe>(), m.st);
+                GBSA_CUDA(cudaMemcpyAsync(out, dout.as<void>(), sizeof(gbsa_query_randstrobe) * total,
+                                          cudaMemcpyDeviceToHost, m.st));
+                GBSA_CUDA(cudaStreamSynchronize(m.st));
+            }
+            return;
+        }
+        throw Error(GBSA_ERR_DEVICE_STATUS, "query arena kept overflowing");
+    });
+}
+
+int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint32_t max_reads, uint64_t max_bases,
+                       gbsa_mapper** out) {
+    return guarded([&] {
+        *out = nullptr;
+        require_device();
+        std::unique_ptr<gbsa_mapper> m(new gbsa_mapper());
+        m->idx = idx;
+        m->opt = *opt;
+        m->cfg.rescue_level = opt->rescue_level;
+        m->cfg.rescue_cutoff = opt->rescue_level < 100 ? (uint32_t)(opt->rescue_level * (int)idx->filter_cutoff)
+                                                       : 100u;   // step2/main.cu:4204
+        m->cfg.count_cap = opt->rescue_count_cap;
+        m->cfg.sort_mode = opt->sort_mode;
+        m->max_reads = std::max<uint32_t>(max_reads, 1);
+        m->max_bases = std::max<uint64_t>(max_bases, 1);
+        GBSA_CUDA(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+        mapper_reserve(*m, m->max_reads, m->max_bases);
+        *out = m.release();
+    });
+}
+
+void gbsa_mapper_free(gbsa_mapper* m) {
+    if (!m) return;
+    if (m->st) {
+        cudaStreamSynchronize(m->st);
+        cudaStreamDestroy(m->st);
+    }
+    delete m;
+}
+
+int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths, uint32_t n_reads,
+                   gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets, float* frac, uint8_t* rescued) {
+    return guarded([&] {
+        cudaStream_t st = m->st;
+        uint64_t done_nams = 0;
+        nam_offsets[0] = 0;
+        for (uint32_t b0 = 0; b0 < n_reads || (n_reads == 0 && b0 == 0); b0 += m->max_reads) {
+            const uint32_t n = std::min(m->max_reads, n_reads - b0);
+            if (n == 0) break;
+            stage_reads(*m, seqs, offsets + b0, lengths + b0, n, st);
+            const uint64_t total =
+                run_pipeline(*m, m->seqs.as<uint8_t>(), m->offs.as<uint64_t>(), m->lens.as<uint32_t>(), n, false, st);
+            // offsets
+            GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, m->out_off.as<uint64_t>(), 8ull * (n + 1),
+                                      cudaMemcpyDeviceToHost, st));
+            m->out_nams.resize(sizeof(gbsa_nam) * (total + 1));
+            launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(),
+                               m->out_nams.as<gbsa_nam>(), m->out_frac.as<float>(), m->out_resc.as<uint8_t>(), st);
+            if (frac) GBSA_CUDA(cudaMemcpyAsync(frac + b0, m->out_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, st));
+            if (rescued)
+                GBSA_CUDA(cudaMemcpyAsync(rescued + b0, m->out_resc.as<void>(), n, cudaMemcpyDeviceToHost, st));
+            if (done_nams + total <= nam_capacity && total)
+                GBSA_CUDA(cudaMemcpyAsync(nams + done_nams, m->out_nams.as<void>(), sizeof(gbsa_nam) * total,
+                                          cudaMemcpyDeviceToHost, st));
+            GBSA_CUDA(cudaStreamSynchronize(st));
+            for (uint32_t i = 0; i <= n; ++i) nam_offsets[b0 + i] += done_nams;
+            done_nams += total;
+        }
+        if (done_nams > nam_capacity) throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
+    });
+}
+
+int gbsa_map_reads_device(gbsa_mapper* m, const char* d_seqs, const uint64_t* d_offsets, const uint32_t* d_lengths,
+                          uint32_t n_reads, gbsa_nam* d_nams, uint64_t nam_capacity, uint64_t* d_nam_offsets,
+                          float* d_frac, uint8_t* d_rescued, uint64_t* nam_total, void* stream) {
+    return guarded([&] {
+        cudaStream_t st = stream ? (cudaStream_t)stream : m->st;
+        mapper_reserve(*m, n_reads, m->max_bases);
+        const uint64_t total = run_pipeline(*m, reinterpret_cast<const uint8_t*>(d_seqs), d_offsets, d_lengths,
+                                            n_reads, false, st);
+        if (nam_total) *nam_total = total;
+        GBSA_CUDA(cudaMemcpyAsync(d_nam_offsets, m->out_off.as<void>(), 8ull * (n_reads + 1),
+                                  cudaMemcpyDeviceToDevice, st));
+        if (total > nam_capacity) {
+            GBSA_CUDA(cudaStreamSynchronize(st));
+            throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
+        }
+        launch_gather_nams(n_reads, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(), d_nams,
+                           d_frac, d_rescued, st);
+    });
+}
+
+int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries, const uint64_t* q_offsets, uint32_t n_reads,
+                   int rescue, uint32_t rescue_cutoff, gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets,
+                   float* frac) {
+    return guarded([&] {
+        cudaStream_t st = m->st;
+        const uint32_t n = n_reads;
+        const uint64_t nqt = q_offsets[n] - q_offsets[0];
+        mapper_reserve(*m, n, std::max<uint64_t>(64, nqt));
+        if (m->q_cap < nqt + 1) {
+            m->q_cap = nqt + 1;
+            m->q.release();
+            m->q.resize(sizeof(Query) * m->q_cap);
+            m->qaux.release();
+            m->qaux.resize(4 * m->q_cap);
+            m->qpos.release();
+            m->qpos.resize(8 * m->q_cap);
+        }
+        // Lay the queries of each read out forward-first, each orientation ordered by
+        // start (stable), which is the order randstrobes_query produces and in which the
+        // reference's (query_start, ref_start) hit sort leaves them.
+        std::vector<Query> hq(nqt + 1);
+        std::vector<ReadRec> hr(n);
+        std::vector<uint32_t> ord;
+        uint64_t o = 0;
+        for (uint32_t r = 0; r < n; ++r) {
+            const uint64_t a = q_offsets[r], b = q_offsets[r + 1];
+            ord.resize(b - a);
+            std::iota(ord.begin(), ord.end(), 0u);
+            std::stable_sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) {
+                const auto& qx = queries[a + x];
+                const auto& qy = queries[a + y];
+                if ((qx.is_reverse != 0) != (qy.is_reverse != 0)) return qx.is_reverse == 0;
+                return qx.start < qy.start;
+            });
+            uint32_t nf = 0;
+            for (uint32_t j = 0; j < ord.size(); ++j) {
+                const auto& q = queries[a + ord[j]];
+                hq[o + j] = Query{q.hash, q.start, q.end};
+                nf += q.is_reverse ? 0 : 1;
+            }
+            ReadRec R{};
+            R.q_off = o;
+            R.nq = nf;
+            R.nq2 = (uint32_t)(b - a);
+            hr[r] = R;
+            o += b - a;
+        }
+        if (nqt) GBSA_CUDA(cudaMemcpyAsync(m->q.as<void>(), hq.data(), sizeof(Query) * nqt, cudaMemcpyHostToDevice, st));
+        GBSA_CUDA(cudaMemcpyAsync(m->rec.as<void>(), hr.data(), sizeof(ReadRec) * n, cudaMemcpyHostToDevice, st));
+        const MapConfig saved = m->cfg;
+        m->cfg.rescue_level = 0;          // find_nams alone, or
+        m->cfg.force_rescue = rescue ? 1 : 0;   // find_nams_rescue for every read
+        m->cfg.rescue_cutoff = rescue_cutoff;
+        uint64_t total = 0;
+        try {
+            total = run_pipeline(*m, nullptr, nullptr, nullptr, n, true, st);
+        } catch (...) {
+            m->cfg = saved;
+            throw;
+        }
+        m->cfg = saved;
+        GBSA_CUDA(cudaMemcpyAsync(nam_offsets, m->out_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost, st));
+        m->out_nams.resize(sizeof(gbsa_nam) * (total + 1));
+        launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(),
+                           m->out_nams.as<gbsa_nam>(), m->out_frac.as<float>(), nullptr, st);
+        if (frac) GBSA_CUDA(cudaMemcpyAsync(frac, m->out_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, st));
+        if (total <= nam_capacity && total)
+            GBSA_CUDA(cudaMemcpyAsync(nams, m->out_nams.as<void>(), sizeof(gbsa_nam) * total, cudaMemcpyDeviceToHost,
+                                      st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        if (total > nam_capacity) throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
+    });
+}
+
+// Instrumentation used by the benchmark: enable the algorithmic-byte counter and read
+// the value of the last batch.
+void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on) { m->count_bytes = on; }
+uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m) { return m->alg_bytes; }
+
+}  // extern "C"

@@ -1,0 +1,100 @@
+// map.cuh — the mapper: device work areas and the kernels of the read → NAM path.
+#pragma once
+
+#include "index.h"
+#include "nam.cuh"
+#include "seed.cuh"
+
+namespace gbsa {
+
+// Per-read bookkeeping of one batch.
+struct ReadRec {
+    uint64_t q_off;      // first query randstrobe in the query arena
+    uint32_t nq;         // forward query randstrobes (they come first, by start)
+    uint32_t nq2;        // all query randstrobes (the reverse ones follow, by start)
+    uint32_t flags;      // kRead* bits
+    uint32_t pad0;
+    uint64_t hit_off;    // first hit in the hit arena
+    uint32_t n_hits;
+    float frac;          // nonrepetitive_fraction
+    uint64_t nam_off;    // first NAM in the NAM arena
+    uint32_t n_nams;
+    uint32_t n_found;    // query randstrobes found in the index
+};
+
+constexpr uint32_t kReadRescue = 1u << 0;   // NAMs come from the rescue path
+constexpr uint32_t kReadLong = 1u << 1;     // seeded by the scratch-memory kernel
+constexpr uint32_t kReadFailed = 1u << 2;   // a capacity limit was hit
+
+// Device counters of one batch (bump allocators, work lists, status).
+struct Counters {
+    unsigned long long q_used;
+    unsigned long long hit_used;
+    unsigned long long nam_used;
+    unsigned long long scratch_used;
+    unsigned long long alg_bytes;   // roofline numerator (see k_lookup)
+    unsigned int n_rescue;
+    unsigned int n_long;
+    unsigned int status;
+    unsigned int pad;
+};
+
+struct Arenas {
+    Query* q;
+    uint64_t q_cap;
+    uint32_t* q_aux;         // per query: hits emitted (lookup) / exclusive offset
+    uint64_t* q_pos;         // per query: index position of its hash (or kNotFound)
+    HitRec* hits;
+    uint64_t hit_cap;
+    gbsa_nam* nams;
+    uint64_t nam_cap;
+    uint8_t* slots;          // per-warp scratch slots of the NAM / rescue kernels
+    uint64_t slot_bytes;
+    uint8_t* ovf;            // shared overflow scratch (bump-allocated)
+    uint64_t ovf_cap;
+    uint32_t* rescue_list;
+    uint32_t* long_list;
+};
+
+struct MapConfig {
+    int rescue_level;
+    uint32_t rescue_cutoff;
+    uint32_t count_cap;
+    int sort_mode;
+    int count_bytes;    // accumulate algorithmic bytes
+    int force_rescue;   // every read takes the rescue path (find_nams_rescue entry point)
+};
+
+// Reads shorter than this (and with at most kSmemSyncmers syncmers) are seeded
+// with shared-memory buffers; the rest by the scratch-memory kernel.
+constexpr uint32_t kSmemMaxLen = 1024;
+constexpr uint32_t kSmemSyncmers = 256;
+// Global scratch per warp of the long-read seeding kernel.
+constexpr uint32_t kLongWords = GBSA_MAX_READ_LEN / 32 + 4;
+constexpr size_t kLongSlotBytes = (size_t)kLongWords * 8 + (size_t)kLongWords * 4 + 64 * 8 +
+                                  (size_t)GBSA_MAX_READ_LEN * 8 + (size_t)GBSA_MAX_READ_LEN * 4;
+
+// Warps launched by the NAM and rescue kernels (one scratch slot each).
+uint32_t nam_kernel_warps(uint32_t n_reads);
+
+void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens, uint32_t n,
+                 ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
+void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens,
+                      ReadRec* rec, Arenas A, Counters* ctr, uint8_t* long_scratch, uint32_t long_warps,
+                      cudaStream_t st);
+void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                   cudaStream_t st);
+void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                 cudaStream_t st);
+void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
+                   cudaStream_t st);
+void launch_gather_nams(uint32_t n, const ReadRec* rec, const gbsa_nam* arena, const uint64_t* out_off,
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st);
+void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
+                           gbsa_query_randstrobe* out, cudaStream_t st);
+void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st);
+void launch_get_count(const IndexView& I, const uint64_t* pos, uint64_t n, uint32_t* counts, cudaStream_t st);
+void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st);
+void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st);
+
+}  // namespace gbsa

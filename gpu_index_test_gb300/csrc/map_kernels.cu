@@ -1,0 +1,599 @@
+// map_kernels.cu — kernels of the read → NAM path (plain form: one kernel per stage,
+// a warp per read, intermediates in HBM arenas).
+//
+//   k_seed_smem / k_seed_long   randstrobes_query (step2/randstrobes.cu:195-241)
+//   k_lookup                    the query loop of find_nams (step2/nam.cu:748-790):
+//                               find, is_filtered, add_to_hits_per_ref; the rescue
+//                               decision of step2/main.cu:3209-3216
+//   k_nams                      merge_hits_into_nams_forward_and_reverse(sort=true)
+//                               (step2/nam.cu:515-539, 347-513) + NAM sort
+//   k_rescue                    find_nams_rescue (step2/nam.cu:927-985) + NAM sort
+#include <algorithm>
+
+#include "map.cuh"
+#include "runtime.h"
+
+namespace gbsa {
+
+namespace {
+
+constexpr int kSeedWarps = 8;
+constexpr int kWarpsPerBlock = 8;
+
+__device__ __forceinline__ uint32_t warp_global_id() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ uint32_t warp_count() { return (gridDim.x * blockDim.x) >> 5; }
+
+__device__ __forceinline__ uint64_t warp_bump(unsigned long long* ctr, uint64_t n) {
+    uint64_t off = 0;
+    if (lane_id() == 0) off = atomicAdd(ctr, (unsigned long long)n);
+    return __shfl_sync(0xFFFFFFFFu, off, 0);
+}
+
+__device__ __forceinline__ void warp_fail(ReadRec& rec, Counters* ctr, uint32_t bit) {
+    if (lane_id() == 0) {
+        rec.flags |= kReadFailed;
+        atomicOr(&ctr->status, bit);
+    }
+}
+
+// Writes the query randstrobes of read r from its syncmers.
+__device__ __forceinline__ void emit_read_queries(const DevParams& P, const uint64_t* sh, const uint32_t* sp,
+                                                  uint32_t ns, uint32_t L, ReadRec& rec, const Arenas& A,
+                                                  Counters* ctr) {
+    const uint32_t nq = n_query_per_dir(P, ns, L);
+    const uint64_t off = warp_bump(&ctr->q_used, 2ull * nq);
+    if (off + 2ull * nq > A.q_cap) {
+        warp_fail(rec, ctr, kStatusQueryOverflow);
+        if (lane_id() == 0) rec.nq = rec.nq2 = 0;
+        return;
+    }
+    warp_write_queries(P, sh, sp, ns, L, nq, A.q + off);
+    if (lane_id() == 0) {
+        rec.q_off = off;
+        rec.nq = nq;
+        rec.nq2 = 2 * nq;
+    }
+}
+
+__global__ void __launch_bounds__(32 * kSeedWarps) k_seed_smem(DevParams P, const uint8_t* __restrict__ seqs,
+                                                                const uint64_t* __restrict__ offs,
+                                                                const uint32_t* __restrict__ lens, uint32_t n,
+                                                                ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    __shared__ uint64_t s_pk[kSeedWarps][kSmemMaxLen / 32 + 4];
+    __shared__ uint32_t s_nm[kSeedWarps][kSmemMaxLen / 32 + 4];
+    __shared__ uint64_t s_hb[kSeedWarps][64];
+    __shared__ uint64_t s_sh[kSeedWarps][kSmemSyncmers];
+    __shared__ uint32_t s_sp[kSeedWarps][kSmemSyncmers];
+    const uint32_t w = threadIdx.x >> 5;
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        const uint32_t L = lens[r];
+        ReadRec& R = rec[r];
+        if (L > GBSA_MAX_READ_LEN) {
+            warp_fail(R, ctr, kStatusReadTooLong);
+            continue;
+        }
+        uint32_t ns = 0xFFFFFFFFu;
+        if (L <= kSmemMaxLen)
+            ns = warp_read_syncmers(P, seqs + offs[r], L, s_pk[w], s_nm[w], s_hb[w], s_sh[w], s_sp[w], kSmemSyncmers);
+        if (ns == 0xFFFFFFFFu) {
+            if (lane_id() == 0) {
+                R.flags |= kReadLong;
+                A.long_list[atomicAdd(&ctr->n_long, 1u)] = r;
+            }
+            continue;
+        }
+        emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
+        __syncwarp();
+    }
+}
+
+// Reads that did not fit the shared-memory buffers: same code on a per-warp slot of
+// global scratch memory sized for GBSA_MAX_READ_LEN.
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_seed_long(DevParams P, const uint8_t* __restrict__ seqs,
+                                                                    const uint64_t* __restrict__ offs,
+                                                                    const uint32_t* __restrict__ lens,
+                                                                    ReadRec* __restrict__ rec, Arenas A, Counters* ctr,
+                                                                    uint8_t* scratch) {
+    const uint32_t n_long = *(volatile unsigned int*)&ctr->n_long;
+    uint8_t* slot = scratch + (size_t)warp_global_id() * kLongSlotBytes;
+    uint64_t* pk = reinterpret_cast<uint64_t*>(slot);
+    uint32_t* nm = reinterpret_cast<uint32_t*>(pk + kLongWords);
+    uint64_t* hb = reinterpret_cast<uint64_t*>(nm + kLongWords);
+    uint64_t* sh = hb + 64;
+    uint32_t* sp = reinterpret_cast<uint32_t*>(sh + GBSA_MAX_READ_LEN);
+    for (uint32_t t = warp_global_id(); t < n_long; t += warp_count()) {
+        const uint32_t r = A.long_list[t];
+        const uint32_t L = lens[r];
+        ReadRec& R = rec[r];
+        const uint32_t ns = warp_read_syncmers(P, seqs + offs[r], L, pk, nm, hb, sh, sp, GBSA_MAX_READ_LEN);
+        if (ns == 0xFFFFFFFFu) {
+            warp_fail(R, ctr, kStatusSyncmerOverflow);
+            continue;
+        }
+        emit_read_queries(P, sh, sp, ns, L, R, A, ctr);
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
+                                                                 ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    const uint32_t lane = lane_id();
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        ReadRec& R = rec[r];
+        if (R.flags & kReadFailed) continue;
+        const uint32_t nq = R.nq, nq2 = R.nq2;
+        Query* Q = A.q + R.q_off;
+        uint32_t* aux = A.q_aux + R.q_off;
+        uint32_t tot = 0, good = 0;
+        uint64_t bytes = 0;
+        for (uint32_t i = lane; i < nq2; i += 32) {
+            const Query q = Q[i];
+            uint32_t ex = 0;
+            const uint64_t pos = index_find(I, q.hash, &ex);
+            uint32_t nh = 0;
+            bytes += 16 + 16ull * ex;
+            if (pos != kNotFound) {
+                ++tot;
+                bytes += 16;
+                if (!index_is_filtered(I, pos)) {
+                    ++good;
+                    uint32_t run = 0;
+                    nh = walk_hit_run(I, (int)q.start, (int)q.end, pos, [&](uint32_t, int, int) {}, &run);
+                    bytes += 16ull * run;
+                }
+            }
+            A.q_pos[R.q_off + i] = pos;
+            aux[i] = nh;
+        }
+        tot = warp_sum(tot);
+        good = warp_sum(good);
+        if (C.count_bytes) {
+            bytes = warp_sum(bytes);
+            if (lane == 0) atomicAdd(&ctr->alg_bytes, (unsigned long long)bytes);
+        }
+        // nonrepetitive_fraction (step2/nam.cu:892) and the rescue trigger: a double
+        // comparison of the float ratio with 0.7, or no hits (step2/main.cu:3211)
+        const float frac = tot > 0 ? ((float)good) / ((float)tot) : 1.0f;
+        const bool rescue = C.force_rescue || (C.rescue_level > 1 && (good == 0 || (double)frac < 0.7));
+        if (lane == 0) {
+            R.frac = frac;
+            R.n_found = tot;
+        }
+        if (rescue) {
+            if (lane == 0) {
+                R.flags |= kReadRescue;
+                A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
+                R.n_hits = 0;
+            }
+            continue;
+        }
+        // hit offsets in generation order (query order, then run order)
+        uint64_t running = 0;
+        for (uint32_t base = 0; base < nq2; base += 32) {
+            const uint32_t i = base + lane;
+            const uint32_t v = i < nq2 ? aux[i] : 0;
+            const uint32_t inc = warp_inclusive_sum(v);
+            if (i < nq2) aux[i] = (uint32_t)running + inc - v;
+            running += __shfl_sync(0xFFFFFFFFu, inc, 31);
+        }
+        __syncwarp();
+        const uint64_t H = running;
+        const uint64_t hoff = warp_bump(&ctr->hit_used, H);
+        if (hoff + H > A.hit_cap) {
+            warp_fail(R, ctr, kStatusHitOverflow);
+            continue;
+        }
+        const uint64_t* qp = A.q_pos + R.q_off;
+        for (uint32_t i = lane; i < nq2; i += 32) {
+            const uint64_t pos = qp[i];
+            if (pos == kNotFound || index_is_filtered(I, pos)) continue;
+            const uint32_t dir = i >= nq ? 1u : 0u;
+            HitRec* out = A.hits + hoff + aux[i];
+            uint32_t k = 0;
+            const int qs = (int)Q[i].start, qe = (int)Q[i].end;
+            walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
+                HitRec h;
+                h.ref_rc = (dir << 31) | ref;
+                h.qs = qs;
+                h.qe = qe;
+                h.rs = rs;
+                h.re = re;
+                out[k++] = h;
+            });
+        }
+        if (lane == 0) {
+            R.hit_off = hoff;
+            R.n_hits = (uint32_t)H;
+        }
+    }
+}
+
+// Scratch of `bytes` for the calling warp: its own slot from byte `slot_off` on when
+// the request fits, else a bump allocation in the shared overflow arena (nullptr
+// when that is full too).
+__device__ __forceinline__ uint8_t* warp_scratch(const Arenas& A, Counters* ctr, uint64_t slot_off, uint64_t bytes) {
+    if (slot_off + bytes <= A.slot_bytes) return A.slots + (uint64_t)warp_global_id() * A.slot_bytes + slot_off;
+    const uint64_t o = warp_bump(&ctr->scratch_used, bytes);
+    if (o + bytes > A.ovf_cap) return nullptr;
+    return A.ovf + o;
+}
+
+// Carves consecutive regions out of a scratch block.
+struct Carver {
+    uint8_t* p;
+    __device__ void* take(uint64_t bytes) {
+        void* r = p;
+        p += (bytes + 15) & ~15ull;
+        return r;
+    }
+};
+
+__device__ __forceinline__ uint64_t nam_scratch_bytes(uint32_t H) {
+    const uint64_t P = next_pow2(H);
+    return 16 * 8 + 8 * P + 4 * P + 4 * P + 32ull * H * 2 + 4ull * (H + 1) * 2 + H + 64;
+}
+
+// Groups hits[0..H) by (orientation, ref id) keeping generation order, merges each
+// group with one lane, sorts the NAMs and writes them to the NAM arena.
+template <bool kNamMajor>
+__device__ void warp_hits_to_nams(const MapConfig& C, const HitRec* hits, uint32_t H, uint8_t* scratch, ReadRec& R,
+                                  const Arenas& A, Counters* ctr) {
+    const uint32_t lane = lane_id();
+    const uint32_t P2 = next_pow2(H);
+    Carver cv{scratch};
+    uint64_t* keys = (uint64_t*)cv.take(8ull * P2);
+    uint32_t* order = (uint32_t*)cv.take(4ull * P2);
+    uint32_t* idx = (uint32_t*)cv.take(4ull * P2);
+    NamState* states = (NamState*)cv.take(32ull * H);
+    NamState* compact = (NamState*)cv.take(32ull * H);
+    uint32_t* gstart = (uint32_t*)cv.take(4ull * (H + 1));
+    uint32_t* gcount = (uint32_t*)cv.take(4ull * (H + 1));
+    uint8_t* taken = (uint8_t*)cv.take(H);
+
+    for (uint32_t i = lane; i < H; i += 32) keys[i] = ((uint64_t)hits[i].ref_rc << 32) | i;
+    __syncwarp();
+    warp_sort_u64(keys, H);
+    for (uint32_t i = lane; i < H; i += 32) order[i] = (uint32_t)keys[i];
+    __syncwarp();
+    // group starts
+    uint32_t G = 0;
+    for (uint32_t base = 0; base < H; base += 32) {
+        const uint32_t i = base + lane;
+        const bool st = i < H && (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32));
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, st);
+        if (st) gstart[G + __popc(m & lanemask_lt())] = i;
+        G += __popc(m);
+    }
+    if (lane == 0) gstart[G] = H;
+    __syncwarp();
+    for (uint32_t g = lane; g < G; g += 32) {
+        const uint32_t b = gstart[g], e = gstart[g + 1];
+        gcount[g] = kNamMajor ? merge_group_nam_major(hits, order, b, e, states + b, taken + b)
+                              : merge_group_hit_major(hits, order, b, e, states + b);
+    }
+    __syncwarp();
+    // compact the NAMs of all groups
+    uint32_t NN = 0;
+    for (uint32_t base = 0; base < G; base += 32) {
+        const uint32_t g = base + lane;
+        const uint32_t v = g < G ? gcount[g] : 0;
+        const uint32_t inc = warp_inclusive_sum(v);
+        if (g < G) {
+            const uint32_t dst = NN + inc - v, b = gstart[g];
+            for (uint32_t j = 0; j < v; ++j) compact[dst + j] = states[b + j];
+        }
+        NN += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    }
+    __syncwarp();
+    warp_sort_nams(compact, idx, NN, C.sort_mode);
+    const uint64_t noff = warp_bump(&ctr->nam_used, NN);
+    if (noff + NN > A.nam_cap) {
+        warp_fail(R, ctr, kStatusNamOverflow);
+        return;
+    }
+    for (uint32_t j = lane; j < NN; j += 32) to_gbsa_nam(compact[idx[j]], (int)j, A.nams[noff + j]);
+    if (lane == 0) {
+        R.nam_off = noff;
+        R.n_nams = NN;
+    }
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
+                                                               Arenas A, Counters* ctr) {
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        ReadRec& R = rec[r];
+        if (R.flags & (kReadFailed | kReadRescue)) continue;
+        const uint32_t H = R.n_hits;
+        if (H == 0) continue;
+        uint8_t* sc = warp_scratch(A, ctr, 0, nam_scratch_bytes(H));
+        if (!sc) {
+            warp_fail(R, ctr, kStatusScratchOverflow);
+            continue;
+        }
+        warp_hits_to_nams<false>(C, A.hits + R.hit_off, H, sc, R, A, ctr);
+        __syncwarp();
+    }
+}
+
+// find_nams_rescue for the reads on the rescue list.
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
+                                                                 Arenas A, Counters* ctr) {
+    const uint32_t lane = lane_id();
+    const uint32_t n_rescue = *(volatile unsigned int*)&ctr->n_rescue;
+    for (uint32_t t = warp_global_id(); t < n_rescue; t += warp_count()) {
+        const uint32_t r = A.rescue_list[t];
+        ReadRec& R = rec[r];
+        const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
+        const Query* Qd[2] = {A.q + R.q_off, A.q + R.q_off + R.nq};
+        const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
+        const uint32_t nqm = nqd[0] > nqd[1] ? nqd[0] : nqd[1];
+        const uint32_t Pq = next_pow2(nqm > 0 ? nqm : 1);
+        // phase 1 scratch: rescue-hit keys and taken keys, per orientation
+        const uint64_t b1 = 4ull * 8 * Pq + 64;
+        uint8_t* sc1 = warp_scratch(A, ctr, 0, b1);
+        if (!sc1) {
+            warp_fail(R, ctr, kStatusScratchOverflow);
+            continue;
+        }
+        Carver cv{sc1};
+        uint64_t* rk[2] = {(uint64_t*)cv.take(8ull * Pq), (uint64_t*)cv.take(8ull * Pq)};
+        uint64_t* tk[2] = {(uint64_t*)cv.take(8ull * Pq), (uint64_t*)cv.take(8ull * Pq)};
+        uint32_t m[2];
+        for (int d = 0; d < 2; ++d) {
+            // RescueHit{position, count, qs, qe} of every found query, keyed by
+            // (count, query_start) — query_start is unique per orientation, so this is
+            // the reference's (count, query_start, query_end) order (cmp1, nam.cu:909-912)
+            uint32_t nd = 0;
+            const uint32_t nq = nqd[d];
+            for (uint32_t base = 0; base < nq; base += 32) {
+                const uint32_t qi = base + lane;
+                bool f = false;
+                uint64_t key = 0;
+                if (qi < nq) {
+                    const Query q = Qd[d][qi];
+                    const uint64_t pos = Pd[d][qi];
+                    if (pos != kNotFound) {
+                        f = true;
+                        const uint32_t cnt = index_get_count(I, pos);
+                        key = ((uint64_t)cnt << 32) | ((uint64_t)q.start << 16) | qi;
+                    }
+                }
+                const uint32_t bm = __ballot_sync(0xFFFFFFFFu, f);
+                if (f) rk[d][nd + __popc(bm & lanemask_lt())] = key;
+                nd += __popc(bm);
+            }
+            __syncwarp();
+            warp_sort_u64(rk[d], nd);
+            // prefix of the sorted list until (count > rescue_cutoff && taken >= 5) or
+            // count > cap (step2/nam.cu:960-969)
+            uint32_t stop = nd;
+            for (uint32_t base = 0; base < nd; base += 32) {
+                const uint32_t j = base + lane;
+                bool brk = false;
+                if (j < nd) {
+                    const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
+                    brk = (cnt > C.rescue_cutoff && j >= 5) || cnt > C.count_cap;
+                }
+                const uint32_t bm = __ballot_sync(0xFFFFFFFFu, brk);
+                if (bm) {
+                    stop = base + (__ffs(bm) - 1);
+                    break;
+                }
+            }
+            m[d] = stop;
+            // re-sort the taken ones by query_start (cmp2)
+            for (uint32_t j = lane; j < stop; j += 32) tk[d][j] = rk[d][j] & 0xFFFFFFFFull;
+            __syncwarp();
+            warp_sort_u64(tk[d], stop);
+        }
+        // hit counts of the taken rescue hits, in (orientation, query_start) order
+        uint64_t TH = 0;
+        for (int d = 0; d < 2; ++d) {
+            for (uint32_t j = lane; j < m[d]; j += 32) {
+                const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
+                const Query q = Qd[d][qi];
+                const uint32_t c = walk_hit_run(I, (int)q.start, (int)q.end, Pd[d][qi], [](uint32_t, int, int) {});
+                TH += c;
+            }
+        }
+        TH = warp_sum(TH);
+        const uint32_t H = (uint32_t)TH;
+        const uint64_t b2 = 20ull * H + nam_scratch_bytes(H) + 64;
+        uint8_t* sc2 = TH > 0xFFFFFFFull ? nullptr : warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
+        if (!sc2) {
+            warp_fail(R, ctr, kStatusScratchOverflow);
+            continue;
+        }
+        HitRec* hits = (HitRec*)sc2;
+        uint8_t* nscratch = sc2 + ((20ull * H + 15) & ~15ull);
+        // write hits in generation order: prefix sums over the taken lists
+        uint32_t running = 0;
+        for (int d = 0; d < 2; ++d) {
+            for (uint32_t base = 0; base < m[d]; base += 32) {
+                const uint32_t j = base + lane;
+                uint32_t c = 0;
+                Query q{};
+                uint64_t pos = 0;
+                if (j < m[d]) {
+                    const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
+                    q = Qd[d][qi];
+                    pos = Pd[d][qi];
+                    c = walk_hit_run(I, (int)q.start, (int)q.end, pos, [](uint32_t, int, int) {});
+                }
+                const uint32_t inc = warp_inclusive_sum(c);
+                if (j < m[d]) {
+                    HitRec* out = hits + running + inc - c;
+                    uint32_t k = 0;
+                    const int qs = (int)q.start, qe = (int)q.end;
+                    walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
+                        HitRec h;
+                        h.ref_rc = ((uint32_t)d << 31) | ref;
+                        h.qs = qs;
+                        h.qe = qe;
+                        h.rs = rs;
+                        h.re = re;
+                        out[k++] = h;
+                    });
+                }
+                running += __shfl_sync(0xFFFFFFFFu, inc, 31);
+            }
+        }
+        __syncwarp();
+        if (H == 0) {
+            if (lane == 0) R.n_nams = 0;
+            continue;
+        }
+        warp_hits_to_nams<true>(C, hits, H, nscratch, R, A, ctr);
+        __syncwarp();
+    }
+}
+
+__global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const gbsa_nam* __restrict__ arena,
+                              const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, float* frac,
+                              uint8_t* rescued) {
+    const uint32_t lane = lane_id();
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        const ReadRec R = rec[r];
+        const uint64_t o = out_off[r];
+        for (uint32_t j = lane; j < R.n_nams; j += 32) out[o + j] = arena[R.nam_off + j];
+        if (lane == 0) {
+            if (frac) frac[r] = R.frac;
+            if (rescued) rescued[r] = (R.flags & kReadRescue) ? 1 : 0;
+        }
+    }
+}
+
+__global__ void k_gather_queries(uint32_t n, const ReadRec* __restrict__ rec, const Query* __restrict__ arena,
+                                 const uint64_t* __restrict__ out_off, gbsa_query_randstrobe* __restrict__ out) {
+    const uint32_t lane = lane_id();
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        const ReadRec R = rec[r];
+        const uint64_t o = out_off[r];
+        for (uint32_t j = lane; j < R.nq2; j += 32) {
+            const Query q = arena[R.q_off + j];
+            gbsa_query_randstrobe x;
+            x.hash = q.hash;
+            x.start = q.start;
+            x.end = q.end;
+            x.is_reverse = j >= R.nq ? 1 : 0;
+            for (int b = 0; b < 7; ++b) x._pad[b] = 0;
+            out[o + j] = x;
+        }
+    }
+}
+
+__global__ void k_read_counts(uint32_t n, const ReadRec* __restrict__ rec, int what, uint64_t* __restrict__ out) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        out[r] = what == 0 ? rec[r].n_nams : (uint64_t)rec[r].nq2;
+}
+
+__global__ void k_reset_recs(uint32_t n, ReadRec* __restrict__ rec) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        ReadRec& R = rec[r];
+        R.flags = 0;
+        R.hit_off = 0;
+        R.n_hits = 0;
+        R.frac = 0.0f;
+        R.nam_off = 0;
+        R.n_nams = 0;
+        R.n_found = 0;
+    }
+}
+
+__global__ void k_find(IndexView I, const uint64_t* __restrict__ h, uint64_t n, uint64_t* __restrict__ pos) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        pos[i] = index_find(I, h[i]);
+}
+
+__global__ void k_get_count(IndexView I, const uint64_t* __restrict__ p, uint64_t n, uint32_t* __restrict__ c) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        c[i] = p[i] < I.n ? index_get_count(I, p[i]) : 0;
+}
+
+unsigned warp_grid(uint64_t items, int warps_per_block) {
+    const int sms = device_sm_count();
+    const uint64_t want = (items + warps_per_block - 1) / warps_per_block;
+    const uint64_t cap = (uint64_t)sms * 16;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, cap));
+}
+
+}  // namespace
+
+uint32_t nam_kernel_warps(uint32_t n_reads) { return warp_grid(n_reads, kWarpsPerBlock) * kWarpsPerBlock; }
+
+void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens, uint32_t n,
+                 ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    if (!n) return;
+    k_seed_smem<<<warp_grid(n, kSeedWarps), 32 * kSeedWarps, 0, st>>>(P, seqs, offs, lens, n, rec, A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens,
+                      ReadRec* rec, Arenas A, Counters* ctr, uint8_t* long_scratch, uint32_t long_warps,
+                      cudaStream_t st) {
+    const unsigned blocks = std::max(1u, long_warps / kWarpsPerBlock);
+    k_seed_long<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(P, seqs, offs, lens, rec, A, ctr, long_scratch);
+    GBSA_LAUNCHED();
+}
+
+void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                   cudaStream_t st) {
+    if (!n) return;
+    k_lookup<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                 cudaStream_t st) {
+    if (!n) return;
+    k_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(C, n, rec, A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
+                   cudaStream_t st) {
+    if (!n_reads) return;
+    k_rescue<<<warp_grid(n_reads, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_gather_nams(uint32_t n, const ReadRec* rec, const gbsa_nam* arena, const uint64_t* out_off,
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st) {
+    if (!n) return;
+    k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out, frac,
+                                                                                rescued);
+    GBSA_LAUNCHED();
+}
+
+void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
+                           gbsa_query_randstrobe* out, cudaStream_t st) {
+    if (!n) return;
+    k_gather_queries<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out);
+    GBSA_LAUNCHED();
+}
+
+void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st) {
+    if (!n) return;
+    k_find<<<grid_for(n, 256, 1u << 20), 256, 0, st>>>(I, hashes, n, pos);
+    GBSA_LAUNCHED();
+}
+
+void launch_get_count(const IndexView& I, const uint64_t* pos, uint64_t n, uint32_t* counts, cudaStream_t st) {
+    if (!n) return;
+    k_get_count<<<grid_for(n, 256, 1u << 20), 256, 0, st>>>(I, pos, n, counts);
+    GBSA_LAUNCHED();
+}
+
+void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st) {
+    if (!n) return;
+    k_reset_recs<<<grid_for(n, 256, 1u << 16), 256, 0, st>>>(n, rec);
+    GBSA_LAUNCHED();
+}
+
+void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st) {
+    if (!n) return;
+    k_read_counts<<<grid_for(n, 256, 1u << 16), 256, 0, st>>>(n, rec, what, out);
+    GBSA_LAUNCHED();
+}
+
+}  // namespace gbsa

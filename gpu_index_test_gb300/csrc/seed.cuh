@@ -1,0 +1,318 @@
+// seed.cuh — warp-cooperative canonical syncmers and randstrobes.
+//
+// Restates, for a warp of 32 lanes, the reference's per-base syncmer state machine
+// (SyncmerIterator::next, step2/randstrobes.cu:18-79) and randstrobe selection
+// (RandstrobeIterator::get, step2/randstrobes.cu:136-159; query driver
+// randstrobes_query, step2/randstrobes.cu:195-241).
+//
+// Syncmer rule.  Window w is the k-mer starting at base w; it holds the W = k-s+1
+// s-mers w .. w+W-1.  The reference keeps (min value, min position m) over a queue
+// of s-mer hashes:
+//   first window after a reset:  m = leftmost minimum (forward scan, strict <)
+//   minimum popped (m == w-1):   m = rightmost minimum of the window (reverse scan)
+//   newest s-mer strictly below: m = w+W-1
+//   otherwise:                   m unchanged
+// and emits a syncmer when m == w+t-1.  m is always *an* argmin of the window, so
+// whenever the window's minimum is unique m is that argmin, whatever came before.
+// The warp therefore decides all windows with a unique minimum in parallel (one
+// lane per window) and replays the exact state machine, over 32 windows at a time
+// with warp shuffles, only for chunks that contain a window with a tied minimum
+// (low-complexity sequence) — the replay needs just each window's leftmost and
+// rightmost argmin, computed in parallel.  A window whose values are all UINT64_MAX
+// is handled like the reference (state "none").
+#pragma once
+
+#include "common.cuh"
+
+namespace gbsa {
+
+// Per-window facts needed by the replay, packed in a u32:
+//   bit 0 valid, bit 1 first, bit 2 all-max, bits 8..15 leftmost argmin offset,
+//   bits 16..23 rightmost argmin offset.
+struct WinInfo {
+    static __device__ __forceinline__ uint32_t pack(bool valid, bool first, bool allmax, uint32_t lo, uint32_t ro) {
+        return (valid ? 1u : 0u) | (first ? 2u : 0u) | (allmax ? 4u : 0u) | (lo << 8) | (ro << 16);
+    }
+};
+
+// 2-bit packing of ASCII bases into MSB-first 64-bit words plus an N bitmask
+// (LSB-first 32-bit words; bases at or beyond L count as N).  Writes
+// nwords = ceil(L/32) + 2 words to each array.  Coalesced: each warp load covers
+// 32 consecutive bytes.
+__device__ __forceinline__ uint64_t spread_bits(uint32_t x) {
+    uint64_t v = x;
+    v = (v | (v << 16)) & 0x0000FFFF0000FFFFULL;
+    v = (v | (v << 8)) & 0x00FF00FF00FF00FFULL;
+    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0FULL;
+    v = (v | (v << 2)) & 0x3333333333333333ULL;
+    v = (v | (v << 1)) & 0x5555555555555555ULL;
+    return v;
+}
+
+__device__ __forceinline__ void warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
+    const uint32_t lane = lane_id();
+    const uint32_t nw = (L + 31) / 32;
+    for (uint32_t it = 0; it < nw + 2; ++it) {
+        const uint32_t p = it * 32 + lane;
+        const uint32_t c = p < L ? nt4(seq[p]) : 4u;
+        const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, c & 1u);
+        const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, (c >> 1) & 1u);
+        const uint32_t bn = __ballot_sync(0xFFFFFFFFu, c == 4u);
+        if (lane == (it & 31)) {
+            const uint64_t lo = spread_bits(__brev(b0 & ~bn));
+            const uint64_t hi = spread_bits(__brev(b1 & ~bn));
+            packed[it] = lo | (hi << 1);
+            nmask[it] = bn;
+        }
+    }
+    __syncwarp();
+}
+
+// n (<= 32) bits of an LSB-first u32 bitmask stream starting at bit p.
+__device__ __forceinline__ uint32_t nbits32(const uint32_t* m, uint64_t p, int n) {
+    const uint64_t wi = p >> 5;
+    const uint32_t sh = (uint32_t)(p & 31);
+    uint64_t v = ((uint64_t)m[wi + 1] << 32) | m[wi];
+    v >>= sh;
+    return n >= 32 ? (uint32_t)v : (uint32_t)(v & ((1ULL << n) - 1));
+}
+
+__device__ __forceinline__ uint64_t smer_hash(const DevParams& P, const uint64_t* packed, uint64_t p) {
+    const uint64_t f = extract_bases(packed, p, P.s);
+    const uint64_t r = revcomp_bits(f, P.s);
+    return xxh64(f < r ? f : r);
+}
+
+__device__ __forceinline__ uint64_t kmer_hash(const DevParams& P, const uint64_t* packed, uint64_t p) {
+    const uint64_t f = extract_bases(packed, p, P.k);
+    const uint64_t r = revcomp_bits(f, P.k);
+    return xxh64(f < r ? f : r);
+}
+
+// Facts of window w of a sequence whose base 0 sits at stream position `base`
+// (valid when w < nwin and the k-mer holds no N).  hw points at the W s-mer hashes
+// of the window.
+__device__ __forceinline__ uint32_t window_info(const DevParams& P, const uint32_t* nmask, uint64_t base, uint32_t w,
+                                                uint32_t nwin, const uint64_t* hw) {
+    if (w >= nwin) return 0;
+    if (nbits32(nmask, base + w, P.k) != 0) return 0;
+    uint64_t mv = hw[0];
+    uint32_t lo = 0, ro = 0;
+    for (int d = 1; d < P.W; ++d) {
+        const uint64_t v = hw[d];
+        if (v < mv) {
+            mv = v;
+            lo = ro = (uint32_t)d;
+        } else if (v == mv) {
+            ro = (uint32_t)d;
+        }
+    }
+    const bool first = (w == 0) || (nbits32(nmask, base + w - 1, 1) != 0);
+    return WinInfo::pack(true, first, mv == ~0ULL, lo, ro);
+}
+
+// A window's state is "determined" (independent of the past) when it is the first
+// of a run of valid windows or its minimum is unique (and not UINT64_MAX).
+__device__ __forceinline__ bool win_determined(uint32_t inf) {
+    const bool first = inf & 2u, allmax = inf & 4u;
+    const uint32_t lo = (inf >> 8) & 0xFF, ro = (inf >> 16) & 0xFF;
+    return first || (lo == ro && !allmax);
+}
+
+// One step of the reference state machine for valid window w with facts inf,
+// entering with state m (position of the current minimum, or none).
+__device__ __forceinline__ uint32_t win_step(uint32_t m, uint32_t inf, uint32_t w) {
+    const bool first = inf & 2u, allmax = inf & 4u;
+    const uint32_t lo = (inf >> 8) & 0xFF, ro = (inf >> 16) & 0xFF;
+    if (first) return allmax ? kNoneState : w + lo;       // forward scan, leftmost minimum
+    if (lo == ro && !allmax) return w + lo;                // unique minimum: any path lands on it
+    if (m != kNoneState && m == w - 1) return w + ro;      // popped: reverse scan, rightmost minimum
+    return m;                                              // tie, not popped: the older minimum stays
+}
+
+// Processes windows [w_begin, w_end) of one sequence (base 0 at stream position
+// `base` of packed/nmask, any address space; nwin windows in total) and calls
+// emit(index, window) for every syncmer with window >= w_emit, in order, index
+// counting from 0.  Window w_begin must be determined, invalid, or window 0, so
+// that the state entering it never matters.  hbuf: 64 u64 of warp-private
+// scratch.  Returns the number of syncmers emitted.
+template <class Emit>
+__device__ uint32_t warp_syncmer_scan(const DevParams& P, const uint64_t* packed, const uint32_t* nmask, uint64_t base,
+                                      uint32_t nwin, uint32_t w_begin, uint32_t w_end, uint32_t w_emit, uint64_t* hbuf,
+                                      Emit&& emit) {
+    const uint32_t lane = lane_id();
+    uint32_t count = 0;
+    uint32_t carry = kNoneState;
+    const uint32_t tpos = (uint32_t)(P.t - 1);
+    for (uint32_t c = w_begin; c < w_end; c += 32) {
+        const uint32_t w = c + lane;
+        hbuf[lane] = smer_hash(P, packed, base + w);
+        if (lane < (uint32_t)(P.W - 1)) hbuf[32 + lane] = smer_hash(P, packed, base + c + 32 + lane);
+        __syncwarp();
+        const uint32_t inf = (w < w_end) ? window_info(P, nmask, base, w, nwin, hbuf + lane) : 0u;
+        const bool valid = inf & 1u;
+        const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
+        const uint32_t umask = __ballot_sync(0xFFFFFFFFu, valid && !win_determined(inf));
+        bool sync;
+        if (umask == 0) {
+            const uint32_t m = valid ? win_step(kNoneState, inf, w) : kNoneState;
+            sync = valid && m != kNoneState && m == w + tpos;
+            if (vmask) carry = __shfl_sync(0xFFFFFFFFu, m, 31 - __clz(vmask));
+        } else {
+            // exact replay of the reference state machine over this chunk
+            uint32_t m = carry;
+            uint32_t bits = 0;
+            for (int j = 0; j < 32; ++j) {
+                const uint32_t ij = __shfl_sync(0xFFFFFFFFu, inf, j);
+                if (ij & 1u) {
+                    const uint32_t wj = c + (uint32_t)j;
+                    m = win_step(m, ij, wj);
+                    if (m != kNoneState && m == wj + tpos) bits |= 1u << j;
+                }
+            }
+            sync = (bits >> lane) & 1u;
+            carry = m;
+        }
+        const bool out = sync && w >= w_emit;
+        const uint32_t smask = __ballot_sync(0xFFFFFFFFu, out);
+        if (out) emit(count + __popc(smask & lanemask_lt()), w);
+        count += __popc(smask);
+        __syncwarp();
+    }
+    return count;
+}
+
+// Largest window d <= w0 from which a scan can start without knowing the past:
+// window 0, an invalid window, or a determined one (for segments of long contigs).
+__device__ inline uint32_t warp_find_anchor(const DevParams& P, const uint64_t* packed, const uint32_t* nmask, uint64_t base,
+                                     uint32_t nwin, uint32_t w0, uint64_t* hbuf) {
+    const uint32_t lane = lane_id();
+    uint32_t top = w0;   // examine windows (top-31 .. top]
+    for (;;) {
+        const uint32_t lo_w = top >= 31 ? top - 31 : 0;
+        const uint32_t w = lo_w + lane;
+        hbuf[lane] = smer_hash(P, packed, base + w);
+        if (lane < (uint32_t)(P.W - 1)) hbuf[32 + lane] = smer_hash(P, packed, base + lo_w + 32 + lane);
+        __syncwarp();
+        bool ok = false;
+        if (w <= top) {
+            const uint32_t inf = window_info(P, nmask, base, w, nwin, hbuf + lane);
+            ok = !(inf & 1u) || win_determined(inf) || w == 0;
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        __syncwarp();
+        if (m) return lo_w + (31 - __clz(m));
+        if (lo_w == 0) return 0;
+        top = lo_w - 1;
+    }
+}
+
+// Forward randstrobe with strobe 1 = syncmer j of n (RandstrobeIterator::get).
+__device__ __forceinline__ void randstrobe_fwd(const DevParams& P, const uint64_t* sh, const uint32_t* sp, uint32_t n,
+                                               uint32_t j, uint64_t& hash, uint32_t& s1, uint32_t& s2) {
+    const uint32_t w_end = min(j + P.w_max, n - 1);
+    const uint64_t h1 = sh[j];
+    const uint32_t p1 = sp[j];
+    const uint64_t max_pos = (uint64_t)p1 + P.max_dist;
+    uint64_t h2 = h1;
+    uint32_t p2 = p1;
+    uint32_t best = 0xFFFFFFFFu;
+    for (uint32_t i = j + P.w_min; i <= w_end && sp[i] <= max_pos; ++i) {
+        const uint32_t sc = __popcll((h1 ^ sh[i]) & P.q);
+        if (sc < best) {
+            best = sc;
+            h2 = sh[i];
+            p2 = sp[i];
+        }
+    }
+    hash = h1 + h2;
+    s1 = p1;
+    s2 = p2;
+}
+
+// Reverse-complement randstrobe number jr of n: the reference reverses the syncmer
+// vector and maps positions to L - pos - k (step2/randstrobes.cu:221-224), then
+// runs the same selection.
+__device__ __forceinline__ void randstrobe_rev(const DevParams& P, const uint64_t* sh, const uint32_t* sp, uint32_t n,
+                                               uint32_t L, uint32_t jr, uint64_t& hash, uint32_t& s1, uint32_t& s2) {
+    const uint32_t k = (uint32_t)P.k;
+    const uint32_t w_end = min(jr + P.w_max, n - 1);
+    const uint32_t i1 = n - 1 - jr;
+    const uint64_t h1 = sh[i1];
+    const uint32_t p1 = L - sp[i1] - k;
+    const uint64_t max_pos = (uint64_t)p1 + P.max_dist;
+    uint64_t h2 = h1;
+    uint32_t p2 = p1;
+    uint32_t best = 0xFFFFFFFFu;
+    for (uint32_t x = jr + P.w_min; x <= w_end; ++x) {
+        const uint32_t ix = n - 1 - x;
+        const uint32_t px = L - sp[ix] - k;
+        if (px > max_pos) break;
+        const uint32_t sc = __popcll((h1 ^ sh[ix]) & P.q);
+        if (sc < best) {
+            best = sc;
+            h2 = sh[ix];
+            p2 = px;
+        }
+    }
+    hash = h1 + h2;
+    s1 = p1;
+    s2 = p2;
+}
+
+// Internal compact query randstrobe: is_reverse is implied by the index (the
+// forward ones of a read come first, as in randstrobes_query).
+struct Query {
+    uint64_t hash;
+    uint32_t start;
+    uint32_t end;
+};
+
+// Seeds one read with the warp: packs it into pk/nm (capacity for L bases), finds
+// its syncmers into sh/sp (capacity cap) and returns the syncmer count, or
+// 0xFFFFFFFF when more than cap syncmers exist.
+__device__ __forceinline__ uint32_t warp_read_syncmers(const DevParams& P, const uint8_t* seq, uint32_t L, uint64_t* pk,
+                                                       uint32_t* nm, uint64_t* hbuf, uint64_t* sh, uint32_t* sp,
+                                                       uint32_t cap) {
+    if (L < (uint32_t)P.k) return 0;
+    warp_pack_read(seq, L, pk, nm);
+    const uint32_t nwin = L - (uint32_t)P.k + 1;
+    bool over = false;
+    const uint32_t n = warp_syncmer_scan(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, [&](uint32_t idx, uint32_t w) {
+        if (idx < cap) {
+            sh[idx] = kmer_hash(P, pk, w);
+            sp[idx] = w;
+        } else {
+            over = true;
+        }
+    });
+    __syncwarp();
+    if (__any_sync(0xFFFFFFFFu, over)) return 0xFFFFFFFFu;
+    return n;
+}
+
+// Number of query randstrobes per orientation for n syncmers of a read of length L
+// (randstrobes_query returns none when L < w_max, step2/randstrobes.cu:197).
+__device__ __forceinline__ uint32_t n_query_per_dir(const DevParams& P, uint32_t n, uint32_t L) {
+    if (L < P.w_max) return 0;
+    return n > P.w_min ? n - P.w_min : 0;
+}
+
+// Writes the 2*nq query randstrobes of a read (forward, then reverse complement).
+__device__ __forceinline__ void warp_write_queries(const DevParams& P, const uint64_t* sh, const uint32_t* sp,
+                                                   uint32_t n, uint32_t L, uint32_t nq, Query* out) {
+    const uint32_t lane = lane_id();
+    for (uint32_t j = lane; j < 2 * nq; j += 32) {
+        uint64_t h;
+        uint32_t s1, s2;
+        if (j < nq) randstrobe_fwd(P, sh, sp, n, j, h, s1, s2);
+        else randstrobe_rev(P, sh, sp, n, L, j - nq, h, s1, s2);
+        Query q;
+        q.hash = h;
+        q.start = s1;
+        q.end = s2 + (uint32_t)P.k;
+        out[j] = q;
+    }
+}
+
+}  // namespace gbsa

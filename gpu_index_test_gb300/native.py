@@ -1,0 +1,263 @@
+"""ctypes binding of libgbsa.so (the C-ABI declared in include/gbsa.h).
+
+Mirrors the reference interfaces of the path:
+  IndexParameters.from_read_length   step2/indexparameters.cpp:150-182
+  StrobemerIndex (populate, find, get_count, is_filtered, read, write)
+                                     step2/index.hpp:37-183, step2/index.cu:73-134
+  randstrobes_query                  step2/randstrobes.cu:195-241
+  find_nams / find_nams_rescue       step2/nam.hpp:11-20
+Errors raise GbsaError carrying the C status code (BadParameter → GBSA_ERR_PARAM,
+InvalidIndexFile → GBSA_ERR_INDEX_FILE, …).  There is no CPU fallback: when the
+library is missing or no GPU is visible, calls fail loudly.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import abi
+from ._build_paths import GBSA_SO, INCLUDE_DIR
+
+_lib = None
+
+
+class GbsaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbsa error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(GBSA_SO):
+            raise RuntimeError(f"CUDA library missing: {GBSA_SO} (run __graft_entry__.build())")
+        L = C.CDLL(GBSA_SO)
+        P = C.POINTER(abi.Params)
+        vp, u64, u32, i32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int
+        proto = {
+            "gbsa_last_error": (C.c_char_p, []),
+            "gbsa_version": (i32, []),
+            "gbsa_launch_count": (u64, []),
+            "gbsa_params_from_read_length": (i32, [i32] * 7 + [P]),
+            "gbsa_params_make": (i32, [u64, i32, i32, i32, i32, i32, i32, P]),
+            "gbsa_pick_bits": (i32, [P, u64]),
+            "gbsa_index_build": (i32, [P, vp, vp, vp, u32, i32, C.c_float, C.POINTER(vp)]),
+            "gbsa_index_load": (i32, [P, vp, u64, vp, i32, u32, C.POINTER(vp)]),
+            "gbsa_index_read_sti": (i32, [C.c_char_p, P, C.POINTER(vp)]),
+            "gbsa_index_write_sti": (i32, [vp, C.c_char_p]),
+            "gbsa_index_get_info": (i32, [vp, C.POINTER(abi.IndexInfo)]),
+            "gbsa_index_get_params": (i32, [vp, P]),
+            "gbsa_index_export": (i32, [vp, vp, vp]),
+            "gbsa_index_free": (None, [vp]),
+            "gbsa_find": (i32, [vp, vp, u64, vp]),
+            "gbsa_get_count": (i32, [vp, vp, u64, vp]),
+            "gbsa_randstrobes_query": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64)]),
+            "gbsa_mapper_create": (i32, [vp, C.POINTER(abi.MapOptions), u32, u64, C.POINTER(vp)]),
+            "gbsa_mapper_free": (None, [vp]),
+            "gbsa_map_reads": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp]),
+            "gbsa_map_reads_device": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, C.POINTER(u64), vp]),
+            "gbsa_find_nams": (i32, [vp, vp, vp, u32, i32, u32, vp, u64, vp, vp]),
+            "gbsa_mapper_set_count_bytes": (None, [vp, i32]),
+            "gbsa_mapper_last_alg_bytes": (u64, [vp]),
+        }
+        for name, (res, args) in proto.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def header_symbols():
+    """Function names declared in include/gbsa.h."""
+    txt = open(os.path.join(INCLUDE_DIR, "gbsa.h")).read()
+    return sorted(set(re.findall(r"\b(gbsa_[a-z0-9_]+)\s*\(", txt)))
+
+
+def _check(rc):
+    if rc != abi.GBSA_OK:
+        raise GbsaError(rc, lib().gbsa_last_error().decode())
+
+
+def launch_count():
+    return lib().gbsa_launch_count()
+
+
+def params_from_read_length(r, k=abi.GBSA_DEFAULT, s=abi.GBSA_DEFAULT, l=abi.GBSA_DEFAULT, u=abi.GBSA_DEFAULT,
+                            c=abi.GBSA_DEFAULT, max_seed_len=abi.GBSA_DEFAULT):
+    p = abi.Params()
+    _check(lib().gbsa_params_from_read_length(r, k, s, l, u, c, max_seed_len, C.byref(p)))
+    return p
+
+
+def _u8(a):
+    a = np.ascontiguousarray(a, np.uint8)
+    return a if len(a) else np.zeros(1, np.uint8)
+
+
+class Index:
+    """Device-resident StrobemerIndex."""
+
+    def __init__(self, handle, params):
+        self.h = C.c_void_p(handle)
+        self.params = params
+
+    @classmethod
+    def build(cls, params, genome, bits=-1, f=0.0002):
+        h = C.c_void_p()
+        _check(lib().gbsa_index_build(C.byref(params), _u8(genome.seq).ctypes.data,
+                                      np.ascontiguousarray(genome.offsets, np.uint64).ctypes.data,
+                                      np.ascontiguousarray(genome.lengths, np.uint64).ctypes.data,
+                                      len(genome.lengths), bits, f, C.byref(h)))
+        return cls(h.value, params)
+
+    @classmethod
+    def load(cls, params, randstrobes, starts, bits, filter_cutoff):
+        rs = np.ascontiguousarray(randstrobes)
+        st = np.ascontiguousarray(starts, np.uint64)
+        h = C.c_void_p()
+        _check(lib().gbsa_index_load(C.byref(params), rs.ctypes.data if len(rs) else None, len(rs), st.ctypes.data,
+                                     bits, filter_cutoff, C.byref(h)))
+        return cls(h.value, params)
+
+    @classmethod
+    def read_sti(cls, path, params):
+        h = C.c_void_p()
+        _check(lib().gbsa_index_read_sti(path.encode(), C.byref(params), C.byref(h)))
+        return cls(h.value, params)
+
+    def write_sti(self, path):
+        _check(lib().gbsa_index_write_sti(self.h, path.encode()))
+
+    def free(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().gbsa_index_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def info(self):
+        i = abi.IndexInfo()
+        _check(lib().gbsa_index_get_info(self.h, C.byref(i)))
+        return i
+
+    def export(self):
+        i = self.info()
+        rs = np.zeros(max(1, i.size), abi.REF_RANDSTROBE)
+        st = np.zeros((1 << i.bits) + 1, np.uint64)
+        _check(lib().gbsa_index_export(self.h, rs.ctypes.data, st.ctypes.data))
+        return rs[: i.size], st
+
+    def find(self, hashes):
+        h = np.ascontiguousarray(hashes, np.uint64)
+        out = np.zeros(max(1, len(h)), np.uint64)
+        _check(lib().gbsa_find(self.h, h.ctypes.data, len(h), out.ctypes.data))
+        return out[: len(h)]
+
+    def get_count(self, positions):
+        p = np.ascontiguousarray(positions, np.uint64)
+        out = np.zeros(max(1, len(p)), np.uint32)
+        _check(lib().gbsa_get_count(self.h, p.ctypes.data, len(p), out.ctypes.data))
+        return out[: len(p)]
+
+
+def randstrobes_query(params, reads):
+    """Query randstrobes of every read: (records, offsets[n+1])."""
+    n = reads.n
+    offs = np.zeros(n + 1, np.uint64)
+    tot = C.c_uint64()
+    cap = int(reads.lengths.sum()) * 2 // 3 + 64
+    while True:
+        out = np.zeros(max(1, cap), abi.QUERY_RANDSTROBE)
+        rc = lib().gbsa_randstrobes_query(C.byref(params), _u8(reads.seq).ctypes.data,
+                                          np.ascontiguousarray(reads.offsets, np.uint64).ctypes.data,
+                                          np.ascontiguousarray(reads.lengths, np.uint32).ctypes.data, n,
+                                          out.ctypes.data, cap, offs.ctypes.data, C.byref(tot))
+        if rc == abi.GBSA_ERR_CAPACITY:
+            cap = tot.value
+            continue
+        _check(rc)
+        return out[: tot.value], offs
+
+
+class Mapper:
+    """Device work areas for batches of reads through seed → lookup → NAM (+ rescue)."""
+
+    def __init__(self, index, opt=None, max_reads=1 << 20, max_bases=None):
+        self.index = index
+        self.opt = opt or abi.map_options()
+        h = C.c_void_p()
+        _check(lib().gbsa_mapper_create(index.h, C.byref(self.opt), max_reads,
+                                        max_bases or max_reads * 160, C.byref(h)))
+        self.h = h
+
+    def free(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().gbsa_mapper_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def set_count_bytes(self, on=True):
+        lib().gbsa_mapper_set_count_bytes(self.h, 1 if on else 0)
+
+    def last_alg_bytes(self):
+        return lib().gbsa_mapper_last_alg_bytes(self.h)
+
+    def map_reads(self, reads, capacity=None):
+        n = reads.n
+        cap = capacity or max(1024, 24 * n)
+        seq = _u8(reads.seq)
+        offs_in = np.ascontiguousarray(reads.offsets, np.uint64)
+        lens = np.ascontiguousarray(reads.lengths, np.uint32)
+        while True:
+            nams = np.zeros(cap, abi.NAM)
+            offs = np.zeros(n + 1, np.uint64)
+            frac = np.zeros(max(1, n), np.float32)
+            resc = np.zeros(max(1, n), np.uint8)
+            rc = lib().gbsa_map_reads(self.h, seq.ctypes.data, offs_in.ctypes.data, lens.ctypes.data, n,
+                                      nams.ctypes.data, cap, offs.ctypes.data, frac.ctypes.data, resc.ctypes.data)
+            if rc == abi.GBSA_ERR_CAPACITY:
+                cap = int(offs[-1]) + 16
+                continue
+            _check(rc)
+            return nams[: int(offs[-1])], offs, frac[:n], resc[:n]
+
+    def map_reads_device(self, d_seq, d_offsets, d_lengths, n, d_nams, nam_capacity, d_nam_offsets, d_frac=None,
+                         d_rescued=None, stream=None):
+        """All arguments are device pointers (ints); returns the NAM total."""
+        tot = C.c_uint64()
+        rc = lib().gbsa_map_reads_device(self.h, d_seq, d_offsets, d_lengths, n, d_nams, nam_capacity, d_nam_offsets,
+                                         d_frac, d_rescued, C.byref(tot), stream)
+        if rc == abi.GBSA_ERR_CAPACITY:
+            return tot.value
+        _check(rc)
+        return tot.value
+
+    def find_nams(self, queries, q_offsets, rescue=False, rescue_cutoff=0):
+        q = np.ascontiguousarray(queries)
+        qo = np.ascontiguousarray(q_offsets, np.uint64)
+        n = len(qo) - 1
+        cap = max(1024, 4 * len(q))
+        while True:
+            nams = np.zeros(cap, abi.NAM)
+            offs = np.zeros(n + 1, np.uint64)
+            frac = np.zeros(max(1, n), np.float32)
+            rc = lib().gbsa_find_nams(self.h, q.ctypes.data if len(q) else None, qo.ctypes.data, n,
+                                      1 if rescue else 0, rescue_cutoff, nams.ctypes.data, cap, offs.ctypes.data,
+                                      frac.ctypes.data)
+            if rc == abi.GBSA_ERR_CAPACITY:
+                cap = int(offs[-1]) + 16
+                continue
+            _check(rc)
+            return nams[: int(offs[-1])], offs, frac[:n]

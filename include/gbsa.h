@@ -1,0 +1,228 @@
+/*
+ * gbsa.h — C-ABI of the GB300-native strobealign seeding → index lookup → NAM path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an
+ * int status (GBSA_OK == 0) and never throws across the boundary.  The text of
+ * the last error on the calling thread is returned by gbsa_last_error().
+ *
+ * Record layouts are byte-identical to the reference structs so that buffers can
+ * be handed over without conversion:
+ *   gbsa_ref_randstrobe   == RefRandstrobe   (step2/randstrobes.hpp:65-94, 16 B)
+ *   gbsa_query_randstrobe == QueryRandstrobe (step2/randstrobes.hpp:96-101, 24 B)
+ *   gbsa_nam              == Nam             (step2/my_struct.hpp:48-93, 44 B)
+ *   gbsa_params           mirrors IndexParameters (step2/indexparameters.hpp:72-95)
+ *
+ * Entry points that take HOST buffers copy them to the device and the results
+ * back inside the call (one CUDA stream per call).  Entry points whose name ends
+ * in `_device` take DEVICE pointers and a cudaStream_t (passed as void*) and do
+ * no host<->device copies of the payload.
+ */
+#ifndef GBSA_H
+#define GBSA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define GBSA_OK                 0
+#define GBSA_ERR_PARAM          1  /* BadParameter (step2/exceptions.hpp:7-10) */
+#define GBSA_ERR_CUDA           2  /* a CUDA runtime call failed */
+#define GBSA_ERR_NOMEM          3  /* device or pinned allocation failed */
+#define GBSA_ERR_INDEX_FILE     4  /* InvalidIndexFile (step2/exceptions.hpp:17-20) */
+#define GBSA_ERR_CAPACITY       5  /* a caller-sized output buffer is too small */
+#define GBSA_ERR_READ_TOO_LONG  6  /* a read exceeds GBSA_MAX_READ_LEN */
+#define GBSA_ERR_NO_DEVICE      7  /* no CUDA device visible */
+#define GBSA_ERR_DEVICE_STATUS  8  /* a kernel reported an internal limit */
+
+/* Longest read (bases) accepted by the seeding kernels. */
+#define GBSA_MAX_READ_LEN 4096
+
+/* "use the profile default" marker of IndexParameters::from_read_length
+ * (step2/indexparameters.hpp:78, numeric_limits<int>::min()). */
+#define GBSA_DEFAULT (-2147483647 - 1)
+
+/* ---- records -------------------------------------------------------------- */
+
+/* IndexParameters (step2/indexparameters.hpp:72-95) flattened. */
+typedef struct gbsa_params {
+    int32_t  canonical_read_length;
+    int32_t  k;
+    int32_t  s;
+    int32_t  t_syncmer;       /* (k - s) / 2 + 1 */
+    int32_t  l;
+    int32_t  u;
+    uint64_t q;               /* 2^c - 1 */
+    int32_t  max_dist;
+    uint32_t w_min;           /* max(0, k/(k-s+1) + l) */
+    uint32_t w_max;           /* k/(k-s+1) + u */
+    int32_t  _pad;
+} gbsa_params;
+
+/* RefRandstrobe (step2/randstrobes.hpp:65-94). packed = ref_index << 8 | strobe2 offset. */
+typedef struct gbsa_ref_randstrobe {
+    uint64_t hash;
+    uint32_t position;
+    uint32_t packed;
+} gbsa_ref_randstrobe;
+
+/* QueryRandstrobe (step2/randstrobes.hpp:96-101). */
+typedef struct gbsa_query_randstrobe {
+    uint64_t hash;
+    uint32_t start;
+    uint32_t end;
+    uint8_t  is_reverse;
+    uint8_t  _pad[7];
+} gbsa_query_randstrobe;
+
+/* Nam (step2/my_struct.hpp:48-62). */
+typedef struct gbsa_nam {
+    int32_t nam_id;
+    int32_t query_start;
+    int32_t query_end;
+    int32_t query_prev_hit_startpos;
+    int32_t ref_start;
+    int32_t ref_end;
+    int32_t ref_prev_hit_startpos;
+    int32_t n_hits;
+    int32_t ref_id;
+    float   score;
+    uint8_t is_rc;
+    uint8_t _pad[3];
+} gbsa_nam;
+
+/* IndexCreationStatistics (step2/index.hpp:22-35), counters only. */
+typedef struct gbsa_index_info {
+    uint64_t size;                 /* number of RefRandstrobe entries */
+    int32_t  bits;
+    uint32_t filter_cutoff;
+    uint64_t tot_strobemer_count;
+    uint64_t tot_occur_once;
+    uint64_t tot_high_ab;
+    uint64_t tot_mid_ab;
+    uint64_t index_cutoff;
+    uint64_t distinct_strobemers;
+} gbsa_index_info;
+
+/* NAM output order. */
+#define GBSA_SORT_SCORE       0  /* score desc, is_rc, ref_id, qs, qe, rs, re, n_hits desc */
+#define GBSA_SORT_REF_MATE2   1  /* Nam::operator< (step2/my_struct.hpp:78-92) made total */
+#define GBSA_SORT_REF_MATE1   2  /* sort_nams_single2 (step2/main.cu:2271-2289) made total */
+
+typedef struct gbsa_map_options {
+    int32_t  rescue_level;      /* R (step2/cmdline.hpp:56); rescue runs when R > 1 */
+    uint32_t rescue_count_cap;  /* 1000 = CPU find_nams_rescue (step2/nam.cu:964); 100 = step2/main.cu:39 */
+    int32_t  sort_mode;         /* GBSA_SORT_* */
+    int32_t  _pad;
+} gbsa_map_options;
+
+typedef struct gbsa_index  gbsa_index;
+typedef struct gbsa_mapper gbsa_mapper;
+
+/* ---- errors / device ------------------------------------------------------- */
+const char* gbsa_last_error(void);
+int gbsa_version(void);
+/* Number of kernel launches this library has issued in this process (all threads). */
+uint64_t gbsa_launch_count(void);
+
+/* ---- parameters ------------------------------------------------------------ */
+/* IndexParameters::from_read_length (step2/indexparameters.cpp:150-182). */
+int gbsa_params_from_read_length(int read_length, int k, int s, int l, int u, int c,
+                                 int max_seed_len, gbsa_params* out);
+/* IndexParameters(r, k, s, l, u, q, max_dist) (step2/indexparameters.hpp:80-85). */
+int gbsa_params_make(uint64_t canonical_read_length, int k, int s, int l, int u, int q,
+                     int max_dist, gbsa_params* out);
+
+/* ---- index ------------------------------------------------------------------ */
+/* StrobemerIndex::pick_bits (step2/index.cu:137-141). */
+int gbsa_pick_bits(const gbsa_params* p, uint64_t total_length);
+
+/* StrobemerIndex(references, parameters, bits) + populate(f, n_threads)
+ * (step2/index.hpp:39-54; body restated from step2/index.cu:143-311).
+ * Contig i is seqs[offsets[i] .. offsets[i] + lengths[i]).  bits == -1 picks bits. */
+int gbsa_index_build(const gbsa_params* p, const char* seqs, const uint64_t* offsets,
+                     const uint64_t* lengths, uint32_t n_contigs, int bits, float f,
+                     gbsa_index** out);
+/* Upload an index held in host memory (e.g. read from a .sti file). */
+int gbsa_index_load(const gbsa_params* p, const gbsa_ref_randstrobe* randstrobes, uint64_t n,
+                    const uint64_t* start_indices, int bits, uint32_t filter_cutoff,
+                    gbsa_index** out);
+/* StrobemerIndex::read / write, .sti format version 2 (step2/index.cu:73-134). */
+int gbsa_index_read_sti(const char* path, const gbsa_params* p, gbsa_index** out);
+int gbsa_index_write_sti(const gbsa_index* idx, const char* path);
+int gbsa_index_get_info(const gbsa_index* idx, gbsa_index_info* out);
+int gbsa_index_get_params(const gbsa_index* idx, gbsa_params* out);
+/* Copy the device tables to host: randstrobes[size], start_indices[2^bits + 1]. */
+int gbsa_index_export(const gbsa_index* idx, gbsa_ref_randstrobe* randstrobes,
+                      uint64_t* start_indices);
+void gbsa_index_free(gbsa_index* idx);
+
+/* StrobemerIndex::find (step2/index.hpp:57-81) for a batch; not found = UINT64_MAX. */
+int gbsa_find(const gbsa_index* idx, const uint64_t* hashes, uint64_t n, uint64_t* positions);
+/* StrobemerIndex::get_count (step2/index.hpp:115-147) for found positions. */
+int gbsa_get_count(const gbsa_index* idx, const uint64_t* positions, uint64_t n, uint32_t* counts);
+
+/* ---- seeding ------------------------------------------------------------------ */
+/* randstrobes_query (step2/randstrobes.cu:195-241) for a batch of reads.  Read i is
+ * seqs[offsets[i] .. offsets[i] + lengths[i]).  Randstrobes of read i are written to
+ * out[out_offsets[i] .. out_offsets[i+1]) (forward ones first, then reverse-complement
+ * ones, as the reference orders them).  *out_total receives the total; if it exceeds
+ * out_capacity, GBSA_ERR_CAPACITY is returned and nothing but out_offsets is written. */
+int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_t* offsets,
+                           const uint32_t* lengths, uint32_t n_reads,
+                           gbsa_query_randstrobe* out, uint64_t out_capacity,
+                           uint64_t* out_offsets, uint64_t* out_total);
+
+/* ---- NAM path ---------------------------------------------------------------- */
+/* A mapper owns the device work areas for batches of up to max_reads reads with up
+ * to max_bases bases in total; both grow on demand. */
+int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt,
+                       uint32_t max_reads, uint64_t max_bases, gbsa_mapper** out);
+void gbsa_mapper_free(gbsa_mapper* m);
+
+/* Reads → NAMs: randstrobes_query + find_nams (+ find_nams_rescue when
+ * nonrepetitive_fraction < 0.7 or no NAM was found and rescue_level > 1) + NAM sort,
+ * for every read (step2/main.cu:4461-4597 chain; CPU find_nams step2/nam.cu:748-905).
+ * NAMs of read i go to nams[nam_offsets[i] .. nam_offsets[i+1]).  frac[i] receives
+ * nonrepetitive_fraction, rescued[i] is 1 when the rescue path produced the NAMs.
+ * frac and rescued may be NULL.  If the NAM total exceeds nam_capacity the call
+ * returns GBSA_ERR_CAPACITY with nam_offsets filled so that the caller can resize. */
+int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets,
+                   const uint32_t* lengths, uint32_t n_reads,
+                   gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets,
+                   float* frac, uint8_t* rescued);
+
+/* Same, with every buffer in device memory and work queued on `stream`.  The call
+ * returns after the stream work is queued and the NAM total is known (it syncs
+ * the stream once to read the total). */
+int gbsa_map_reads_device(gbsa_mapper* m, const char* d_seqs, const uint64_t* d_offsets,
+                          const uint32_t* d_lengths, uint32_t n_reads,
+                          gbsa_nam* d_nams, uint64_t nam_capacity, uint64_t* d_nam_offsets,
+                          float* d_frac, uint8_t* d_rescued, uint64_t* nam_total,
+                          void* stream);
+
+/* find_nams (step2/nam.hpp:11-14) / find_nams_rescue (step2/nam.hpp:16-20) for a batch
+ * of already-seeded reads: queries of read i are queries[q_offsets[i] .. q_offsets[i+1]).
+ * rescue == 0 runs find_nams (frac receives nonrepetitive_fraction), rescue == 1 runs
+ * find_nams_rescue with rescue_cutoff.  NAMs are returned in the mapper's sort order. */
+int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
+                   const uint64_t* q_offsets, uint32_t n_reads, int rescue,
+                   uint32_t rescue_cutoff, gbsa_nam* nams, uint64_t nam_capacity,
+                   uint64_t* nam_offsets, float* frac);
+
+/* ---- instrumentation ---------------------------------------------------------- */
+/* Count the algorithmic bytes of the lookup stage (roofline numerator) in later
+ * calls; gbsa_mapper_last_alg_bytes returns the count of the last batch.  No
+ * reference counterpart (the reference prints wall-clock stage times only,
+ * step2/main.cu:4743-4746). */
+void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on);
+uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSA_H */

@@ -1,0 +1,915 @@
+/*
+ * oracle.cpp — CPU restatement of strobealign's seeding → index lookup → NAM path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker that the CUDA path is compared with.  Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library.
+ *
+ * Every function cites the reference code it restates (paths inside the reference
+ * project; step2/ unless noted).  The restatement keeps the reference's arithmetic
+ * and control flow where they decide results (queue-minimum tie rules, strict vs
+ * non-strict comparisons, the bucket-table build including its first-bucket quirk,
+ * float products and ratios), and differs only where the reference leaves a result
+ * unspecified or undefined:
+ *   - NAMs are returned in emission order of the restated merge; callers compare
+ *     them after oracle_sort_nams (the reference orders by robin_hood map iteration,
+ *     step2/nam.cu:368, which is not a specified order).
+ *   - The index is sorted by (hash, position, packed); the reference's pdqsort by
+ *     (hash, position) leaves cross-contig ties unordered (step2/randstrobes.hpp:77-80).
+ *   - k == 32 uses an all-ones k-mer mask; the reference shifts by 64 (UB).
+ *   - find() treats a lower_bound that lands at the end of the table as "not found";
+ *     the reference dereferences end() there (step2/index.hpp:79).
+ *   - Hit-run walks stop at the end of the table; the reference walks past it
+ *     forever when a hash equals UINT64_MAX (step2/nam.cu:52).
+ */
+#include "oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+/* ---- hash.hpp:97-119 : single-u64 reduced xxh64 ---------------------------- */
+constexpr uint64_t kPrime1 = 0x9E3779B185EBCA87ULL;
+constexpr uint64_t kPrime2 = 0xC2B2AE3D27D4EB4FULL;
+constexpr uint64_t kPrime3 = 0x165667B19E3779F9ULL;
+constexpr uint64_t kPrime4 = 0x85EBCA77C2B2AE63ULL;
+constexpr uint64_t kPrime5 = 0x27D4EB2F165667C5ULL;
+
+inline uint64_t rotl64(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+
+inline uint64_t xxh64(uint64_t v) {
+    uint64_t acc = kPrime5 + 8;
+    acc ^= rotl64(v * kPrime2, 31) * kPrime1;
+    acc = rotl64(acc, 27) * kPrime1 + kPrime4;
+    acc = (acc ^ (acc >> 33)) * kPrime2;
+    acc = (acc ^ (acc >> 29)) * kPrime3;
+    return acc ^ (acc >> 32);
+}
+
+/* ---- randstrobes.hpp:26-43 : base → 2-bit code, 4 = not ACGTU -------------- */
+struct Nt4Table {
+    unsigned char v[256];
+    Nt4Table() {
+        for (int i = 0; i < 256; ++i) v[i] = 4;
+        for (int i = 0; i < 4; ++i) v[i] = (unsigned char)i;   /* raw codes 0..3 */
+        const char* up = "ACGT";
+        const char* lo = "acgt";
+        for (int i = 0; i < 4; ++i) {
+            v[(unsigned char)up[i]] = (unsigned char)i;
+            v[(unsigned char)lo[i]] = (unsigned char)i;
+        }
+        v[(unsigned char)'U'] = 3;
+        v[(unsigned char)'u'] = 3;
+    }
+};
+const Nt4Table kNt4;
+
+struct Syncmer {
+    uint64_t hash;
+    uint64_t pos;
+};
+
+/* ---- indexparameters.{hpp,cpp} ------------------------------------------------ */
+bool verify_params(const gbsa_params& p) {
+    if (p.k <= 7 || p.k > 32) return false;               /* indexparameters.hpp:25 */
+    if (p.s > p.k) return false;                          /* :28 */
+    if ((p.k - p.s) % 2 != 0) return false;               /* :31 */
+    if (p.max_dist > 255) return false;                   /* :62 */
+    if (p.w_min > p.w_max) return false;                  /* :65 */
+    return true;
+}
+
+bool make_params(uint64_t r, int k, int s, int l, int u, int q, int max_dist, gbsa_params* out) {
+    gbsa_params p{};
+    p.canonical_read_length = (int32_t)r;
+    p.k = k;
+    p.s = s;
+    p.t_syncmer = (k - s) / 2 + 1;                         /* indexparameters.hpp:19 */
+    p.l = l;
+    p.u = u;
+    p.q = (uint64_t)(int64_t)q;
+    p.max_dist = max_dist;
+    if (k - s + 1 <= 0) return false;
+    p.w_min = (unsigned)std::max(0, k / (k - s + 1) + l);  /* indexparameters.hpp:83 */
+    p.w_max = (unsigned)(k / (k - s + 1) + u);
+    if (!verify_params(p)) return false;
+    *out = p;
+    return true;
+}
+
+/* ---- randstrobes.cu:18-79 : canonical open syncmers ---------------------------- */
+void canonical_syncmers(const gbsa_params& p, const char* seq, size_t len, std::vector<Syncmer>& out) {
+    out.clear();
+    const size_t k = (size_t)p.k, s = (size_t)p.s, t = (size_t)p.t_syncmer;
+    const size_t W = k - s + 1;
+    const uint64_t kmask = (k >= 32) ? ~0ULL : ((1ULL << (2 * k)) - 1);
+    const uint64_t smask = (s >= 32) ? ~0ULL : ((1ULL << (2 * s)) - 1);
+    const unsigned kshift = (unsigned)((k - 1) * 2);
+    const unsigned sshift = (unsigned)((s - 1) * 2);
+
+    std::vector<uint64_t> ring(W + 1);   /* queue of the last W s-mer hashes */
+    size_t qhead = 0, qsize = 0;
+    auto qat = [&](size_t j) -> uint64_t { return ring[(qhead + j) % (W + 1)]; };
+
+    uint64_t min_val = UINT64_MAX;
+    size_t min_pos = (size_t)-1;
+    size_t l = 0;
+    uint64_t xk0 = 0, xk1 = 0, xs0 = 0, xs1 = 0;
+    for (size_t i = 0; i < len; ++i) {
+        const int c = kNt4.v[(unsigned char)seq[i]];
+        if (c >= 4) {                                   /* "N": restart (:70-76) */
+            min_val = UINT64_MAX;
+            min_pos = (size_t)-1;
+            l = 0;
+            xk0 = xk1 = xs0 = xs1 = 0;
+            qhead = qsize = 0;
+            continue;
+        }
+        xk0 = ((xk0 << 2) | (uint64_t)c) & kmask;
+        xk1 = (xk1 >> 2) | ((uint64_t)(3 - c) << kshift);
+        xs0 = ((xs0 << 2) | (uint64_t)c) & smask;
+        xs1 = (xs1 >> 2) | ((uint64_t)(3 - c) << sshift);
+        if (++l < s) continue;
+        const uint64_t hs = xxh64(std::min(xs0, xs1));
+        ring[(qhead + qsize) % (W + 1)] = hs;
+        ++qsize;
+        if (qsize < W) continue;
+        if (qsize == W) {
+            /* first full window: leftmost minimum (forward scan, strict <) (:38-45) */
+            for (size_t j = 0; j < qsize; ++j) {
+                if (qat(j) < min_val) {
+                    min_val = qat(j);
+                    min_pos = i - k + j + 1;
+                }
+            }
+        } else {
+            qhead = (qhead + 1) % (W + 1);               /* pop_front (:48) */
+            --qsize;
+            if (min_pos == i - k) {
+                /* popped the minimum: rightmost minimum by reverse scan (:50-58) */
+                min_val = UINT64_MAX;
+                min_pos = i - s + 1;
+                for (size_t jj = qsize; jj-- > 0;) {
+                    if (qat(jj) < min_val) {
+                        min_val = qat(jj);
+                        min_pos = i - k + jj + 1;
+                    }
+                }
+            } else if (hs < min_val) {                  /* newest is a new strict minimum (:59-62) */
+                min_val = hs;
+                min_pos = i - s + 1;
+            }
+        }
+        if (min_pos == i - k + t) {                     /* minimum at the t-th s-mer (:64-69) */
+            out.push_back(Syncmer{xxh64(std::min(xk0, xk1)), i - k + 1});
+        }
+    }
+}
+
+/* ---- randstrobes.cu:136-159 : RandstrobeIterator::get ------------------------ */
+struct Strobe {
+    uint64_t hash;
+    uint32_t s1;
+    uint32_t s2;
+};
+
+Strobe randstrobe_at(const gbsa_params& p, const std::vector<Syncmer>& v, unsigned j) {
+    const unsigned w_end = (unsigned)std::min((size_t)(j + p.w_max), v.size() - 1);
+    const Syncmer s1 = v[j];
+    const uint64_t max_position = s1.pos + (unsigned)p.max_dist;
+    Syncmer s2 = s1;
+    uint64_t best = UINT64_MAX;
+    for (unsigned i = j + p.w_min; i <= w_end && v[i].pos <= max_position; ++i) {
+        const uint64_t score = (uint64_t)__builtin_popcountll((s1.hash ^ v[i].hash) & p.q);
+        if (score < best) {                           /* first minimum wins */
+            best = score;
+            s2 = v[i];
+        }
+    }
+    return Strobe{s1.hash + s2.hash, (uint32_t)s1.pos, (uint32_t)s2.pos};   /* randstrobes.hpp:61-63 */
+}
+
+/* ---- randstrobes.cu:195-241 : randstrobes_query --------------------------------- */
+void randstrobes_query(const gbsa_params& p, const char* seq, size_t len,
+                       std::vector<gbsa_query_randstrobe>& out) {
+    out.clear();
+    if (len < p.w_max) return;
+    std::vector<Syncmer> sm;
+    canonical_syncmers(p, seq, len, sm);
+    if (sm.empty()) return;
+    auto emit = [&](bool rev) {
+        for (unsigned j = 0; j + p.w_min < sm.size(); ++j) {
+            const Strobe r = randstrobe_at(p, sm, j);
+            gbsa_query_randstrobe q{};
+            q.hash = r.hash;
+            q.start = r.s1;
+            q.end = r.s2 + (uint32_t)p.k;
+            q.is_reverse = rev ? 1 : 0;
+            out.push_back(q);
+        }
+    };
+    emit(false);
+    std::reverse(sm.begin(), sm.end());
+    for (auto& x : sm) x.pos = len - x.pos - (size_t)p.k;
+    emit(true);
+}
+
+/* ---- index.hpp / index.cu ------------------------------------------------------- */
+int pick_bits(const gbsa_params& p, uint64_t size) {           /* index.cu:137-141 */
+    const uint64_t est = size / (uint64_t)(p.k - p.s + 1);
+    if (est == 0) return 8;   /* log2(0) = -inf; the reference's int cast is UB there */
+    const int b = (int)std::log2((double)est) - 1;
+    return std::clamp(b, 8, 31);
+}
+
+struct IndexCpu {
+    gbsa_params p{};
+    int bits = 0;
+    uint32_t filter_cutoff = 0;
+    std::vector<gbsa_ref_randstrobe> rs;
+    std::vector<uint64_t> starts;
+    gbsa_index_info info{};
+
+    uint64_t get_hash(uint64_t pos) const {                   /* index.hpp:83-89 */
+        return pos < rs.size() ? rs[pos].hash : UINT64_MAX;
+    }
+    bool is_filtered(uint64_t pos) const {                    /* index.hpp:91-93 */
+        return get_hash(pos) == get_hash(pos + filter_cutoff);
+    }
+    uint64_t find(uint64_t key) const {                       /* index.hpp:57-81 */
+        const unsigned top = (unsigned)(key >> (64 - bits));
+        uint64_t a = starts[top];
+        const uint64_t b = starts[top + 1];
+        if (a == b) return UINT64_MAX;
+        if (b - a < 4) {
+            for (; a < b; ++a) {
+                if (rs[a].hash == key) return a;
+                if (rs[a].hash > key) return UINT64_MAX;
+            }
+            return UINT64_MAX;
+        }
+        auto it = std::lower_bound(rs.begin() + (long)a, rs.begin() + (long)b, key,
+                                   [](const gbsa_ref_randstrobe& e, uint64_t k) { return e.hash < k; });
+        if (it != rs.end() && it->hash == key) return (uint64_t)(it - rs.begin());
+        return UINT64_MAX;
+    }
+    uint32_t get_count(uint64_t pos) const {                  /* index.hpp:115-147 */
+        const uint64_t key = rs[pos].hash;
+        const unsigned top = (unsigned)(key >> (64 - bits));
+        const uint64_t end = starts[top + 1];
+        if (end - pos < 8) {
+            uint64_t count = 1;
+            for (uint64_t q = pos + 1; q < end; ++q) {
+                if (rs[q].hash == key) ++count;
+                else break;
+            }
+            return (uint32_t)count;
+        }
+        auto it = std::upper_bound(rs.begin() + (long)pos, rs.begin() + (long)end, key,
+                                   [](uint64_t k, const gbsa_ref_randstrobe& e) { return k < e.hash; });
+        return (uint32_t)((it - rs.begin()) - (long)pos);
+    }
+};
+
+/* index.cu:28-41 (count_randstrobes), 280-311 (assign_randstrobes with the
+ * RandstrobeGenerator of randstrobes.cu:161-190), 143-244 (populate). */
+void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+              uint32_t n_contigs, float f) {
+    const gbsa_params& p = idx.p;
+    std::vector<std::vector<Syncmer>> sms(n_contigs);
+    std::vector<uint64_t> counts(n_contigs), offs(n_contigs);
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < n_contigs; ++c) {
+        canonical_syncmers(p, seqs + offsets[c], lengths[c], sms[c]);
+        const uint64_t n = sms[c].size();
+        counts[c] = n < p.w_min ? 0 : n - p.w_min;
+        offs[c] = total;
+        total += counts[c];
+    }
+    idx.info.tot_strobemer_count = total;
+    idx.rs.assign(total, gbsa_ref_randstrobe{0, 0, 0});
+    for (uint32_t c = 0; c < n_contigs; ++c) {
+        if (lengths[c] < p.w_max) continue;               /* index.cu:282-284 */
+        uint64_t o = offs[c];
+        const auto& v = sms[c];
+        for (unsigned j = 0; j + p.w_min < v.size(); ++j) {
+            const Strobe r = randstrobe_at(p, v, j);
+            uint32_t packed = (uint32_t)((uint64_t)c << 8);
+            packed = packed + (r.s2 - r.s1);
+            idx.rs[o++] = gbsa_ref_randstrobe{r.hash, r.s1, packed};
+        }
+    }
+    std::sort(idx.rs.begin(), idx.rs.end(), [](const gbsa_ref_randstrobe& a, const gbsa_ref_randstrobe& b) {
+        if (a.hash != b.hash) return a.hash < b.hash;
+        if (a.position != b.position) return a.position < b.position;
+        return a.packed < b.packed;
+    });
+
+    /* bucket table and repetition statistics, index.cu:176-243 */
+    const int bits = idx.bits;
+    const uint64_t nb = (1ULL << bits) + 1;
+    auto& st = idx.starts;
+    st.clear();
+    st.reserve(nb);
+    std::vector<uint64_t> rep_counts;
+    uint64_t once = 0, high = 0, mid = 0;
+    uint64_t unique = idx.rs.empty() ? 0 : 1;
+    uint64_t prev = idx.rs.empty() ? 0 : idx.rs[0].hash;
+    unsigned run = 0;
+    auto close_run = [&](unsigned cnt) {
+        if (cnt == 1) {
+            ++once;
+        } else {
+            if (cnt > 100) ++high;
+            else ++mid;
+            rep_counts.push_back(cnt);
+        }
+    };
+    for (uint64_t pos = 0; pos < idx.rs.size(); ++pos) {
+        const uint64_t cur = idx.rs[pos].hash;
+        if (cur == prev) {
+            ++run;
+            continue;
+        }
+        ++unique;
+        close_run(run);
+        run = 1;
+        const unsigned top = (unsigned)(cur >> (64 - bits));
+        /* Buckets up to `top` start here; bucket top(hash[0]) and the empty ones
+         * before it therefore start at the second distinct hash (index.cu:207-210). */
+        while (st.size() <= top) st.push_back(pos);
+        prev = cur;
+    }
+    close_run(run);
+    while (st.size() < nb) st.push_back(idx.rs.size());
+
+    std::sort(rep_counts.begin(), rep_counts.end(), [](uint64_t a, uint64_t b) { return a > b; });
+    const uint64_t index_cutoff = (uint64_t)((float)unique * f);   /* float product, index.cu:232 */
+    unsigned fc;
+    if (!rep_counts.empty()) {
+        fc = (unsigned)(index_cutoff < rep_counts.size() ? rep_counts[index_cutoff] : rep_counts.back());
+        fc = std::max(30U, fc);
+        fc = std::min(100U, fc);
+    } else {
+        fc = 30;
+    }
+    idx.filter_cutoff = fc;
+    idx.info.tot_occur_once = once;
+    idx.info.tot_high_ab = high;
+    idx.info.tot_mid_ab = mid;
+    idx.info.index_cutoff = index_cutoff;
+    idx.info.distinct_strobemers = unique;
+}
+
+/* ---- nam.cu ------------------------------------------------------------------ */
+struct Hit {
+    int qs, qe, rs, re;
+};
+inline bool hit_less(const Hit& a, const Hit& b) {            /* my_struct.hpp:100-103 */
+    if (a.qs == b.qs) return a.rs < b.rs;
+    return a.qs < b.qs;
+}
+using HitsPerRef = std::unordered_map<unsigned, std::vector<Hit>>;
+
+/* nam.cu:45-62 : add_to_hits_per_ref, the running-minimum length-difference filter */
+template <class Fn>
+void walk_run(const IndexCpu& idx, int qs, int qe, uint64_t pos, Fn&& emit) {
+    int min_diff = INT_MAX;
+    const uint64_t key = idx.get_hash(pos);
+    for (; pos < idx.rs.size() && idx.rs[pos].hash == key; ++pos) {
+        const int rs = (int)idx.rs[pos].position;
+        const int re = rs + (int)(idx.rs[pos].packed & 0xFF) + idx.p.k;
+        const int diff = std::abs((qe - qs) - (re - rs));
+        if (diff <= min_diff) {
+            emit((unsigned)(idx.rs[pos].packed >> 8), Hit{qs, qe, rs, re});
+            min_diff = diff;
+        }
+    }
+}
+
+void add_to_hits_per_ref(HitsPerRef& hpr, int qs, int qe, const IndexCpu& idx, uint64_t pos) {
+    walk_run(idx, qs, qe, pos, [&](unsigned ref, const Hit& h) { hpr[ref].push_back(h); });
+}
+
+inline float nam_score(const gbsa_nam& n) {                   /* nam.cu:454-463 */
+    const int qspan = n.query_end - n.query_start;
+    const int rspan = n.ref_end - n.ref_start;
+    const int mx = std::max(qspan, rspan), mn = std::min(qspan, rspan);
+    return (2 * mn - mx) > 0 ? (float)(n.n_hits * (2 * mn - mx)) : 1.0f;
+}
+
+gbsa_nam new_nam(const Hit& h, unsigned ref, bool rc) {
+    gbsa_nam n{};
+    n.query_start = h.qs;
+    n.query_end = h.qe;
+    n.ref_start = h.rs;
+    n.ref_end = h.re;
+    n.ref_id = (int)ref;
+    n.query_prev_hit_startpos = h.qs;
+    n.ref_prev_hit_startpos = h.rs;
+    n.n_hits = 1;
+    n.is_rc = rc ? 1 : 0;
+    return n;
+}
+
+void flush_passed(std::vector<gbsa_nam>& open, int qs, std::vector<gbsa_nam>& nams) {
+    for (auto& n : open) {
+        if (n.query_end < qs) {
+            n.score = nam_score(n);
+            n.nam_id = (int)nams.size();
+            nams.push_back(n);
+        }
+    }
+    open.erase(std::remove_if(open.begin(), open.end(), [qs](const gbsa_nam& n) { return n.query_end < qs; }),
+               open.end());
+}
+
+void flush_all(std::vector<gbsa_nam>& open, std::vector<gbsa_nam>& nams) {
+    for (auto& n : open) {
+        n.score = nam_score(n);
+        n.nam_id = (int)nams.size();
+        nams.push_back(n);
+    }
+}
+
+/* nam.cu:347-513 : merge_hits_into_nams (hit-major) */
+void merge_hit_major(std::vector<Hit>& hits, unsigned ref, int k, bool sort, bool rc, std::vector<gbsa_nam>& nams) {
+    if (sort) std::sort(hits.begin(), hits.end(), hit_less);
+    std::vector<gbsa_nam> open;
+    unsigned prev_q_start = 0;
+    for (const Hit& h : hits) {
+        bool added = false;
+        for (auto& o : open) {
+            if (o.query_prev_hit_startpos < h.qs && h.qs <= o.query_end &&
+                o.ref_prev_hit_startpos < h.rs && h.rs <= o.ref_end) {
+                if (h.qe > o.query_end && h.re > o.ref_end) {
+                    o.query_end = h.qe;
+                    o.ref_end = h.re;
+                    o.query_prev_hit_startpos = h.qs;
+                    o.ref_prev_hit_startpos = h.rs;
+                    ++o.n_hits;
+                    added = true;
+                    break;
+                } else if (h.qe <= o.query_end && h.re <= o.ref_end) {
+                    o.query_prev_hit_startpos = h.qs;
+                    o.ref_prev_hit_startpos = h.rs;
+                    ++o.n_hits;
+                    added = true;
+                    break;
+                }
+            }
+        }
+        if (!added) open.push_back(new_nam(h, ref, rc));
+        if ((unsigned)h.qs > prev_q_start + (unsigned)k) {
+            flush_passed(open, h.qs, nams);
+            prev_q_start = (unsigned)h.qs;
+        }
+    }
+    flush_all(open, nams);
+}
+
+/* nam.cu:94-343 : merge_hits_into_nams_fast (NAM-major, one query_start group at a time) */
+void merge_nam_major(std::vector<Hit>& hits, unsigned ref, int k, bool sort, bool rc, std::vector<gbsa_nam>& nams) {
+    if (sort) std::sort(hits.begin(), hits.end(), hit_less);
+    std::vector<gbsa_nam> open;
+    unsigned prev_q_start = 0;
+    std::vector<char> added;
+    for (size_t i = 0; i < hits.size();) {
+        const size_t g0 = i;
+        size_t g1 = i + 1;
+        while (g1 < hits.size() && hits[g1].qs == hits[i].qs) ++g1;
+        i = g1;
+        const size_t gn = g1 - g0;
+        added.assign(gn, 0);
+        const int qs = hits[g0].qs;
+        size_t done = 0;
+        std::sort(hits.begin() + (long)g0, hits.begin() + (long)g1, hit_less);
+        for (auto& o : open) {
+            auto lb = [&](int value) {
+                return (size_t)(std::lower_bound(hits.begin() + (long)g0, hits.begin() + (long)g1, value,
+                                                 [](const Hit& h, int v) { return h.rs < v; }) -
+                                hits.begin());
+            };
+            const size_t lo = lb(o.ref_prev_hit_startpos + 1);
+            const size_t hi = lb(o.ref_end + 1);
+            for (size_t j = lo; j < hi; ++j) {
+                if (added[j - g0]) continue;
+                if (qs <= o.query_end) {
+                    const Hit& h = hits[j];
+                    if (o.ref_prev_hit_startpos < h.rs && h.rs <= o.ref_end) {
+                        if (h.qe > o.query_end && h.re > o.ref_end) {
+                            o.query_end = h.qe;
+                            o.ref_end = h.re;
+                            o.query_prev_hit_startpos = h.qs;
+                            o.ref_prev_hit_startpos = h.rs;
+                            ++o.n_hits;
+                            added[j - g0] = 1;
+                            ++done;
+                            break;
+                        } else if (h.qe <= o.query_end && h.re <= o.ref_end) {
+                            o.query_prev_hit_startpos = h.qs;
+                            o.ref_prev_hit_startpos = h.rs;
+                            ++o.n_hits;
+                            added[j - g0] = 1;
+                            ++done;
+                            break;
+                        }
+                    }
+                }
+            }
+            if (done == gn) break;
+        }
+        for (size_t j = 0; j < gn; ++j) {
+            if (!added[j]) open.push_back(new_nam(hits[g0 + j], ref, rc));
+        }
+        if ((unsigned)qs > prev_q_start + (unsigned)k) {
+            flush_passed(open, qs, nams);
+            prev_q_start = (unsigned)qs;
+        }
+    }
+    flush_all(open, nams);
+}
+
+/* nam.cu:748-905 : find_nams (untimed variant; same arithmetic as :553-747) */
+std::vector<gbsa_nam> find_nams(const IndexCpu& idx, const gbsa_query_randstrobe* q, size_t nq, float* frac) {
+    HitsPerRef hpr[2];
+    int nr_good = 0, total = 0;
+    for (size_t i = 0; i < nq; ++i) {
+        const uint64_t pos = idx.find(q[i].hash);
+        if (pos == UINT64_MAX) continue;
+        ++total;
+        if (idx.is_filtered(pos)) continue;
+        ++nr_good;
+        add_to_hits_per_ref(hpr[q[i].is_reverse ? 1 : 0], (int)q[i].start, (int)q[i].end, idx, pos);
+    }
+    *frac = total > 0 ? ((float)nr_good) / ((float)total) : 1.0f;
+    std::vector<gbsa_nam> nams;
+    for (int rc = 0; rc < 2; ++rc) {
+        for (auto& kv : hpr[rc]) merge_hit_major(kv.second, kv.first, idx.p.k, true, rc == 1, nams);
+    }
+    return nams;
+}
+
+/* nam.cu:927-985 : find_nams_rescue (pre_sort variant) */
+struct RescueHit {
+    uint64_t position;
+    unsigned count, qs, qe;
+};
+std::vector<gbsa_nam> find_nams_rescue(const IndexCpu& idx, const gbsa_query_randstrobe* q, size_t nq,
+                                       unsigned rescue_cutoff, unsigned count_cap) {
+    std::vector<RescueHit> by_dir[2];
+    for (size_t i = 0; i < nq; ++i) {
+        const uint64_t pos = idx.find(q[i].hash);
+        if (pos == UINT64_MAX) continue;
+        by_dir[q[i].is_reverse ? 1 : 0].push_back(RescueHit{pos, idx.get_count(pos), q[i].start, q[i].end});
+    }
+    HitsPerRef hpr[2];
+    for (int d = 0; d < 2; ++d) {
+        auto& v = by_dir[d];
+        std::sort(v.begin(), v.end(), [](const RescueHit& a, const RescueHit& b) {   /* cmp1, nam.cu:909-912 */
+            if (a.count != b.count) return a.count < b.count;
+            if (a.qs != b.qs) return a.qs < b.qs;
+            return a.qe < b.qe;
+        });
+        std::vector<RescueHit> taken;
+        int cnt = 0;
+        for (const auto& rh : v) {
+            if ((rh.count > rescue_cutoff && cnt >= 5) || rh.count > count_cap) break;
+            taken.push_back(rh);
+            ++cnt;
+        }
+        std::sort(taken.begin(), taken.end(), [](const RescueHit& a, const RescueHit& b) { return a.qs < b.qs; });
+        for (const auto& rh : taken) add_to_hits_per_ref(hpr[d], (int)rh.qs, (int)rh.qe, idx, rh.position);
+    }
+    std::vector<gbsa_nam> nams;
+    for (int rc = 0; rc < 2; ++rc) {
+        for (auto& kv : hpr[rc]) merge_nam_major(kv.second, kv.first, idx.p.k, false, rc == 1, nams);
+    }
+    return nams;
+}
+
+/* ---- NAM orders ------------------------------------------------------------- */
+inline int score_key(const gbsa_nam& n) { return (int)n.score; }   /* integer valued, < 2^24 */
+
+bool less_score(const gbsa_nam& a, const gbsa_nam& b) {
+    if (a.score != b.score) return a.score > b.score;
+    if (a.is_rc != b.is_rc) return a.is_rc < b.is_rc;
+    if (a.ref_id != b.ref_id) return a.ref_id < b.ref_id;
+    if (a.query_start != b.query_start) return a.query_start < b.query_start;
+    if (a.query_end != b.query_end) return a.query_end < b.query_end;
+    if (a.ref_start != b.ref_start) return a.ref_start < b.ref_start;
+    if (a.ref_end != b.ref_end) return a.ref_end < b.ref_end;
+    return a.n_hits > b.n_hits;
+}
+
+/* my_struct.hpp:78-92 (mate 2) and main.cu:2271-2289 (mate 1), ties broken by the
+ * remaining compared fields so that the order is total. */
+bool less_ref(const gbsa_nam& a, const gbsa_nam& b, bool with_diag) {
+    if (a.is_rc != b.is_rc) return a.is_rc < b.is_rc;
+    if (a.ref_id != b.ref_id) return a.ref_id < b.ref_id;
+    if (with_diag) {
+        const int d1 = std::max(0, a.ref_start - a.query_start);
+        const int d2 = std::max(0, b.ref_start - b.query_start);
+        if (d1 != d2) return d1 < d2;
+    }
+    if (a.n_hits != b.n_hits) return a.n_hits > b.n_hits;
+    if (a.query_end != b.query_end) return a.query_end < b.query_end;
+    if (a.query_start != b.query_start) return a.query_start < b.query_start;
+    if (a.ref_end != b.ref_end) return a.ref_end < b.ref_end;
+    if (a.ref_start != b.ref_start) return a.ref_start < b.ref_start;
+    return score_key(a) > score_key(b);
+}
+
+void sort_nams(gbsa_nam* v, size_t n, int mode) {
+    if (mode == GBSA_SORT_REF_MATE2) {
+        std::sort(v, v + n, [](const gbsa_nam& a, const gbsa_nam& b) { return less_ref(a, b, true); });
+    } else if (mode == GBSA_SORT_REF_MATE1) {
+        std::sort(v, v + n, [](const gbsa_nam& a, const gbsa_nam& b) { return less_ref(a, b, false); });
+    } else {
+        std::sort(v, v + n, less_score);
+    }
+}
+
+/* Rescue trigger and cutoff: step2/main.cu:3211 (nonrepetitive_fraction < 0.7, a
+ * double comparison, or no hits) and step2/main.cu:4204 (R * filter_cutoff). */
+unsigned rescue_cutoff_for(const IndexCpu& idx, int rescue_level) {
+    return rescue_level < 100 ? (unsigned)(rescue_level * (int)idx.filter_cutoff) : 100u;
+}
+
+struct ReadResult {
+    std::vector<gbsa_nam> nams;
+    float frac = 1.0f;
+    bool rescued = false;
+};
+
+void map_one(const IndexCpu& idx, const gbsa_map_options& opt, const char* seq, size_t len,
+             std::vector<gbsa_query_randstrobe>& qbuf, ReadResult& r) {
+    randstrobes_query(idx.p, seq, len, qbuf);
+    r.nams = find_nams(idx, qbuf.data(), qbuf.size(), &r.frac);
+    r.rescued = false;
+    if (opt.rescue_level > 1 && (r.nams.empty() || (double)r.frac < 0.7)) {
+        r.nams = find_nams_rescue(idx, qbuf.data(), qbuf.size(), rescue_cutoff_for(idx, opt.rescue_level),
+                                  opt.rescue_count_cap);
+        r.rescued = true;
+    }
+    sort_nams(r.nams.data(), r.nams.size(), opt.sort_mode);
+}
+
+template <class Fn>
+void parallel_for(uint32_t n, int n_threads, Fn&& fn) {
+    if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (n_threads == 1 || n < 64) {
+        for (uint32_t i = 0; i < n; ++i) fn(i, 0);
+        return;
+    }
+    std::atomic<uint32_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t) {
+        th.emplace_back([&, t]() {
+            for (;;) {
+                const uint32_t a = next.fetch_add(256);
+                if (a >= n) break;
+                const uint32_t b = std::min(n, a + 256);
+                for (uint32_t i = a; i < b; ++i) fn(i, t);
+            }
+        });
+    }
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+struct oracle_index {
+    IndexCpu idx;
+};
+
+extern "C" {
+
+uint64_t oracle_xxh64(uint64_t x) { return xxh64(x); }
+
+/* indexparameters.cpp:137-182 */
+int oracle_params_from_read_length(int read_length, int k, int s, int l, int u, int c, int max_seed_len,
+                                   gbsa_params* out) {
+    struct Profile { int r, thr, k, s_off, l, u; };
+    static const Profile profiles[] = {
+        {50, 90, 20, -4, -3, 2},   {100, 110, 20, -4, -2, 2}, {125, 135, 20, -4, -1, 4},
+        {150, 175, 20, -4, 1, 7},  {250, 275, 20, -4, 4, 13}, {300, 375, 22, -4, 2, 12},
+        {400, INT_MAX, 23, -6, 2, 12},
+    };
+    uint64_t canonical = 50;
+    for (const auto& pr : profiles) {
+        if (read_length <= pr.thr) {
+            if (k == GBSA_DEFAULT) k = pr.k;
+            if (s == GBSA_DEFAULT) s = k + pr.s_off;
+            if (l == GBSA_DEFAULT) l = pr.l;
+            if (u == GBSA_DEFAULT) u = pr.u;
+            canonical = (uint64_t)pr.r;
+            break;
+        }
+    }
+    int max_dist;
+    if (max_seed_len == GBSA_DEFAULT) {
+        max_dist = std::max((int)canonical - 70, k);
+        max_dist = std::min(255, max_dist);
+    } else {
+        max_dist = max_seed_len - k;
+    }
+    const int q = (int)(std::pow(2, c == GBSA_DEFAULT ? 8 : c) - 1);
+    return make_params(canonical, k, s, l, u, q, max_dist, out) ? GBSA_OK : GBSA_ERR_PARAM;
+}
+
+int oracle_pick_bits(const gbsa_params* p, uint64_t total_length) { return pick_bits(*p, total_length); }
+
+int64_t oracle_syncmers(const gbsa_params* p, const char* seq, uint64_t len, uint64_t* hashes,
+                        uint64_t* positions, uint64_t cap) {
+    std::vector<Syncmer> v;
+    canonical_syncmers(*p, seq, len, v);
+    const uint64_t n = std::min<uint64_t>(cap, v.size());
+    for (uint64_t i = 0; i < n; ++i) {
+        hashes[i] = v[i].hash;
+        positions[i] = v[i].pos;
+    }
+    return (int64_t)v.size();
+}
+
+int64_t oracle_randstrobes_query(const gbsa_params* p, const char* seq, uint64_t len,
+                                 gbsa_query_randstrobe* out, uint64_t cap) {
+    std::vector<gbsa_query_randstrobe> v;
+    randstrobes_query(*p, seq, len, v);
+    if (v.size() > cap) return -(int64_t)v.size() - 1;
+    if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(gbsa_query_randstrobe));
+    return (int64_t)v.size();
+}
+
+oracle_index* oracle_index_build(const gbsa_params* p, const char* seqs, const uint64_t* offsets,
+                                 const uint64_t* lengths, uint32_t n_contigs, int bits, float f) {
+    auto* h = new oracle_index();
+    h->idx.p = *p;
+    uint64_t total_len = 0;
+    for (uint32_t c = 0; c < n_contigs; ++c) total_len += lengths[c];
+    h->idx.bits = bits == -1 ? pick_bits(*p, total_len) : bits;
+    if (h->idx.bits < 8 || h->idx.bits > 31) {
+        delete h;
+        return nullptr;
+    }
+    populate(h->idx, seqs, offsets, lengths, n_contigs, f);
+    h->idx.info.size = h->idx.rs.size();
+    h->idx.info.bits = h->idx.bits;
+    h->idx.info.filter_cutoff = h->idx.filter_cutoff;
+    return h;
+}
+
+oracle_index* oracle_index_load(const gbsa_params* p, const gbsa_ref_randstrobe* rs, uint64_t n,
+                                const uint64_t* starts, int bits, uint32_t filter_cutoff) {
+    auto* h = new oracle_index();
+    h->idx.p = *p;
+    h->idx.bits = bits;
+    h->idx.filter_cutoff = filter_cutoff;
+    h->idx.rs.assign(rs, rs + n);
+    h->idx.starts.assign(starts, starts + (1ULL << bits) + 1);
+    h->idx.info.size = n;
+    h->idx.info.bits = bits;
+    h->idx.info.filter_cutoff = filter_cutoff;
+    return h;
+}
+
+void oracle_index_free(oracle_index* idx) { delete idx; }
+void oracle_index_info(const oracle_index* idx, gbsa_index_info* out) { *out = idx->idx.info; }
+const gbsa_ref_randstrobe* oracle_index_randstrobes(const oracle_index* idx) { return idx->idx.rs.data(); }
+const uint64_t* oracle_index_starts(const oracle_index* idx) { return idx->idx.starts.data(); }
+
+/* index.cu:73-89 (write) with io.hpp:11-26 and indexparameters.cpp:184-192 */
+int oracle_index_write_sti(const oracle_index* h, const char* path) {
+    std::ofstream os(path, std::ios::binary);
+    if (!os) return GBSA_ERR_INDEX_FILE;
+    auto w32 = [&](int32_t v) { os.write(reinterpret_cast<const char*>(&v), 4); };
+    auto w64 = [&](uint64_t v) { os.write(reinterpret_cast<const char*>(&v), 8); };
+    const IndexCpu& x = h->idx;
+    os.write("STI\1", 4);
+    w32(2);
+    w64(8);
+    const char zeros[8] = {0};
+    os.write(zeros, 8);
+    w32((int32_t)x.filter_cutoff);
+    w32(x.bits);
+    w32(x.p.canonical_read_length);
+    w32(x.p.k);
+    w32(x.p.s);
+    w32(x.p.l);
+    w32(x.p.u);
+    w32((int32_t)x.p.q);
+    w32(x.p.max_dist);
+    w64(x.rs.size());
+    os.write(reinterpret_cast<const char*>(x.rs.data()), (std::streamsize)(x.rs.size() * sizeof(gbsa_ref_randstrobe)));
+    w64(x.starts.size());
+    os.write(reinterpret_cast<const char*>(x.starts.data()), (std::streamsize)(x.starts.size() * 8));
+    return os ? GBSA_OK : GBSA_ERR_INDEX_FILE;
+}
+
+uint64_t oracle_find(const oracle_index* idx, uint64_t hash) { return idx->idx.find(hash); }
+uint32_t oracle_get_count(const oracle_index* idx, uint64_t position) { return idx->idx.get_count(position); }
+int oracle_is_filtered(const oracle_index* idx, uint64_t position) { return idx->idx.is_filtered(position) ? 1 : 0; }
+
+int64_t oracle_find_nams(const oracle_index* idx, const gbsa_query_randstrobe* q, uint64_t nq, gbsa_nam* out,
+                         uint64_t cap, float* frac) {
+    float fr = 1.0f;
+    auto v = find_nams(idx->idx, q, nq, &fr);
+    if (frac) *frac = fr;
+    if (v.size() > cap) return -(int64_t)v.size() - 1;
+    if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(gbsa_nam));
+    return (int64_t)v.size();
+}
+
+int64_t oracle_find_nams_rescue(const oracle_index* idx, const gbsa_query_randstrobe* q, uint64_t nq,
+                                uint32_t rescue_cutoff, uint32_t count_cap, gbsa_nam* out, uint64_t cap) {
+    auto v = find_nams_rescue(idx->idx, q, nq, rescue_cutoff, count_cap);
+    if (v.size() > cap) return -(int64_t)v.size() - 1;
+    if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(gbsa_nam));
+    return (int64_t)v.size();
+}
+
+void oracle_sort_nams(gbsa_nam* nams, uint64_t n, int sort_mode) { sort_nams(nams, n, sort_mode); }
+
+int oracle_map_reads(const oracle_index* h, const gbsa_map_options* opt, const char* seqs, const uint64_t* offsets,
+                     const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity,
+                     uint64_t* nam_offsets, float* frac, uint8_t* rescued, int n_threads) {
+    std::vector<ReadResult> res(n_reads);
+    const int nt = n_threads <= 0 ? (int)std::max(1u, std::thread::hardware_concurrency()) : n_threads;
+    std::vector<std::vector<gbsa_query_randstrobe>> qbufs((size_t)nt);
+    parallel_for(n_reads, nt, [&](uint32_t i, int t) {
+        map_one(h->idx, *opt, seqs + offsets[i], lengths[i], qbufs[(size_t)t], res[i]);
+    });
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n_reads; ++i) {
+        nam_offsets[i] = total;
+        total += res[i].nams.size();
+    }
+    nam_offsets[n_reads] = total;
+    if (frac)
+        for (uint32_t i = 0; i < n_reads; ++i) frac[i] = res[i].frac;
+    if (rescued)
+        for (uint32_t i = 0; i < n_reads; ++i) rescued[i] = res[i].rescued ? 1 : 0;
+    if (total > nam_capacity) return GBSA_ERR_CAPACITY;
+    for (uint32_t i = 0; i < n_reads; ++i) {
+        if (!res[i].nams.empty())
+            std::memcpy(nams + nam_offsets[i], res[i].nams.data(), res[i].nams.size() * sizeof(gbsa_nam));
+    }
+    return GBSA_OK;
+}
+
+/* Roofline numerator.  Per read: ceil(L/4) bytes of 2-bit input; per query randstrobe
+ * 16 B for the bucket bound pair, 16 B per table entry the in-bucket search examines
+ * (entries before the first one whose hash is >= the key, plus that one, capped at
+ * the bucket size), and for a found key 16 B for the filter probe plus, when not
+ * filtered, 16 B per entry of the equal-hash run; 44 B per NAM written.  Work of the
+ * rescue path beyond this is not counted (the figure is a lower bound). */
+int oracle_algorithmic_bytes(const oracle_index* h, const gbsa_map_options* opt, const char* seqs,
+                             const uint64_t* offsets, const uint32_t* lengths, uint32_t n_reads,
+                             uint64_t* bytes_out, int n_threads) {
+    const IndexCpu& idx = h->idx;
+    const int nt = n_threads <= 0 ? (int)std::max(1u, std::thread::hardware_concurrency()) : n_threads;
+    std::vector<uint64_t> per(n_reads, 0);
+    std::vector<std::vector<gbsa_query_randstrobe>> qbufs((size_t)nt);
+    parallel_for(n_reads, nt, [&](uint32_t i, int t) {
+        auto& q = qbufs[(size_t)t];
+        uint64_t b = (lengths[i] + 3) / 4;
+        randstrobes_query(idx.p, seqs + offsets[i], lengths[i], q);
+        for (const auto& qr : q) {
+            b += 16;
+            const unsigned top = (unsigned)(qr.hash >> (64 - idx.bits));
+            const uint64_t a = idx.starts[top], e = idx.starts[top + 1];
+            uint64_t ex = 0;
+            for (uint64_t x = a; x < e; ++x) {
+                ++ex;
+                if (idx.rs[x].hash >= qr.hash) break;
+            }
+            b += 16 * ex;
+            const uint64_t pos = idx.find(qr.hash);
+            if (pos == UINT64_MAX) continue;
+            b += 16;
+            if (idx.is_filtered(pos)) continue;
+            uint64_t run = 0;
+            for (uint64_t x = pos; x < idx.rs.size() && idx.rs[x].hash == qr.hash; ++x) ++run;
+            b += 16 * run;
+        }
+        ReadResult r;
+        map_one(idx, *opt, seqs + offsets[i], lengths[i], q, r);
+        b += 44 * (uint64_t)r.nams.size();
+        per[i] = b;
+    });
+    uint64_t tot = 0;
+    for (auto x : per) tot += x;
+    *bytes_out = tot;
+    return GBSA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+"""ctypes wrapper of oracle/liboracle.so — TEST INFRASTRUCTURE ONLY.
+
+The CPU restatement of the reference path that the CUDA path is checked against.
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg only.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from gpu_index_test_gb300 import abi
+from gpu_index_test_gb300._build_paths import ORACLE_SO
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            raise RuntimeError(f"oracle library missing: {ORACLE_SO} (run __graft_entry__.build())")
+        L = C.CDLL(ORACLE_SO)
+        P = C.POINTER(abi.Params)
+        L.oracle_xxh64.restype = C.c_uint64
+        L.oracle_xxh64.argtypes = [C.c_uint64]
+        L.oracle_params_from_read_length.restype = C.c_int
+        L.oracle_params_from_read_length.argtypes = [C.c_int] * 7 + [P]
+        L.oracle_pick_bits.restype = C.c_int
+        L.oracle_pick_bits.argtypes = [P, C.c_uint64]
+        L.oracle_syncmers.restype = C.c_int64
+        L.oracle_syncmers.argtypes = [P, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64]
+        L.oracle_randstrobes_query.restype = C.c_int64
+        L.oracle_randstrobes_query.argtypes = [P, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+        L.oracle_index_build.restype = C.c_void_p
+        L.oracle_index_build.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_float]
+        L.oracle_index_load.restype = C.c_void_p
+        L.oracle_index_load.argtypes = [P, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int, C.c_uint32]
+        L.oracle_index_free.restype = None
+        L.oracle_index_free.argtypes = [C.c_void_p]
+        L.oracle_index_info.restype = None
+        L.oracle_index_info.argtypes = [C.c_void_p, C.POINTER(abi.IndexInfo)]
+        L.oracle_index_randstrobes.restype = C.c_void_p
+        L.oracle_index_randstrobes.argtypes = [C.c_void_p]
+        L.oracle_index_starts.restype = C.c_void_p
+        L.oracle_index_starts.argtypes = [C.c_void_p]
+        L.oracle_index_write_sti.restype = C.c_int
+        L.oracle_index_write_sti.argtypes = [C.c_void_p, C.c_char_p]
+        L.oracle_find.restype = C.c_uint64
+        L.oracle_find.argtypes = [C.c_void_p, C.c_uint64]
+        L.oracle_get_count.restype = C.c_uint32
+        L.oracle_get_count.argtypes = [C.c_void_p, C.c_uint64]
+        L.oracle_is_filtered.restype = C.c_int
+        L.oracle_is_filtered.argtypes = [C.c_void_p, C.c_uint64]
+        L.oracle_find_nams.restype = C.c_int64
+        L.oracle_find_nams.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.POINTER(C.c_float)]
+        L.oracle_find_nams_rescue.restype = C.c_int64
+        L.oracle_find_nams_rescue.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64]
+        L.oracle_sort_nams.restype = None
+        L.oracle_sort_nams.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
+        L.oracle_map_reads.restype = C.c_int
+        L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_algorithmic_bytes.restype = C.c_int
+        L.oracle_algorithmic_bytes.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64), C.c_int]
+        _lib = L
+    return _lib
+
+
+def xxh64(x):
+    return lib().oracle_xxh64(int(x))
+
+
+def params_from_read_length(r, k=abi.GBSA_DEFAULT, s=abi.GBSA_DEFAULT, l=abi.GBSA_DEFAULT, u=abi.GBSA_DEFAULT,
+                            c=abi.GBSA_DEFAULT, max_seed_len=abi.GBSA_DEFAULT):
+    p = abi.Params()
+    rc = lib().oracle_params_from_read_length(r, k, s, l, u, c, max_seed_len, C.byref(p))
+    if rc != abi.GBSA_OK:
+        raise ValueError("bad parameters")
+    return p
+
+
+def syncmers(p, seq: bytes):
+    buf = np.frombuffer(seq, np.uint8) if len(seq) else np.zeros(1, np.uint8)
+    cap = max(1, len(seq))
+    h = np.zeros(cap, np.uint64)
+    pos = np.zeros(cap, np.uint64)
+    n = lib().oracle_syncmers(C.byref(p), buf.ctypes.data, len(seq), h.ctypes.data, pos.ctypes.data, cap)
+    return h[:n].copy(), pos[:n].copy()
+
+
+def randstrobes_query(p, seq: bytes):
+    buf = np.frombuffer(seq, np.uint8) if len(seq) else np.zeros(1, np.uint8)
+    cap = 2 * max(1, len(seq)) + 2
+    out = np.zeros(cap, abi.QUERY_RANDSTROBE)
+    n = lib().oracle_randstrobes_query(C.byref(p), buf.ctypes.data, len(seq), out.ctypes.data, cap)
+    assert n >= 0
+    return out[:n].copy()
+
+
+class Index:
+    def __init__(self, handle, p):
+        self.h = handle
+        self.params = p
+
+    @classmethod
+    def build(cls, p, genome, bits=-1, f=0.0002):
+        h = lib().oracle_index_build(C.byref(p), genome.seq.ctypes.data, genome.offsets.ctypes.data,
+                                     genome.lengths.ctypes.data, len(genome.lengths), bits, f)
+        if not h:
+            raise ValueError("bad bits")
+        return cls(h, p)
+
+    @classmethod
+    def load(cls, p, randstrobes, starts, bits, filter_cutoff):
+        randstrobes = np.ascontiguousarray(randstrobes)
+        starts = np.ascontiguousarray(starts, np.uint64)
+        h = lib().oracle_index_load(C.byref(p), randstrobes.ctypes.data, len(randstrobes), starts.ctypes.data,
+                                    bits, filter_cutoff)
+        return cls(h, p)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_index_free(self.h)
+            self.h = None
+
+    def info(self):
+        i = abi.IndexInfo()
+        lib().oracle_index_info(self.h, C.byref(i))
+        return i
+
+    def randstrobes(self):
+        i = self.info()
+        if i.size == 0:
+            return np.zeros(0, abi.REF_RANDSTROBE)
+        a = (C.c_char * (16 * i.size)).from_address(lib().oracle_index_randstrobes(self.h))
+        return np.frombuffer(a, abi.REF_RANDSTROBE).copy()
+
+    def starts(self):
+        i = self.info()
+        n = (1 << i.bits) + 1
+        a = (C.c_char * (8 * n)).from_address(lib().oracle_index_starts(self.h))
+        return np.frombuffer(a, np.uint64).copy()
+
+    def write_sti(self, path):
+        assert lib().oracle_index_write_sti(self.h, path.encode()) == 0
+
+    def find(self, h):
+        return lib().oracle_find(self.h, int(h))
+
+    def get_count(self, pos):
+        return lib().oracle_get_count(self.h, int(pos))
+
+    def is_filtered(self, pos):
+        return bool(lib().oracle_is_filtered(self.h, int(pos)))
+
+    def find_nams(self, queries):
+        q = np.ascontiguousarray(queries)
+        cap = 64 + 200 * len(q)
+        out = np.zeros(cap, abi.NAM)
+        fr = C.c_float()
+        n = lib().oracle_find_nams(self.h, q.ctypes.data if len(q) else None, len(q), out.ctypes.data, cap, C.byref(fr))
+        assert n >= 0
+        return out[:n].copy(), fr.value
+
+    def find_nams_rescue(self, queries, rescue_cutoff, count_cap=1000):
+        q = np.ascontiguousarray(queries)
+        cap = 64 + 2000 * len(q)
+        out = np.zeros(cap, abi.NAM)
+        n = lib().oracle_find_nams_rescue(self.h, q.ctypes.data if len(q) else None, len(q), rescue_cutoff,
+                                          count_cap, out.ctypes.data, cap)
+        assert n >= 0
+        return out[:n].copy()
+
+    def map_reads(self, reads, opt=None, n_threads=0, capacity=None):
+        opt = opt or abi.map_options()
+        n = reads.n
+        cap = capacity or max(1024, 64 * n)
+        while True:
+            nams = np.zeros(cap, abi.NAM)
+            offs = np.zeros(n + 1, np.uint64)
+            frac = np.zeros(n, np.float32)
+            resc = np.zeros(n, np.uint8)
+            rc = lib().oracle_map_reads(self.h, C.byref(opt), reads.seq.ctypes.data, reads.offsets.ctypes.data,
+                                        reads.lengths.ctypes.data, n, nams.ctypes.data, cap, offs.ctypes.data,
+                                        frac.ctypes.data, resc.ctypes.data, n_threads)
+            if rc == abi.GBSA_ERR_CAPACITY:
+                cap = int(offs[-1]) + 16
+                continue
+            assert rc == 0
+            return nams[: int(offs[-1])], offs, frac, resc
+
+    def algorithmic_bytes(self, reads, opt=None, n_threads=0):
+        opt = opt or abi.map_options()
+        out = C.c_uint64()
+        lib().oracle_algorithmic_bytes(self.h, C.byref(opt), reads.seq.ctypes.data, reads.offsets.ctypes.data,
+                                       reads.lengths.ctypes.data, reads.n, C.byref(out), n_threads)
+        return out.value
+
+
+def sort_nams(nams, mode=abi.GBSA_SORT_SCORE):
+    a = np.ascontiguousarray(nams).copy()
+    if len(a):
+        lib().oracle_sort_nams(a.ctypes.data, len(a), mode)
+    return a

@@ -1,0 +1,176 @@
+"""CUDA path against the oracle and the reference's golden outputs (GB300 only).
+
+Every comparison is bit-exact: randstrobe hashes and coordinates, index contents
+and order, bucket table, find / get_count results, nonrepetitive_fraction, the
+rescue decision, and the NAM records (ref_id, query/ref start/end, n_hits, score,
+is_rc) in the defined order.
+"""
+import hashlib
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from golden_cases import CASE_NAMES, Case, nams_equal
+from gpu_index_test_gb300 import abi, native, synth
+from oracle import oracle_py
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=CASE_NAMES)
+def gcase(request):
+    c = Case(request.param)
+    p = native.params_from_read_length(c.read_length_param)
+    idx = native.Index.build(p, c.genome)
+    return c, p, idx
+
+
+def test_index_build_matches_golden(gcase):
+    c, p, idx = gcase
+    info = idx.info()
+    assert (info.bits, info.filter_cutoff, info.size) == (c.bits, c.filter_cutoff, c.index_size)
+    rs, st = idx.export()
+    h = hashlib.sha256()
+    h.update(rs.tobytes())
+    h.update(st.tobytes())
+    assert h.hexdigest() == c.index_sha256
+
+
+def test_index_stats_match_oracle(gcase):
+    c, p, idx = gcase
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(c.read_length_param), c.genome)
+    a, b = idx.info(), o.info()
+    for f in ("size", "bits", "filter_cutoff", "tot_strobemer_count", "tot_occur_once", "tot_high_ab", "tot_mid_ab",
+              "index_cutoff", "distinct_strobemers"):
+        assert getattr(a, f) == getattr(b, f), f
+
+
+def test_randstrobes_match_reference(gcase):
+    c, p, _ = gcase
+    q, offs = native.randstrobes_query(p, c.reads)
+    assert (offs == c.ref_query_offsets).all()
+    for f in ("hash", "start", "end", "is_reverse"):
+        assert (q[f] == c.ref_queries[f]).all(), f
+
+
+def test_find_and_count_match_oracle(gcase):
+    c, p, idx = gcase
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(c.read_length_param), c.genome)
+    rs, _ = idx.export()
+    rng = np.random.default_rng(3)
+    keys = np.concatenate([rs["hash"][:: max(1, len(rs) // 5000)], rng.integers(0, 2**63, 3000, dtype=np.uint64),
+                           c.ref_queries["hash"][:5000], rs["hash"][:3]])
+    got = idx.find(keys)
+    exp = np.array([o.find(int(k)) for k in keys], np.uint64)
+    assert (got == exp).all()
+    found = got[got != np.uint64(2**64 - 1)]
+    cnt = idx.get_count(found)
+    assert (cnt == np.array([o.get_count(int(x)) for x in found], np.uint32)).all()
+
+
+def test_nams_match_reference(gcase):
+    c, p, idx = gcase
+    m = native.Mapper(idx, abi.map_options(rescue_level=c.rescue_level))
+    nams, offs, frac, resc = m.map_reads(c.reads)
+    assert (frac == c.ref_frac).all()
+    assert (resc == c.ref_rescued).all()
+    assert (offs == c.ref_nam_offsets).all()
+    bad = [i for i in range(c.reads.n)
+           if not nams_equal(nams[int(offs[i]):int(offs[i + 1])],
+                             c.ref_nams[int(c.ref_nam_offsets[i]):int(c.ref_nam_offsets[i + 1])])]
+    assert not bad, bad[:10]
+
+
+def test_find_nams_entry_points_match_oracle(gcase):
+    c, p, idx = gcase
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(c.read_length_param), c.genome)
+    m = native.Mapper(idx)
+    q, qoff = c.ref_queries, c.ref_query_offsets
+    full = np.zeros(len(q), abi.QUERY_RANDSTROBE)
+    for f in ("hash", "start", "end", "is_reverse"):
+        full[f] = q[f]
+    nams, offs, frac = m.find_nams(full, qoff)
+    cutoff = 2 * idx.info().filter_cutoff
+    rn, roffs, _ = m.find_nams(full, qoff, rescue=True, rescue_cutoff=cutoff)
+    for i in range(0, c.reads.n, 3):
+        qi = full[int(qoff[i]):int(qoff[i + 1])]
+        on, ofr = o.find_nams(qi)
+        assert ofr == frac[i]
+        assert nams_equal(nams[int(offs[i]):int(offs[i + 1])], oracle_py.sort_nams(on)), i
+        orr = o.find_nams_rescue(qi, cutoff)
+        assert nams_equal(rn[int(roffs[i]):int(roffs[i + 1])], oracle_py.sort_nams(orr)), i
+
+
+def test_sti_round_trip(gcase):
+    c, p, idx = gcase
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "x.sti")
+        idx.write_sti(path)
+        assert hashlib.sha256(open(path, "rb").read()).hexdigest() == c.sti_sha256
+        back = native.Index.read_sti(path, p)
+        a, b = idx.export(), back.export()
+        assert (a[0] == b[0]).all() and (a[1] == b[1]).all()
+        assert back.info().filter_cutoff == idx.info().filter_cutoff
+        bad = native.params_from_read_length(250)
+        with pytest.raises(native.GbsaError) as e:
+            native.Index.read_sti(path, bad)
+        assert e.value.code == abi.GBSA_ERR_INDEX_FILE
+
+
+@pytest.mark.parametrize("mode", [abi.GBSA_SORT_REF_MATE2, abi.GBSA_SORT_REF_MATE1])
+def test_reference_sort_modes(gcase, mode):
+    c, p, idx = gcase
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(c.read_length_param), c.genome)
+    opt = abi.map_options(rescue_level=2, sort_mode=mode)
+    sub = c.reads.subset(np.arange(0, c.reads.n, 4))
+    a = native.Mapper(idx, opt).map_reads(sub)
+    b = o.map_reads(sub, opt, n_threads=4)
+    assert (a[1] == b[1]).all()
+    assert nams_equal(a[0], b[0])
+
+
+def test_rescue_cap_100(gcase):
+    c, p, idx = gcase
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(c.read_length_param), c.genome)
+    opt = abi.map_options(rescue_level=2, rescue_count_cap=100)
+    rescued = np.nonzero(c.ref_rescued)[0]
+    sub = c.reads.subset(rescued if len(rescued) else np.arange(10))
+    a = native.Mapper(idx, opt).map_reads(sub)
+    b = o.map_reads(sub, opt, n_threads=4)
+    assert (a[1] == b[1]).all() and nams_equal(a[0], b[0])
+
+
+def test_larger_repeat_rich_genome_against_oracle():
+    gp = synth.genome_params("C2", scale=0.05, seed=77)   # 5 Mbp, 20 contigs, duplications + STRs
+    g = synth.make_genome(gp)
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=4000, seed=78))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    a, b = idx.export(), (o.randstrobes(), o.starts())
+    assert (a[0] == b[0]).all() and (a[1] == b[1]).all()
+    assert idx.info().filter_cutoff == o.info().filter_cutoff
+    x = native.Mapper(idx).map_reads(reads)
+    y = o.map_reads(reads, n_threads=8)
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+    assert nams_equal(x[0], y[0])
+
+
+def test_variable_length_reads_against_oracle():
+    g = synth.make_genome(synth.genome_params("C1", scale=0.1, seed=5))
+    reads = synth.make_reads(g, synth.read_params("C3", n_units=3000, seed=6))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    x = native.Mapper(idx).map_reads(reads)
+    y = o.map_reads(reads, n_threads=8)
+    assert (x[1] == y[1]).all() and nams_equal(x[0], y[0])
+
+
+def test_launch_count_grows():
+    before = native.launch_count()
+    g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
+    native.Index.build(native.params_from_read_length(150), g)
+    assert native.launch_count() > before
