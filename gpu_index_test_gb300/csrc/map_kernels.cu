@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
 // the request fits, else a bump allocation in the shared overflow arena (nullptr
 // when that is full too).
 __device__ __forceinline__ uint8_t* warp_scratch(const Arenas& A, Counters* ctr, uint64_t slot_off, uint64_t bytes) {
+    bytes = (bytes + 255) & ~255ull;   // keep every region 256-byte aligned
     if (slot_off + bytes <= A.slot_bytes) return A.slots + (uint64_t)warp_global_id() * A.slot_bytes + slot_off;
     const uint64_t o = warp_bump(&ctr->scratch_used, bytes);
     if (o + bytes > A.ovf_cap) return nullptr;
