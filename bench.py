@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Throughput of the strobealign seed → lookup → NAM path on GB300.
+
+Workload (one "step"): the repeat-rich mid-size configuration — a synthetic 100 Mbp
+reference in 20 contigs (5% of bases in duplicated 1-10 kb segments copied 2-20x at
+0.5-2% divergence, plus short tandem repeats), indexed on the GPU with the
+150 bp parameters, and 1M paired-end 2x150 bp read pairs (2M reads, insert
+~Normal(300, 30), 1% substitutions, 0.1% 1-3 bp indels).  A step maps all 2M reads:
+randstrobes, index lookup, hit collection, NAM merge, rescue and NAM sort.
+
+value  reads/s with inputs resident in HBM (device C-ABI entry point, CUDA events on
+       the launching stream).
+e2e    reads/s through the host C-ABI entry point (gbsa_map_reads): pinned host
+       reads in, NAMs / offsets / fractions back to host, copies inside the timing.
+The CPU baseline is the CPU restatement of the reference path on a bounded sample
+of the same reads with all host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbsa|reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbsa", choices=["gbsa", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(scale, rank):
+    from gpu_index_test_gb300 import synth
+
+    gp = synth.genome_params("C2", scale=scale, seed=1)
+    rp = synth.read_params("C2", n_units=max(1000, int(1_000_000 * scale)), seed=11 + rank)
+    t0 = time.perf_counter()
+    g = synth.make_genome(gp)
+    reads = synth.make_reads(g, rp)
+    return g, reads, time.perf_counter() - t0, gp, rp
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(g, reads, target_s, gpu_result=None):
+    """The oracle (CPU restatement of the reference path) on a bounded sample."""
+    from gpu_index_test_gb300 import abi
+    from oracle import oracle_py
+
+    p = oracle_py.params_from_read_length(150)
+    t0 = time.perf_counter()
+    idx = oracle_py.Index.build(p, g)
+    build_s = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    opt = abi.map_options()
+    cal = reads.subset(np.arange(min(reads.n, 20000)))
+    t0 = time.perf_counter()
+    idx.map_reads(cal, opt, n_threads=cores)
+    per_read = (time.perf_counter() - t0) / cal.n
+    n = int(min(reads.n, max(cal.n, target_s / max(per_read, 1e-9))))
+    sample = reads.subset(np.arange(n))
+    t0 = time.perf_counter()
+    nams, offs, frac, resc = idx.map_reads(sample, opt, n_threads=cores)
+    dt = time.perf_counter() - t0
+    exact = None
+    if gpu_result is not None:
+        gn, go, gf, gr = gpu_result
+        exact = bool((go[: n + 1] == offs).all() and (gf[:n] == frac).all() and (gr[:n] == resc).all())
+        if exact:
+            k = int(offs[-1])
+            exact = all((gn[f][:k] == nams[f]).all() for f in abi.NAM_COMPARED)
+    return {"value": n / dt, "unit": "reads/s", "cores": cores, "kind": "port",
+            "sample": f"first {n} of the {reads.n} reads, all {cores} host threads, {dt:.1f} s",
+            "index_build_s": round(build_s, 2)}, exact
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference path on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from gpu_index_test_gb300 import abi
+    from oracle import oracle_py
+    import __graft_entry__
+
+    __graft_entry__.build()
+    g, reads, _, gp, rp = workload(args.scale, 0)
+    p = oracle_py.params_from_read_length(150)
+    idx = oracle_py.Index.build(p, g)
+    cores = os.cpu_count() or 1
+    opt = abi.map_options()
+    cal = reads.subset(np.arange(min(reads.n, 20000)))
+    t0 = time.perf_counter()
+    idx.map_reads(cal, opt, n_threads=cores)
+    per_read = (time.perf_counter() - t0) / cal.n
+    step_budget = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+    n = int(min(reads.n, max(1000, step_budget / max(per_read, 1e-9))))
+    sample = reads.subset(np.arange(n))
+    for _ in range(args.warmup):
+        idx.map_reads(sample, opt, n_threads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        idx.map_reads(sample, opt, n_threads=cores)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = n / dt
+    line = {
+        "impl": "reference", "metric": "reads/s seed+lookup+NAM", "value": v, "unit": "reads/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": config_of(gp, rp, reads, args),
+        "cpu_baseline": {"value": v, "unit": "reads/s", "cores": cores, "kind": "port",
+                         "sample": f"first {n} of {reads.n} reads per step, {cores} host threads"},
+        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def config_of(gp, rp, reads, args):
+    return {
+        "workload": "C2 repeat-rich mid-size: synthetic 100 Mbp / 20 contigs (5% segmental duplications, STRs), "
+                    "1M paired-end 2x150 bp pairs = 2M reads per step",
+        "genome_bp": gp.total_len, "contigs": gp.n_contigs, "reads_per_step": reads.n, "read_len": rp.len_min,
+        "paired": True, "params": "from_read_length(150): k=20 s=16 l=1 u=7 q=255 max_dist=80",
+        "rescue": "R=2, rescue_cutoff=2*filter_cutoff, count cap 1000", "nam_order": "score",
+        "l2": "inputs larger than L2 (2M reads = 300 MB of bases; index 320 MB + 64 MB bucket table)",
+        "scale": args.scale,
+    }
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from gpu_index_test_gb300 import abi, native
+
+    g, reads, gen_s, gp, rp = workload(args.scale, rank)
+    p = native.params_from_read_length(150)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = native.Index.build(p, g)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    info = idx.info()
+    n = reads.n
+    m = native.Mapper(idx, abi.map_options(), max_reads=n, max_bases=int(reads.lengths.sum()))
+
+    dev = torch.device("cuda", local)
+    d_seq = torch.from_numpy(reads.seq).to(dev)
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).to(dev)
+    d_len = torch.from_numpy(reads.lengths.view(np.int32)).to(dev)
+    cap = 30 * n
+    d_nams = torch.empty(cap * 44, dtype=torch.uint8, device=dev)
+    d_noff = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    d_frac = torch.empty(n, dtype=torch.float32, device=dev)
+    d_resc = torch.empty(n, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        tot = m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_nams.data_ptr(), cap,
+                                 d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), stream.cuda_stream)
+        if tot > cap:
+            raise RuntimeError("NAM capacity too small")
+        return tot
+
+    # warm-up (first one also counts algorithmic bytes of the lookup stage)
+    m.set_count_bytes(True)
+    total_nams = step()
+    alg_lookup = m.last_alg_bytes()
+    counts = m.last_counts()
+    m.set_count_bytes(False)
+    for _ in range(max(0, args.warmup - 1)):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region
+    m.set_profile(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = native.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    stage_acc = {}
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+        for k, v in m.stage_ms().items():
+            stage_acc[k] = stage_acc.get(k, 0.0) + v
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = native.launch_count() - l0
+    clocks = sampler.stop()
+    m.set_profile(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3)
+
+    # device results of the last step, for the parity check in the CPU-baseline leg
+    gpu_res = None
+    if rank == 0 and not args.no_cpu_baseline:
+        k = total_nams
+        raw = d_nams[: k * 44].cpu().numpy()
+        gpu_res = (raw.view(abi.NAM), d_noff.cpu().numpy().view(np.uint64), d_frac.cpu().numpy(),
+                   d_resc.cpu().numpy())
+
+    # end-to-end through the host entry point: pinned host reads in, results out
+    h_seq = torch.from_numpy(reads.seq).pin_memory()
+    h_nams = torch.empty(cap * 44, dtype=torch.uint8).pin_memory()
+    h_noff = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    h_frac = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_resc = torch.empty(n, dtype=torch.uint8).pin_memory()
+    offs_np = reads.offsets
+    lens_np = reads.lengths
+    L = native.lib()
+
+    def e2e_step():
+        rc = L.gbsa_map_reads(m.h, h_seq.data_ptr(), offs_np.ctypes.data, lens_np.ctypes.data, n, h_nams.data_ptr(),
+                              cap, h_noff.data_ptr(), h_frac.data_ptr(), h_resc.data_ptr())
+        if rc != 0:
+            raise RuntimeError(f"gbsa_map_reads failed: {rc}")
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    tot_nams_e2e = int(h_noff[n].item())
+    h2d = int(reads.seq.nbytes) + 12 * n
+    d2h = 44 * tot_nams_e2e + 8 * (n + 1) + 4 * n + n
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # roofline of the dominant stage
+    stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
+    dom = max(stage_ms, key=stage_ms.get)
+    q, hits, nams_n = counts["queries"], counts["hits"], counts["nams"]
+    bases = int(reads.lengths.sum())
+    alg = {
+        "seed": bases + 16 * q,                          # ASCII bases in, query randstrobes out
+        "seed_long": 0,
+        "lookup": alg_lookup + 16 * q + 8 * q + 20 * hits,  # probes + queries in + positions + hits out
+        "nams": 20 * hits + 44 * nams_n,                 # hits in, NAMs out
+        "rescue": 0,
+    }
+    peak, peak_kind = peaks()
+    achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
+    tr = ncu_traffic().get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": tr, "alg_bytes_per_launch": alg[dom], "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}}
+
+    cpu = None
+    exact = None
+    if not args.no_cpu_baseline:
+        cpu, exact = cpu_baseline(g, reads, args.cpu_seconds, gpu_res)
+
+    line = {
+        "metric": "reads/s seed+lookup+NAM", "value": round(value, 1), "unit": "reads/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": dict(config_of(gp, rp, reads, args), index_entries=int(info.size), index_bits=int(info.bits),
+                       filter_cutoff=int(info.filter_cutoff), index_build_gpu_s=round(build_s, 3),
+                       form="plain (one kernel per stage, warp per read)"),
+        "e2e": {"value": round(world * n / e2e_s, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "bit_exact_vs_cpu_sample": exact,
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+        "work": dict(counts, nams_per_step=int(total_nams)),
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -139,6 +139,10 @@ struct gbsa_mapper {
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
     int count_bytes = 0;
+    int profile = 0;          // record per-stage CUDA events
+    cudaEvent_t ev[8] = {};
+    float stage_ms[7] = {};
+    gbsa::Counters last{};    // device counters of the last batch
 };
 
 namespace gbsa {
@@ -229,17 +233,27 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         Arenas A = arenas_of(m);
         MapConfig C = m.cfg;
         C.count_bytes = m.count_bytes;
-        if (!seeded) {
-            launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+        auto mark = [&](int i) {
+            if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[i], st));
+        };
+        mark(0);
+        if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+        mark(1);
+        if (!seeded)
             launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr,
                              m.long_scratch.as<uint8_t>(), m.long_warps, st);
-        }
+        mark(2);
         launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        mark(3);
         launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        mark(4);
         launch_rescue(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        mark(5);
         Counters h{};
         GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
         GBSA_CUDA(cudaStreamSynchronize(st));
+        if (m.profile)
+            for (int i = 0; i < 5; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[i], m.ev[i + 1]));
         if (h.status & kStatusReadTooLong)
             throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
         if (h.status & kStatusSyncmerOverflow)
@@ -268,6 +282,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         }
         if (retry) continue;
         m.alg_bytes = h.alg_bytes;
+        m.last = h;
         // per-read NAM counts → offsets
         uint64_t* cnt = m.cnt.as<uint64_t>();
         uint64_t* off = m.out_off.as<uint64_t>();
@@ -595,6 +610,8 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
 
 void gbsa_mapper_free(gbsa_mapper* m) {
     if (!m) return;
+    for (auto& e : m->ev)
+        if (e) cudaEventDestroy(e);
     if (m->st) {
         cudaStreamSynchronize(m->st);
         cudaStreamDestroy(m->st);
@@ -732,5 +749,28 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries, const u
 // the value of the last batch.
 void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on) { m->count_bytes = on; }
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m) { return m->alg_bytes; }
+
+int gbsa_mapper_set_profile(gbsa_mapper* m, int on) {
+    return guarded([&] {
+        if (on && !m->ev[0])
+            for (auto& e : m->ev) GBSA_CUDA(cudaEventCreate(&e));
+        m->profile = on;
+    });
+}
+
+int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
+    out[0] = m->last.q_used;
+    out[1] = m->last.hit_used;
+    out[2] = m->last.nam_used;
+    out[3] = m->last.n_rescue;
+    out[4] = m->last.n_long;
+    out[5] = m->last.scratch_used;
+    return GBSA_OK;
+}
+
+int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n) {
+    for (int i = 0; i < n && i < 5; ++i) ms[i] = m->stage_ms[i];
+    return GBSA_OK;
+}
 
 }  // extern "C"

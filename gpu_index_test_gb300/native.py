@@ -61,6 +61,9 @@ def lib():
             "gbsa_find_nams": (i32, [vp, vp, vp, u32, i32, u32, vp, u64, vp, vp]),
             "gbsa_mapper_set_count_bytes": (None, [vp, i32]),
             "gbsa_mapper_last_alg_bytes": (u64, [vp]),
+            "gbsa_mapper_set_profile": (i32, [vp, i32]),
+            "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
+            "gbsa_mapper_last_counts": (i32, [vp, vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -213,6 +216,21 @@ class Mapper:
 
     def last_alg_bytes(self):
         return lib().gbsa_mapper_last_alg_bytes(self.h)
+
+    STAGES = ("seed", "seed_long", "lookup", "nams", "rescue")
+
+    def set_profile(self, on=True):
+        _check(lib().gbsa_mapper_set_profile(self.h, 1 if on else 0))
+
+    def last_counts(self):
+        a = np.zeros(6, np.uint64)
+        lib().gbsa_mapper_last_counts(self.h, a.ctypes.data)
+        return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes"), (int(x) for x in a)))
+
+    def stage_ms(self):
+        a = np.zeros(5, np.float32)
+        lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 5)
+        return dict(zip(self.STAGES, a.tolist()))
 
     def map_reads(self, reads, capacity=None):
         n = reads.n

@@ -220,6 +220,15 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
  * step2/main.cu:4743-4746). */
 void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on);
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m);
+/* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
+ * returns the last batch's milliseconds for: seeding, long-read seeding, lookup,
+ * NAM merge + sort, rescue.  No reference counterpart. */
+int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
+int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
+/* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
+ * path, [2] NAMs, [3] rescued reads, [4] reads seeded by the long-read kernel,
+ * [5] overflow scratch bytes.  No reference counterpart. */
+int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
 
 #ifdef __cplusplus
 }
