@@ -64,6 +64,7 @@ def lib():
             "gbsa_mapper_set_profile": (i32, [vp, i32]),
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
+            "gbsa_randstrobes_query_noalloc": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64), vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)

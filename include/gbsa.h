@@ -176,6 +176,24 @@ int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_
                            gbsa_query_randstrobe* out, uint64_t out_capacity,
                            uint64_t* out_offsets, uint64_t* out_total);
 
+/* randstrobes_query for callers that cannot allocate device memory: callers whose
+ * device memory is owned by a host framework's pool, and serving loops that must
+ * not call cudaMalloc / cudaFree (cudaFree waits for the whole device).  No
+ * counterpart in the reference.  Reads and outputs are in device memory and work is
+ * queued on `stream`; the call allocates nothing.  Its only scratch is a file-scope
+ * device array of about 3.3 MB (64 warp slots for reads of up to GBSA_MAX_READ_LEN
+ * bases), held by every GPU that loads the library until the process exits.  The
+ * first call on a device looks up that array's address (make it before any stream
+ * capture); calls that overlap on the GPU race on the array.  d_out_offsets has
+ * n_reads + 1 entries and is always filled; *out_total receives the total; reads
+ * longer than GBSA_MAX_READ_LEN give GBSA_ERR_READ_TOO_LONG and a total above
+ * out_capacity gives GBSA_ERR_CAPACITY (nothing written to d_out). */
+int gbsa_randstrobes_query_noalloc(const gbsa_params* p, const char* d_seqs,
+                                   const uint64_t* d_offsets, const uint32_t* d_lengths,
+                                   uint32_t n_reads, gbsa_query_randstrobe* d_out,
+                                   uint64_t out_capacity, uint64_t* d_out_offsets,
+                                   uint64_t* out_total, void* stream);
+
 /* ---- NAM path ---------------------------------------------------------------- */
 /* A mapper owns the device work areas for batches of up to max_reads reads with up
  * to max_bases bases in total; both grow on demand. */
