@@ -219,99 +219,91 @@ __device__ __forceinline__ uint8_t* warp_scratch(const Arenas& A, Counters* ctr,
     return A.ovf + o;
 }
 
-// Carves consecutive regions out of a scratch block.
-struct Carver {
-    uint8_t* p;
-    __device__ void* take(uint64_t bytes) {
-        void* r = p;
-        p += (bytes + 15) & ~15ull;
-        return r;
-    }
-};
 
-__device__ __forceinline__ uint64_t nam_scratch_bytes(uint32_t H) {
-    const uint64_t P = next_pow2(H);
-    return 16 * 8 + 8 * P + 4 * P + 4 * P + 32ull * H * 2 + 4ull * (H + 1) * 2 + H + 64;
-}
-
-// Groups hits[0..H) by (orientation, ref id) keeping generation order, merges each
-// group with one lane, sorts the NAMs and writes them to the NAM arena.
-template <bool kNamMajor>
-__device__ void warp_hits_to_nams(const MapConfig& C, const HitRec* hits, uint32_t H, uint8_t* scratch, ReadRec& R,
-                                  const Arenas& A, Counters* ctr) {
+// Scores, sorts and writes the closed NAMs of a read to the NAM arena.  keys needs
+// room for next_pow2(n_closed) entries.
+__device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* keys, ReadRec& R, const Arenas& A,
+                                 Counters* ctr) {
     const uint32_t lane = lane_id();
-    const uint32_t P2 = next_pow2(H);
-    Carver cv{scratch};
-    uint64_t* keys = (uint64_t*)cv.take(8ull * P2);
-    uint32_t* order = (uint32_t*)cv.take(4ull * P2);
-    uint32_t* idx = (uint32_t*)cv.take(4ull * P2);
-    NamState* states = (NamState*)cv.take(32ull * H);
-    NamState* compact = (NamState*)cv.take(32ull * H);
-    uint32_t* gstart = (uint32_t*)cv.take(4ull * (H + 1));
-    uint32_t* gcount = (uint32_t*)cv.take(4ull * (H + 1));
-    uint8_t* taken = (uint8_t*)cv.take(H);
-
-    for (uint32_t i = lane; i < H; i += 32) keys[i] = ((uint64_t)hits[i].ref_rc << 32) | i;
+    const uint32_t NN = L.n_closed;
+    for (uint32_t t = lane; t < NN; t += 32) keys[t] = nam_key(L.closed[t], t, C.sort_mode);
     __syncwarp();
-    warp_sort_u64(keys, H);
-    for (uint32_t i = lane; i < H; i += 32) order[i] = (uint32_t)keys[i];
-    __syncwarp();
-    // group starts
-    uint32_t G = 0;
-    for (uint32_t base = 0; base < H; base += 32) {
-        const uint32_t i = base + lane;
-        const bool st = i < H && (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32));
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, st);
-        if (st) gstart[G + __popc(m & lanemask_lt())] = i;
-        G += __popc(m);
-    }
-    if (lane == 0) gstart[G] = H;
-    __syncwarp();
-    for (uint32_t g = lane; g < G; g += 32) {
-        const uint32_t b = gstart[g], e = gstart[g + 1];
-        gcount[g] = kNamMajor ? merge_group_nam_major(hits, order, b, e, states + b, taken + b)
-                              : merge_group_hit_major(hits, order, b, e, states + b);
-    }
-    __syncwarp();
-    // compact the NAMs of all groups
-    uint32_t NN = 0;
-    for (uint32_t base = 0; base < G; base += 32) {
-        const uint32_t g = base + lane;
-        const uint32_t v = g < G ? gcount[g] : 0;
-        const uint32_t inc = warp_inclusive_sum(v);
-        if (g < G) {
-            const uint32_t dst = NN + inc - v, b = gstart[g];
-            for (uint32_t j = 0; j < v; ++j) compact[dst + j] = states[b + j];
-        }
-        NN += __shfl_sync(0xFFFFFFFFu, inc, 31);
-    }
-    __syncwarp();
-    warp_sort_nams(compact, idx, NN, C.sort_mode);
+    warp_sort_keys(keys, NN);
     const uint64_t noff = warp_bump(&ctr->nam_used, NN);
     if (noff + NN > A.nam_cap) {
         warp_fail(R, ctr, kStatusNamOverflow);
         return;
     }
-    for (uint32_t j = lane; j < NN; j += 32) to_gbsa_nam(compact[idx[j]], (int)j, A.nams[noff + j]);
+    for (uint32_t t = lane; t < NN; t += 32) to_gbsa_nam(L.closed[keys[t].idx], (int)t, A.nams[noff + t]);
     if (lane == 0) {
         R.nam_off = noff;
         R.n_nams = NN;
     }
 }
 
+constexpr uint32_t kNamSmem = 64;   // reads with at most this many hits merge in shared memory
+
+// find_nams after the lookup: the read's hits arrive in (orientation, query_start,
+// position) order, one query randstrobe after another; they are merged hit-major.
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
                                                                Arenas A, Counters* ctr) {
+    __shared__ NamState s_lists[kWarpsPerBlock][2 * kNamSmem];
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
         ReadRec& R = rec[r];
         if (R.flags & (kReadFailed | kReadRescue)) continue;
         const uint32_t H = R.n_hits;
         if (H == 0) continue;
-        uint8_t* sc = warp_scratch(A, ctr, 0, nam_scratch_bytes(H));
-        if (!sc) {
-            warp_fail(R, ctr, kStatusScratchOverflow);
-            continue;
+        const HitRec* hits = A.hits + R.hit_off;
+        NamLists L;
+        NamKey* keys;
+        if (H <= kNamSmem) {
+            L.open = s_lists[w];
+            L.closed = s_lists[w] + kNamSmem;
+            keys = reinterpret_cast<NamKey*>(s_lists[w]);   // the open list is empty when keys are built
+        } else {
+            const uint64_t P2 = next_pow2(H);
+            uint8_t* sc = warp_scratch(A, ctr, 0, 64ull * H + 32ull * P2 + 64);
+            if (!sc) {
+                warp_fail(R, ctr, kStatusScratchOverflow);
+                continue;
+            }
+            L.open = reinterpret_cast<NamState*>(sc);
+            L.closed = L.open + H;
+            keys = reinterpret_cast<NamKey*>(L.closed + H);
         }
-        warp_hits_to_nams<false>(C, A.hits + R.hit_off, H, sc, R, A, ctr);
+        L.n_open = L.n_closed = 0;
+        L.cap = H;
+        uint32_t cur_dir = 0;
+        for (uint32_t i = 0; i < H;) {
+            const HitRec x = hits[i];
+            const uint32_t dir = x.ref_rc >> 31;
+            // end of this query randstrobe's hits
+            uint32_t j = i + 1;
+            for (;;) {
+                const uint32_t t = j + lane;
+                bool same = false;
+                if (t < H) {
+                    const HitRec y = hits[t];
+                    same = (y.ref_rc >> 31) == dir && y.qs == x.qs;
+                }
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, same);
+                if (m != 0xFFFFFFFFu) {
+                    j += __ffs(~m) - 1;
+                    break;
+                }
+                j += 32;
+            }
+            if (dir != cur_dir) {
+                nam_close_passed(L, 0x7FFFFFFF);
+                cur_dir = dir;
+            }
+            nam_close_passed(L, x.qs);
+            nam_merge_hit_major(L, hits + i, j - i);
+            i = j;
+        }
+        nam_close_passed(L, 0x7FFFFFFF);
+        warp_finish_nams(C, L, keys, R, A, ctr);
         __syncwarp();
     }
 }
@@ -329,17 +321,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
         const uint32_t nqm = nqd[0] > nqd[1] ? nqd[0] : nqd[1];
         const uint32_t Pq = next_pow2(nqm > 0 ? nqm : 1);
-        // phase 1 scratch: rescue-hit keys and taken keys, per orientation
         const uint64_t b1 = 4ull * 8 * Pq + 64;
         uint8_t* sc1 = warp_scratch(A, ctr, 0, b1);
         if (!sc1) {
             warp_fail(R, ctr, kStatusScratchOverflow);
             continue;
         }
-        Carver cv{sc1};
-        uint64_t* rk[2] = {(uint64_t*)cv.take(8ull * Pq), (uint64_t*)cv.take(8ull * Pq)};
-        uint64_t* tk[2] = {(uint64_t*)cv.take(8ull * Pq), (uint64_t*)cv.take(8ull * Pq)};
+        uint64_t* rk[2] = {reinterpret_cast<uint64_t*>(sc1), reinterpret_cast<uint64_t*>(sc1) + Pq};
+        uint64_t* tk[2] = {reinterpret_cast<uint64_t*>(sc1) + 2 * Pq, reinterpret_cast<uint64_t*>(sc1) + 3 * Pq};
         uint32_t m[2];
+        uint64_t bound = 0;     // sum of run lengths of the taken rescue hits
+        uint32_t maxrun = 0;
         for (int d = 0; d < 2; ++d) {
             // RescueHit{position, count, qs, qe} of every found query, keyed by
             // (count, query_start) — query_start is unique per orientation, so this is
@@ -351,12 +343,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
                 bool f = false;
                 uint64_t key = 0;
                 if (qi < nq) {
-                    const Query q = Qd[d][qi];
                     const uint64_t pos = Pd[d][qi];
                     if (pos != kNotFound) {
                         f = true;
                         const uint32_t cnt = index_get_count(I, pos);
-                        key = ((uint64_t)cnt << 32) | ((uint64_t)q.start << 16) | qi;
+                        key = ((uint64_t)cnt << 32) | ((uint64_t)Qd[d][qi].start << 16) | qi;
                     }
                 }
                 const uint32_t bm = __ballot_sync(0xFFFFFFFFu, f);
@@ -365,8 +356,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
             }
             __syncwarp();
             warp_sort_u64(rk[d], nd);
-            // prefix of the sorted list until (count > rescue_cutoff && taken >= 5) or
-            // count > cap (step2/nam.cu:960-969)
+            // prefix until (count > rescue_cutoff && taken >= 5) or count > cap
+            // (step2/nam.cu:960-969)
             uint32_t stop = nd;
             for (uint32_t base = 0; base < nd; base += 32) {
                 const uint32_t j = base + lane;
@@ -382,69 +373,59 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
                 }
             }
             m[d] = stop;
-            // re-sort the taken ones by query_start (cmp2)
-            for (uint32_t j = lane; j < stop; j += 32) tk[d][j] = rk[d][j] & 0xFFFFFFFFull;
+            uint64_t bsum = 0;
+            uint32_t bmax = 0;
+            for (uint32_t j = lane; j < stop; j += 32) {
+                const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
+                bsum += cnt;
+                bmax = cnt > bmax ? cnt : bmax;
+                tk[d][j] = rk[d][j] & 0xFFFFFFFFull;   // re-sorted by query_start (cmp2)
+            }
+            bound += warp_sum(bsum);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint32_t v = __shfl_xor_sync(0xFFFFFFFFu, bmax, o);
+                bmax = v > bmax ? v : bmax;
+            }
+            maxrun = bmax > maxrun ? bmax : maxrun;
             __syncwarp();
             warp_sort_u64(tk[d], stop);
         }
-        // hit counts of the taken rescue hits, in (orientation, query_start) order
-        uint64_t TH = 0;
-        for (int d = 0; d < 2; ++d) {
-            for (uint32_t j = lane; j < m[d]; j += 32) {
-                const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
-                const Query q = Qd[d][qi];
-                const uint32_t c = walk_hit_run(I, (int)q.start, (int)q.end, Pd[d][qi], [](uint32_t, int, int) {});
-                TH += c;
-            }
+        if (bound == 0) {
+            if (lane == 0) R.n_nams = 0;
+            continue;
         }
-        TH = warp_sum(TH);
-        const uint32_t H = (uint32_t)TH;
-        const uint64_t b2 = 20ull * H + nam_scratch_bytes(H) + 64;
-        uint8_t* sc2 = TH > 0xFFFFFFFull ? nullptr : warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
+        if (bound > 0xFFFFFFFull) {
+            warp_fail(R, ctr, kStatusScratchOverflow);
+            continue;
+        }
+        const uint32_t H = (uint32_t)bound;
+        const uint64_t P2 = next_pow2(H);
+        const uint64_t b2 = 64ull * H + 32ull * P2 + 20ull * maxrun + maxrun + 256;
+        uint8_t* sc2 = warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
         if (!sc2) {
             warp_fail(R, ctr, kStatusScratchOverflow);
             continue;
         }
-        HitRec* hits = (HitRec*)sc2;
-        uint8_t* nscratch = sc2 + ((20ull * H + 15) & ~15ull);
-        // write hits in generation order: prefix sums over the taken lists
-        uint32_t running = 0;
+        NamLists L;
+        L.open = reinterpret_cast<NamState*>(sc2);
+        L.closed = L.open + H;
+        NamKey* keys = reinterpret_cast<NamKey*>(L.closed + H);
+        HitRec* hb = reinterpret_cast<HitRec*>(keys + P2);
+        uint8_t* tb = reinterpret_cast<uint8_t*>(hb + maxrun);
+        L.n_open = L.n_closed = 0;
+        L.cap = H;
         for (int d = 0; d < 2; ++d) {
-            for (uint32_t base = 0; base < m[d]; base += 32) {
-                const uint32_t j = base + lane;
-                uint32_t c = 0;
-                Query q{};
-                uint64_t pos = 0;
-                if (j < m[d]) {
-                    const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
-                    q = Qd[d][qi];
-                    pos = Pd[d][qi];
-                    c = walk_hit_run(I, (int)q.start, (int)q.end, pos, [](uint32_t, int, int) {});
-                }
-                const uint32_t inc = warp_inclusive_sum(c);
-                if (j < m[d]) {
-                    HitRec* out = hits + running + inc - c;
-                    uint32_t k = 0;
-                    const int qs = (int)q.start, qe = (int)q.end;
-                    walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
-                        HitRec h;
-                        h.ref_rc = ((uint32_t)d << 31) | ref;
-                        h.qs = qs;
-                        h.qe = qe;
-                        h.rs = rs;
-                        h.re = re;
-                        out[k++] = h;
-                    });
-                }
-                running += __shfl_sync(0xFFFFFFFFu, inc, 31);
+            for (uint32_t j = 0; j < m[d]; ++j) {
+                const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
+                const Query q = Qd[d][qi];
+                const uint32_t nh = warp_walk_run(I, (int)q.start, (int)q.end, Pd[d][qi], (uint32_t)d, hb, maxrun);
+                nam_close_passed(L, (int)q.start);
+                nam_merge_nam_major(L, hb, nh, (int)q.start, tb);
             }
+            nam_close_passed(L, 0x7FFFFFFF);
         }
-        __syncwarp();
-        if (H == 0) {
-            if (lane == 0) R.n_nams = 0;
-            continue;
-        }
-        warp_hits_to_nams<true>(C, hits, H, nscratch, R, A, ctr);
+        warp_finish_nams(C, L, keys, R, A, ctr);
         __syncwarp();
     }
 }

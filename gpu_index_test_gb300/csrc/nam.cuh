@@ -1,14 +1,27 @@
-// nam.cuh — hit → NAM merging and NAM ordering, as warp-level device functions.
+// nam.cuh — hit → NAM merging and NAM ordering, warp-cooperative.
 //
-// Hits of one read are grouped by (orientation, reference id) — the reference keeps
-// them in robin_hood maps keyed by ref id, one per orientation (step2/nam.cu:45-62)
-// — and each group is merged by one lane:
-//   merge_group_hit_major  merge_hits_into_nams, step2/nam.cu:347-513 (find_nams)
-//   merge_group_nam_major  merge_hits_into_nams_fast, step2/nam.cu:94-343
-//                          (find_nams_rescue)
-// Both keep the reference's open-NAM order (creation order; flushing a NAM whose
-// query_end is behind the current query_start removes one that could no longer
-// take any later hit, so skipping such NAMs is the same as removing them).
+// The reference keeps one hit list per (orientation, reference id) in robin_hood
+// maps (step2/nam.cu:45-62) and merges each list on its own:
+//   merge_hits_into_nams      (hit-major, step2/nam.cu:347-513; find_nams)
+//   merge_hits_into_nams_fast (NAM-major, step2/nam.cu:94-343; find_nams_rescue)
+// over hits sorted by (query_start, ref_start).  Lists never interact, so the warp
+// processes all of them at once, one query randstrobe at a time: the hits of one
+// query randstrobe share query_start, arrive sorted by ref_start (a hash run is
+// sorted by position) and only meet NAMs of their own (orientation, reference id).
+//
+// Open NAMs are kept in creation order (the reference's open list order).  A NAM
+// whose query_end is behind the current query_start can take no later hit; it is
+// moved to the closed list before each query (the reference removes such NAMs at its
+// flush points; which NAMs are removed when only changes iteration, not results).
+//
+//   hit-major: for each hit (ref_start order), the first open NAM in creation order
+//     that accepts it takes it — found with a warp ballot over 32 NAMs at a time.
+//   NAM-major: for each open NAM (creation order), the first untaken hit of the
+//     query with ref_start in (ref_prev, ref_end] that extends it or lies inside it.
+//     32 NAMs pick candidates in parallel; if two pick the same hit, the NAMs before
+//     the first such clash are final and the rest pick again (each round settles at
+//     least one more NAM, and a NAM is final exactly when no earlier NAM in the
+//     round took a hit it would have considered).
 #pragma once
 
 #include "lookup.cuh"
@@ -17,7 +30,8 @@ namespace gbsa {
 
 // Working state of one NAM (step2/my_struct.hpp:48-62 fields used by the merge).
 struct NamState {
-    int32_t qs, qe, qprev, rs, re, rprev, n_hits, ref_rc;
+    int32_t qs, qe, qprev, rs, re, rprev, n_hits;
+    uint32_t ref_rc;
 };
 
 __device__ __forceinline__ NamState nam_from_hit(const HitRec& h) {
@@ -29,108 +43,157 @@ __device__ __forceinline__ NamState nam_from_hit(const HitRec& h) {
     n.re = h.re;
     n.rprev = h.rs;
     n.n_hits = 1;
-    n.ref_rc = (int32_t)h.ref_rc;
+    n.ref_rc = h.ref_rc;
     return n;
 }
 
-// Hits hits[order[b..e)] (sorted by query_start, then ref_start) → NAMs out[0..),
-// hit-major: each hit joins the first open NAM that accepts it.  Returns the count.
-__device__ __forceinline__ uint32_t merge_group_hit_major(const HitRec* hits, const uint32_t* order, uint32_t b,
-                                                          uint32_t e, NamState* out) {
-    uint32_t nn = 0;
-    uint32_t first_open = 0;   // NAMs before this index are all closed
-    for (uint32_t i = b; i < e; ++i) {
-        const HitRec h = hits[order[i]];
-        bool added = false;
-        while (first_open < nn && out[first_open].qe < h.qs) ++first_open;
-        for (uint32_t o = first_open; o < nn; ++o) {
-            NamState& n = out[o];
-            if (n.qe < h.qs) continue;   // closed
-            if (n.qprev < h.qs && h.qs <= n.qe && n.rprev < h.rs && h.rs <= n.re) {
-                if (h.qe > n.qe && h.re > n.re) {
-                    n.qe = h.qe;
-                    n.re = h.re;
-                    n.qprev = h.qs;
-                    n.rprev = h.rs;
-                    ++n.n_hits;
-                    added = true;
-                    break;
-                } else if (h.qe <= n.qe && h.re <= n.re) {
-                    n.qprev = h.qs;
-                    n.rprev = h.rs;
-                    ++n.n_hits;
-                    added = true;
-                    break;
-                }
-            }
-        }
-        if (!added) out[nn++] = nam_from_hit(h);
-    }
-    return nn;
+// Extend-or-contain rule shared by both merges (step2/nam.cu:386-410, 167-192).
+__device__ __forceinline__ bool nam_takes(const NamState& n, const HitRec& h) {
+    return (h.qe > n.qe && h.re > n.re) || (h.qe <= n.qe && h.re <= n.re);
 }
 
-// NAM-major variant: hits are taken one query_start group at a time; each open NAM
-// (in creation order) takes the first not-yet-taken hit of the group with
-// ref_start in (rprev, re] that extends it or lies inside it.  `taken` is per-hit
-// scratch of the group's size.  Returns the NAM count.
-__device__ __forceinline__ uint32_t merge_group_nam_major(const HitRec* hits, const uint32_t* order, uint32_t b,
-                                                          uint32_t e, NamState* out, uint8_t* taken) {
-    uint32_t nn = 0;
-    for (uint32_t g0 = b; g0 < e;) {
-        const int qs = hits[order[g0]].qs;
-        uint32_t g1 = g0 + 1;
-        while (g1 < e && hits[order[g1]].qs == qs) ++g1;
-        const uint32_t gn = g1 - g0;
-        for (uint32_t j = 0; j < gn; ++j) taken[j] = 0;
-        uint32_t done = 0;
-        const uint32_t nn_before = nn;
-        for (uint32_t o = 0; o < nn_before && done < gn; ++o) {
-            NamState& n = out[o];
-            if (n.qe < qs) continue;   // closed (cannot take this or later groups)
-            // first hit with rs >= rprev + 1 (hits of the group are sorted by rs)
-            uint32_t lo = g0, hi = g1;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) / 2;
-                if (hits[order[mid]].rs < n.rprev + 1) lo = mid + 1;
-                else hi = mid;
+__device__ __forceinline__ void nam_add(NamState& n, const HitRec& h) {
+    if (h.qe > n.qe && h.re > n.re) {
+        n.qe = h.qe;
+        n.re = h.re;
+    }
+    n.qprev = h.qs;
+    n.rprev = h.rs;
+    ++n.n_hits;
+}
+
+// Open and closed NAM lists of one read (any address space).
+struct NamLists {
+    NamState* open;
+    NamState* closed;
+    uint32_t n_open, n_closed;
+    uint32_t cap;   // capacity of each list
+};
+
+// Moves open NAMs with query_end < qs (or all, when qs == INT_MAX) to the closed
+// list, keeping the order of both lists.
+__device__ __forceinline__ void nam_close_passed(NamLists& L, int qs) {
+    const uint32_t lane = lane_id();
+    uint32_t keep = 0, done = 0;
+    for (uint32_t base = 0; base < L.n_open; base += 32) {
+        const uint32_t o = base + lane;
+        NamState n;
+        bool valid = o < L.n_open, stay = false;
+        if (valid) {
+            n = L.open[o];
+            stay = n.qe >= qs;
+        }
+        const uint32_t ms = __ballot_sync(0xFFFFFFFFu, valid && stay);
+        const uint32_t mc = __ballot_sync(0xFFFFFFFFu, valid && !stay);
+        __syncwarp();
+        if (valid && stay) L.open[keep + __popc(ms & lanemask_lt())] = n;
+        if (valid && !stay) L.closed[L.n_closed + done + __popc(mc & lanemask_lt())] = n;
+        keep += __popc(ms);
+        done += __popc(mc);
+        __syncwarp();
+    }
+    L.n_open = keep;
+    L.n_closed += done;
+}
+
+// Hit-major merge of the hits h[0..nh) of one query randstrobe (sorted by rs).
+__device__ __forceinline__ void nam_merge_hit_major(NamLists& L, const HitRec* h, uint32_t nh) {
+    const uint32_t lane = lane_id();
+    const uint32_t nn = L.n_open;   // NAMs made by this query cannot take its other hits
+    for (uint32_t j = 0; j < nh; ++j) {
+        const HitRec x = h[j];
+        int found = -1;
+        for (uint32_t base = 0; base < nn; base += 32) {
+            const uint32_t o = base + lane;
+            bool ok = false;
+            if (o < nn) {
+                const NamState& n = L.open[o];
+                ok = n.ref_rc == x.ref_rc && n.qprev < x.qs && x.qs <= n.qe && n.rprev < x.rs && x.rs <= n.re &&
+                     nam_takes(n, x);
             }
-            for (uint32_t j = lo; j < g1; ++j) {
-                const HitRec h = hits[order[j]];
-                if (h.rs > n.re) break;   // upper bound rs <= re
-                if (taken[j - g0]) continue;
-                if (h.qe > n.qe && h.re > n.re) {
-                    n.qe = h.qe;
-                    n.re = h.re;
-                    n.qprev = h.qs;
-                    n.rprev = h.rs;
-                    ++n.n_hits;
-                    taken[j - g0] = 1;
-                    ++done;
-                    break;
-                } else if (h.qe <= n.qe && h.re <= n.re) {
-                    n.qprev = h.qs;
-                    n.rprev = h.rs;
-                    ++n.n_hits;
-                    taken[j - g0] = 1;
-                    ++done;
-                    break;
-                }
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+            if (m) {
+                found = (int)(base + __ffs(m) - 1);
+                break;
             }
         }
-        for (uint32_t j = 0; j < gn; ++j)
-            if (!taken[j]) out[nn++] = nam_from_hit(hits[order[g0 + j]]);
-        g0 = g1;
+        if (lane == 0) {
+            if (found >= 0) nam_add(L.open[found], x);
+            else L.open[L.n_open] = nam_from_hit(x);
+        }
+        if (found < 0) ++L.n_open;
+        __syncwarp();
     }
-    return nn;
+}
+
+// First untaken hit of h[0..nh) (sorted by rs) that NAM n would take, or -1.
+__device__ __forceinline__ int nam_candidate(const NamState& n, const HitRec* h, uint32_t nh, const uint8_t* taken) {
+    uint32_t lo = 0, hi = nh;
+    const int from = n.rprev + 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (h[mid].rs < from) lo = mid + 1;
+        else hi = mid;
+    }
+    for (uint32_t j = lo; j < nh; ++j) {
+        const HitRec x = h[j];
+        if (x.rs > n.re) break;
+        if (x.ref_rc != n.ref_rc || taken[j]) continue;
+        if (nam_takes(n, x)) return (int)j;
+    }
+    return -1;
+}
+
+// NAM-major merge of the hits h[0..nh) of one query randstrobe with query_start qs
+// (sorted by rs).  taken: nh bytes of scratch.
+__device__ __forceinline__ void nam_merge_nam_major(NamLists& L, const HitRec* h, uint32_t nh, int qs,
+                                                    uint8_t* taken) {
+    const uint32_t lane = lane_id();
+    for (uint32_t j = lane; j < nh; j += 32) taken[j] = 0;
+    __syncwarp();
+    const uint32_t nn = L.n_open;
+    for (uint32_t base = 0; base < nn; base += 32) {
+        const uint32_t o = base + lane;
+        bool resolved = !(o < nn) || L.open[o].qe < qs;
+        for (;;) {
+            int cand = -1;
+            if (!resolved) cand = nam_candidate(L.open[o], h, nh, taken);
+            const uint32_t key = cand < 0 ? 0xFFFFFFFFu : (uint32_t)cand;
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+            const bool clash = cand >= 0 && (peers & lanemask_lt()) != 0;
+            const uint32_t cm = __ballot_sync(0xFFFFFFFFu, clash);
+            const uint32_t lim = cm ? (uint32_t)(__ffs(cm) - 1) : 32u;
+            if (!resolved && lane < lim) {
+                if (cand >= 0) {
+                    taken[cand] = 1;
+                    nam_add(L.open[o], h[cand]);
+                }
+                resolved = true;
+            }
+            __syncwarp();
+            if (!cm) break;
+        }
+    }
+    // untaken hits open new NAMs, in ref_start order
+    uint32_t added = 0;
+    for (uint32_t b = 0; b < nh; b += 32) {
+        const uint32_t j = b + lane;
+        const bool mk = j < nh && !taken[j];
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, mk);
+        if (mk) L.open[L.n_open + added + __popc(m & lanemask_lt())] = nam_from_hit(h[j]);
+        added += __popc(m);
+    }
+    L.n_open += added;
+    __syncwarp();
 }
 
 // Score (step2/nam.cu:454-463): n_hits * (2*min_span - max_span) if positive, else 1.
-__device__ __forceinline__ float nam_score(const NamState& n) {
+__device__ __forceinline__ int nam_score_int(const NamState& n) {
     const int qspan = n.qe - n.qs, rspan = n.re - n.rs;
     const int mx = qspan > rspan ? qspan : rspan;
     const int mn = qspan < rspan ? qspan : rspan;
     const int v = 2 * mn - mx;
-    return v > 0 ? (float)(n.n_hits * v) : 1.0f;
+    return v > 0 ? n.n_hits * v : 1;
 }
 
 __device__ __forceinline__ void to_gbsa_nam(const NamState& n, int id, gbsa_nam& o) {
@@ -142,48 +205,87 @@ __device__ __forceinline__ void to_gbsa_nam(const NamState& n, int id, gbsa_nam&
     o.ref_end = n.re;
     o.ref_prev_hit_startpos = n.rprev;
     o.n_hits = n.n_hits;
-    o.ref_id = (int32_t)((uint32_t)n.ref_rc & 0x7FFFFFFFu);
-    o.score = nam_score(n);
-    o.is_rc = ((uint32_t)n.ref_rc >> 31) ? 1 : 0;
+    o.ref_id = (int32_t)(n.ref_rc & 0x7FFFFFFFu);
+    o.score = (float)nam_score_int(n);
+    o.is_rc = (n.ref_rc >> 31) ? 1 : 0;
     o._pad[0] = o._pad[1] = o._pad[2] = 0;
 }
 
-// NAM orders (GBSA_SORT_*): true when a goes before b.  The score order is
-// (score desc, is_rc, ref_id, qs, qe, rs, re, n_hits desc); the two reference
-// orders follow Nam::operator< (step2/my_struct.hpp:78-92, mate 2) and
-// sort_nams_single2 (step2/main.cu:2271-2289, mate 1) with the remaining compared
-// field appended so that the order is total.
-__device__ __forceinline__ bool nam_before(const NamState& a, const NamState& b, int mode) {
-    const uint32_t arc = (uint32_t)a.ref_rc >> 31, brc = (uint32_t)b.ref_rc >> 31;
-    const int32_t aref = a.ref_rc & 0x7FFFFFFF, bref = b.ref_rc & 0x7FFFFFFF;
+// Sort key of a NAM: three u64 compared in order, then the index (stable).
+//   GBSA_SORT_SCORE:     score desc, is_rc, ref_id, qs | qe, rs, re | n_hits desc
+//   GBSA_SORT_REF_MATE2: is_rc, ref_id, max(0, rs-qs) | n_hits desc, qe, qs | re, rs
+//                        (Nam::operator<, step2/my_struct.hpp:78-92)
+//   GBSA_SORT_REF_MATE1: is_rc, ref_id | n_hits desc, qe, qs | re, rs
+//                        (sort_nams_single2, step2/main.cu:2271-2289)
+// All compared fields enter a key, so the order is total over the compared fields
+// (the score is a function of n_hits and the coordinates).  Field widths: ref_id <
+// 2^24 (RefRandstrobe packs it in 24 bits), query coordinates <= GBSA_MAX_READ_LEN,
+// score < 2^24, NAM ref spans < 2^19.
+struct NamKey {
+    uint64_t k1, k2, k3;
+    uint32_t idx;
+    uint32_t pad;
+};
+
+__device__ __forceinline__ NamKey nam_key(const NamState& n, uint32_t idx, int mode) {
+    const uint64_t rc = n.ref_rc >> 31, ref = n.ref_rc & 0xFFFFFFu;
+    NamKey k;
+    k.idx = idx;
+    k.pad = 0;
     if (mode == GBSA_SORT_SCORE) {
-        const float sa = nam_score(a), sb = nam_score(b);
-        if (sa != sb) return sa > sb;
-        if (arc != brc) return arc < brc;
-        if (aref != bref) return aref < bref;
-        if (a.qs != b.qs) return a.qs < b.qs;
-        if (a.qe != b.qe) return a.qe < b.qe;
-        if (a.rs != b.rs) return a.rs < b.rs;
-        if (a.re != b.re) return a.re < b.re;
-        return a.n_hits > b.n_hits;
+        const uint64_t sc = (uint64_t)nam_score_int(n);
+        k.k1 = ((0xFFFFFFull - sc) << 40) | (rc << 39) | (ref << 15) | ((uint64_t)n.qs & 0x7FFF);
+        k.k2 = ((uint64_t)n.qe << 51) | ((uint64_t)(uint32_t)n.rs << 19) | ((uint64_t)(n.re - n.rs) & 0x7FFFF);
+        k.k3 = 0xFFFFFFFFull - (uint32_t)n.n_hits;
+    } else {
+        const int d = n.rs - n.qs;
+        const uint64_t diag = mode == GBSA_SORT_REF_MATE2 ? (uint64_t)(uint32_t)(d > 0 ? d : 0) : 0;
+        k.k1 = (rc << 56) | (ref << 32) | diag;
+        k.k2 = ((0xFFFFull - (uint32_t)n.n_hits) << 48) | ((uint64_t)n.qe << 24) | (uint64_t)n.qs;
+        k.k3 = ((uint64_t)(uint32_t)n.re << 32) | (uint32_t)n.rs;
     }
-    if (arc != brc) return arc < brc;
-    if (aref != bref) return aref < bref;
-    if (mode == GBSA_SORT_REF_MATE2) {
-        const int da = a.rs - a.qs > 0 ? a.rs - a.qs : 0;
-        const int db = b.rs - b.qs > 0 ? b.rs - b.qs : 0;
-        if (da != db) return da < db;
-    }
-    if (a.n_hits != b.n_hits) return a.n_hits > b.n_hits;
-    if (a.qe != b.qe) return a.qe < b.qe;
-    if (a.qs != b.qs) return a.qs < b.qs;
-    if (a.re != b.re) return a.re < b.re;
-    if (a.rs != b.rs) return a.rs < b.rs;
-    return nam_score(a) > nam_score(b);
+    return k;
+}
+
+__device__ __forceinline__ bool key_less(const NamKey& a, const NamKey& b) {
+    if (a.k1 != b.k1) return a.k1 < b.k1;
+    if (a.k2 != b.k2) return a.k2 < b.k2;
+    if (a.k3 != b.k3) return a.k3 < b.k3;
+    return a.idx < b.idx;
 }
 
 __device__ __forceinline__ uint32_t next_pow2(uint32_t n) {
     return n <= 1 ? 1 : 1u << (32 - __clz(n - 1));
+}
+
+// Warp bitonic sort of n keys; keys must have room for next_pow2(n) entries.
+__device__ inline void warp_sort_keys(NamKey* keys, uint32_t n) {
+    const uint32_t lane = lane_id();
+    const uint32_t P = next_pow2(n);
+    for (uint32_t i = n + lane; i < P; i += 32) {
+        NamKey k;
+        k.k1 = k.k2 = k.k3 = ~0ULL;
+        k.idx = 0xFFFFFFFFu;
+        k.pad = 0;
+        keys[i] = k;
+    }
+    __syncwarp();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < P; i += 32) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const NamKey a = keys[i], b = keys[ixj];
+                    const bool up = (i & k) == 0;
+                    if (key_less(b, a) == up) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
 }
 
 // Warp bitonic sort of u64 keys; keys must have room for next_pow2(n) entries.
@@ -210,34 +312,68 @@ __device__ inline void warp_sort_u64(uint64_t* keys, uint32_t n) {
     }
 }
 
-// Warp bitonic sort of indices into nams[] by nam_before; idx must have room for
-// next_pow2(n) entries.
-__device__ inline void warp_sort_nams(const NamState* nams, uint32_t* idx, uint32_t n, int mode) {
+// Warp-cooperative add_to_hits_per_ref (step2/nam.cu:45-62) for one query: walks
+// the equal-hash run from pos 32 entries at a time; an entry is kept when its
+// length difference is <= every earlier difference of the run (the reference's
+// running minimum), found with a warp prefix-min.  Writes the kept hits to out (in
+// run order, i.e. by position) and returns their count (at most cap are written).
+__device__ __forceinline__ uint32_t warp_walk_run(const IndexView& I, int qs, int qe, uint64_t pos, uint32_t dir,
+                                                  HitRec* out, uint32_t cap) {
     const uint32_t lane = lane_id();
-    const uint32_t P = next_pow2(n);
-    for (uint32_t i = lane; i < P; i += 32) idx[i] = i < n ? i : 0xFFFFFFFFu;
-    __syncwarp();
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = lane; i < P; i += 32) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const uint32_t a = idx[i], b = idx[ixj];
-                    // padding (0xFFFFFFFF) sorts last
-                    bool a_after_b;
-                    if (a == 0xFFFFFFFFu) a_after_b = b != 0xFFFFFFFFu;
-                    else if (b == 0xFFFFFFFFu) a_after_b = false;
-                    else a_after_b = nam_before(nams[b], nams[a], mode);
-                    const bool up = (i & k) == 0;
-                    if (a_after_b == up) {
-                        idx[i] = b;
-                        idx[ixj] = a;
-                    }
-                }
-            }
-            __syncwarp();
+    const uint64_t key = get_hash(I, pos);
+    int carry = 0x7FFFFFFF;
+    uint32_t n = 0;
+    for (uint64_t base = pos;; base += 32) {
+        const uint64_t p = base + lane;
+        bool in = false;
+        gbsa_ref_randstrobe e;
+        int diff = 0x7FFFFFFF;
+        if (p < I.n) {
+            e = I.rs[p];
+            in = e.hash == key;
         }
+        const uint32_t inm = __ballot_sync(0xFFFFFFFFu, in);
+        // the run is contiguous: lanes after the first miss are out
+        const uint32_t runm = (~inm) ? (inm & ((1u << __ffs(~inm) - 1) - 1)) : inm;
+        const bool mine = (runm >> lane) & 1u;
+        int rs = 0, re = 0;
+        if (mine) {
+            rs = (int)e.position;
+            re = rs + (int)(e.packed & 0xFF) + I.k;
+            const int d = (qe - qs) - (re - rs);
+            diff = d < 0 ? -d : d;
+        }
+        // exclusive prefix minimum of diff over earlier lanes, with the carry
+        int pm = diff;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xFFFFFFFFu, pm, o);
+            if (lane >= (uint32_t)o) pm = v < pm ? v : pm;
+        }
+        int excl = __shfl_up_sync(0xFFFFFFFFu, pm, 1);
+        if (lane == 0) excl = 0x7FFFFFFF;
+        excl = excl < carry ? excl : carry;
+        const bool keep = mine && diff <= excl;
+        const uint32_t km = __ballot_sync(0xFFFFFFFFu, keep);
+        if (keep) {
+            const uint32_t k = n + __popc(km & lanemask_lt());
+            if (k < cap) {
+                HitRec h;
+                h.ref_rc = (dir << 31) | (e.packed >> 8);
+                h.qs = qs;
+                h.qe = qe;
+                h.rs = rs;
+                h.re = re;
+                out[k] = h;
+            }
+        }
+        n += __popc(km);
+        const int tot = __shfl_sync(0xFFFFFFFFu, pm, 31);
+        carry = tot < carry ? tot : carry;
+        if (runm != 0xFFFFFFFFu) break;
     }
+    __syncwarp();
+    return n;
 }
 
 }  // namespace gbsa
