@@ -293,7 +293,15 @@ def main():
         torch.distributed.barrier()
     launches = native.launch_count() - l0
     clocks = sampler.stop()
+    rc_cyc = m.rescue_cycles()
     m.set_profile(False)
+    rescue_profile = None
+    if len(rc_cyc):
+        mhz = clocks.get("sm_mhz") or 2000.0
+        us = np.sort(rc_cyc.astype(np.float64)) / mhz
+        rescue_profile = {"reads": int(len(us)), "us_p50": round(float(us[len(us) // 2]), 1),
+                          "us_p99": round(float(us[int(len(us) * 0.99)]), 1), "us_max": round(float(us[-1]), 1),
+                          "us_sum": round(float(us.sum()), 1)}
     ms = ev0.elapsed_time(ev1) / args.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -385,7 +393,7 @@ def main():
         "bit_exact_vs_cpu_sample": exact,
         "clocks": clocks,
         "gpu_launches": int(launches),
-        "work": dict(counts, nams_per_step=int(total_nams)),
+        "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile),
     }
     print(json.dumps(line))
     if world > 1:

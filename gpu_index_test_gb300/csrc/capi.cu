@@ -133,7 +133,7 @@ struct gbsa_mapper {
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
-        out_off, out_nams, out_frac, out_resc;
+        out_off, out_nams, out_frac, out_resc, resc_cycles;
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
@@ -152,12 +152,13 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     m.offs.resize(8ull * (n + 1));
     m.lens.resize(4ull * (n + 1));
     m.rec.resize(sizeof(ReadRec) * (n + 1));
-    m.lists.resize(8ull * (n + 1));
+    m.lists.resize(16ull * (n + 1));
     m.ctr.resize(sizeof(Counters));
     m.cnt.resize(8ull * (n + 1));
     m.out_off.resize(8ull * (n + 1));
     m.out_frac.resize(4ull * (n + 1));
     m.out_resc.resize(n + 1);
+    if (m.profile) m.resc_cycles.resize(8ull * (n + 1));
     // query randstrobes: ~2 per 5 bases plus slack
     const uint64_t q_need = std::max<uint64_t>(4096, bases / 2 + 64ull * n / 8);
     if (m.q_cap < q_need) {
@@ -172,7 +173,7 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     }
     if (m.nam_cap < q_need) {
         m.nam_cap = q_need;
-        m.nams.resize(sizeof(gbsa_nam) * m.nam_cap);
+        m.nams.resize(sizeof(NamState) * m.nam_cap);
     }
     const uint32_t warps = nam_kernel_warps(std::max<uint32_t>(n, 1));
     if (m.slot_bytes == 0) m.slot_bytes = 32 * 1024;
@@ -195,14 +196,18 @@ static Arenas arenas_of(gbsa_mapper& m) {
     A.q_pos = m.qpos.as<uint64_t>();
     A.hits = m.hits.as<HitRec>();
     A.hit_cap = m.hit_cap;
-    A.nams = m.nams.as<gbsa_nam>();
+    A.nams = m.nams.as<NamState>();
     A.nam_cap = m.nam_cap;
     A.slots = m.slots.as<uint8_t>();
     A.slot_bytes = m.slot_bytes;
     A.ovf = m.ovf.as<uint8_t>();
     A.ovf_cap = m.ovf_cap;
+    const size_t per = m.lists.size() / 16;   // u32 entries per list
     A.rescue_list = m.lists.as<uint32_t>();
-    A.long_list = m.lists.as<uint32_t>() + (m.lists.size() / 8);
+    A.long_list = m.lists.as<uint32_t>() + per;
+    A.big_list = m.lists.as<uint32_t>() + 2 * per;
+    A.heavy_list = m.lists.as<uint32_t>() + 3 * per;
+    A.rescue_cycles = m.profile ? m.resc_cycles.as<uint64_t>() : nullptr;
     return A;
 }
 
@@ -273,7 +278,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
             retry = true;
         }
         if (h.status & kStatusNamOverflow) {
-            grow(m.nams, m.nam_cap, h.nam_used, sizeof(gbsa_nam));
+            grow(m.nams, m.nam_cap, h.nam_used, sizeof(NamState));
             retry = true;
         }
         if (h.status & kStatusScratchOverflow) {
@@ -635,7 +640,7 @@ int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, co
             GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, m->out_off.as<uint64_t>(), 8ull * (n + 1),
                                       cudaMemcpyDeviceToHost, st));
             m->out_nams.resize(sizeof(gbsa_nam) * (total + 1));
-            launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(),
+            launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(),
                                m->out_nams.as<gbsa_nam>(), m->out_frac.as<float>(), m->out_resc.as<uint8_t>(), st);
             if (frac) GBSA_CUDA(cudaMemcpyAsync(frac + b0, m->out_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, st));
             if (rescued)
@@ -666,7 +671,7 @@ int gbsa_map_reads_device(gbsa_mapper* m, const char* d_seqs, const uint64_t* d_
             GBSA_CUDA(cudaStreamSynchronize(st));
             throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
         }
-        launch_gather_nams(n_reads, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(), d_nams,
+        launch_gather_nams(n_reads, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(), d_nams,
                            d_frac, d_rescued, st);
     });
 }
@@ -734,7 +739,7 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries, const u
         m->cfg = saved;
         GBSA_CUDA(cudaMemcpyAsync(nam_offsets, m->out_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost, st));
         m->out_nams.resize(sizeof(gbsa_nam) * (total + 1));
-        launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<gbsa_nam>(), m->out_off.as<uint64_t>(),
+        launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(),
                            m->out_nams.as<gbsa_nam>(), m->out_frac.as<float>(), nullptr, st);
         if (frac) GBSA_CUDA(cudaMemcpyAsync(frac, m->out_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, st));
         if (total <= nam_capacity && total)
@@ -765,7 +770,17 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
     out[3] = m->last.n_rescue;
     out[4] = m->last.n_long;
     out[5] = m->last.scratch_used;
+    out[6] = m->last.n_big;
     return GBSA_OK;
+}
+
+int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out) {
+    return guarded([&] {
+        const uint32_t n = std::min<uint32_t>(cap, m->last.n_rescue);
+        *n_out = m->last.n_rescue;
+        if (m->profile && n && m->resc_cycles.size() >= 8ull * n)
+            GBSA_CUDA(cudaMemcpy(out, m->resc_cycles.as<void>(), 8ull * n, cudaMemcpyDeviceToHost));
+    });
 }
 
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n) {

@@ -36,7 +36,9 @@ struct Counters {
     unsigned int n_rescue;
     unsigned int n_long;
     unsigned int status;
-    unsigned int pad;
+    unsigned int n_big;    // reads merged by the warp-cooperative NAM kernel
+    unsigned int n_heavy;  // rescued reads handled by the block-per-read kernel
+    unsigned int pad2;
 };
 
 struct Arenas {
@@ -46,7 +48,7 @@ struct Arenas {
     uint64_t* q_pos;         // per query: index position of its hash (or kNotFound)
     HitRec* hits;
     uint64_t hit_cap;
-    gbsa_nam* nams;
+    NamState* nams;          // per read, sorted (converted to Nam records on output)
     uint64_t nam_cap;
     uint8_t* slots;          // per-warp scratch slots of the NAM / rescue kernels
     uint64_t slot_bytes;
@@ -54,6 +56,9 @@ struct Arenas {
     uint64_t ovf_cap;
     uint32_t* rescue_list;
     uint32_t* long_list;
+    uint32_t* big_list;
+    uint32_t* heavy_list;
+    uint64_t* rescue_cycles;   // optional: SM cycles spent on each rescued read
 };
 
 struct MapConfig {
@@ -88,7 +93,7 @@ void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* re
                  cudaStream_t st);
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
-void launch_gather_nams(uint32_t n, const ReadRec* rec, const gbsa_nam* arena, const uint64_t* out_off,
+void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
                         gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st);
 void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
                            gbsa_query_randstrobe* out, cudaStream_t st);

@@ -234,7 +234,7 @@ __device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* 
         warp_fail(R, ctr, kStatusNamOverflow);
         return;
     }
-    for (uint32_t t = lane; t < NN; t += 32) to_gbsa_nam(L.closed[keys[t].idx], (int)t, A.nams[noff + t]);
+    for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = L.closed[keys[t].idx];
     if (lane == 0) {
         R.nam_off = noff;
         R.n_nams = NN;
@@ -242,14 +242,154 @@ __device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* 
 }
 
 constexpr uint32_t kNamSmem = 64;   // reads with at most this many hits merge in shared memory
+constexpr uint32_t kLaneMaxHits = 160;
+constexpr uint32_t kLaneOpen = 10;   // open NAMs a lane keeps in shared memory
+constexpr int kLaneWarps = 4;
+
+__device__ __forceinline__ bool nam_key3_less(const NamKey& a, const NamKey& b) {
+    if (a.k1 != b.k1) return a.k1 < b.k1;
+    if (a.k2 != b.k2) return a.k2 < b.k2;
+    return a.k3 < b.k3;
+}
+
+// Open NAMs of the lanes of a block, one field per array ([slot][thread]) so that a
+// warp touching slot o reads 32 consecutive words.
+struct LaneOpen {
+    int32_t qs[kLaneOpen][32 * kLaneWarps], qe[kLaneOpen][32 * kLaneWarps], qprev[kLaneOpen][32 * kLaneWarps];
+    int32_t rs[kLaneOpen][32 * kLaneWarps], re[kLaneOpen][32 * kLaneWarps], rprev[kLaneOpen][32 * kLaneWarps];
+    int32_t nh[kLaneOpen][32 * kLaneWarps];
+    uint32_t ref[kLaneOpen][32 * kLaneWarps];
+    __device__ NamState get(uint32_t o, uint32_t t) const {
+        NamState n;
+        n.qs = qs[o][t];
+        n.qe = qe[o][t];
+        n.qprev = qprev[o][t];
+        n.rs = rs[o][t];
+        n.re = re[o][t];
+        n.rprev = rprev[o][t];
+        n.n_hits = nh[o][t];
+        n.ref_rc = ref[o][t];
+        return n;
+    }
+    __device__ void put(uint32_t o, uint32_t t, const NamState& n) {
+        qs[o][t] = n.qs;
+        qe[o][t] = n.qe;
+        qprev[o][t] = n.qprev;
+        rs[o][t] = n.rs;
+        re[o][t] = n.re;
+        rprev[o][t] = n.rprev;
+        nh[o][t] = n.n_hits;
+        ref[o][t] = n.ref_rc;
+    }
+};
+
+// find_nams merge with one lane per read, for reads with at most kLaneMaxHits hits
+// whose open-NAM list stays within kLaneOpen (the common case: one locus chain plus
+// scattered single hits).  Same hit-major rule as nam_merge_hit_major: hits in
+// (orientation, query_start, position) order, each joins the first open NAM in
+// creation order of its (orientation, ref id) that accepts it.  Open NAMs live in
+// shared memory; a NAM is closed (written to the read's slots in the NAM arena) when
+// the open list is full and the current query start has passed it, or at the end.
+// The read's NAMs are then insertion-sorted in place.  Reads that do not fit go to
+// the warp-cooperative kernel.
+__global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
+                                                               Arenas A, Counters* ctr) {
+    __shared__ LaneOpen S;
+    const uint32_t t = threadIdx.x;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        ReadRec& R = rec[r];
+        const uint32_t flags = R.flags;
+        const uint32_t H = R.n_hits;
+        if ((flags & (kReadFailed | kReadRescue)) || H == 0) continue;
+        if (H > kLaneMaxHits) {
+            A.big_list[atomicAdd(&ctr->n_big, 1u)] = r;
+            continue;
+        }
+        const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)H);
+        if (noff + H > A.nam_cap) {
+            R.flags = flags | kReadFailed;
+            atomicOr(&ctr->status, kStatusNamOverflow);
+            continue;
+        }
+        const HitRec* hits = A.hits + R.hit_off;
+        NamState* out = A.nams + noff;
+        uint32_t n_open = 0, n_closed = 0, cur_dir = 0;
+        bool overflow = false;
+        for (uint32_t i = 0; i < H; ++i) {
+            const HitRec x = hits[i];
+            const uint32_t dir = x.ref_rc >> 31;
+            if (dir != cur_dir) {   // the other orientation's NAMs can take no more hits
+                for (uint32_t o = 0; o < n_open; ++o) out[n_closed++] = S.get(o, t);
+                n_open = 0;
+                cur_dir = dir;
+            }
+            int found = -1;
+            for (uint32_t o = 0; o < n_open; ++o) {
+                if (S.ref[o][t] == x.ref_rc && S.qprev[o][t] < x.qs && x.qs <= S.qe[o][t] && S.rprev[o][t] < x.rs &&
+                    x.rs <= S.re[o][t]) {
+                    const bool ext = x.qe > S.qe[o][t] && x.re > S.re[o][t];
+                    if (ext || (x.qe <= S.qe[o][t] && x.re <= S.re[o][t])) {
+                        if (ext) {
+                            S.qe[o][t] = x.qe;
+                            S.re[o][t] = x.re;
+                        }
+                        S.qprev[o][t] = x.qs;
+                        S.rprev[o][t] = x.rs;
+                        S.nh[o][t] += 1;
+                        found = (int)o;
+                        break;
+                    }
+                }
+            }
+            if (found >= 0) continue;
+            if (n_open == kLaneOpen) {
+                // close NAMs the current query start has passed (order kept)
+                uint32_t k = 0;
+                for (uint32_t o = 0; o < n_open; ++o) {
+                    const NamState m = S.get(o, t);
+                    if (m.qe < x.qs) out[n_closed++] = m;
+                    else S.put(k++, t, m);
+                }
+                n_open = k;
+                if (n_open == kLaneOpen) {
+                    overflow = true;
+                    break;
+                }
+            }
+            S.put(n_open++, t, nam_from_hit(x));
+        }
+        if (overflow) {
+            A.big_list[atomicAdd(&ctr->n_big, 1u)] = r;
+            continue;
+        }
+        for (uint32_t o = 0; o < n_open; ++o) out[n_closed++] = S.get(o, t);
+        // insertion sort by the NAM order
+        for (uint32_t i = 1; i < n_closed; ++i) {
+            const NamState x = out[i];
+            const NamKey kx = nam_key(x, 0, C.sort_mode);
+            uint32_t j = i;
+            while (j > 0) {
+                const NamState y = out[j - 1];
+                if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
+                out[j] = y;
+                --j;
+            }
+            out[j] = x;
+        }
+        R.nam_off = noff;
+        R.n_nams = n_closed;
+    }
+}
 
 // find_nams after the lookup: the read's hits arrive in (orientation, query_start,
 // position) order, one query randstrobe after another; they are merged hit-major.
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
-                                                               Arenas A, Counters* ctr) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
+                                                               Counters* ctr) {
     __shared__ NamState s_lists[kWarpsPerBlock][2 * kNamSmem];
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
-    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+    const uint32_t n_big = *(volatile unsigned int*)&ctr->n_big;
+    for (uint32_t b = warp_global_id(); b < n_big; b += warp_count()) {
+        const uint32_t r = A.big_list[b];
         ReadRec& R = rec[r];
         if (R.flags & (kReadFailed | kReadRescue)) continue;
         const uint32_t H = R.n_hits;
@@ -308,14 +448,121 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, uint3
     }
 }
 
-// find_nams_rescue for the reads on the rescue list.
+// Phase 1 of find_nams_rescue for one read (warp): RescueHit{position, count, qs,
+// qe} of every found query of each orientation, sorted by (count, query_start) —
+// query_start is unique per orientation, so this is the reference's
+// (count, query_start, query_end) order (cmp1, step2/nam.cu:909-912); the prefix
+// taken until (count > rescue_cutoff && taken >= 5) || count > cap
+// (step2/nam.cu:960-969); re-sorted by query_start (cmp2).  rk/tk: 2 x Pq u64 each.
+// Returns the sum and the maximum of the run lengths of the taken ones.
+struct RescuePlan {
+    uint32_t m[2];
+    uint64_t bound;
+    uint32_t maxrun;
+};
+
+__device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, const Query* const* Qd,
+                                     const uint64_t* const* Pd, const uint32_t* nqd, uint32_t Pq, uint64_t* buf) {
+    const uint32_t lane = lane_id();
+    RescuePlan plan{};
+    uint64_t* rk[2] = {buf, buf + Pq};
+    uint64_t* tk[2] = {buf + 2 * Pq, buf + 3 * Pq};
+    for (int d = 0; d < 2; ++d) {
+        uint32_t nd = 0;
+        const uint32_t nq = nqd[d];
+        for (uint32_t base = 0; base < nq; base += 32) {
+            const uint32_t qi = base + lane;
+            bool f = false;
+            uint64_t key = 0;
+            if (qi < nq) {
+                const uint64_t pos = Pd[d][qi];
+                if (pos != kNotFound) {
+                    f = true;
+                    const uint32_t cnt = index_get_count(I, pos);
+                    key = ((uint64_t)cnt << 32) | ((uint64_t)Qd[d][qi].start << 16) | qi;
+                }
+            }
+            const uint32_t bm = __ballot_sync(0xFFFFFFFFu, f);
+            if (f) rk[d][nd + __popc(bm & lanemask_lt())] = key;
+            nd += __popc(bm);
+        }
+        __syncwarp();
+        warp_sort_u64(rk[d], nd);
+        uint32_t stop = nd;
+        for (uint32_t base = 0; base < nd; base += 32) {
+            const uint32_t j = base + lane;
+            bool brk = false;
+            if (j < nd) {
+                const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
+                brk = (cnt > C.rescue_cutoff && j >= 5) || cnt > C.count_cap;
+            }
+            const uint32_t bm = __ballot_sync(0xFFFFFFFFu, brk);
+            if (bm) {
+                stop = base + (__ffs(bm) - 1);
+                break;
+            }
+        }
+        plan.m[d] = stop;
+        uint64_t bsum = 0;
+        uint32_t bmax = 0;
+        for (uint32_t j = lane; j < stop; j += 32) {
+            const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
+            bsum += cnt;
+            bmax = cnt > bmax ? cnt : bmax;
+            tk[d][j] = rk[d][j] & 0xFFFFFFFFull;
+        }
+        plan.bound += warp_sum(bsum);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint32_t v = __shfl_xor_sync(0xFFFFFFFFu, bmax, o);
+            bmax = v > bmax ? v : bmax;
+        }
+        plan.maxrun = bmax > plan.maxrun ? bmax : plan.maxrun;
+        __syncwarp();
+        warp_sort_u64(tk[d], stop);
+    }
+    return plan;
+}
+
+// Phase 2 (warp): walk the runs of the taken rescue hits in (orientation,
+// query_start) order and merge them NAM-major; all NAMs end in L.closed.
+__device__ void rescue_merge(const IndexView& I, const Query* const* Qd, const uint64_t* const* Pd,
+                             const RescuePlan& plan, const uint64_t* tkbuf, uint32_t Pq, NamLists& L, HitRec* hb,
+                             uint8_t* tb) {
+    const uint64_t* tk[2] = {tkbuf + 2 * Pq, tkbuf + 3 * Pq};
+    for (int d = 0; d < 2; ++d) {
+        for (uint32_t j = 0; j < plan.m[d]; ++j) {
+            const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
+            const Query q = Qd[d][qi];
+            const uint32_t nh = warp_walk_run(I, (int)q.start, (int)q.end, Pd[d][qi], (uint32_t)d, hb, plan.maxrun);
+            nam_close_passed(L, (int)q.start);
+            nam_merge_nam_major(L, hb, nh, (int)q.start, tb);
+        }
+        nam_close_passed(L, 0x7FFFFFFF);
+    }
+}
+
+constexpr uint64_t kHeavyBound = 1024;   // rescued reads with more candidate hits go to k_rescue_heavy
+
+// find_nams_rescue for the reads on the rescue list (a warp per read).  Reads whose
+// taken rescue hits span more than kHeavyBound index entries are handed to
+// k_rescue_heavy.
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
                                                                  Arenas A, Counters* ctr) {
     const uint32_t lane = lane_id();
     const uint32_t n_rescue = *(volatile unsigned int*)&ctr->n_rescue;
     for (uint32_t t = warp_global_id(); t < n_rescue; t += warp_count()) {
+        const long long t_start = clock64();
         const uint32_t r = A.rescue_list[t];
         ReadRec& R = rec[r];
+        struct CycleNote {
+            const Arenas& A;
+            uint32_t t;
+            long long t0;
+            __device__ ~CycleNote() {
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[t] = (uint64_t)(clock64() - t0);
+            }
+        } note{A, t, t_start};
         const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
         const Query* Qd[2] = {A.q + R.q_off, A.q + R.q_off + R.nq};
         const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
@@ -327,81 +574,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
             warp_fail(R, ctr, kStatusScratchOverflow);
             continue;
         }
-        uint64_t* rk[2] = {reinterpret_cast<uint64_t*>(sc1), reinterpret_cast<uint64_t*>(sc1) + Pq};
-        uint64_t* tk[2] = {reinterpret_cast<uint64_t*>(sc1) + 2 * Pq, reinterpret_cast<uint64_t*>(sc1) + 3 * Pq};
-        uint32_t m[2];
-        uint64_t bound = 0;     // sum of run lengths of the taken rescue hits
-        uint32_t maxrun = 0;
-        for (int d = 0; d < 2; ++d) {
-            // RescueHit{position, count, qs, qe} of every found query, keyed by
-            // (count, query_start) — query_start is unique per orientation, so this is
-            // the reference's (count, query_start, query_end) order (cmp1, nam.cu:909-912)
-            uint32_t nd = 0;
-            const uint32_t nq = nqd[d];
-            for (uint32_t base = 0; base < nq; base += 32) {
-                const uint32_t qi = base + lane;
-                bool f = false;
-                uint64_t key = 0;
-                if (qi < nq) {
-                    const uint64_t pos = Pd[d][qi];
-                    if (pos != kNotFound) {
-                        f = true;
-                        const uint32_t cnt = index_get_count(I, pos);
-                        key = ((uint64_t)cnt << 32) | ((uint64_t)Qd[d][qi].start << 16) | qi;
-                    }
-                }
-                const uint32_t bm = __ballot_sync(0xFFFFFFFFu, f);
-                if (f) rk[d][nd + __popc(bm & lanemask_lt())] = key;
-                nd += __popc(bm);
-            }
-            __syncwarp();
-            warp_sort_u64(rk[d], nd);
-            // prefix until (count > rescue_cutoff && taken >= 5) or count > cap
-            // (step2/nam.cu:960-969)
-            uint32_t stop = nd;
-            for (uint32_t base = 0; base < nd; base += 32) {
-                const uint32_t j = base + lane;
-                bool brk = false;
-                if (j < nd) {
-                    const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
-                    brk = (cnt > C.rescue_cutoff && j >= 5) || cnt > C.count_cap;
-                }
-                const uint32_t bm = __ballot_sync(0xFFFFFFFFu, brk);
-                if (bm) {
-                    stop = base + (__ffs(bm) - 1);
-                    break;
-                }
-            }
-            m[d] = stop;
-            uint64_t bsum = 0;
-            uint32_t bmax = 0;
-            for (uint32_t j = lane; j < stop; j += 32) {
-                const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
-                bsum += cnt;
-                bmax = cnt > bmax ? cnt : bmax;
-                tk[d][j] = rk[d][j] & 0xFFFFFFFFull;   // re-sorted by query_start (cmp2)
-            }
-            bound += warp_sum(bsum);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const uint32_t v = __shfl_xor_sync(0xFFFFFFFFu, bmax, o);
-                bmax = v > bmax ? v : bmax;
-            }
-            maxrun = bmax > maxrun ? bmax : maxrun;
-            __syncwarp();
-            warp_sort_u64(tk[d], stop);
-        }
-        if (bound == 0) {
+        uint64_t* buf = reinterpret_cast<uint64_t*>(sc1);
+        const RescuePlan plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
+        if (plan.bound == 0) {
             if (lane == 0) R.n_nams = 0;
             continue;
         }
-        if (bound > 0xFFFFFFFull) {
-            warp_fail(R, ctr, kStatusScratchOverflow);
+        if (plan.bound > kHeavyBound) {
+            if (lane == 0) A.heavy_list[atomicAdd(&ctr->n_heavy, 1u)] = r;
             continue;
         }
-        const uint32_t H = (uint32_t)bound;
+        const uint32_t H = (uint32_t)plan.bound;
         const uint64_t P2 = next_pow2(H);
-        const uint64_t b2 = 64ull * H + 32ull * P2 + 20ull * maxrun + maxrun + 256;
+        const uint64_t b2 = 64ull * H + 32ull * P2 + 20ull * plan.maxrun + plan.maxrun + 256;
         uint8_t* sc2 = warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
         if (!sc2) {
             warp_fail(R, ctr, kStatusScratchOverflow);
@@ -412,32 +597,144 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         L.closed = L.open + H;
         NamKey* keys = reinterpret_cast<NamKey*>(L.closed + H);
         HitRec* hb = reinterpret_cast<HitRec*>(keys + P2);
-        uint8_t* tb = reinterpret_cast<uint8_t*>(hb + maxrun);
+        uint8_t* tb = reinterpret_cast<uint8_t*>(hb + plan.maxrun);
         L.n_open = L.n_closed = 0;
         L.cap = H;
-        for (int d = 0; d < 2; ++d) {
-            for (uint32_t j = 0; j < m[d]; ++j) {
-                const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
-                const Query q = Qd[d][qi];
-                const uint32_t nh = warp_walk_run(I, (int)q.start, (int)q.end, Pd[d][qi], (uint32_t)d, hb, maxrun);
-                nam_close_passed(L, (int)q.start);
-                nam_merge_nam_major(L, hb, nh, (int)q.start, tb);
-            }
-            nam_close_passed(L, 0x7FFFFFFF);
-        }
+        rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hb, tb);
         warp_finish_nams(C, L, keys, R, A, ctr);
         __syncwarp();
     }
 }
 
-__global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const gbsa_nam* __restrict__ arena,
+// Block bitonic sort of n keys (room for next_pow2(n)) by all threads of the block.
+__device__ void block_sort_keys(NamKey* keys, uint32_t n) {
+    const uint32_t P = next_pow2(n);
+    for (uint32_t i = n + threadIdx.x; i < P; i += blockDim.x) {
+        NamKey k;
+        k.k1 = k.k2 = k.k3 = ~0ULL;
+        k.idx = 0xFFFFFFFFu;
+        k.pad = 0;
+        keys[i] = k;
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const NamKey a = keys[i], b = keys[ixj];
+                    const bool up = (i & k) == 0;
+                    if (key_less(b, a) == up) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+constexpr uint32_t kHeavyThreads = 256;
+constexpr uint32_t kHeavyHits = 1024;   // hits of one query held in shared memory
+
+// Rescued reads with many candidate hits (typically reads inside short tandem
+// repeats, whose taken queries each occur hundreds of times): one block per read.
+// Warp 0 merges with the current query's hits in shared memory; the whole block
+// sorts the NAMs.
+__global__ void __launch_bounds__(kHeavyThreads) k_rescue_heavy(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
+                                                                 Arenas A, Counters* ctr) {
+    __shared__ HitRec s_hits[kHeavyHits];
+    __shared__ uint8_t s_taken[kHeavyHits];
+    __shared__ uint64_t s_ptr[4];
+    __shared__ uint32_t s_nn;
+    const uint32_t lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_heavy;
+    for (uint32_t h = blockIdx.x; h < n_heavy; h += gridDim.x) {
+        const uint32_t r = A.heavy_list[h];
+        ReadRec& R = rec[r];
+        const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
+        const Query* Qd[2] = {A.q + R.q_off, A.q + R.q_off + R.nq};
+        const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
+        const uint32_t nqm = nqd[0] > nqd[1] ? nqd[0] : nqd[1];
+        const uint32_t Pq = next_pow2(nqm > 0 ? nqm : 1);
+        if (wid == 0) {
+            const uint64_t b1 = 4ull * 8 * Pq + 64;
+            const uint64_t o1 = warp_bump(&ctr->scratch_used, (b1 + 255) & ~255ull);
+            uint64_t* buf = (o1 + b1 <= A.ovf_cap) ? reinterpret_cast<uint64_t*>(A.ovf + o1) : nullptr;
+            uint8_t* sc2 = nullptr;
+            RescuePlan plan{};
+            uint64_t P2 = 0;
+            if (buf) {
+                plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
+                const uint32_t H = (uint32_t)plan.bound;
+                P2 = next_pow2(H);
+                // a query's hits stay in shared memory unless a run is longer than kHeavyHits
+                const uint64_t bh = plan.maxrun > kHeavyHits ? 21ull * plan.maxrun + 64 : 0;
+                const uint64_t b2 = 64ull * H + 32ull * P2 + bh + 256;
+                const uint64_t o2 = warp_bump(&ctr->scratch_used, (b2 + 255) & ~255ull);
+                if (plan.bound <= 0xFFFFFFFull && o2 + b2 <= A.ovf_cap) sc2 = A.ovf + o2;
+            }
+            if (!sc2) {
+                warp_fail(R, ctr, kStatusScratchOverflow);
+                if (lane == 0) s_ptr[0] = 0;
+            } else {
+                const uint32_t H = (uint32_t)plan.bound;
+                NamLists L;
+                L.open = reinterpret_cast<NamState*>(sc2);
+                L.closed = L.open + H;
+                L.n_open = L.n_closed = 0;
+                L.cap = H;
+                HitRec* hb = s_hits;
+                uint8_t* tb = s_taken;
+                if (plan.maxrun > kHeavyHits) {
+                    hb = reinterpret_cast<HitRec*>(reinterpret_cast<NamKey*>(L.closed + H) + P2);
+                    tb = reinterpret_cast<uint8_t*>(hb + plan.maxrun);
+                }
+                rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hb, tb);
+                if (lane == 0) {
+                    s_ptr[0] = reinterpret_cast<uint64_t>(L.closed);
+                    s_ptr[1] = reinterpret_cast<uint64_t>(L.closed + H);   // keys
+                    s_nn = L.n_closed;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_ptr[0]) {
+            const NamState* closed = reinterpret_cast<const NamState*>(s_ptr[0]);
+            NamKey* keys = reinterpret_cast<NamKey*>(s_ptr[1]);
+            const uint32_t NN = s_nn;
+            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) keys[i] = nam_key(closed[i], i, C.sort_mode);
+            __syncthreads();
+            block_sort_keys(keys, NN);
+            if (wid == 0) {
+                const uint64_t noff = warp_bump(&ctr->nam_used, NN);
+                if (lane == 0) s_ptr[2] = noff;
+                if (noff + NN > A.nam_cap) {
+                    warp_fail(R, ctr, kStatusNamOverflow);
+                    if (lane == 0) s_ptr[2] = ~0ULL;
+                } else if (lane == 0) {
+                    R.nam_off = noff;
+                    R.n_nams = NN;
+                }
+            }
+            __syncthreads();
+            const uint64_t noff = s_ptr[2];
+            if (noff != ~0ULL)
+                for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) A.nams[noff + i] = closed[keys[i].idx];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const NamState* __restrict__ arena,
                               const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, float* frac,
                               uint8_t* rescued) {
     const uint32_t lane = lane_id();
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
         const ReadRec R = rec[r];
         const uint64_t o = out_off[r];
-        for (uint32_t j = lane; j < R.n_nams; j += 32) out[o + j] = arena[R.nam_off + j];
+        for (uint32_t j = lane; j < R.n_nams; j += 32) to_gbsa_nam(arena[R.nam_off + j], (int)j, out[o + j]);
         if (lane == 0) {
             if (frac) frac[r] = R.frac;
             if (rescued) rescued[r] = (R.flags & kReadRescue) ? 1 : 0;
@@ -528,7 +825,10 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
-    k_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(C, n, rec, A, ctr);
+    k_nams_lane<<<grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * 5), 32 * kLaneWarps, 0, st>>>(C, n, rec,
+                                                                                                        A, ctr);
+    GBSA_LAUNCHED();
+    k_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
@@ -537,9 +837,11 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
     if (!n_reads) return;
     k_rescue<<<warp_grid(n_reads, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
     GBSA_LAUNCHED();
+    k_rescue_heavy<<<(unsigned)device_sm_count() * 4, kHeavyThreads, 0, st>>>(I, C, rec, A, ctr);
+    GBSA_LAUNCHED();
 }
 
-void launch_gather_nams(uint32_t n, const ReadRec* rec, const gbsa_nam* arena, const uint64_t* out_off,
+void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
                         gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st) {
     if (!n) return;
     k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out, frac,

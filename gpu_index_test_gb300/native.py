@@ -65,6 +65,7 @@ def lib():
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
             "gbsa_randstrobes_query_noalloc": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64), vp]),
+            "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, C.POINTER(u32)]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -224,9 +225,16 @@ class Mapper:
         _check(lib().gbsa_mapper_set_profile(self.h, 1 if on else 0))
 
     def last_counts(self):
-        a = np.zeros(6, np.uint64)
+        a = np.zeros(7, np.uint64)
         lib().gbsa_mapper_last_counts(self.h, a.ctypes.data)
-        return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes"), (int(x) for x in a)))
+        return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes", "warp_nam_reads"),
+                        (int(x) for x in a)))
+
+    def rescue_cycles(self, cap=1 << 22):
+        a = np.zeros(cap, np.uint64)
+        n = C.c_uint32()
+        _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, C.byref(n)))
+        return a[: min(cap, n.value)]
 
     def stage_ms(self):
         a = np.zeros(5, np.float32)

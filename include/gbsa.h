@@ -245,8 +245,13 @@ int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
 /* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
  * path, [2] NAMs, [3] rescued reads, [4] reads seeded by the long-read kernel,
- * [5] overflow scratch bytes.  No reference counterpart. */
+ * [5] overflow scratch bytes, [6] reads merged by the warp-cooperative NAM kernel.
+ * out must hold 7 values.  No reference counterpart. */
 int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
+/* With profiling on: SM clock cycles the rescue kernel spent on each rescued read of
+ * the last batch (up to cap values); *n_out receives the number of rescued reads.
+ * No reference counterpart. */
+int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out);
 
 #ifdef __cplusplus
 }
