@@ -293,15 +293,25 @@ def main():
         torch.distributed.barrier()
     launches = native.launch_count() - l0
     clocks = sampler.stop()
-    rc_cyc = m.rescue_cycles()
+    warp_cyc, heavy_cyc = m.rescue_cycles()
     m.set_profile(False)
-    rescue_profile = None
-    if len(rc_cyc):
-        mhz = clocks.get("sm_mhz") or 2000.0
-        us = np.sort(rc_cyc.astype(np.float64)) / mhz
-        rescue_profile = {"reads": int(len(us)), "us_p50": round(float(us[len(us) // 2]), 1),
-                          "us_p99": round(float(us[int(len(us) * 0.99)]), 1), "us_max": round(float(us[-1]), 1),
-                          "us_sum": round(float(us.sum()), 1)}
+    mhz = clocks.get("sm_mhz") or 2000.0
+
+    def cyc_stats(a):
+        if not len(a):
+            return None
+        us = np.sort(a.astype(np.float64)) / mhz
+        return {"n": int(len(us)), "p50": round(float(us[len(us) // 2]), 1),
+                "p99": round(float(us[int(len(us) * 0.99)]), 1), "max": round(float(us[-1]), 1),
+                "sum": round(float(us.sum()), 1)}
+
+    rescue_profile = {
+        "warp_total_us": cyc_stats(warp_cyc[:, 0]) if len(warp_cyc) else None,
+        "warp_plan_us": cyc_stats(warp_cyc[:, 1]) if len(warp_cyc) else None,
+        "warp_merge_us": cyc_stats(warp_cyc[:, 2]) if len(warp_cyc) else None,
+        "warp_sort_us": cyc_stats(warp_cyc[:, 3]) if len(warp_cyc) else None,
+        "block_sorted_reads": int(len(heavy_cyc)),
+    }
     ms = ev0.elapsed_time(ev1) / args.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -366,6 +376,7 @@ def main():
         "lookup": alg_lookup + 16 * q + 8 * q + 20 * hits,  # probes + queries in + positions + hits out
         "nams": 20 * hits + 44 * nams_n,                 # hits in, NAMs out
         "rescue": 0,
+        "rescue_sort": 0,
     }
     peak, peak_kind = peaks()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0

@@ -133,7 +133,7 @@ struct gbsa_mapper {
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
-        out_off, out_nams, out_frac, out_resc, resc_cycles;
+        out_off, out_nams, out_frac, out_resc, resc_cycles, jobs;
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
@@ -153,12 +153,13 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     m.lens.resize(4ull * (n + 1));
     m.rec.resize(sizeof(ReadRec) * (n + 1));
     m.lists.resize(16ull * (n + 1));
+    m.jobs.resize(sizeof(SortJob) * (n + 1));
     m.ctr.resize(sizeof(Counters));
     m.cnt.resize(8ull * (n + 1));
     m.out_off.resize(8ull * (n + 1));
     m.out_frac.resize(4ull * (n + 1));
     m.out_resc.resize(n + 1);
-    if (m.profile) m.resc_cycles.resize(8ull * (n + 1));
+    if (m.profile) m.resc_cycles.resize(64ull * (n + 1));
     // query randstrobes: ~2 per 5 bases plus slack
     const uint64_t q_need = std::max<uint64_t>(4096, bases / 2 + 64ull * n / 8);
     if (m.q_cap < q_need) {
@@ -206,7 +207,7 @@ static Arenas arenas_of(gbsa_mapper& m) {
     A.rescue_list = m.lists.as<uint32_t>();
     A.long_list = m.lists.as<uint32_t>() + per;
     A.big_list = m.lists.as<uint32_t>() + 2 * per;
-    A.heavy_list = m.lists.as<uint32_t>() + 3 * per;
+    A.sort_jobs = m.jobs.as<SortJob>();
     A.rescue_cycles = m.profile ? m.resc_cycles.as<uint64_t>() : nullptr;
     return A;
 }
@@ -236,6 +237,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
             launch_reset_recs(n, m.rec.as<ReadRec>(), st);
         }
         Arenas A = arenas_of(m);
+        if (A.rescue_cycles) GBSA_CUDA(cudaMemsetAsync(A.rescue_cycles, 0, m.resc_cycles.size(), st));
         MapConfig C = m.cfg;
         C.count_bytes = m.count_bytes;
         auto mark = [&](int i) {
@@ -254,11 +256,13 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         mark(4);
         launch_rescue(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
         mark(5);
+        if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), A, ctr, st);
+        mark(6);
         Counters h{};
         GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
         GBSA_CUDA(cudaStreamSynchronize(st));
         if (m.profile)
-            for (int i = 0; i < 5; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[i], m.ev[i + 1]));
+            for (int i = 0; i < 6; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[i], m.ev[i + 1]));
         if (h.status & kStatusReadTooLong)
             throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
         if (h.status & kStatusSyncmerOverflow)
@@ -776,15 +780,17 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
 
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out) {
     return guarded([&] {
-        const uint32_t n = std::min<uint32_t>(cap, m->last.n_rescue);
-        *n_out = m->last.n_rescue;
-        if (m->profile && n && m->resc_cycles.size() >= 8ull * n)
-            GBSA_CUDA(cudaMemcpy(out, m->resc_cycles.as<void>(), 8ull * n, cudaMemcpyDeviceToHost));
+        const uint32_t total = m->last.n_rescue + m->last.n_heavy;
+        const uint32_t n = std::min<uint32_t>(cap / 4, total);
+        n_out[0] = m->last.n_rescue;
+        n_out[1] = m->last.n_heavy;
+        if (m->profile && n && m->resc_cycles.size() >= 32ull * n)
+            GBSA_CUDA(cudaMemcpy(out, m->resc_cycles.as<void>(), 32ull * n, cudaMemcpyDeviceToHost));
     });
 }
 
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n) {
-    for (int i = 0; i < n && i < 5; ++i) ms[i] = m->stage_ms[i];
+    for (int i = 0; i < n && i < 6; ++i) ms[i] = m->stage_ms[i];
     return GBSA_OK;
 }
 

@@ -37,8 +37,16 @@ struct Counters {
     unsigned int n_long;
     unsigned int status;
     unsigned int n_big;    // reads merged by the warp-cooperative NAM kernel
-    unsigned int n_heavy;  // rescued reads handled by the block-per-read kernel
+    unsigned int n_heavy;  // rescued reads whose NAMs the block-per-read sort kernel orders
     unsigned int pad2;
+};
+
+// A read whose NAMs are sorted by the block-per-read sort kernel.
+struct SortJob {
+    NamState* closed;   // its NAMs (unsorted)
+    NamKey* keys;       // room for next_pow2(n) sort keys
+    uint32_t n;
+    uint32_t read;
 };
 
 struct Arenas {
@@ -57,7 +65,7 @@ struct Arenas {
     uint32_t* rescue_list;
     uint32_t* long_list;
     uint32_t* big_list;
-    uint32_t* heavy_list;
+    SortJob* sort_jobs;
     uint64_t* rescue_cycles;   // optional: SM cycles spent on each rescued read
 };
 
@@ -93,6 +101,7 @@ void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* re
                  cudaStream_t st);
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
+void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
                         gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st);
 void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,

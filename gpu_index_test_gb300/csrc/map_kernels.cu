@@ -525,31 +525,44 @@ __device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, con
 }
 
 // Phase 2 (warp): walk the runs of the taken rescue hits in (orientation,
-// query_start) order and merge them NAM-major; all NAMs end in L.closed.
+// query_start) order and merge them NAM-major; all NAMs end in L.closed.  The hits
+// of the current query are held in compact form in hrs/hpk/tb (room for
+// plan.maxrun hits).
 __device__ void rescue_merge(const IndexView& I, const Query* const* Qd, const uint64_t* const* Pd,
-                             const RescuePlan& plan, const uint64_t* tkbuf, uint32_t Pq, NamLists& L, HitRec* hb,
-                             uint8_t* tb) {
+                             const RescuePlan& plan, const uint64_t* tkbuf, uint32_t Pq, NamLists& L, uint32_t* hrs,
+                             uint32_t* hpk, uint8_t* tb) {
     const uint64_t* tk[2] = {tkbuf + 2 * Pq, tkbuf + 3 * Pq};
     for (int d = 0; d < 2; ++d) {
         for (uint32_t j = 0; j < plan.m[d]; ++j) {
             const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
             const Query q = Qd[d][qi];
-            const uint32_t nh = warp_walk_run(I, (int)q.start, (int)q.end, Pd[d][qi], (uint32_t)d, hb, plan.maxrun);
-            nam_close_passed(L, (int)q.start);
-            nam_merge_nam_major(L, hb, nh, (int)q.start, tb);
+            QueryHits Q;
+            Q.rs = hrs;
+            Q.packed = hpk;
+            Q.qs = (int)q.start;
+            Q.qe = (int)q.end;
+            Q.dir = (uint32_t)d;
+            Q.k = I.k;
+            Q.n = warp_walk_run_q(I, Q.qs, Q.qe, Pd[d][qi], hrs, hpk, plan.maxrun);
+            nam_close_passed(L, Q.qs);
+            nam_merge_nam_major_q(L, Q, tb);
         }
         nam_close_passed(L, 0x7FFFFFFF);
     }
 }
 
-constexpr uint64_t kHeavyBound = 1024;   // rescued reads with more candidate hits go to k_rescue_heavy
+constexpr uint32_t kWarpSortMax = 256;   // rescued reads with more NAMs are sorted by k_sort_jobs
 
-// find_nams_rescue for the reads on the rescue list (a warp per read).  Reads whose
-// taken rescue hits span more than kHeavyBound index entries are handed to
-// k_rescue_heavy.
+// find_nams_rescue for the reads on the rescue list (a warp per read).  Reads that
+// end with more than kWarpSortMax NAMs leave the sort to k_sort_jobs.
+constexpr uint32_t kRescueSmemHits = 1024;   // per-warp shared buffer for one query's hits
+
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
                                                                  Arenas A, Counters* ctr) {
-    const uint32_t lane = lane_id();
+    __shared__ uint32_t s_hrs[kWarpsPerBlock][kRescueSmemHits];
+    __shared__ uint32_t s_hpk[kWarpsPerBlock][kRescueSmemHits];
+    __shared__ uint8_t s_tb[kWarpsPerBlock][kRescueSmemHits];
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t n_rescue = *(volatile unsigned int*)&ctr->n_rescue;
     for (uint32_t t = warp_global_id(); t < n_rescue; t += warp_count()) {
         const long long t_start = clock64();
@@ -560,7 +573,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
             uint32_t t;
             long long t0;
             __device__ ~CycleNote() {
-                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[t] = (uint64_t)(clock64() - t0);
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[4ull * t] = (uint64_t)(clock64() - t0);
+            }
+            __device__ void phase(int k, long long since) const {
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[4ull * t + k] = (uint64_t)(clock64() - since);
             }
         } note{A, t, t_start};
         const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
@@ -576,17 +592,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         }
         uint64_t* buf = reinterpret_cast<uint64_t*>(sc1);
         const RescuePlan plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
+        note.phase(1, t_start);
         if (plan.bound == 0) {
             if (lane == 0) R.n_nams = 0;
             continue;
         }
-        if (plan.bound > kHeavyBound) {
-            if (lane == 0) A.heavy_list[atomicAdd(&ctr->n_heavy, 1u)] = r;
-            continue;
-        }
         const uint32_t H = (uint32_t)plan.bound;
         const uint64_t P2 = next_pow2(H);
-        const uint64_t b2 = 64ull * H + 32ull * P2 + 20ull * plan.maxrun + plan.maxrun + 256;
+        const bool big_run = plan.maxrun > kRescueSmemHits;
+        const uint64_t b2 = 64ull * H + 32ull * P2 + (big_run ? 9ull * plan.maxrun + 64 : 0) + 256;
         uint8_t* sc2 = warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
         if (!sc2) {
             warp_fail(R, ctr, kStatusScratchOverflow);
@@ -596,18 +610,58 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         L.open = reinterpret_cast<NamState*>(sc2);
         L.closed = L.open + H;
         NamKey* keys = reinterpret_cast<NamKey*>(L.closed + H);
-        HitRec* hb = reinterpret_cast<HitRec*>(keys + P2);
-        uint8_t* tb = reinterpret_cast<uint8_t*>(hb + plan.maxrun);
+        uint32_t* hrs = s_hrs[w];
+        uint32_t* hpk = s_hpk[w];
+        uint8_t* tb = s_tb[w];
+        if (big_run) {
+            hrs = reinterpret_cast<uint32_t*>(keys + P2);
+            hpk = hrs + plan.maxrun;
+            tb = reinterpret_cast<uint8_t*>(hpk + plan.maxrun);
+        }
         L.n_open = L.n_closed = 0;
         L.cap = H;
-        rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hb, tb);
+        const long long t_merge = clock64();
+        rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hrs, hpk, tb);
+        note.phase(2, t_merge);
+        if (L.n_closed > kWarpSortMax) {
+            // many NAMs: the block-per-read sort kernel orders them
+            if (lane == 0) {
+                const uint32_t j = atomicAdd(&ctr->n_heavy, 1u);
+                SortJob job;
+                job.closed = L.closed;
+                job.keys = keys;
+                job.n = L.n_closed;
+                job.read = r;
+                A.sort_jobs[j] = job;
+            }
+            continue;
+        }
+        const long long t_fin = clock64();
         warp_finish_nams(C, L, keys, R, A, ctr);
+        note.phase(3, t_fin);
         __syncwarp();
     }
 }
 
-// Block bitonic sort of n keys (room for next_pow2(n)) by all threads of the block.
-__device__ void block_sort_keys(NamKey* keys, uint32_t n) {
+constexpr uint32_t kSortTile = 2048;   // keys per shared-memory tile of the block sort
+
+__device__ __forceinline__ void cmp_swap(NamKey* keys, uint32_t i, uint32_t j, uint32_t k) {
+    const uint32_t ixj = i ^ j;
+    if (ixj > i) {
+        const NamKey a = keys[i], b = keys[ixj];
+        const bool up = (i & k) == 0;
+        if (key_less(b, a) == up) {
+            keys[i] = b;
+            keys[ixj] = a;
+        }
+    }
+}
+
+// Block bitonic sort of n keys (room for next_pow2(n) in global memory) by all
+// threads of the block.  Every stage whose partner distance is below kSortTile runs
+// on a shared-memory tile of kSortTile keys (tile[] has kSortTile entries); only the
+// stages with larger distances touch global memory.
+__device__ void block_sort_keys(NamKey* keys, uint32_t n, NamKey* tile) {
     const uint32_t P = next_pow2(n);
     for (uint32_t i = n + threadIdx.x; i < P; i += blockDim.x) {
         NamKey k;
@@ -617,112 +671,80 @@ __device__ void block_sort_keys(NamKey* keys, uint32_t n) {
         keys[i] = k;
     }
     __syncthreads();
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const NamKey a = keys[i], b = keys[ixj];
-                    const bool up = (i & k) == 0;
-                    if (key_less(b, a) == up) {
-                        keys[i] = b;
-                        keys[ixj] = a;
+    const uint32_t T = P < kSortTile ? P : kSortTile;
+    // Runs all stages (k, j) with j < T inside each tile; k is the current merge size
+    // (k <= T: the tile-local sort from scratch; k > T: finish merge level k).
+    auto tile_pass = [&](uint32_t k_from, uint32_t k_to, uint32_t j_from) {
+        for (uint32_t t0 = 0; t0 < P; t0 += T) {
+            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) tile[i] = keys[t0 + i];
+            __syncthreads();
+            for (uint32_t k = k_from; k <= k_to; k <<= 1) {
+                for (uint32_t j = (k == k_from ? j_from : k >> 1); j > 0; j >>= 1) {
+                    for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
+                        // direction uses the global index
+                        const uint32_t gi = t0 + i, ixj = i ^ j;
+                        if (ixj > i) {
+                            const NamKey a = tile[i], b = tile[ixj];
+                            const bool up = (gi & k) == 0;
+                            if (key_less(b, a) == up) {
+                                tile[i] = b;
+                                tile[ixj] = a;
+                            }
+                        }
                     }
+                    __syncthreads();
                 }
             }
+            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) keys[t0 + i] = tile[i];
             __syncthreads();
         }
+    };
+    tile_pass(2, T, 1);
+    for (uint32_t k = 2 * T; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j >= T; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) cmp_swap(keys, i, j, k);
+            __syncthreads();
+        }
+        tile_pass(k, k, T >> 1);
     }
 }
 
-constexpr uint32_t kHeavyThreads = 256;
-constexpr uint32_t kHeavyHits = 1024;   // hits of one query held in shared memory
+constexpr uint32_t kSortThreads = 256;
 
-// Rescued reads with many candidate hits (typically reads inside short tandem
-// repeats, whose taken queries each occur hundreds of times): one block per read.
-// Warp 0 merges with the current query's hits in shared memory; the whole block
-// sorts the NAMs.
-__global__ void __launch_bounds__(kHeavyThreads) k_rescue_heavy(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
-                                                                 Arenas A, Counters* ctr) {
-    __shared__ HitRec s_hits[kHeavyHits];
-    __shared__ uint8_t s_taken[kHeavyHits];
-    __shared__ uint64_t s_ptr[4];
-    __shared__ uint32_t s_nn;
-    const uint32_t lane = lane_id(), wid = threadIdx.x >> 5;
-    const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_heavy;
-    for (uint32_t h = blockIdx.x; h < n_heavy; h += gridDim.x) {
-        const uint32_t r = A.heavy_list[h];
-        ReadRec& R = rec[r];
-        const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
-        const Query* Qd[2] = {A.q + R.q_off, A.q + R.q_off + R.nq};
-        const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
-        const uint32_t nqm = nqd[0] > nqd[1] ? nqd[0] : nqd[1];
-        const uint32_t Pq = next_pow2(nqm > 0 ? nqm : 1);
-        if (wid == 0) {
-            const uint64_t b1 = 4ull * 8 * Pq + 64;
-            const uint64_t o1 = warp_bump(&ctr->scratch_used, (b1 + 255) & ~255ull);
-            uint64_t* buf = (o1 + b1 <= A.ovf_cap) ? reinterpret_cast<uint64_t*>(A.ovf + o1) : nullptr;
-            uint8_t* sc2 = nullptr;
-            RescuePlan plan{};
-            uint64_t P2 = 0;
-            if (buf) {
-                plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
-                const uint32_t H = (uint32_t)plan.bound;
-                P2 = next_pow2(H);
-                // a query's hits stay in shared memory unless a run is longer than kHeavyHits
-                const uint64_t bh = plan.maxrun > kHeavyHits ? 21ull * plan.maxrun + 64 : 0;
-                const uint64_t b2 = 64ull * H + 32ull * P2 + bh + 256;
-                const uint64_t o2 = warp_bump(&ctr->scratch_used, (b2 + 255) & ~255ull);
-                if (plan.bound <= 0xFFFFFFFull && o2 + b2 <= A.ovf_cap) sc2 = A.ovf + o2;
-            }
-            if (!sc2) {
-                warp_fail(R, ctr, kStatusScratchOverflow);
-                if (lane == 0) s_ptr[0] = 0;
+// Sorts the NAMs of the rescued reads with more than kWarpSortMax NAMs (typically
+// reads inside short tandem repeats, with hundreds to thousands of NAMs): one block
+// per read, bitonic sort tiled through shared memory, then the read's NAMs are
+// written to the NAM arena in order.
+__global__ void __launch_bounds__(kSortThreads) k_sort_jobs(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
+                                                              Counters* ctr) {
+    extern __shared__ __align__(16) uint8_t s_dyn[];   // kSortTile sort keys
+    __shared__ uint64_t s_noff;
+    NamKey* s_tile = reinterpret_cast<NamKey*>(s_dyn);
+    const uint32_t n_jobs = *(volatile unsigned int*)&ctr->n_heavy;
+    for (uint32_t h = blockIdx.x; h < n_jobs; h += gridDim.x) {
+        const SortJob job = A.sort_jobs[h];
+        ReadRec& R = rec[job.read];
+        const NamState* closed = job.closed;
+        const uint32_t NN = job.n;
+        for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) job.keys[i] = nam_key(closed[i], i, C.sort_mode);
+        __syncthreads();
+        block_sort_keys(job.keys, NN, s_tile);
+        if (threadIdx.x == 0) {
+            const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)NN);
+            if (noff + NN > A.nam_cap) {
+                R.flags |= kReadFailed;
+                atomicOr(&ctr->status, kStatusNamOverflow);
+                s_noff = ~0ULL;
             } else {
-                const uint32_t H = (uint32_t)plan.bound;
-                NamLists L;
-                L.open = reinterpret_cast<NamState*>(sc2);
-                L.closed = L.open + H;
-                L.n_open = L.n_closed = 0;
-                L.cap = H;
-                HitRec* hb = s_hits;
-                uint8_t* tb = s_taken;
-                if (plan.maxrun > kHeavyHits) {
-                    hb = reinterpret_cast<HitRec*>(reinterpret_cast<NamKey*>(L.closed + H) + P2);
-                    tb = reinterpret_cast<uint8_t*>(hb + plan.maxrun);
-                }
-                rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hb, tb);
-                if (lane == 0) {
-                    s_ptr[0] = reinterpret_cast<uint64_t>(L.closed);
-                    s_ptr[1] = reinterpret_cast<uint64_t>(L.closed + H);   // keys
-                    s_nn = L.n_closed;
-                }
+                R.nam_off = noff;
+                R.n_nams = NN;
+                s_noff = noff;
             }
         }
         __syncthreads();
-        if (s_ptr[0]) {
-            const NamState* closed = reinterpret_cast<const NamState*>(s_ptr[0]);
-            NamKey* keys = reinterpret_cast<NamKey*>(s_ptr[1]);
-            const uint32_t NN = s_nn;
-            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) keys[i] = nam_key(closed[i], i, C.sort_mode);
-            __syncthreads();
-            block_sort_keys(keys, NN);
-            if (wid == 0) {
-                const uint64_t noff = warp_bump(&ctr->nam_used, NN);
-                if (lane == 0) s_ptr[2] = noff;
-                if (noff + NN > A.nam_cap) {
-                    warp_fail(R, ctr, kStatusNamOverflow);
-                    if (lane == 0) s_ptr[2] = ~0ULL;
-                } else if (lane == 0) {
-                    R.nam_off = noff;
-                    R.n_nams = NN;
-                }
-            }
-            __syncthreads();
-            const uint64_t noff = s_ptr[2];
-            if (noff != ~0ULL)
-                for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) A.nams[noff + i] = closed[keys[i].idx];
-        }
+        const uint64_t noff = s_noff;
+        if (noff != ~0ULL)
+            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) A.nams[noff + i] = closed[job.keys[i].idx];
         __syncthreads();
     }
 }
@@ -837,7 +859,16 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
     if (!n_reads) return;
     k_rescue<<<warp_grid(n_reads, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
     GBSA_LAUNCHED();
-    k_rescue_heavy<<<(unsigned)device_sm_count() * 4, kHeavyThreads, 0, st>>>(I, C, rec, A, ctr);
+}
+
+void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kSortTile * sizeof(NamKey))));
+        attr = true;
+    }
+    k_sort_jobs<<<(unsigned)device_sm_count() * 3, kSortThreads, kSortTile * sizeof(NamKey), st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

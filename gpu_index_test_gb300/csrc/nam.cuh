@@ -126,6 +126,151 @@ __device__ __forceinline__ void nam_merge_hit_major(NamLists& L, const HitRec* h
     }
 }
 
+// Hits of one query randstrobe in compact form: they share query_start, query_end
+// and orientation, so each hit is its ref_start and (ref id << 8 | ref span - k's
+// offset), i.e. the RefRandstrobe position and packed word.
+struct QueryHits {
+    const uint32_t* rs;
+    const uint32_t* packed;
+    uint32_t n;
+    int qs, qe;
+    uint32_t dir;
+    int k;
+    __device__ HitRec get(uint32_t j) const {
+        HitRec h;
+        h.ref_rc = (dir << 31) | (packed[j] >> 8);
+        h.qs = qs;
+        h.qe = qe;
+        h.rs = (int)rs[j];
+        h.re = (int)rs[j] + (int)(packed[j] & 0xFF) + k;
+        return h;
+    }
+};
+
+// First untaken hit of the query (sorted by rs) that NAM n would take, or -1.
+__device__ __forceinline__ int nam_candidate_q(const NamState& n, const QueryHits& Q, const uint8_t* taken) {
+    uint32_t lo = 0, hi = Q.n;
+    const int from = n.rprev + 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((int)Q.rs[mid] < from) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint32_t want = n.ref_rc & 0x7FFFFFFFu;
+    for (uint32_t j = lo; j < Q.n; ++j) {
+        const int rs = (int)Q.rs[j];
+        if (rs > n.re) break;
+        if ((Q.packed[j] >> 8) != want || taken[j]) continue;
+        const int re = rs + (int)(Q.packed[j] & 0xFF) + Q.k;
+        if ((Q.qe > n.qe && re > n.re) || (Q.qe <= n.qe && re <= n.re)) return (int)j;
+    }
+    return -1;
+}
+
+// NAM-major merge of one query's hits in compact form (same rule as
+// nam_merge_nam_major).  taken: Q.n bytes of scratch.
+__device__ __forceinline__ void nam_merge_nam_major_q(NamLists& L, const QueryHits& Q, uint8_t* taken) {
+    const uint32_t lane = lane_id();
+    const uint32_t nh = Q.n;
+    for (uint32_t j = lane; j < nh; j += 32) taken[j] = 0;
+    __syncwarp();
+    const uint32_t nn = L.n_open;
+    const uint32_t dirbit = Q.dir << 31;
+    for (uint32_t base = 0; base < nn; base += 32) {
+        const uint32_t o = base + lane;
+        NamState mine;
+        bool resolved = true;
+        if (o < nn) {
+            mine = L.open[o];
+            resolved = mine.qe < Q.qs || (mine.ref_rc & 0x80000000u) != dirbit;
+        }
+        bool dirty = false;
+        for (;;) {
+            int cand = -1;
+            if (!resolved) cand = nam_candidate_q(mine, Q, taken);
+            const uint32_t key = cand < 0 ? 0xFFFFFFFFu : (uint32_t)cand;
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+            const bool clash = cand >= 0 && (peers & lanemask_lt()) != 0;
+            const uint32_t cm = __ballot_sync(0xFFFFFFFFu, clash);
+            const uint32_t lim = cm ? (uint32_t)(__ffs(cm) - 1) : 32u;
+            if (!resolved && lane < lim) {
+                if (cand >= 0) {
+                    taken[cand] = 1;
+                    nam_add(mine, Q.get((uint32_t)cand));
+                    dirty = true;
+                }
+                resolved = true;
+            }
+            __syncwarp();
+            if (!cm) break;
+        }
+        if (dirty) L.open[o] = mine;
+    }
+    // untaken hits open new NAMs, in ref_start order
+    uint32_t added = 0;
+    for (uint32_t b = 0; b < nh; b += 32) {
+        const uint32_t j = b + lane;
+        const bool mk = j < nh && !taken[j];
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, mk);
+        if (mk) L.open[L.n_open + added + __popc(m & lanemask_lt())] = nam_from_hit(Q.get(j));
+        added += __popc(m);
+    }
+    L.n_open += added;
+    __syncwarp();
+}
+
+// Warp-cooperative add_to_hits_per_ref for one query (as warp_walk_run) writing the
+// kept hits in compact form: rs[] = position, pk[] = packed.  Returns their count
+// (at most cap are written).
+__device__ __forceinline__ uint32_t warp_walk_run_q(const IndexView& I, int qs, int qe, uint64_t pos, uint32_t* rs_out,
+                                                    uint32_t* pk_out, uint32_t cap) {
+    const uint32_t lane = lane_id();
+    const uint64_t key = get_hash(I, pos);
+    int carry = 0x7FFFFFFF;
+    uint32_t n = 0;
+    for (uint64_t base = pos;; base += 32) {
+        const uint64_t p = base + lane;
+        bool in = false;
+        gbsa_ref_randstrobe e;
+        int diff = 0x7FFFFFFF;
+        if (p < I.n) {
+            e = I.rs[p];
+            in = e.hash == key;
+        }
+        const uint32_t inm = __ballot_sync(0xFFFFFFFFu, in);
+        const uint32_t runm = (~inm) ? (inm & ((1u << (__ffs(~inm) - 1)) - 1)) : inm;
+        const bool mine = (runm >> lane) & 1u;
+        if (mine) {
+            const int d = (qe - qs) - ((int)(e.packed & 0xFF) + I.k);
+            diff = d < 0 ? -d : d;
+        }
+        int pm = diff;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xFFFFFFFFu, pm, o);
+            if (lane >= (uint32_t)o) pm = v < pm ? v : pm;
+        }
+        int excl = __shfl_up_sync(0xFFFFFFFFu, pm, 1);
+        if (lane == 0) excl = 0x7FFFFFFF;
+        excl = excl < carry ? excl : carry;
+        const bool keep = mine && diff <= excl;
+        const uint32_t km = __ballot_sync(0xFFFFFFFFu, keep);
+        if (keep) {
+            const uint32_t k = n + __popc(km & lanemask_lt());
+            if (k < cap) {
+                rs_out[k] = e.position;
+                pk_out[k] = e.packed;
+            }
+        }
+        n += __popc(km);
+        const int tot = __shfl_sync(0xFFFFFFFFu, pm, 31);
+        carry = tot < carry ? tot : carry;
+        if (runm != 0xFFFFFFFFu) break;
+    }
+    __syncwarp();
+    return n;
+}
+
 // First untaken hit of h[0..nh) (sorted by rs) that NAM n would take, or -1.
 __device__ __forceinline__ int nam_candidate(const NamState& n, const HitRec* h, uint32_t nh, const uint8_t* taken) {
     uint32_t lo = 0, hi = nh;

@@ -65,7 +65,7 @@ def lib():
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
             "gbsa_randstrobes_query_noalloc": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64), vp]),
-            "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, C.POINTER(u32)]),
+            "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -219,7 +219,7 @@ class Mapper:
     def last_alg_bytes(self):
         return lib().gbsa_mapper_last_alg_bytes(self.h)
 
-    STAGES = ("seed", "seed_long", "lookup", "nams", "rescue")
+    STAGES = ("seed", "seed_long", "lookup", "nams", "rescue", "rescue_sort")
 
     def set_profile(self, on=True):
         _check(lib().gbsa_mapper_set_profile(self.h, 1 if on else 0))
@@ -232,13 +232,15 @@ class Mapper:
 
     def rescue_cycles(self, cap=1 << 22):
         a = np.zeros(cap, np.uint64)
-        n = C.c_uint32()
-        _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, C.byref(n)))
-        return a[: min(cap, n.value)]
+        n = (C.c_uint32 * 2)()
+        _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, n))
+        k = min(cap // 4, n[0] + n[1])
+        a = a[: 4 * k].reshape(-1, 4)
+        return a[: n[0]], a[n[0]:k]
 
     def stage_ms(self):
-        a = np.zeros(5, np.float32)
-        lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 5)
+        a = np.zeros(6, np.float32)
+        lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 6)
         return dict(zip(self.STAGES, a.tolist()))
 
     def map_reads(self, reads, capacity=None):

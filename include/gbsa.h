@@ -240,7 +240,8 @@ void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on);
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
  * returns the last batch's milliseconds for: seeding, long-read seeding, lookup,
- * NAM merge + sort, rescue.  No reference counterpart. */
+ * NAM merge + sort, rescue, sorting of the rescued reads with many NAMs.  No
+ * reference counterpart. */
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
 /* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
@@ -248,8 +249,10 @@ int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
  * [5] overflow scratch bytes, [6] reads merged by the warp-cooperative NAM kernel.
  * out must hold 7 values.  No reference counterpart. */
 int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
-/* With profiling on: SM clock cycles the rescue kernel spent on each rescued read of
- * the last batch (up to cap values); *n_out receives the number of rescued reads.
+/* With profiling on: SM clock cycles spent on each rescued read of the last batch, 4
+ * values per read (total, planning, merge, sort; for reads of the block-per-read
+ * kernel: total, planning + merge, sort, NAM count), the warp kernel's reads first;
+ * n_out[0] / n_out[1] receive the two read counts; out holds up to cap values.
  * No reference counterpart. */
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out);
 
