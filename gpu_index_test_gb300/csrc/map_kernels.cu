@@ -643,7 +643,46 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
     }
 }
 
-constexpr uint32_t kSortTile = 2048;   // keys per shared-memory tile of the block sort
+// Shared-memory tile of the block sort, one array per key field so that a warp's
+// accesses are conflict-free and a compare usually reads only k1.
+struct SortTile {
+    uint64_t* k1;
+    uint64_t* k2;
+    uint64_t* k3;
+    uint32_t* idx;
+    __device__ NamKey get(uint32_t i) const {
+        NamKey k;
+        k.k1 = k1[i];
+        k.k2 = k2[i];
+        k.k3 = k3[i];
+        k.idx = idx[i];
+        k.pad = 0;
+        return k;
+    }
+    __device__ void put(uint32_t i, const NamKey& k) {
+        k1[i] = k.k1;
+        k2[i] = k.k2;
+        k3[i] = k.k3;
+        idx[i] = k.idx;
+    }
+    // b < a, reading the secondary fields only when the first ones tie
+    __device__ bool less_at(uint32_t b, uint32_t a) const {
+        const uint64_t x = k1[b], y = k1[a];
+        if (x != y) return x < y;
+        const uint64_t x2 = k2[b], y2 = k2[a];
+        if (x2 != y2) return x2 < y2;
+        const uint64_t x3 = k3[b], y3 = k3[a];
+        if (x3 != y3) return x3 < y3;
+        return idx[b] < idx[a];
+    }
+    __device__ void swap(uint32_t i, uint32_t j) {
+        const NamKey a = get(i), b = get(j);
+        put(i, b);
+        put(j, a);
+    }
+};
+
+constexpr uint32_t kSortTile = 2048;   // keys per shared-memory tile (56 KB)
 
 __device__ __forceinline__ void cmp_swap(NamKey* keys, uint32_t i, uint32_t j, uint32_t k) {
     const uint32_t ixj = i ^ j;
@@ -659,9 +698,9 @@ __device__ __forceinline__ void cmp_swap(NamKey* keys, uint32_t i, uint32_t j, u
 
 // Block bitonic sort of n keys (room for next_pow2(n) in global memory) by all
 // threads of the block.  Every stage whose partner distance is below kSortTile runs
-// on a shared-memory tile of kSortTile keys (tile[] has kSortTile entries); only the
-// stages with larger distances touch global memory.
-__device__ void block_sort_keys(NamKey* keys, uint32_t n, NamKey* tile) {
+// on a shared-memory tile of kSortTile keys; only the stages with larger distances
+// touch global memory.
+__device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile) {
     const uint32_t P = next_pow2(n);
     for (uint32_t i = n + threadIdx.x; i < P; i += blockDim.x) {
         NamKey k;
@@ -676,26 +715,21 @@ __device__ void block_sort_keys(NamKey* keys, uint32_t n, NamKey* tile) {
     // (k <= T: the tile-local sort from scratch; k > T: finish merge level k).
     auto tile_pass = [&](uint32_t k_from, uint32_t k_to, uint32_t j_from) {
         for (uint32_t t0 = 0; t0 < P; t0 += T) {
-            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) tile[i] = keys[t0 + i];
+            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) tile.put(i, keys[t0 + i]);
             __syncthreads();
             for (uint32_t k = k_from; k <= k_to; k <<= 1) {
                 for (uint32_t j = (k == k_from ? j_from : k >> 1); j > 0; j >>= 1) {
-                    for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
-                        // direction uses the global index
-                        const uint32_t gi = t0 + i, ixj = i ^ j;
-                        if (ixj > i) {
-                            const NamKey a = tile[i], b = tile[ixj];
-                            const bool up = (gi & k) == 0;
-                            if (key_less(b, a) == up) {
-                                tile[i] = b;
-                                tile[ixj] = a;
-                            }
-                        }
+                    // one compare per thread and pair: i is the lower index of the pair
+                    for (uint32_t q = threadIdx.x; q < T / 2; q += blockDim.x) {
+                        const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                        const uint32_t ixj = i | j;
+                        const bool up = ((t0 + i) & k) == 0;   // direction uses the global index
+                        if (tile.less_at(ixj, i) == up) tile.swap(i, ixj);
                     }
                     __syncthreads();
                 }
             }
-            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) keys[t0 + i] = tile[i];
+            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) keys[t0 + i] = tile.get(i);
             __syncthreads();
         }
     };
@@ -717,9 +751,13 @@ constexpr uint32_t kSortThreads = 256;
 // written to the NAM arena in order.
 __global__ void __launch_bounds__(kSortThreads) k_sort_jobs(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
                                                               Counters* ctr) {
-    extern __shared__ __align__(16) uint8_t s_dyn[];   // kSortTile sort keys
+    extern __shared__ __align__(16) uint8_t s_dyn[];   // kSortTile sort keys, one array per field
     __shared__ uint64_t s_noff;
-    NamKey* s_tile = reinterpret_cast<NamKey*>(s_dyn);
+    SortTile s_tile;
+    s_tile.k1 = reinterpret_cast<uint64_t*>(s_dyn);
+    s_tile.k2 = s_tile.k1 + kSortTile;
+    s_tile.k3 = s_tile.k2 + kSortTile;
+    s_tile.idx = reinterpret_cast<uint32_t*>(s_tile.k3 + kSortTile);
     const uint32_t n_jobs = *(volatile unsigned int*)&ctr->n_heavy;
     for (uint32_t h = blockIdx.x; h < n_jobs; h += gridDim.x) {
         const SortJob job = A.sort_jobs[h];
@@ -865,10 +903,10 @@ void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr,
     static bool attr = false;
     if (!attr) {
         GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(kSortTile * sizeof(NamKey))));
+                                       (int)(kSortTile * 28)));
         attr = true;
     }
-    k_sort_jobs<<<(unsigned)device_sm_count() * 3, kSortThreads, kSortTile * sizeof(NamKey), st>>>(C, rec, A, ctr);
+    k_sort_jobs<<<(unsigned)device_sm_count() * 4, kSortThreads, kSortTile * 28, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
