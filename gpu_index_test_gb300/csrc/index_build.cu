@@ -76,10 +76,10 @@ __global__ void __launch_bounds__(32 * kSegWarps) k_contig_syncmers(DevParams P,
         const uint32_t anchor = warp_find_anchor(P, packed, nmask, base, nwin, w0, hbuf);
         if (kWrite) {
             const uint64_t o = seg_off[s];
-            warp_syncmer_scan(P, packed, nmask, base, nwin, anchor, w1, w0, hbuf, [&](uint32_t idx, uint32_t w) {
-                sh[o + idx] = kmer_hash(P, packed, base + w);
-                sp[o + idx] = w;
-            });
+            const uint32_t n = warp_syncmer_scan(P, packed, nmask, base, nwin, anchor, w1, w0, hbuf,
+                                                 [&](uint32_t idx, uint32_t w) { sp[o + idx] = w; });
+            __syncwarp();
+            for (uint32_t i = lane_id(); i < n; i += 32) sh[o + i] = kmer_hash(P, packed, base + sp[o + i]);
         } else {
             const uint32_t n = warp_syncmer_scan(P, packed, nmask, base, nwin, anchor, w1, w0, hbuf,
                                                  [](uint32_t, uint32_t) {});

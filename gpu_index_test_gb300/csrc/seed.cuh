@@ -51,18 +51,28 @@ __device__ __forceinline__ uint64_t spread_bits(uint32_t x) {
 
 __device__ __forceinline__ void warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
     const uint32_t lane = lane_id();
-    const uint32_t nw = (L + 31) / 32;
-    for (uint32_t it = 0; it < nw + 2; ++it) {
-        const uint32_t p = it * 32 + lane;
-        const uint32_t c = p < L ? nt4(seq[p]) : 4u;
-        const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, c & 1u);
-        const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, (c >> 1) & 1u);
-        const uint32_t bn = __ballot_sync(0xFFFFFFFFu, c == 4u);
-        if (lane == (it & 31)) {
-            const uint64_t lo = spread_bits(__brev(b0 & ~bn));
-            const uint64_t hi = spread_bits(__brev(b1 & ~bn));
-            packed[it] = lo | (hi << 1);
-            nmask[it] = bn;
+    const uint32_t nw = (L + 31) / 32 + 2;
+    for (uint32_t w0 = 0; w0 < nw; w0 += 32) {
+        // ballots of word w0 + j are kept by lane j, then every lane spreads its own
+        uint32_t m0 = 0, m1 = 0, mn = 0;
+        const uint32_t cnt = nw - w0 < 32 ? nw - w0 : 32;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint32_t p = (w0 + j) * 32 + lane;
+            const uint32_t c = p < L ? nt4(seq[p]) : 4u;
+            const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, c & 1u);
+            const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, (c >> 1) & 1u);
+            const uint32_t bn = __ballot_sync(0xFFFFFFFFu, c == 4u);
+            if (lane == j) {
+                m0 = b0;
+                m1 = b1;
+                mn = bn;
+            }
+        }
+        if (lane < cnt) {
+            const uint64_t lo = spread_bits(__brev(m0 & ~mn));
+            const uint64_t hi = spread_bits(__brev(m1 & ~mn));
+            packed[w0 + lane] = lo | (hi << 1);
+            nmask[w0 + lane] = mn;
         }
     }
     __syncwarp();
@@ -90,16 +100,17 @@ __device__ __forceinline__ uint64_t kmer_hash(const DevParams& P, const uint64_t
 }
 
 // Facts of window w of a sequence whose base 0 sits at stream position `base`
-// (valid when w < nwin and the k-mer holds no N).  hw points at the W s-mer hashes
-// of the window.
+// (valid when w < nwin and the k-mer holds no N).  hw is a 64-entry ring holding the
+// s-mer hash of position p at hw[p & 63].
 __device__ __forceinline__ uint32_t window_info(const DevParams& P, const uint32_t* nmask, uint64_t base, uint32_t w,
                                                 uint32_t nwin, const uint64_t* hw) {
     if (w >= nwin) return 0;
     if (nbits32(nmask, base + w, P.k) != 0) return 0;
-    uint64_t mv = hw[0];
+    uint64_t mv = hw[w & 63];
     uint32_t lo = 0, ro = 0;
+#pragma unroll 8
     for (int d = 1; d < P.W; ++d) {
-        const uint64_t v = hw[d];
+        const uint64_t v = hw[(w + d) & 63];
         if (v < mv) {
             mv = v;
             lo = ro = (uint32_t)d;
@@ -144,12 +155,15 @@ __device__ uint32_t warp_syncmer_scan(const DevParams& P, const uint64_t* packed
     uint32_t count = 0;
     uint32_t carry = kNoneState;
     const uint32_t tpos = (uint32_t)(P.t - 1);
+    const uint32_t W1 = (uint32_t)(P.W - 1);
+    // s-mer hashes live in a 64-entry ring (position p at hbuf[p & 63]); each chunk of
+    // 32 windows needs 32 new ones beyond the W-1 it shares with the previous chunk
+    if (lane < W1 && w_begin < w_end) hbuf[(w_begin + lane) & 63] = smer_hash(P, packed, base + w_begin + lane);
     for (uint32_t c = w_begin; c < w_end; c += 32) {
         const uint32_t w = c + lane;
-        hbuf[lane] = smer_hash(P, packed, base + w);
-        if (lane < (uint32_t)(P.W - 1)) hbuf[32 + lane] = smer_hash(P, packed, base + c + 32 + lane);
+        hbuf[(c + W1 + lane) & 63] = smer_hash(P, packed, base + c + W1 + lane);
         __syncwarp();
-        const uint32_t inf = (w < w_end) ? window_info(P, nmask, base, w, nwin, hbuf + lane) : 0u;
+        const uint32_t inf = (w < w_end) ? window_info(P, nmask, base, w, nwin, hbuf) : 0u;
         const bool valid = inf & 1u;
         const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
         const uint32_t umask = __ballot_sync(0xFFFFFFFFu, valid && !win_determined(inf));
@@ -191,12 +205,12 @@ __device__ inline uint32_t warp_find_anchor(const DevParams& P, const uint64_t* 
     for (;;) {
         const uint32_t lo_w = top >= 31 ? top - 31 : 0;
         const uint32_t w = lo_w + lane;
-        hbuf[lane] = smer_hash(P, packed, base + w);
-        if (lane < (uint32_t)(P.W - 1)) hbuf[32 + lane] = smer_hash(P, packed, base + lo_w + 32 + lane);
+        hbuf[w & 63] = smer_hash(P, packed, base + w);
+        if (lane < (uint32_t)(P.W - 1)) hbuf[(lo_w + 32 + lane) & 63] = smer_hash(P, packed, base + lo_w + 32 + lane);
         __syncwarp();
         bool ok = false;
         if (w <= top) {
-            const uint32_t inf = window_info(P, nmask, base, w, nwin, hbuf + lane);
+            const uint32_t inf = window_info(P, nmask, base, w, nwin, hbuf);
             ok = !(inf & 1u) || win_determined(inf) || w == 0;
         }
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
@@ -277,17 +291,13 @@ __device__ __forceinline__ uint32_t warp_read_syncmers(const DevParams& P, const
     if (L < (uint32_t)P.k) return 0;
     warp_pack_read(seq, L, pk, nm);
     const uint32_t nwin = L - (uint32_t)P.k + 1;
-    bool over = false;
     const uint32_t n = warp_syncmer_scan(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, [&](uint32_t idx, uint32_t w) {
-        if (idx < cap) {
-            sh[idx] = kmer_hash(P, pk, w);
-            sp[idx] = w;
-        } else {
-            over = true;
-        }
+        if (idx < cap) sp[idx] = w;
     });
+    if (n > cap) return 0xFFFFFFFFu;
     __syncwarp();
-    if (__any_sync(0xFFFFFFFFu, over)) return 0xFFFFFFFFu;
+    for (uint32_t i = lane_id(); i < n; i += 32) sh[i] = kmer_hash(P, pk, sp[i]);
+    __syncwarp();
     return n;
 }
 
