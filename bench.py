@@ -293,25 +293,36 @@ def main():
         torch.distributed.barrier()
     launches = native.launch_count() - l0
     clocks = sampler.stop()
-    warp_cyc, heavy_cyc = m.rescue_cycles()
+    resc, n_block_sorted = m.rescue_cycles()
+    nam_cyc = m.nam_cycles()
     m.set_profile(False)
     mhz = clocks.get("sm_mhz") or 2000.0
 
-    def cyc_stats(a):
+    def dist(a, div=1.0):
+        """p50 / p99 / max / sum of a per-read quantity (cycles / div = microseconds)."""
         if not len(a):
             return None
-        us = np.sort(a.astype(np.float64)) / mhz
-        return {"n": int(len(us)), "p50": round(float(us[len(us) // 2]), 1),
-                "p99": round(float(us[int(len(us) * 0.99)]), 1), "max": round(float(us[-1]), 1),
-                "sum": round(float(us.sum()), 1)}
+        v = np.sort(a.astype(np.float64)) / div
+        return {"n": int(len(v)), "p50": round(float(v[len(v) // 2]), 1),
+                "p99": round(float(v[int(len(v) * 0.99)]), 1), "max": round(float(v[-1]), 1),
+                "sum": round(float(v.sum()), 1)}
 
-    rescue_profile = {
-        "warp_total_us": cyc_stats(warp_cyc[:, 0]) if len(warp_cyc) else None,
-        "warp_plan_us": cyc_stats(warp_cyc[:, 1]) if len(warp_cyc) else None,
-        "warp_merge_us": cyc_stats(warp_cyc[:, 2]) if len(warp_cyc) else None,
-        "warp_sort_us": cyc_stats(warp_cyc[:, 3]) if len(warp_cyc) else None,
-        "block_sorted_reads": int(len(heavy_cyc)),
-    }
+    rescue_profile = None
+    if len(resc):
+        worst = resc[np.argsort(resc[:, 0] + resc[:, 3])[-3:]]
+        rescue_profile = {
+            "total_us": dist(resc[:, 0], mhz), "plan_us": dist(resc[:, 1], mhz),
+            "merge_us": dist(resc[:, 2], mhz), "sort_us": dist(resc[:, 3], mhz),
+            "hit_bound": dist(resc[:, 4]), "nams": dist(resc[:, 5]), "queries": dist(resc[:, 6]),
+            "max_run": dist(resc[:, 7]), "block_sorted_reads": n_block_sorted,
+            "worst": worst.tolist(),
+        }
+    nam_profile = None
+    if len(nam_cyc):
+        worst = nam_cyc[np.argsort(nam_cyc[:, 0])[-3:]]
+        nam_profile = {"total_us": dist(nam_cyc[:, 0], mhz), "merge_us": dist(nam_cyc[:, 3], mhz),
+                       "hits": dist(nam_cyc[:, 1]), "nams": dist(nam_cyc[:, 2]),
+                       "worst_cycles_hits_nams": worst[:, :3].tolist()}
     ms = ev0.elapsed_time(ev1) / args.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -374,7 +385,8 @@ def main():
         "seed": bases + 16 * q,                          # ASCII bases in, query randstrobes out
         "seed_long": 0,
         "lookup": alg_lookup + 16 * q + 8 * q + 20 * hits,  # probes + queries in + positions + hits out
-        "nams": 20 * hits + 44 * nams_n,                 # hits in, NAMs out
+        "nams": 20 * hits + 32 * nams_n,                 # hits in, NAM records out
+        "nams_warp": 0,
         "rescue": 0,
         "rescue_sort": 0,
     }
@@ -404,7 +416,7 @@ def main():
         "bit_exact_vs_cpu_sample": exact,
         "clocks": clocks,
         "gpu_launches": int(launches),
-        "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile),
+        "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile, nam_profile=nam_profile),
     }
     print(json.dumps(line))
     if world > 1:

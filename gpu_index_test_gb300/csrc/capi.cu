@@ -130,10 +130,12 @@ struct gbsa_mapper {
     gbsa_map_options opt{};
     gbsa::MapConfig cfg{};
     cudaStream_t st = nullptr;
+    cudaStream_t side = nullptr;                           // rescue chain, beside the NAM kernels
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
-        out_off, out_nams, out_frac, out_resc, resc_cycles, jobs;
+        out_off, out_nams, out_frac, out_resc, resc_cycles, nam_notes, jobs, side_slots;
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
@@ -141,7 +143,7 @@ struct gbsa_mapper {
     int count_bytes = 0;
     int profile = 0;          // record per-stage CUDA events
     cudaEvent_t ev[8] = {};
-    float stage_ms[7] = {};
+    float stage_ms[8] = {};
     gbsa::Counters last{};    // device counters of the last batch
 };
 
@@ -159,7 +161,10 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     m.out_off.resize(8ull * (n + 1));
     m.out_frac.resize(4ull * (n + 1));
     m.out_resc.resize(n + 1);
-    if (m.profile) m.resc_cycles.resize(64ull * (n + 1));
+    if (m.profile) {
+        m.resc_cycles.resize(64ull * (n + 1));
+        m.nam_notes.resize(32ull * (n + 1));
+    }
     // query randstrobes: ~2 per 5 bases plus slack
     const uint64_t q_need = std::max<uint64_t>(4096, bases / 2 + 64ull * n / 8);
     if (m.q_cap < q_need) {
@@ -179,6 +184,7 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     const uint32_t warps = nam_kernel_warps(std::max<uint32_t>(n, 1));
     if (m.slot_bytes == 0) m.slot_bytes = 32 * 1024;
     m.slots.resize((uint64_t)warps * m.slot_bytes);
+    m.side_slots.resize((uint64_t)warps * m.slot_bytes);
     if (m.ovf_cap == 0) {
         m.ovf_cap = 64ull << 20;
         m.ovf.resize(m.ovf_cap);
@@ -205,10 +211,13 @@ static Arenas arenas_of(gbsa_mapper& m) {
     A.ovf_cap = m.ovf_cap;
     const size_t per = m.lists.size() / 16;   // u32 entries per list
     A.rescue_list = m.lists.as<uint32_t>();
+    A.rescue_cap = (uint32_t)per;
     A.long_list = m.lists.as<uint32_t>() + per;
     A.big_list = m.lists.as<uint32_t>() + 2 * per;
     A.sort_jobs = m.jobs.as<SortJob>();
+    A.jobs_cap = (uint32_t)(m.jobs.size() / sizeof(SortJob));
     A.rescue_cycles = m.profile ? m.resc_cycles.as<uint64_t>() : nullptr;
+    A.nam_cycles = m.profile ? m.nam_notes.as<uint64_t>() : nullptr;
     return A;
 }
 
@@ -252,17 +261,32 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         mark(2);
         launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
         mark(3);
+        // The rescue chain works on the rescued reads only and the NAM kernels on the
+        // others: the rescue chain runs on the side stream (with its own scratch
+        // slots) so that its tail of reads with thousands of hits overlaps them.
+        GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
+        GBSA_CUDA(cudaStreamWaitEvent(m.side, m.fork_ev, 0));
+        Arenas As = A;
+        As.slots = m.side_slots.as<uint8_t>();
+        launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, m.side);
+        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[6], m.side));
+        if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, m.side);
+        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[7], m.side));
+        GBSA_CUDA(cudaEventRecord(m.join_ev, m.side));
         launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
         mark(4);
-        launch_rescue(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        launch_nams_warp(C, n, m.rec.as<ReadRec>(), A, ctr, st);
         mark(5);
-        if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), A, ctr, st);
-        mark(6);
+        GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
         Counters h{};
         GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
         GBSA_CUDA(cudaStreamSynchronize(st));
-        if (m.profile)
-            for (int i = 0; i < 6; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[i], m.ev[i + 1]));
+        if (m.profile) {
+            // seed, long seed, lookup, lane NAMs, warp NAMs (main stream); rescue, its
+            // block sorts (side stream, from the fork after the lookup)
+            static const int from[7] = {0, 1, 2, 3, 4, 3, 6}, to[7] = {1, 2, 3, 4, 5, 6, 7};
+            for (int i = 0; i < 7; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[from[i]], m.ev[to[i]]));
+        }
         if (h.status & kStatusReadTooLong)
             throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
         if (h.status & kStatusSyncmerOverflow)
@@ -612,6 +636,9 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
         m->max_reads = std::max<uint32_t>(max_reads, 1);
         m->max_bases = std::max<uint64_t>(max_bases, 1);
         GBSA_CUDA(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+        GBSA_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        GBSA_CUDA(cudaEventCreateWithFlags(&m->fork_ev, cudaEventDisableTiming));
+        GBSA_CUDA(cudaEventCreateWithFlags(&m->join_ev, cudaEventDisableTiming));
         mapper_reserve(*m, m->max_reads, m->max_bases);
         *out = m.release();
     });
@@ -619,12 +646,14 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
 
 void gbsa_mapper_free(gbsa_mapper* m) {
     if (!m) return;
+    if (m->side) cudaStreamSynchronize(m->side);
+    if (m->st) cudaStreamSynchronize(m->st);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
-    if (m->st) {
-        cudaStreamSynchronize(m->st);
-        cudaStreamDestroy(m->st);
-    }
+    if (m->fork_ev) cudaEventDestroy(m->fork_ev);
+    if (m->join_ev) cudaEventDestroy(m->join_ev);
+    if (m->side) cudaStreamDestroy(m->side);
+    if (m->st) cudaStreamDestroy(m->st);
     delete m;
 }
 
@@ -771,7 +800,7 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
     out[0] = m->last.q_used;
     out[1] = m->last.hit_used;
     out[2] = m->last.nam_used;
-    out[3] = m->last.n_rescue;
+    out[3] = m->last.n_rescue + m->last.n_rescue_heavy;
     out[4] = m->last.n_long;
     out[5] = m->last.scratch_used;
     out[6] = m->last.n_big;
@@ -780,17 +809,26 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
 
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out) {
     return guarded([&] {
-        const uint32_t total = m->last.n_rescue + m->last.n_heavy;
-        const uint32_t n = std::min<uint32_t>(cap / 4, total);
-        n_out[0] = m->last.n_rescue;
-        n_out[1] = m->last.n_heavy;
-        if (m->profile && n && m->resc_cycles.size() >= 32ull * n)
-            GBSA_CUDA(cudaMemcpy(out, m->resc_cycles.as<void>(), 32ull * n, cudaMemcpyDeviceToHost));
+        const uint32_t total = m->last.n_rescue + m->last.n_rescue_heavy;
+        const uint32_t n = std::min<uint32_t>(cap / 8, total);
+        n_out[0] = total;
+        n_out[1] = m->last.n_heavy + m->last.n_huge;
+        if (m->profile && n && m->resc_cycles.size() >= 64ull * n)
+            GBSA_CUDA(cudaMemcpy(out, m->resc_cycles.as<void>(), 64ull * n, cudaMemcpyDeviceToHost));
+    });
+}
+
+int gbsa_mapper_nam_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out) {
+    return guarded([&] {
+        const uint32_t n = std::min<uint32_t>(cap / 4, m->last.n_big);
+        n_out[0] = m->last.n_big;
+        if (m->profile && n && m->nam_notes.size() >= 32ull * n)
+            GBSA_CUDA(cudaMemcpy(out, m->nam_notes.as<void>(), 32ull * n, cudaMemcpyDeviceToHost));
     });
 }
 
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n) {
-    for (int i = 0; i < n && i < 6; ++i) ms[i] = m->stage_ms[i];
+    for (int i = 0; i < n && i < 7; ++i) ms[i] = m->stage_ms[i];
     return GBSA_OK;
 }
 

@@ -33,11 +33,13 @@ struct Counters {
     unsigned long long nam_used;
     unsigned long long scratch_used;
     unsigned long long alg_bytes;   // roofline numerator (see k_lookup)
-    unsigned int n_rescue;
+    unsigned int n_rescue;        // rescued reads on the light end of the rescue list
     unsigned int n_long;
     unsigned int status;
     unsigned int n_big;    // reads merged by the warp-cooperative NAM kernel
-    unsigned int n_heavy;  // rescued reads whose NAMs the block-per-read sort kernel orders
+    unsigned int n_heavy;  // rescued reads whose NAMs the block-per-read sort kernel orders (small tile)
+    unsigned int n_rescue_heavy;  // rescued reads on the heavy end of the rescue list
+    unsigned int n_huge;   // rescued reads whose NAMs the large-tile block sort orders
     unsigned int pad2;
 };
 
@@ -47,6 +49,8 @@ struct SortJob {
     NamKey* keys;       // room for next_pow2(n) sort keys
     uint32_t n;
     uint32_t read;
+    uint32_t note;      // its index on the rescue list
+    uint32_t pad;
 };
 
 struct Arenas {
@@ -62,11 +66,14 @@ struct Arenas {
     uint64_t slot_bytes;
     uint8_t* ovf;            // shared overflow scratch (bump-allocated)
     uint64_t ovf_cap;
-    uint32_t* rescue_list;
+    uint32_t* rescue_list;   // light reads from the front, heavy ones from the back
+    uint32_t rescue_cap;
     uint32_t* long_list;
     uint32_t* big_list;
-    SortJob* sort_jobs;
-    uint64_t* rescue_cycles;   // optional: SM cycles spent on each rescued read
+    SortJob* sort_jobs;      // small-tile jobs from the front, large-tile ones from the back
+    uint32_t jobs_cap;
+    uint64_t* rescue_cycles;   // optional: 8 notes per rescued read (cycles per phase, sizes)
+    uint64_t* nam_cycles;      // optional: SM cycles, hits and NAMs of each read of the warp NAM kernel
 };
 
 struct MapConfig {
@@ -99,6 +106,7 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
                    cudaStream_t st);
 void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st);
+void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);

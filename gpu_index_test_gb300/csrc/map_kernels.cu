@@ -115,6 +115,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_seed_long(DevParams P, 
     }
 }
 
+constexpr uint32_t kRescueHeavySeeds = 8;   // found but repetitive query randstrobes of a heavy rescued read
+
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
                                                                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
     const uint32_t lane = lane_id();
@@ -162,7 +164,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
         if (rescue) {
             if (lane == 0) {
                 R.flags |= kReadRescue;
-                A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
+                // reads with many repetitive seeds (short tandem repeats) merge thousands of
+                // hits: they go to the heavy end so that their warps start first
+                if (tot - good >= kRescueHeavySeeds)
+                    A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
+                else
+                    A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
                 R.n_hits = 0;
             }
             continue;
@@ -241,7 +248,6 @@ __device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* 
     }
 }
 
-constexpr uint32_t kNamSmem = 64;   // reads with at most this many hits merge in shared memory
 constexpr uint32_t kLaneMaxHits = 160;
 constexpr uint32_t kLaneOpen = 10;   // open NAMs a lane keeps in shared memory
 constexpr int kLaneWarps = 4;
@@ -381,69 +387,240 @@ __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint
     }
 }
 
-// find_nams after the lookup: the read's hits arrive in (orientation, query_start,
-// position) order, one query randstrobe after another; they are merged hit-major.
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_nams(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
-                                                               Counters* ctr) {
-    __shared__ NamState s_lists[kWarpsPerBlock][2 * kNamSmem];
+// Open NAM list of one warp in struct-of-arrays form (field f of NAM o at
+// b[f * stride + o]), so that 32 lanes reading one field of 32 NAMs touch 32
+// consecutive words.
+struct OpenSoA {
+    int32_t* b;
+    uint32_t stride;
+    __device__ int32_t* f(int k) const { return b + (size_t)k * stride; }
+    __device__ NamState get(uint32_t o) const {
+        NamState n;
+        n.qs = b[o];
+        n.qe = b[stride + o];
+        n.qprev = b[2 * stride + o];
+        n.rs = b[3 * stride + o];
+        n.re = b[4 * stride + o];
+        n.rprev = b[5 * stride + o];
+        n.n_hits = b[6 * stride + o];
+        n.ref_rc = (uint32_t)b[7 * stride + o];
+        return n;
+    }
+    __device__ void put(uint32_t o, const NamState& n) const {
+        b[o] = n.qs;
+        b[stride + o] = n.qe;
+        b[2 * stride + o] = n.qprev;
+        b[3 * stride + o] = n.rs;
+        b[4 * stride + o] = n.re;
+        b[5 * stride + o] = n.rprev;
+        b[6 * stride + o] = n.n_hits;
+        b[7 * stride + o] = (int32_t)n.ref_rc;
+    }
+};
+
+// Moves the open NAMs with query_end < qs (all of them when qs == INT_MAX) to the
+// closed list, keeping the order of both lists.
+__device__ __forceinline__ void soa_close_passed(const OpenSoA& O, uint32_t& n_open, NamState* closed,
+                                                 uint32_t& n_closed, int qs) {
+    const uint32_t lane = lane_id();
+    if (qs != 0x7FFFFFFF) {
+        bool any = false;
+        for (uint32_t base = 0; base < n_open && !any; base += 32) {
+            const uint32_t o = base + lane;
+            any = __any_sync(0xFFFFFFFFu, o < n_open && O.b[O.stride + o] < qs);
+        }
+        if (!any) return;
+    }
+    uint32_t keep = 0, done = 0;
+    for (uint32_t base = 0; base < n_open; base += 32) {
+        const uint32_t o = base + lane;
+        const bool valid = o < n_open;
+        NamState n;
+        if (valid) n = O.get(o);
+        const bool stay = valid && n.qe >= qs;
+        const uint32_t ms = __ballot_sync(0xFFFFFFFFu, stay);
+        const uint32_t mc = __ballot_sync(0xFFFFFFFFu, valid && !stay);
+        __syncwarp();
+        if (stay) O.put(keep + __popc(ms & lanemask_lt()), n);
+        else if (valid) closed[n_closed + done + __popc(mc & lanemask_lt())] = n;
+        keep += __popc(ms);
+        done += __popc(mc);
+        __syncwarp();
+    }
+    n_open = keep;
+    n_closed += done;
+}
+
+// Hit-major merge of nh <= 32 hits of one query randstrobe, held one per lane in
+// registers (lane j holds hit j, in ref_start order), against the NAMs [0, nn) that
+// were open when the query started: each hit joins the first of them in creation
+// order that accepts it, else opens a new NAM.  Returns false (with the list
+// unchanged from the failing hit on) when a new NAM would not fit in cap.
+__device__ __forceinline__ bool soa_merge_hits(const OpenSoA& O, uint32_t nn, uint32_t& n_open, uint32_t cap,
+                                               const HitRec& xl, uint32_t nh) {
+    const uint32_t lane = lane_id();
+    const int32_t* fqe = O.f(1);
+    const int32_t* fqprev = O.f(2);
+    const int32_t* fre = O.f(4);
+    const int32_t* frprev = O.f(5);
+    const int32_t* fref = O.f(7);
+    for (uint32_t j = 0; j < nh; ++j) {
+        HitRec x;
+        x.ref_rc = __shfl_sync(0xFFFFFFFFu, xl.ref_rc, j);
+        x.qs = __shfl_sync(0xFFFFFFFFu, xl.qs, j);
+        x.qe = __shfl_sync(0xFFFFFFFFu, xl.qe, j);
+        x.rs = __shfl_sync(0xFFFFFFFFu, xl.rs, j);
+        x.re = __shfl_sync(0xFFFFFFFFu, xl.re, j);
+        bool found = false;
+        for (uint32_t base = 0; base < nn; base += 32) {
+            const uint32_t o = base + lane;
+            bool ok = false;
+            int qe = 0, re = 0;
+            if (o < nn) {
+                qe = fqe[o];
+                re = fre[o];
+                ok = (uint32_t)fref[o] == x.ref_rc && fqprev[o] < x.qs && x.qs <= qe && frprev[o] < x.rs &&
+                     x.rs <= re && ((x.qe > qe && x.re > re) || (x.qe <= qe && x.re <= re));
+            }
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+            if (m) {
+                if (lane == (uint32_t)(__ffs(m) - 1)) {   // the first accepting NAM takes the hit
+                    if (x.qe > qe && x.re > re) {
+                        O.f(1)[o] = x.qe;
+                        O.f(4)[o] = x.re;
+                    }
+                    O.f(2)[o] = x.qs;
+                    O.f(5)[o] = x.rs;
+                    O.f(6)[o] += 1;
+                }
+                found = true;
+                break;
+            }
+        }
+        if (!found) {
+            if (n_open == cap) return false;
+            if (lane == 0) O.put(n_open, nam_from_hit(x));
+            ++n_open;
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+__device__ __forceinline__ HitRec load_hit(const HitRec* __restrict__ hits, uint32_t i, uint32_t H) {
+    HitRec h;
+    if (i < H) {
+        h.ref_rc = __ldg(&hits[i].ref_rc);
+        h.qs = __ldg(&hits[i].qs);
+        h.qe = __ldg(&hits[i].qe);
+        h.rs = __ldg(&hits[i].rs);
+        h.re = __ldg(&hits[i].re);
+    } else {
+        h.ref_rc = 0;
+        h.qs = h.qe = h.rs = h.re = -1;
+    }
+    return h;
+}
+
+// find_nams merge of one read's hits (in (orientation, query_start, position)
+// order) with the open list O (capacity cap); closed NAMs are appended to closed.
+// Each query randstrobe's hits are loaded 32 at a time, one per lane, and the next
+// chunk is fetched while the current one merges.  Returns false when the open list
+// outgrew cap.
+__device__ __forceinline__ bool warp_find_nams(const HitRec* __restrict__ hits, uint32_t H, const OpenSoA& O,
+                                               uint32_t cap, NamState* closed, uint32_t& n_closed) {
+    const uint32_t lane = lane_id();
+    uint32_t n_open = 0, cur_dir = 0;
+    n_closed = 0;
+    uint32_t i = 0;
+    HitRec xl = load_hit(hits, lane, H);
+    while (i < H) {
+        const uint32_t dir = __shfl_sync(0xFFFFFFFFu, xl.ref_rc, 0) >> 31;
+        const int qs = __shfl_sync(0xFFFFFFFFu, xl.qs, 0);
+        if (dir != cur_dir) {   // the other orientation's NAMs can take no more hits
+            soa_close_passed(O, n_open, closed, n_closed, 0x7FFFFFFF);
+            cur_dir = dir;
+        }
+        soa_close_passed(O, n_open, closed, n_closed, qs);
+        const uint32_t nn = n_open;   // NAMs made by this query cannot take its other hits
+        for (;;) {
+            const bool same = i + lane < H && (xl.ref_rc >> 31) == dir && xl.qs == qs;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, same);
+            const uint32_t cnt = m == 0xFFFFFFFFu ? 32u : (uint32_t)(__ffs(~m) - 1);
+            const HitRec nx = load_hit(hits, i + cnt + lane, H);
+            if (!soa_merge_hits(O, nn, n_open, cap, xl, cnt)) return false;
+            i += cnt;
+            xl = nx;
+            if (cnt < 32) break;
+        }
+    }
+    soa_close_passed(O, n_open, closed, n_closed, 0x7FFFFFFF);
+    return true;
+}
+
+constexpr uint32_t kHeavyOpen = 256;   // open NAMs (and sort keys) a warp keeps in shared memory
+constexpr int kHeavyWarps = 4;
+constexpr int kHeavyBlocksPerSm = 5;
+
+// find_nams for the reads the lane kernel passed on (many hits, or many NAMs open
+// at once): a warp per read.  The open list lives in shared memory (in global
+// scratch for a read whose open list outgrows kHeavyOpen); closed NAMs go to the
+// warp's global scratch, which is only written until the sort.  The read's NAMs are
+// then sorted by key in shared memory (in scratch beyond kHeavyOpen NAMs) and
+// gathered to the NAM arena.
+__global__ void __launch_bounds__(32 * kHeavyWarps, kHeavyBlocksPerSm)
+    k_nams(MapConfig C, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    __shared__ __align__(16) int32_t s_open[kHeavyWarps][8 * kHeavyOpen];
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t n_big = *(volatile unsigned int*)&ctr->n_big;
     for (uint32_t b = warp_global_id(); b < n_big; b += warp_count()) {
+        const long long t0 = clock64();
         const uint32_t r = A.big_list[b];
         ReadRec& R = rec[r];
         if (R.flags & (kReadFailed | kReadRescue)) continue;
         const uint32_t H = R.n_hits;
         if (H == 0) continue;
         const HitRec* hits = A.hits + R.hit_off;
-        NamLists L;
-        NamKey* keys;
-        if (H <= kNamSmem) {
-            L.open = s_lists[w];
-            L.closed = s_lists[w] + kNamSmem;
-            keys = reinterpret_cast<NamKey*>(s_lists[w]);   // the open list is empty when keys are built
-        } else {
-            const uint64_t P2 = next_pow2(H);
-            uint8_t* sc = warp_scratch(A, ctr, 0, 64ull * H + 32ull * P2 + 64);
-            if (!sc) {
-                warp_fail(R, ctr, kStatusScratchOverflow);
-                continue;
-            }
-            L.open = reinterpret_cast<NamState*>(sc);
-            L.closed = L.open + H;
-            keys = reinterpret_cast<NamKey*>(L.closed + H);
+        const uint32_t P2 = next_pow2(H);
+        const bool big = H > kHeavyOpen;
+        uint8_t* sc = warp_scratch(A, ctr, 0, 32ull * H + (big ? 32ull * P2 : 0) + 64);
+        if (!sc) {
+            warp_fail(R, ctr, kStatusScratchOverflow);
+            continue;
         }
-        L.n_open = L.n_closed = 0;
-        L.cap = H;
-        uint32_t cur_dir = 0;
-        for (uint32_t i = 0; i < H;) {
-            const HitRec x = hits[i];
-            const uint32_t dir = x.ref_rc >> 31;
-            // end of this query randstrobe's hits
-            uint32_t j = i + 1;
-            for (;;) {
-                const uint32_t t = j + lane;
-                bool same = false;
-                if (t < H) {
-                    const HitRec y = hits[t];
-                    same = (y.ref_rc >> 31) == dir && y.qs == x.qs;
-                }
-                const uint32_t m = __ballot_sync(0xFFFFFFFFu, same);
-                if (m != 0xFFFFFFFFu) {
-                    j += __ffs(~m) - 1;
-                    break;
-                }
-                j += 32;
-            }
-            if (dir != cur_dir) {
-                nam_close_passed(L, 0x7FFFFFFF);
-                cur_dir = dir;
-            }
-            nam_close_passed(L, x.qs);
-            nam_merge_hit_major(L, hits + i, j - i);
-            i = j;
+        NamState* closed = reinterpret_cast<NamState*>(sc);
+        uint32_t NN = 0;
+        OpenSoA O{s_open[w], kHeavyOpen};
+        if (!warp_find_nams(hits, H, O, kHeavyOpen, closed, NN)) {
+            // the open list outgrew shared memory: again with it in scratch
+            __syncwarp();
+            const OpenSoA G{reinterpret_cast<int32_t*>(closed + H), P2};
+            warp_find_nams(hits, H, G, H, closed, NN);
         }
-        nam_close_passed(L, 0x7FFFFFFF);
-        warp_finish_nams(C, L, keys, R, A, ctr);
+        const long long t_merge = clock64();
+        __syncwarp();
+        NamKey* keys = NN <= kHeavyOpen ? reinterpret_cast<NamKey*>(s_open[w]) : reinterpret_cast<NamKey*>(closed + H);
+        for (uint32_t t = lane; t < NN; t += 32) keys[t] = nam_key(closed[t], t, C.sort_mode);
+        __syncwarp();
+        if (NN <= kHeavyOpen) warp_sort_keys(reinterpret_cast<NamKey*>(s_open[w]), NN);
+        else warp_sort_keys(reinterpret_cast<NamKey*>(closed + H), NN);
+        const uint64_t noff = warp_bump(&ctr->nam_used, NN);
+        if (noff + NN > A.nam_cap) {
+            warp_fail(R, ctr, kStatusNamOverflow);
+            continue;
+        }
+        for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = closed[keys[t].idx];
+        if (lane == 0) {
+            R.nam_off = noff;
+            R.n_nams = NN;
+            if (A.nam_cycles) {
+                uint64_t* note = A.nam_cycles + 4ull * b;   // cycles, hits, NAMs, merge cycles
+                note[0] = (uint64_t)(clock64() - t0);
+                note[1] = H;
+                note[2] = NN;
+                note[3] = (uint64_t)(t_merge - t0);
+            }
+        }
         __syncwarp();
     }
 }
@@ -544,14 +721,15 @@ __device__ void rescue_merge(const IndexView& I, const Query* const* Qd, const u
             Q.dir = (uint32_t)d;
             Q.k = I.k;
             Q.n = warp_walk_run_q(I, Q.qs, Q.qe, Pd[d][qi], hrs, hpk, plan.maxrun);
-            nam_close_passed(L, Q.qs);
-            nam_merge_nam_major_q(L, Q, tb);
+            nam_close_merge_q(L, Q, tb);
         }
         nam_close_passed(L, 0x7FFFFFFF);
     }
 }
 
 constexpr uint32_t kWarpSortMax = 256;   // rescued reads with more NAMs are sorted by k_sort_jobs
+constexpr uint32_t kSortTile = 2048;      // keys per shared-memory tile of the small block sort (56 KB)
+constexpr uint32_t kSortTileLarge = 8192; // keys per tile of the large block sort (224 KB)
 
 // find_nams_rescue for the reads on the rescue list (a warp per read).  Reads that
 // end with more than kWarpSortMax NAMs leave the sort to k_sort_jobs.
@@ -563,20 +741,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
     __shared__ uint32_t s_hpk[kWarpsPerBlock][kRescueSmemHits];
     __shared__ uint8_t s_tb[kWarpsPerBlock][kRescueSmemHits];
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
-    const uint32_t n_rescue = *(volatile unsigned int*)&ctr->n_rescue;
+    const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_rescue_heavy;
+    const uint32_t n_rescue = n_heavy + *(volatile unsigned int*)&ctr->n_rescue;
     for (uint32_t t = warp_global_id(); t < n_rescue; t += warp_count()) {
         const long long t_start = clock64();
-        const uint32_t r = A.rescue_list[t];
+        // heavy reads first: the lowest warps (first blocks dispatched) take them
+        const uint32_t r = t < n_heavy ? A.rescue_list[A.rescue_cap - 1 - t] : A.rescue_list[t - n_heavy];
         ReadRec& R = rec[r];
         struct CycleNote {
             const Arenas& A;
             uint32_t t;
             long long t0;
             __device__ ~CycleNote() {
-                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[4ull * t] = (uint64_t)(clock64() - t0);
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[8ull * t] = (uint64_t)(clock64() - t0);
             }
             __device__ void phase(int k, long long since) const {
-                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[4ull * t + k] = (uint64_t)(clock64() - since);
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[8ull * t + k] = (uint64_t)(clock64() - since);
+            }
+            __device__ void set(int k, uint64_t v) const {
+                if (A.rescue_cycles && lane_id() == 0) A.rescue_cycles[8ull * t + k] = v;
             }
         } note{A, t, t_start};
         const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
@@ -593,6 +776,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         uint64_t* buf = reinterpret_cast<uint64_t*>(sc1);
         const RescuePlan plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
         note.phase(1, t_start);
+        note.set(4, plan.bound);
+        note.set(6, plan.m[0] + plan.m[1]);
+        note.set(7, plan.maxrun);
         if (plan.bound == 0) {
             if (lane == 0) R.n_nams = 0;
             continue;
@@ -623,15 +809,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         const long long t_merge = clock64();
         rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hrs, hpk, tb);
         note.phase(2, t_merge);
+        note.set(5, L.n_closed);
         if (L.n_closed > kWarpSortMax) {
             // many NAMs: the block-per-read sort kernel orders them
             if (lane == 0) {
-                const uint32_t j = atomicAdd(&ctr->n_heavy, 1u);
+                const uint32_t j = L.n_closed > kSortTile ? A.jobs_cap - 1 - atomicAdd(&ctr->n_huge, 1u)
+                                                          : atomicAdd(&ctr->n_heavy, 1u);
                 SortJob job;
                 job.closed = L.closed;
                 job.keys = keys;
                 job.n = L.n_closed;
                 job.read = r;
+                job.note = t;
+                job.pad = 0;
                 A.sort_jobs[j] = job;
             }
             continue;
@@ -682,7 +872,6 @@ struct SortTile {
     }
 };
 
-constexpr uint32_t kSortTile = 2048;   // keys per shared-memory tile (56 KB)
 
 __device__ __forceinline__ void cmp_swap(NamKey* keys, uint32_t i, uint32_t j, uint32_t k) {
     const uint32_t ixj = i ^ j;
@@ -697,10 +886,10 @@ __device__ __forceinline__ void cmp_swap(NamKey* keys, uint32_t i, uint32_t j, u
 }
 
 // Block bitonic sort of n keys (room for next_pow2(n) in global memory) by all
-// threads of the block.  Every stage whose partner distance is below kSortTile runs
-// on a shared-memory tile of kSortTile keys; only the stages with larger distances
-// touch global memory.
-__device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile) {
+// threads of the block.  Every stage whose partner distance is below tcap runs on a
+// shared-memory tile of tcap keys; only the stages with larger distances touch
+// global memory.
+__device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile, uint32_t tcap) {
     const uint32_t P = next_pow2(n);
     for (uint32_t i = n + threadIdx.x; i < P; i += blockDim.x) {
         NamKey k;
@@ -710,7 +899,7 @@ __device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile) {
         keys[i] = k;
     }
     __syncthreads();
-    const uint32_t T = P < kSortTile ? P : kSortTile;
+    const uint32_t T = P < tcap ? P : tcap;
     // Runs all stages (k, j) with j < T inside each tile; k is the current merge size
     // (k <= T: the tile-local sort from scratch; k > T: finish merge level k).
     auto tile_pass = [&](uint32_t k_from, uint32_t k_to, uint32_t j_from) {
@@ -743,30 +932,63 @@ __device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile) {
     }
 }
 
-constexpr uint32_t kSortThreads = 256;
+// Bitonic sort of the P (a power of two) keys held in the tile.
+__device__ void tile_sort(SortTile tile, uint32_t P) {
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t q = threadIdx.x; q < P / 2; q += blockDim.x) {
+                const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                const uint32_t ixj = i | j;
+                if (tile.less_at(ixj, i) == ((i & k) == 0)) tile.swap(i, ixj);
+            }
+            __syncthreads();
+        }
+    }
+}
 
 // Sorts the NAMs of the rescued reads with more than kWarpSortMax NAMs (typically
 // reads inside short tandem repeats, with hundreds to thousands of NAMs): one block
-// per read, bitonic sort tiled through shared memory, then the read's NAMs are
-// written to the NAM arena in order.
-__global__ void __launch_bounds__(kSortThreads) k_sort_jobs(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
-                                                              Counters* ctr) {
-    extern __shared__ __align__(16) uint8_t s_dyn[];   // kSortTile sort keys, one array per field
+// per read, then the read's NAMs are written to the NAM arena in order.  A read whose
+// keys fit the tile is sorted in shared memory alone; larger ones through global
+// memory (block_sort_keys).  The small kernel takes the jobs from the front of the
+// job list (at most kSortTile NAMs), the large one those from the back.
+template <int kThreads, uint32_t kTile, bool kLarge>
+__global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
+                                                         Counters* ctr) {
+    extern __shared__ __align__(16) uint8_t s_dyn[];   // kTile sort keys, one array per field
     __shared__ uint64_t s_noff;
-    SortTile s_tile;
-    s_tile.k1 = reinterpret_cast<uint64_t*>(s_dyn);
-    s_tile.k2 = s_tile.k1 + kSortTile;
-    s_tile.k3 = s_tile.k2 + kSortTile;
-    s_tile.idx = reinterpret_cast<uint32_t*>(s_tile.k3 + kSortTile);
-    const uint32_t n_jobs = *(volatile unsigned int*)&ctr->n_heavy;
+    SortTile tile;
+    tile.k1 = reinterpret_cast<uint64_t*>(s_dyn);
+    tile.k2 = tile.k1 + kTile;
+    tile.k3 = tile.k2 + kTile;
+    tile.idx = reinterpret_cast<uint32_t*>(tile.k3 + kTile);
+    const uint32_t n_jobs = kLarge ? *(volatile unsigned int*)&ctr->n_huge : *(volatile unsigned int*)&ctr->n_heavy;
     for (uint32_t h = blockIdx.x; h < n_jobs; h += gridDim.x) {
-        const SortJob job = A.sort_jobs[h];
+        const long long t0 = clock64();
+        const SortJob job = A.sort_jobs[kLarge ? A.jobs_cap - 1 - h : h];
         ReadRec& R = rec[job.read];
         const NamState* closed = job.closed;
         const uint32_t NN = job.n;
-        for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) job.keys[i] = nam_key(closed[i], i, C.sort_mode);
-        __syncthreads();
-        block_sort_keys(job.keys, NN, s_tile);
+        const uint32_t P = next_pow2(NN);
+        const bool in_tile = P <= kTile;
+        if (in_tile) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                NamKey k;
+                if (i < NN) {
+                    k = nam_key(closed[i], i, C.sort_mode);
+                } else {
+                    k.k1 = k.k2 = k.k3 = ~0ULL;
+                    k.idx = 0xFFFFFFFFu;
+                }
+                tile.put(i, k);
+            }
+            __syncthreads();
+            tile_sort(tile, P);
+        } else {
+            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) job.keys[i] = nam_key(closed[i], i, C.sort_mode);
+            __syncthreads();
+            block_sort_keys(job.keys, NN, tile, kTile);
+        }
         if (threadIdx.x == 0) {
             const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)NN);
             if (noff + NN > A.nam_cap) {
@@ -782,8 +1004,10 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_jobs(MapConfig C, ReadRec
         __syncthreads();
         const uint64_t noff = s_noff;
         if (noff != ~0ULL)
-            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) A.nams[noff + i] = closed[job.keys[i].idx];
+            for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x)
+                A.nams[noff + i] = closed[in_tile ? tile.idx[i] : job.keys[i].idx];
         __syncthreads();
+        if (A.rescue_cycles && threadIdx.x == 0) A.rescue_cycles[8ull * job.note + 3] = (uint64_t)(clock64() - t0);
     }
 }
 
@@ -888,7 +1112,14 @@ void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec,
     k_nams_lane<<<grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * 5), 32 * kLaneWarps, 0, st>>>(C, n, rec,
                                                                                                         A, ctr);
     GBSA_LAUNCHED();
-    k_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(C, rec, A, ctr);
+}
+
+void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    if (!n) return;
+    // at most nam_kernel_warps(n) warps: one scratch slot each
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * kHeavyBlocksPerSm,
+                                                         (n + kHeavyWarps - 1) / kHeavyWarps);
+    k_nams<<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
@@ -900,13 +1131,20 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
 }
 
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    constexpr int kSmall = 256, kLarge = 1024;
+    constexpr size_t smem_small = kSortTile * 28, smem_large = kSortTileLarge * 28;
     static bool attr = false;
     if (!attr) {
-        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(kSortTile * 28)));
+        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_small));
+        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kLarge, kSortTileLarge, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_large));
         attr = true;
     }
-    k_sort_jobs<<<(unsigned)device_sm_count() * 4, kSortThreads, kSortTile * 28, st>>>(C, rec, A, ctr);
+    const unsigned sms = (unsigned)device_sm_count();
+    k_sort_jobs<kLarge, kSortTileLarge, true><<<sms, kLarge, smem_large, st>>>(C, rec, A, ctr);
+    GBSA_LAUNCHED();
+    k_sort_jobs<kSmall, kSortTile, false><<<sms * 4, kSmall, smem_small, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

@@ -167,23 +167,33 @@ __device__ __forceinline__ int nam_candidate_q(const NamState& n, const QueryHit
     return -1;
 }
 
-// NAM-major merge of one query's hits in compact form (same rule as
-// nam_merge_nam_major).  taken: Q.n bytes of scratch.
-__device__ __forceinline__ void nam_merge_nam_major_q(NamLists& L, const QueryHits& Q, uint8_t* taken) {
+// One query of the NAM-major merge (hits in compact form), in one pass over the open
+// list: NAMs the query has passed (query_end < query_start) go to the closed list in
+// open-list order, as nam_close_passed; the others are compacted and, 32 at a time,
+// each takes the first untaken hit it accepts (clash-resolved as described at the
+// top of this file); untaken hits then open new NAMs in ref_start order.  taken: Q.n
+// bytes of scratch.  The next 32 open NAMs are loaded while the current ones
+// resolve (writes go only to positions already read).
+__device__ __forceinline__ void nam_close_merge_q(NamLists& L, const QueryHits& Q, uint8_t* taken) {
     const uint32_t lane = lane_id();
     const uint32_t nh = Q.n;
     for (uint32_t j = lane; j < nh; j += 32) taken[j] = 0;
     __syncwarp();
     const uint32_t nn = L.n_open;
     const uint32_t dirbit = Q.dir << 31;
+    uint32_t keep = 0, done = 0;
+    NamState nxt;
+    if (lane < nn) nxt = L.open[lane];
     for (uint32_t base = 0; base < nn; base += 32) {
         const uint32_t o = base + lane;
-        NamState mine;
-        bool resolved = true;
-        if (o < nn) {
-            mine = L.open[o];
-            resolved = mine.qe < Q.qs || (mine.ref_rc & 0x80000000u) != dirbit;
-        }
+        const bool valid = o < nn;
+        NamState mine = nxt;
+        if (o + 32 < nn) nxt = L.open[o + 32];
+        const bool close = valid && mine.qe < Q.qs;
+        const bool stay = valid && !close;
+        const uint32_t mc = __ballot_sync(0xFFFFFFFFu, close);
+        const uint32_t ms = __ballot_sync(0xFFFFFFFFu, stay);
+        bool resolved = !stay || (mine.ref_rc & 0x80000000u) != dirbit;
         bool dirty = false;
         for (;;) {
             int cand = -1;
@@ -204,8 +214,17 @@ __device__ __forceinline__ void nam_merge_nam_major_q(NamLists& L, const QueryHi
             __syncwarp();
             if (!cm) break;
         }
-        if (dirty) L.open[o] = mine;
+        if (close) L.closed[L.n_closed + done + __popc(mc & lanemask_lt())] = mine;
+        if (stay) {
+            const uint32_t to = keep + __popc(ms & lanemask_lt());
+            if (dirty || to != o) L.open[to] = mine;
+        }
+        keep += __popc(ms);
+        done += __popc(mc);
     }
+    L.n_open = keep;
+    L.n_closed += done;
+    __syncwarp();
     // untaken hits open new NAMs, in ref_start order
     uint32_t added = 0;
     for (uint32_t b = 0; b < nh; b += 32) {
@@ -269,67 +288,6 @@ __device__ __forceinline__ uint32_t warp_walk_run_q(const IndexView& I, int qs, 
     }
     __syncwarp();
     return n;
-}
-
-// First untaken hit of h[0..nh) (sorted by rs) that NAM n would take, or -1.
-__device__ __forceinline__ int nam_candidate(const NamState& n, const HitRec* h, uint32_t nh, const uint8_t* taken) {
-    uint32_t lo = 0, hi = nh;
-    const int from = n.rprev + 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (h[mid].rs < from) lo = mid + 1;
-        else hi = mid;
-    }
-    for (uint32_t j = lo; j < nh; ++j) {
-        const HitRec x = h[j];
-        if (x.rs > n.re) break;
-        if (x.ref_rc != n.ref_rc || taken[j]) continue;
-        if (nam_takes(n, x)) return (int)j;
-    }
-    return -1;
-}
-
-// NAM-major merge of the hits h[0..nh) of one query randstrobe with query_start qs
-// (sorted by rs).  taken: nh bytes of scratch.
-__device__ __forceinline__ void nam_merge_nam_major(NamLists& L, const HitRec* h, uint32_t nh, int qs,
-                                                    uint8_t* taken) {
-    const uint32_t lane = lane_id();
-    for (uint32_t j = lane; j < nh; j += 32) taken[j] = 0;
-    __syncwarp();
-    const uint32_t nn = L.n_open;
-    for (uint32_t base = 0; base < nn; base += 32) {
-        const uint32_t o = base + lane;
-        bool resolved = !(o < nn) || L.open[o].qe < qs;
-        for (;;) {
-            int cand = -1;
-            if (!resolved) cand = nam_candidate(L.open[o], h, nh, taken);
-            const uint32_t key = cand < 0 ? 0xFFFFFFFFu : (uint32_t)cand;
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-            const bool clash = cand >= 0 && (peers & lanemask_lt()) != 0;
-            const uint32_t cm = __ballot_sync(0xFFFFFFFFu, clash);
-            const uint32_t lim = cm ? (uint32_t)(__ffs(cm) - 1) : 32u;
-            if (!resolved && lane < lim) {
-                if (cand >= 0) {
-                    taken[cand] = 1;
-                    nam_add(L.open[o], h[cand]);
-                }
-                resolved = true;
-            }
-            __syncwarp();
-            if (!cm) break;
-        }
-    }
-    // untaken hits open new NAMs, in ref_start order
-    uint32_t added = 0;
-    for (uint32_t b = 0; b < nh; b += 32) {
-        const uint32_t j = b + lane;
-        const bool mk = j < nh && !taken[j];
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, mk);
-        if (mk) L.open[L.n_open + added + __popc(m & lanemask_lt())] = nam_from_hit(h[j]);
-        added += __popc(m);
-    }
-    L.n_open += added;
-    __syncwarp();
 }
 
 // Score (step2/nam.cu:454-463): n_hits * (2*min_span - max_span) if positive, else 1.

@@ -66,6 +66,7 @@ def lib():
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
             "gbsa_randstrobes_query_noalloc": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64), vp]),
             "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, vp]),
+            "gbsa_mapper_nam_cycles": (i32, [vp, vp, u32, vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -219,7 +220,7 @@ class Mapper:
     def last_alg_bytes(self):
         return lib().gbsa_mapper_last_alg_bytes(self.h)
 
-    STAGES = ("seed", "seed_long", "lookup", "nams", "rescue", "rescue_sort")
+    STAGES = ("seed", "seed_long", "lookup", "nams", "nams_warp", "rescue", "rescue_sort")
 
     def set_profile(self, on=True):
         _check(lib().gbsa_mapper_set_profile(self.h, 1 if on else 0))
@@ -230,17 +231,26 @@ class Mapper:
         return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes", "warp_nam_reads"),
                         (int(x) for x in a)))
 
-    def rescue_cycles(self, cap=1 << 22):
+    def rescue_cycles(self, cap=1 << 24):
+        """Per rescued read: cycles (total, plan, merge, sort), hit bound, NAMs,
+        queries taken, longest run; and the count of block-sorted reads."""
         a = np.zeros(cap, np.uint64)
         n = (C.c_uint32 * 2)()
         _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, n))
-        k = min(cap // 4, n[0] + n[1])
-        a = a[: 4 * k].reshape(-1, 4)
-        return a[: n[0]], a[n[0]:k]
+        k = min(cap // 8, n[0])
+        return a[: 8 * k].reshape(-1, 8), int(n[1])
+
+    def nam_cycles(self, cap=1 << 22):
+        """Per read of the warp find_nams kernel: (cycles, hits, NAMs, merge cycles)."""
+        a = np.zeros(cap, np.uint64)
+        n = (C.c_uint32 * 1)()
+        _check(lib().gbsa_mapper_nam_cycles(self.h, a.ctypes.data, cap, n))
+        k = min(cap // 4, n[0])
+        return a[: 4 * k].reshape(-1, 4)
 
     def stage_ms(self):
-        a = np.zeros(6, np.float32)
-        lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 6)
+        a = np.zeros(7, np.float32)
+        lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 7)
         return dict(zip(self.STAGES, a.tolist()))
 
     def map_reads(self, reads, capacity=None):

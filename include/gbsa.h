@@ -240,7 +240,9 @@ void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on);
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
  * returns the last batch's milliseconds for: seeding, long-read seeding, lookup,
- * NAM merge + sort, rescue, sorting of the rescued reads with many NAMs.  No
+ * NAM merge + sort (lane per read), NAM merge + sort (warp per read), rescue,
+ * sorting of the rescued reads with many NAMs.  The last two run on a second
+ * stream beside the two NAM stages and are timed from the end of the lookup.  No
  * reference counterpart. */
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
@@ -249,12 +251,18 @@ int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
  * [5] overflow scratch bytes, [6] reads merged by the warp-cooperative NAM kernel.
  * out must hold 7 values.  No reference counterpart. */
 int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
-/* With profiling on: SM clock cycles spent on each rescued read of the last batch, 4
- * values per read (total, planning, merge, sort; for reads of the block-per-read
- * kernel: total, planning + merge, sort, NAM count), the warp kernel's reads first;
- * n_out[0] / n_out[1] receive the two read counts; out holds up to cap values.
- * No reference counterpart. */
+/* With profiling on: 8 values per rescued read of the last batch, in rescue-list
+ * order: SM clock cycles in total (without a block sort), of the planning, of the
+ * merge and of the sort (the block sort, for reads with many NAMs), then the hit
+ * bound, the NAM count, the queries taken and the longest hit run.  n_out[0] receives
+ * the rescued read count, n_out[1] the count of block-sorted reads; out holds up
+ * to cap values.  No reference counterpart. */
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out);
+
+/* With profiling on: per read of the last batch's warp-per-read find_nams kernel,
+ * four values (SM cycles in total, hits, NAMs, SM cycles of the merge); n_out[0]
+ * receives the read count; out holds up to cap values.  No reference counterpart. */
+int gbsa_mapper_nam_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out);
 
 #ifdef __cplusplus
 }
