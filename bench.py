@@ -313,8 +313,10 @@ def main():
         rescue_profile = {
             "total_us": dist(resc[:, 0], mhz), "plan_us": dist(resc[:, 1], mhz),
             "merge_us": dist(resc[:, 2], mhz), "sort_us": dist(resc[:, 3], mhz),
-            "hit_bound": dist(resc[:, 4]), "nams": dist(resc[:, 5]), "queries": dist(resc[:, 6]),
+            "hit_bound": dist(resc[:, 4]), "nams": dist(resc[:, 5]), "walk_us": dist(resc[:, 6], mhz),
             "max_run": dist(resc[:, 7]), "block_sorted_reads": n_block_sorted,
+            "block_sort_small_us": dist(resc[(resc[:, 5] > 256) & (resc[:, 5] <= 2048), 3], mhz),
+            "block_sort_large_us": dist(resc[resc[:, 5] > 2048, 3], mhz),
             "worst": worst.tolist(),
         }
     nam_profile = None

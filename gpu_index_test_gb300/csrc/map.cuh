@@ -40,7 +40,7 @@ struct Counters {
     unsigned int n_heavy;  // rescued reads whose NAMs the block-per-read sort kernel orders (small tile)
     unsigned int n_rescue_heavy;  // rescued reads on the heavy end of the rescue list
     unsigned int n_huge;   // rescued reads whose NAMs the large-tile block sort orders
-    unsigned int pad2;
+    unsigned int rescue_next;  // next rescue-list entry to take (k_rescue's work counter)
 };
 
 // A read whose NAMs are sorted by the block-per-read sort kernel.

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_seed_long(DevParams P, 
     }
 }
 
-constexpr uint32_t kRescueHeavySeeds = 8;   // found but repetitive query randstrobes of a heavy rescued read
+constexpr uint32_t kRescueHeavyHits = 2000;   // estimated merge hits of a heavy rescued read
 
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
                                                                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
@@ -162,14 +162,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
             R.n_found = tot;
         }
         if (rescue) {
+            // Reads inside short tandem repeats merge thousands of hits: their seeds'
+            // runs (up to the count cap) estimate the merge's hits; reads above
+            // kRescueHeavyHits go to the heavy end of the list, whose warps start first.
+            uint32_t w = 0;
+            if (good < tot) {
+                for (uint32_t i = lane; i < nq2; i += 32) {
+                    const uint64_t pos = A.q_pos[R.q_off + i];
+                    if (pos == kNotFound) continue;
+                    const uint32_t c = index_get_count(I, pos);
+                    w += c <= C.count_cap ? c : 0u;
+                }
+                w = warp_sum(w);
+            }
+            const bool heavy = w >= kRescueHeavyHits;
             if (lane == 0) {
                 R.flags |= kReadRescue;
-                // reads with many repetitive seeds (short tandem repeats) merge thousands of
-                // hits: they go to the heavy end so that their warps start first
-                if (tot - good >= kRescueHeavySeeds)
-                    A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
-                else
-                    A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
+                if (heavy) A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
+                else A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
                 R.n_hits = 0;
             }
             continue;
@@ -686,7 +696,7 @@ __device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, con
             const uint32_t cnt = (uint32_t)(rk[d][j] >> 32);
             bsum += cnt;
             bmax = cnt > bmax ? cnt : bmax;
-            tk[d][j] = rk[d][j] & 0xFFFFFFFFull;
+            tk[d][j] = ((rk[d][j] & 0xFFFFFFFFull) << 32) | cnt;   // (start, index) order, run length
         }
         plan.bound += warp_sum(bsum);
 #pragma unroll
@@ -705,13 +715,15 @@ __device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, con
 // query_start) order and merge them NAM-major; all NAMs end in L.closed.  The hits
 // of the current query are held in compact form in hrs/hpk/tb (room for
 // plan.maxrun hits).
-__device__ void rescue_merge(const IndexView& I, const Query* const* Qd, const uint64_t* const* Pd,
-                             const RescuePlan& plan, const uint64_t* tkbuf, uint32_t Pq, NamLists& L, uint32_t* hrs,
-                             uint32_t* hpk, uint8_t* tb) {
+__device__ uint64_t rescue_merge(const IndexView& I, const Query* const* Qd, const uint64_t* const* Pd,
+                                 const RescuePlan& plan, const uint64_t* tkbuf, uint32_t Pq, NamLists& L, uint32_t* hrs,
+                                 uint32_t* hpk, uint8_t* tb) {
+    uint64_t walk_cycles = 0;
     const uint64_t* tk[2] = {tkbuf + 2 * Pq, tkbuf + 3 * Pq};
     for (int d = 0; d < 2; ++d) {
         for (uint32_t j = 0; j < plan.m[d]; ++j) {
-            const uint32_t qi = (uint32_t)(tk[d][j] & 0xFFFF);
+            const uint32_t qi = (uint32_t)(tk[d][j] >> 32) & 0xFFFF;
+            const uint32_t cnt = (uint32_t)tk[d][j];
             const Query q = Qd[d][qi];
             QueryHits Q;
             Q.rs = hrs;
@@ -720,11 +732,14 @@ __device__ void rescue_merge(const IndexView& I, const Query* const* Qd, const u
             Q.qe = (int)q.end;
             Q.dir = (uint32_t)d;
             Q.k = I.k;
-            Q.n = warp_walk_run_q(I, Q.qs, Q.qe, Pd[d][qi], hrs, hpk, plan.maxrun);
+            const long long tw = clock64();
+            Q.n = warp_walk_run_n(I, Q.qs, Q.qe, Pd[d][qi], cnt, hrs, hpk, plan.maxrun);
+            walk_cycles += (uint64_t)(clock64() - tw);
             nam_close_merge_q(L, Q, tb);
         }
         nam_close_passed(L, 0x7FFFFFFF);
     }
+    return walk_cycles;
 }
 
 constexpr uint32_t kWarpSortMax = 256;   // rescued reads with more NAMs are sorted by k_sort_jobs
@@ -743,9 +758,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_rescue_heavy;
     const uint32_t n_rescue = n_heavy + *(volatile unsigned int*)&ctr->n_rescue;
-    for (uint32_t t = warp_global_id(); t < n_rescue; t += warp_count()) {
+    // resident warps take reads in list order, heavy ones first
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&ctr->rescue_next, 1u);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        if (t >= n_rescue) break;
         const long long t_start = clock64();
-        // heavy reads first: the lowest warps (first blocks dispatched) take them
         const uint32_t r = t < n_heavy ? A.rescue_list[A.rescue_cap - 1 - t] : A.rescue_list[t - n_heavy];
         ReadRec& R = rec[r];
         struct CycleNote {
@@ -777,7 +796,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         const RescuePlan plan = rescue_prepare(I, C, Qd, Pd, nqd, Pq, buf);
         note.phase(1, t_start);
         note.set(4, plan.bound);
-        note.set(6, plan.m[0] + plan.m[1]);
         note.set(7, plan.maxrun);
         if (plan.bound == 0) {
             if (lane == 0) R.n_nams = 0;
@@ -807,8 +825,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         L.n_open = L.n_closed = 0;
         L.cap = H;
         const long long t_merge = clock64();
-        rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hrs, hpk, tb);
+        const uint64_t walk = rescue_merge(I, Qd, Pd, plan, buf, Pq, L, hrs, hpk, tb);
         note.phase(2, t_merge);
+        note.set(6, walk);
         note.set(5, L.n_closed);
         if (L.n_closed > kWarpSortMax) {
             // many NAMs: the block-per-read sort kernel orders them
@@ -1126,7 +1145,12 @@ void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Co
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st) {
     if (!n_reads) return;
-    k_rescue<<<warp_grid(n_reads, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
+    // persistent: as many blocks as are resident at once (at most one scratch slot per warp)
+    static int per_sm = 0;
+    if (!per_sm) GBSA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rescue, 32 * kWarpsPerBlock, 0));
+    const unsigned blocks =
+        std::min<unsigned>(warp_grid(n_reads, kWarpsPerBlock), (unsigned)device_sm_count() * std::max(per_sm, 1));
+    k_rescue<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

@@ -238,53 +238,57 @@ __device__ __forceinline__ void nam_close_merge_q(NamLists& L, const QueryHits& 
     __syncwarp();
 }
 
-// Warp-cooperative add_to_hits_per_ref for one query (as warp_walk_run) writing the
-// kept hits in compact form: rs[] = position, pk[] = packed.  Returns their count
-// (at most cap are written).
-__device__ __forceinline__ uint32_t warp_walk_run_q(const IndexView& I, int qs, int qe, uint64_t pos, uint32_t* rs_out,
-                                                    uint32_t* pk_out, uint32_t cap) {
+// Warp-cooperative add_to_hits_per_ref (step2/nam.cu:45-62) for one query whose
+// equal-hash run [pos, pos + cnt) is known: an entry is kept when its length
+// difference is <= every earlier difference of the run (the reference's running
+// minimum), found with a warp prefix minimum.  Writes the kept hits in compact form
+// (rs[] = position, pk[] = packed, in run order) and returns their count (at most
+// cap are written).  The entries are loaded 128 at a time, four per lane, so a run
+// of up to 128 costs one memory round trip.
+__device__ __forceinline__ uint32_t warp_walk_run_n(const IndexView& I, int qs, int qe, uint64_t pos, uint32_t cnt,
+                                                    uint32_t* rs_out, uint32_t* pk_out, uint32_t cap) {
     const uint32_t lane = lane_id();
-    const uint64_t key = get_hash(I, pos);
     int carry = 0x7FFFFFFF;
     uint32_t n = 0;
-    for (uint64_t base = pos;; base += 32) {
-        const uint64_t p = base + lane;
-        bool in = false;
-        gbsa_ref_randstrobe e;
-        int diff = 0x7FFFFFFF;
-        if (p < I.n) {
-            e = I.rs[p];
-            in = e.hash == key;
-        }
-        const uint32_t inm = __ballot_sync(0xFFFFFFFFu, in);
-        const uint32_t runm = (~inm) ? (inm & ((1u << (__ffs(~inm) - 1)) - 1)) : inm;
-        const bool mine = (runm >> lane) & 1u;
-        if (mine) {
-            const int d = (qe - qs) - ((int)(e.packed & 0xFF) + I.k);
-            diff = d < 0 ? -d : d;
-        }
-        int pm = diff;
+    const uint2* ent = reinterpret_cast<const uint2*>(I.rs + pos);   // (position, packed) at offset 8
+    for (uint32_t base = 0; base < cnt; base += 128) {
+        uint2 e[4];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xFFFFFFFFu, pm, o);
-            if (lane >= (uint32_t)o) pm = v < pm ? v : pm;
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = base + 32 * u + lane;
+            e[u] = j < cnt ? __ldg(&ent[2 * (size_t)j + 1]) : make_uint2(0, 0);
         }
-        int excl = __shfl_up_sync(0xFFFFFFFFu, pm, 1);
-        if (lane == 0) excl = 0x7FFFFFFF;
-        excl = excl < carry ? excl : carry;
-        const bool keep = mine && diff <= excl;
-        const uint32_t km = __ballot_sync(0xFFFFFFFFu, keep);
-        if (keep) {
-            const uint32_t k = n + __popc(km & lanemask_lt());
-            if (k < cap) {
-                rs_out[k] = e.position;
-                pk_out[k] = e.packed;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = base + 32 * u + lane;
+            const bool mine = j < cnt;
+            int diff = 0x7FFFFFFF;
+            if (mine) {
+                const int d = (qe - qs) - ((int)(e[u].y & 0xFF) + I.k);
+                diff = d < 0 ? -d : d;
             }
+            int pm = diff;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xFFFFFFFFu, pm, o);
+                if (lane >= (uint32_t)o) pm = v < pm ? v : pm;
+            }
+            int excl = __shfl_up_sync(0xFFFFFFFFu, pm, 1);
+            if (lane == 0) excl = 0x7FFFFFFF;
+            excl = excl < carry ? excl : carry;
+            const bool keep = mine && diff <= excl;
+            const uint32_t km = __ballot_sync(0xFFFFFFFFu, keep);
+            if (keep) {
+                const uint32_t k = n + __popc(km & lanemask_lt());
+                if (k < cap) {
+                    rs_out[k] = e[u].x;
+                    pk_out[k] = e[u].y;
+                }
+            }
+            n += __popc(km);
+            const int tot = __shfl_sync(0xFFFFFFFFu, pm, 31);
+            carry = tot < carry ? tot : carry;
         }
-        n += __popc(km);
-        const int tot = __shfl_sync(0xFFFFFFFFu, pm, 31);
-        carry = tot < carry ? tot : carry;
-        if (runm != 0xFFFFFFFFu) break;
     }
     __syncwarp();
     return n;
@@ -413,70 +417,6 @@ __device__ inline void warp_sort_u64(uint64_t* keys, uint32_t n) {
             __syncwarp();
         }
     }
-}
-
-// Warp-cooperative add_to_hits_per_ref (step2/nam.cu:45-62) for one query: walks
-// the equal-hash run from pos 32 entries at a time; an entry is kept when its
-// length difference is <= every earlier difference of the run (the reference's
-// running minimum), found with a warp prefix-min.  Writes the kept hits to out (in
-// run order, i.e. by position) and returns their count (at most cap are written).
-__device__ __forceinline__ uint32_t warp_walk_run(const IndexView& I, int qs, int qe, uint64_t pos, uint32_t dir,
-                                                  HitRec* out, uint32_t cap) {
-    const uint32_t lane = lane_id();
-    const uint64_t key = get_hash(I, pos);
-    int carry = 0x7FFFFFFF;
-    uint32_t n = 0;
-    for (uint64_t base = pos;; base += 32) {
-        const uint64_t p = base + lane;
-        bool in = false;
-        gbsa_ref_randstrobe e;
-        int diff = 0x7FFFFFFF;
-        if (p < I.n) {
-            e = I.rs[p];
-            in = e.hash == key;
-        }
-        const uint32_t inm = __ballot_sync(0xFFFFFFFFu, in);
-        // the run is contiguous: lanes after the first miss are out
-        const uint32_t runm = (~inm) ? (inm & ((1u << __ffs(~inm) - 1) - 1)) : inm;
-        const bool mine = (runm >> lane) & 1u;
-        int rs = 0, re = 0;
-        if (mine) {
-            rs = (int)e.position;
-            re = rs + (int)(e.packed & 0xFF) + I.k;
-            const int d = (qe - qs) - (re - rs);
-            diff = d < 0 ? -d : d;
-        }
-        // exclusive prefix minimum of diff over earlier lanes, with the carry
-        int pm = diff;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xFFFFFFFFu, pm, o);
-            if (lane >= (uint32_t)o) pm = v < pm ? v : pm;
-        }
-        int excl = __shfl_up_sync(0xFFFFFFFFu, pm, 1);
-        if (lane == 0) excl = 0x7FFFFFFF;
-        excl = excl < carry ? excl : carry;
-        const bool keep = mine && diff <= excl;
-        const uint32_t km = __ballot_sync(0xFFFFFFFFu, keep);
-        if (keep) {
-            const uint32_t k = n + __popc(km & lanemask_lt());
-            if (k < cap) {
-                HitRec h;
-                h.ref_rc = (dir << 31) | (e.packed >> 8);
-                h.qs = qs;
-                h.qe = qe;
-                h.rs = rs;
-                h.re = re;
-                out[k] = h;
-            }
-        }
-        n += __popc(km);
-        const int tot = __shfl_sync(0xFFFFFFFFu, pm, 31);
-        carry = tot < carry ? tot : carry;
-        if (runm != 0xFFFFFFFFu) break;
-    }
-    __syncwarp();
-    return n;
 }
 
 }  // namespace gbsa

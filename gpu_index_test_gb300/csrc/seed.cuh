@@ -37,54 +37,44 @@ struct WinInfo {
 
 // 2-bit packing of ASCII bases into MSB-first 64-bit words plus an N bitmask
 // (LSB-first 32-bit words; bases at or beyond L count as N).  Writes
-// nwords = ceil(L/32) + 2 words to each array.  Coalesced: each warp load covers
-// 32 consecutive bytes.
-__device__ __forceinline__ uint64_t spread_bits(uint32_t x) {
-    uint64_t v = x;
-    v = (v | (v << 16)) & 0x0000FFFF0000FFFFULL;
-    v = (v | (v << 8)) & 0x00FF00FF00FF00FFULL;
-    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0FULL;
-    v = (v | (v << 2)) & 0x3333333333333333ULL;
-    v = (v | (v << 1)) & 0x5555555555555555ULL;
-    return v;
-}
-
+// nwords = ceil(L/32) + 2 words to each array.  Each lane codes 4 consecutive bases
+// per round of 128; 8 lanes then make a word with three xor-shuffles.
 __device__ __forceinline__ void warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
     const uint32_t lane = lane_id();
     const uint32_t nw = (L + 31) / 32 + 2;
-    for (uint32_t w0 = 0; w0 < nw; w0 += 32) {
-        // ballots of word w0 + j are kept by lane j, then every lane spreads its own
-        uint32_t m0 = 0, m1 = 0, mn = 0;
-        const uint32_t cnt = nw - w0 < 32 ? nw - w0 : 32;
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const uint32_t p = (w0 + j) * 32 + lane;
+    const uint32_t sub = lane & 7;   // position of the lane's 4 bases within the word
+    for (uint32_t b0 = 0; b0 < nw * 32; b0 += 128) {
+        uint32_t code8 = 0, nbits = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < 4; ++u) {
+            const uint32_t p = b0 + 4 * lane + u;
             const uint32_t c = p < L ? nt4(seq[p]) : 4u;
-            const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, c & 1u);
-            const uint32_t b1 = __ballot_sync(0xFFFFFFFFu, (c >> 1) & 1u);
-            const uint32_t bn = __ballot_sync(0xFFFFFFFFu, c == 4u);
-            if (lane == j) {
-                m0 = b0;
-                m1 = b1;
-                mn = bn;
-            }
+            code8 = (code8 << 2) | (c & 3u);   // an N packs as 0
+            nbits |= (c == 4u ? 1u : 0u) << u;
         }
-        if (lane < cnt) {
-            const uint64_t lo = spread_bits(__brev(m0 & ~mn));
-            const uint64_t hi = spread_bits(__brev(m1 & ~mn));
-            packed[w0 + lane] = lo | (hi << 1);
-            nmask[w0 + lane] = mn;
+        uint64_t v = (uint64_t)code8 << (8 * (7 - sub));
+        uint32_t nm = nbits << (4 * sub);
+#pragma unroll
+        for (int x = 1; x < 8; x <<= 1) {
+            v |= __shfl_xor_sync(0xFFFFFFFFu, v, x);
+            nm |= __shfl_xor_sync(0xFFFFFFFFu, nm, x);
+        }
+        const uint32_t wi = b0 / 32 + lane / 8;
+        if (sub == 0 && wi < nw) {
+            packed[wi] = v;
+            nmask[wi] = nm;
         }
     }
     __syncwarp();
 }
 
-// n (<= 32) bits of an LSB-first u32 bitmask stream starting at bit p.
-__device__ __forceinline__ uint32_t nbits32(const uint32_t* m, uint64_t p, int n) {
+// n (<= 33) bits of an LSB-first u32 bitmask stream starting at bit p (two words
+// always cover them: the shift within the first word is at most 31).
+__device__ __forceinline__ uint64_t nbits33(const uint32_t* m, uint64_t p, int n) {
     const uint64_t wi = p >> 5;
     const uint32_t sh = (uint32_t)(p & 31);
-    uint64_t v = ((uint64_t)m[wi + 1] << 32) | m[wi];
-    v >>= sh;
-    return n >= 32 ? (uint32_t)v : (uint32_t)(v & ((1ULL << n) - 1));
+    const uint64_t v = (((uint64_t)m[wi + 1] << 32) | m[wi]) >> sh;
+    return v & ((1ULL << n) - 1);
 }
 
 __device__ __forceinline__ uint64_t smer_hash(const DevParams& P, const uint64_t* packed, uint64_t p) {
@@ -101,25 +91,45 @@ __device__ __forceinline__ uint64_t kmer_hash(const DevParams& P, const uint64_t
 
 // Facts of window w of a sequence whose base 0 sits at stream position `base`
 // (valid when w < nwin and the k-mer holds no N).  hw is a 64-entry ring holding the
-// s-mer hash of position p at hw[p & 63].
+// s-mer hash of position p at hw[p & 63].  The minimum is found on the high 32 bits
+// of the hashes; a unique high-word minimum is the unique minimum, and only windows
+// with a high-word tie (or an all-ones high word) compare the full 64-bit values.
 __device__ __forceinline__ uint32_t window_info(const DevParams& P, const uint32_t* nmask, uint64_t base, uint32_t w,
                                                 uint32_t nwin, const uint64_t* hw) {
     if (w >= nwin) return 0;
-    if (nbits32(nmask, base + w, P.k) != 0) return 0;
-    uint64_t mv = hw[w & 63];
-    uint32_t lo = 0, ro = 0;
+    // the k-mer's N bits and, for w > 0, the base before it (N before: a new run)
+    const uint32_t s1 = w > 0 ? 1u : 0u;
+    const uint64_t nb = nbits33(nmask, base + w - s1, P.k + (int)s1);
+    if ((nb >> s1) != 0) return 0;
+    const bool first = s1 == 0 || (nb & 1u);
+    const uint32_t* h32 = reinterpret_cast<const uint32_t*>(hw);
+    uint32_t mh = h32[2 * (w & 63) + 1];
+    uint32_t eq = 1;
 #pragma unroll 8
     for (int d = 1; d < P.W; ++d) {
-        const uint64_t v = hw[(w + d) & 63];
-        if (v < mv) {
-            mv = v;
-            lo = ro = (uint32_t)d;
-        } else if (v == mv) {
-            ro = (uint32_t)d;
-        }
+        const uint32_t v = h32[2 * ((w + d) & 63) + 1];
+        eq = v < mh ? 1u << d : (v == mh ? eq | 1u << d : eq);
+        mh = v < mh ? v : mh;
     }
-    const bool first = (w == 0) || (nbits32(nmask, base + w - 1, 1) != 0);
-    return WinInfo::pack(true, first, mv == ~0ULL, lo, ro);
+    uint32_t lo, ro;
+    bool allmax = false;
+    if ((eq & (eq - 1)) == 0 && mh != 0xFFFFFFFFu) {
+        lo = ro = (uint32_t)(__ffs(eq) - 1);
+    } else {
+        uint64_t mv = hw[w & 63];
+        lo = ro = 0;
+        for (int d = 1; d < P.W; ++d) {
+            const uint64_t v = hw[(w + d) & 63];
+            if (v < mv) {
+                mv = v;
+                lo = ro = (uint32_t)d;
+            } else if (v == mv) {
+                ro = (uint32_t)d;
+            }
+        }
+        allmax = mv == ~0ULL;
+    }
+    return WinInfo::pack(true, first, allmax, lo, ro);
 }
 
 // A window's state is "determined" (independent of the past) when it is the first

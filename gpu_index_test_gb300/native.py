@@ -233,7 +233,7 @@ class Mapper:
 
     def rescue_cycles(self, cap=1 << 24):
         """Per rescued read: cycles (total, plan, merge, sort), hit bound, NAMs,
-        queries taken, longest run; and the count of block-sorted reads."""
+        cycles of the run walks, longest run; and the count of block-sorted reads."""
         a = np.zeros(cap, np.uint64)
         n = (C.c_uint32 * 2)()
         _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, n))

@@ -254,7 +254,8 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the
  * merge and of the sort (the block sort, for reads with many NAMs), then the hit
- * bound, the NAM count, the queries taken and the longest hit run.  n_out[0] receives
+ * bound, the NAM count, the SM cycles of the run walks within the merge and the
+ * longest hit run.  n_out[0] receives
  * the rescued read count, n_out[1] the count of block-sorted reads; out holds up
  * to cap values.  No reference counterpart. */
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out);
