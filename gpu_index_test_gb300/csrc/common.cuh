@@ -79,13 +79,11 @@ inline DevParams make_dev_params(const gbsa_params& p) {
 // (first base in the highest pair).  Equals the reference's rolling reverse
 // strand word xk[1] / xs[1] (step2/randstrobes.cu:24-26).
 __device__ __forceinline__ uint64_t revcomp_bits(uint64_t x, int n) {
-    x = ~x;
-    // reverse the order of 2-bit groups in a 64-bit word
-    x = ((x >> 2) & 0x3333333333333333ULL) | ((x & 0x3333333333333333ULL) << 2);
-    x = ((x >> 4) & 0x0F0F0F0F0F0F0F0FULL) | ((x & 0x0F0F0F0F0F0F0F0FULL) << 4);
-    x = ((x >> 8) & 0x00FF00FF00FF00FFULL) | ((x & 0x00FF00FF00FF00FFULL) << 8);
-    x = ((x >> 16) & 0x0000FFFF0000FFFFULL) | ((x & 0x0000FFFF0000FFFFULL) << 16);
-    x = (x >> 32) | (x << 32);
+    // a bit reversal puts the 2-bit groups in reverse order with the two bits of
+    // each group swapped; swapping them back and complementing gives the reverse
+    // complement of the 32 bases, of which the last n are kept
+    x = __brevll(~x);
+    x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
     return n >= 32 ? x : (x >> (64 - 2 * n));
 }
 
@@ -94,9 +92,8 @@ __device__ __forceinline__ uint64_t revcomp_bits(uint64_t x, int n) {
 __device__ __forceinline__ uint64_t extract_bases(const uint64_t* words, uint64_t p, int n) {
     const uint64_t wi = p >> 5;
     const uint32_t sh = (uint32_t)(p & 31) * 2;
-    uint64_t hi = words[wi];
-    uint64_t v = hi << sh;
-    if (sh) v |= words[wi + 1] >> (64 - sh);
+    // (lo >> 1) >> (63 - sh) is lo >> (64 - sh) for sh > 0 and 0 for sh == 0
+    const uint64_t v = (words[wi] << sh) | ((words[wi + 1] >> 1) >> (63 - sh));
     return n >= 32 ? v : (v >> (64 - 2 * n));
 }
 

@@ -78,6 +78,21 @@ __device__ __forceinline__ uint64_t nbits33(const uint32_t* m, uint64_t p, int n
 }
 
 __device__ __forceinline__ uint64_t smer_hash(const DevParams& P, const uint64_t* packed, uint64_t p) {
+    if (P.s <= 16) {
+        // s-mers of up to 16 bases in 32 bits: the stream seen as 32-bit groups of 16
+        // bases (group g is the high half of word g/2 for even g, the low half for odd
+        // g; little-endian halves sit at u32 index g ^ 1)
+        const uint32_t* w32 = reinterpret_cast<const uint32_t*>(packed);
+        const uint64_t g = p >> 4;
+        const uint32_t sh = (uint32_t)(p & 15) * 2;
+        const uint32_t hi = w32[g ^ 1], lo = w32[(g + 1) ^ 1];
+        uint32_t f = __funnelshift_l(lo, hi, sh);
+        f >>= 32 - 2 * P.s;   // P.s >= 1
+        uint32_t r = __brev(~f);
+        r = ((r >> 1) & 0x55555555u) | ((r & 0x55555555u) << 1);
+        r >>= 32 - 2 * P.s;
+        return xxh64((uint64_t)(f < r ? f : r));
+    }
     const uint64_t f = extract_bases(packed, p, P.s);
     const uint64_t r = revcomp_bits(f, P.s);
     return xxh64(f < r ? f : r);
@@ -231,27 +246,39 @@ __device__ inline uint32_t warp_find_anchor(const DevParams& P, const uint64_t* 
     }
 }
 
-// Forward randstrobe with strobe 1 = syncmer j of n (RandstrobeIterator::get).
+// Forward randstrobe with strobe 1 = syncmer j of n (RandstrobeIterator::get): the
+// candidate with the smallest popcount((h1 ^ h2) & q), the first one on ties.  When
+// q fits in 32 bits only the hashes' low words are compared.
 __device__ __forceinline__ void randstrobe_fwd(const DevParams& P, const uint64_t* sh, const uint32_t* sp, uint32_t n,
                                                uint32_t j, uint64_t& hash, uint32_t& s1, uint32_t& s2) {
     const uint32_t w_end = min(j + P.w_max, n - 1);
     const uint64_t h1 = sh[j];
     const uint32_t p1 = sp[j];
     const uint64_t max_pos = (uint64_t)p1 + P.max_dist;
-    uint64_t h2 = h1;
-    uint32_t p2 = p1;
+    uint32_t bi = j;
     uint32_t best = 0xFFFFFFFFu;
-    for (uint32_t i = j + P.w_min; i <= w_end && sp[i] <= max_pos; ++i) {
-        const uint32_t sc = __popcll((h1 ^ sh[i]) & P.q);
-        if (sc < best) {
-            best = sc;
-            h2 = sh[i];
-            p2 = sp[i];
+    if ((P.q >> 32) == 0) {
+        const uint32_t* shl = reinterpret_cast<const uint32_t*>(sh);
+        const uint32_t q32 = (uint32_t)P.q, h1l = (uint32_t)h1;
+        for (uint32_t i = j + P.w_min; i <= w_end && sp[i] <= max_pos; ++i) {
+            const uint32_t sc = __popc((h1l ^ shl[2 * i]) & q32);
+            if (sc < best) {
+                best = sc;
+                bi = i;
+            }
+        }
+    } else {
+        for (uint32_t i = j + P.w_min; i <= w_end && sp[i] <= max_pos; ++i) {
+            const uint32_t sc = __popcll((h1 ^ sh[i]) & P.q);
+            if (sc < best) {
+                best = sc;
+                bi = i;
+            }
         }
     }
-    hash = h1 + h2;
+    hash = h1 + sh[bi];
     s1 = p1;
-    s2 = p2;
+    s2 = sp[bi];
 }
 
 // Reverse-complement randstrobe number jr of n: the reference reverses the syncmer
@@ -265,23 +292,34 @@ __device__ __forceinline__ void randstrobe_rev(const DevParams& P, const uint64_
     const uint64_t h1 = sh[i1];
     const uint32_t p1 = L - sp[i1] - k;
     const uint64_t max_pos = (uint64_t)p1 + P.max_dist;
-    uint64_t h2 = h1;
-    uint32_t p2 = p1;
+    uint32_t bi = i1;
     uint32_t best = 0xFFFFFFFFu;
-    for (uint32_t x = jr + P.w_min; x <= w_end; ++x) {
-        const uint32_t ix = n - 1 - x;
-        const uint32_t px = L - sp[ix] - k;
-        if (px > max_pos) break;
-        const uint32_t sc = __popcll((h1 ^ sh[ix]) & P.q);
-        if (sc < best) {
-            best = sc;
-            h2 = sh[ix];
-            p2 = px;
+    if ((P.q >> 32) == 0) {
+        const uint32_t* shl = reinterpret_cast<const uint32_t*>(sh);
+        const uint32_t q32 = (uint32_t)P.q, h1l = (uint32_t)h1;
+        for (uint32_t x = jr + P.w_min; x <= w_end; ++x) {
+            const uint32_t ix = n - 1 - x;
+            if (L - sp[ix] - k > max_pos) break;
+            const uint32_t sc = __popc((h1l ^ shl[2 * ix]) & q32);
+            if (sc < best) {
+                best = sc;
+                bi = ix;
+            }
+        }
+    } else {
+        for (uint32_t x = jr + P.w_min; x <= w_end; ++x) {
+            const uint32_t ix = n - 1 - x;
+            if (L - sp[ix] - k > max_pos) break;
+            const uint32_t sc = __popcll((h1 ^ sh[ix]) & P.q);
+            if (sc < best) {
+                best = sc;
+                bi = ix;
+            }
         }
     }
-    hash = h1 + h2;
+    hash = h1 + sh[bi];
     s1 = p1;
-    s2 = p2;
+    s2 = L - sp[bi] - k;
 }
 
 // Internal compact query randstrobe: is_reverse is implied by the index (the

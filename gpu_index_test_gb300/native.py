@@ -98,6 +98,13 @@ def params_from_read_length(r, k=abi.GBSA_DEFAULT, s=abi.GBSA_DEFAULT, l=abi.GBS
     return p
 
 
+def params_make(canonical_read_length, k, s, l, u, q, max_dist):
+    """Explicit parameters (IndexParameters(r, k, s, l, u, q, max_dist)); q = -1 sets all 64 mask bits."""
+    p = abi.Params()
+    _check(lib().gbsa_params_make(canonical_read_length, k, s, l, u, q, max_dist, C.byref(p)))
+    return p
+
+
 def _u8(a):
     a = np.ascontiguousarray(a, np.uint8)
     return a if len(a) else np.zeros(1, np.uint8)

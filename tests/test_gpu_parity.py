@@ -169,6 +169,49 @@ def test_variable_length_reads_against_oracle():
     assert (x[1] == y[1]).all() and nams_equal(x[0], y[0])
 
 
+def _compare_profile(p, g, reads):
+    """Index, query randstrobes and NAMs of the CUDA path against the oracle for params p."""
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(p, g)
+    a, b = idx.export(), (o.randstrobes(), o.starts())
+    assert (a[0] == b[0]).all() and (a[1] == b[1]).all()
+    q, offs = native.randstrobes_query(p, reads)
+    for r in range(0, reads.n, 7):
+        o0, o1 = int(reads.offsets[r]), int(reads.offsets[r]) + int(reads.lengths[r])
+        ref = oracle_py.randstrobes_query(p, bytes(reads.seq[o0:o1]))
+        got = q[int(offs[r]):int(offs[r + 1])]
+        assert len(got) == len(ref)
+        for f in ("hash", "start", "end", "is_reverse"):
+            assert (got[f] == ref[f]).all(), (r, f)
+    x = native.Mapper(idx).map_reads(reads)
+    y = o.map_reads(reads, n_threads=8)
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+    assert nams_equal(x[0], y[0])
+
+
+@pytest.mark.parametrize("read_len,len_min,len_max", [(300, 300, 300), (500, 500, 500), (500, 1200, 3000)])
+def test_long_read_profiles_against_oracle(read_len, len_min, len_max):
+    """Profiles for 300 / 500 bp reads (k=22 s=18, k=23 s=17): s-mers wider than 16
+    bases take the 64-bit hashing path; reads above 1024 bases take the long-read
+    seeding kernel."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.003, seed=31))
+    reads = synth.make_reads(g, synth.ReadParams(seed=32, n_units=800 if len_max <= 500 else 150, len_min=len_min,
+                                                 len_max=len_max, paired_frac=1.0, insert_mean=2 * len_max + 100,
+                                                 insert_sd=30))
+    p = native.params_from_read_length(read_len)
+    assert p.s > 16
+    _compare_profile(p, g, reads)
+
+
+def test_wide_strobe_mask_against_oracle():
+    """A strobe mask wider than 32 bits (q = all ones) takes the 64-bit selection path."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.003, seed=33))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=800, seed=34))
+    p = native.params_make(150, 20, 16, 1, 7, -1, 80)
+    assert p.q == (1 << 64) - 1
+    _compare_profile(p, g, reads)
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
