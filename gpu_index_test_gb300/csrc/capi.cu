@@ -135,7 +135,7 @@ struct gbsa_mapper {
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
-        out_off, out_nams, out_frac, out_resc, resc_cycles, nam_notes, jobs, side_slots;
+        out_off, out_nams, out_frac, out_resc, resc_cycles, nam_notes, jobs, side_slots, lane_lists;
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
@@ -155,6 +155,7 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     m.lens.resize(4ull * (n + 1));
     m.rec.resize(sizeof(ReadRec) * (n + 1));
     m.lists.resize(16ull * (n + 1));
+    m.lane_lists.resize(4ull * kLaneBuckets * (n + 1));
     m.jobs.resize(sizeof(SortJob) * (n + 1));
     m.ctr.resize(sizeof(Counters));
     m.cnt.resize(8ull * (n + 1));
@@ -214,6 +215,8 @@ static Arenas arenas_of(gbsa_mapper& m) {
     A.rescue_cap = (uint32_t)per;
     A.long_list = m.lists.as<uint32_t>() + per;
     A.big_list = m.lists.as<uint32_t>() + 2 * per;
+    A.lane_lists = m.lane_lists.as<uint32_t>();
+    A.lane_cap = (uint32_t)(m.lane_lists.size() / (4ull * kLaneBuckets));
     A.sort_jobs = m.jobs.as<SortJob>();
     A.jobs_cap = (uint32_t)(m.jobs.size() / sizeof(SortJob));
     A.rescue_cycles = m.profile ? m.resc_cycles.as<uint64_t>() : nullptr;
@@ -260,6 +263,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
                              m.long_scratch.as<uint8_t>(), m.long_warps, st);
         mark(2);
         launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+        launch_bucket_reads(n, m.rec.as<ReadRec>(), A, ctr, st);
         mark(3);
         // The rescue chain works on the rescued reads only and the NAM kernels on the
         // others: the rescue chain runs on the side stream (with its own scratch

@@ -41,7 +41,10 @@ struct Counters {
     unsigned int n_rescue_heavy;  // rescued reads on the heavy end of the rescue list
     unsigned int n_huge;   // rescued reads whose NAMs the large-tile block sort orders
     unsigned int rescue_next;  // next rescue-list entry to take (k_rescue's work counter)
+    unsigned int lane_cnt[16]; // reads per hit-count bucket of the lane NAM kernel
 };
+
+constexpr uint32_t kLaneBuckets = 13;   // hit-count buckets of the lane NAM kernel (<= 16)
 
 // A read whose NAMs are sorted by the block-per-read sort kernel.
 struct SortJob {
@@ -70,6 +73,8 @@ struct Arenas {
     uint32_t rescue_cap;
     uint32_t* long_list;
     uint32_t* big_list;
+    uint32_t* lane_lists;    // kLaneBuckets lists of lane_cap reads each
+    uint32_t lane_cap;
     SortJob* sort_jobs;      // small-tile jobs from the front, large-tile ones from the back
     uint32_t jobs_cap;
     uint64_t* rescue_cycles;   // optional: 8 notes per rescued read (cycles per phase, sizes)
@@ -106,6 +111,7 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
                    cudaStream_t st);
 void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st);
+void launch_bucket_reads(uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);

@@ -10,6 +10,8 @@
 //   k_rescue                    find_nams_rescue (step2/nam.cu:927-985) + NAM sort
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "map.cuh"
 #include "runtime.h"
 
@@ -261,6 +263,11 @@ __device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* 
 constexpr uint32_t kLaneMaxHits = 160;
 constexpr uint32_t kLaneOpen = 10;   // open NAMs a lane keeps in shared memory
 constexpr int kLaneWarps = 4;
+// The rescue chain runs beside the two NAM kernels on another stream; the persistent
+// grids are sized so that their shared memory fits one SM together: rescue 1 x 72 KB,
+// lane kernel 3 x 40 KB, warp kernel 4 x 32 KB.
+constexpr int kLaneBlocksPerSm = 3;
+constexpr int kRescueBlocksPerSm = 1;
 
 __device__ __forceinline__ bool nam_key3_less(const NamKey& a, const NamKey& b) {
     if (a.k1 != b.k1) return a.k1 < b.k1;
@@ -308,19 +315,57 @@ struct LaneOpen {
 // the open list is full and the current query start has passed it, or at the end.
 // The read's NAMs are then insertion-sorted in place.  Reads that do not fit go to
 // the warp-cooperative kernel.
+// Hit-count bucket of a read for the lane kernel: 8 wide up to 64 hits, 16 wide up
+// to 128, then one bucket up to kLaneMaxHits.
+__device__ __forceinline__ uint32_t lane_bucket(uint32_t H) {
+    if (H <= 64) return (H - 1) >> 3;
+    if (H <= 128) return 8 + ((H - 65) >> 4);
+    return 12;
+}
+
+// Sorts the reads with hits for the NAM kernels: more than kLaneMaxHits hits to the
+// warp kernel's list, the others into lists by hit count, so that the lanes of a
+// warp of the lane kernel merge reads of similar size (a warp runs as long as its
+// longest read).  Appends are aggregated per warp and bucket.
+__global__ void k_bucket_reads(uint32_t n, const ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    const uint32_t lane = lane_id();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t r = base + threadIdx.x;
+        uint32_t key = 0xFFFFFFFFu;   // no list
+        if (r < n) {
+            const uint32_t flags = rec[r].flags;
+            const uint32_t H = rec[r].n_hits;
+            if (!(flags & (kReadFailed | kReadRescue)) && H > 0) key = H > kLaneMaxHits ? 16u : lane_bucket(H);
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t at = 0;
+        if (key != 0xFFFFFFFFu && lane == leader)
+            at = atomicAdd(key == 16u ? &ctr->n_big : &ctr->lane_cnt[key], (unsigned)__popc(peers));
+        at = __shfl_sync(0xFFFFFFFFu, at, leader) + __popc(peers & lanemask_lt());
+        if (key == 16u) A.big_list[at] = r;
+        else if (key != 0xFFFFFFFFu) A.lane_lists[(size_t)key * A.lane_cap + at] = r;
+    }
+}
+
 __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
                                                                Arenas A, Counters* ctr) {
     __shared__ LaneOpen S;
+    __shared__ uint32_t s_cnt[kLaneBuckets];
     const uint32_t t = threadIdx.x;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    if (t < kLaneBuckets) s_cnt[t] = *(volatile unsigned int*)&ctr->lane_cnt[t];
+    __syncthreads();
+    uint32_t total = 0;
+    for (uint32_t b = 0; b < kLaneBuckets; ++b) total += s_cnt[b];
+    // reads by bucket, the most hits first
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        uint32_t b = kLaneBuckets - 1, j = i;
+        while (j >= s_cnt[b]) j -= s_cnt[b--];
+        const uint32_t r = A.lane_lists[(size_t)b * A.lane_cap + j];
         ReadRec& R = rec[r];
         const uint32_t flags = R.flags;
         const uint32_t H = R.n_hits;
-        if ((flags & (kReadFailed | kReadRescue)) || H == 0) continue;
-        if (H > kLaneMaxHits) {
-            A.big_list[atomicAdd(&ctr->n_big, 1u)] = r;
-            continue;
-        }
         const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)H);
         if (noff + H > A.nam_cap) {
             R.flags = flags | kReadFailed;
@@ -570,7 +615,8 @@ __device__ __forceinline__ bool warp_find_nams(const HitRec* __restrict__ hits, 
 
 constexpr uint32_t kHeavyOpen = 256;   // open NAMs (and sort keys) a warp keeps in shared memory
 constexpr int kHeavyWarps = 4;
-constexpr int kHeavyBlocksPerSm = 5;
+constexpr int kHeavyBlocksPerSm = 5;   // register budget
+constexpr int kHeavyGridPerSm = 4;     // blocks launched per SM (32 KB each)
 
 // find_nams for the reads the lane kernel passed on (many hits, or many NAMs open
 // at once): a warp per read.  The open list lives in shared memory (in global
@@ -744,7 +790,6 @@ __device__ uint64_t rescue_merge(const IndexView& I, const Query* const* Qd, con
 
 constexpr uint32_t kWarpSortMax = 256;   // rescued reads with more NAMs are sorted by k_sort_jobs
 constexpr uint32_t kSortTile = 2048;      // keys per shared-memory tile of the small block sort (56 KB)
-constexpr uint32_t kSortTileLarge = 8192; // keys per tile of the large block sort (224 KB)
 
 // find_nams_rescue for the reads on the rescue list (a warp per read).  Reads that
 // end with more than kWarpSortMax NAMs leave the sort to k_sort_jobs.
@@ -965,13 +1010,11 @@ __device__ void tile_sort(SortTile tile, uint32_t P) {
     }
 }
 
-// Sorts the NAMs of the rescued reads with more than kWarpSortMax NAMs (typically
-// reads inside short tandem repeats, with hundreds to thousands of NAMs): one block
-// per read, then the read's NAMs are written to the NAM arena in order.  A read whose
-// keys fit the tile is sorted in shared memory alone; larger ones through global
-// memory (block_sort_keys).  The small kernel takes the jobs from the front of the
-// job list (at most kSortTile NAMs), the large one those from the back.
-template <int kThreads, uint32_t kTile, bool kLarge>
+// Sorts the NAMs of the rescued reads with kWarpSortMax < NAMs <= kSortTile
+// (typically reads inside short tandem repeats): one block per read, bitonic sort in
+// a shared-memory tile, then the read's NAMs are written to the NAM arena in order.
+// The jobs are at the front of the job list.
+template <int kThreads, uint32_t kTile>
 __global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __restrict__ rec, Arenas A,
                                                          Counters* ctr) {
     extern __shared__ __align__(16) uint8_t s_dyn[];   // kTile sort keys, one array per field
@@ -981,10 +1024,10 @@ __global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __
     tile.k2 = tile.k1 + kTile;
     tile.k3 = tile.k2 + kTile;
     tile.idx = reinterpret_cast<uint32_t*>(tile.k3 + kTile);
-    const uint32_t n_jobs = kLarge ? *(volatile unsigned int*)&ctr->n_huge : *(volatile unsigned int*)&ctr->n_heavy;
+    const uint32_t n_jobs = *(volatile unsigned int*)&ctr->n_heavy;
     for (uint32_t h = blockIdx.x; h < n_jobs; h += gridDim.x) {
         const long long t0 = clock64();
-        const SortJob job = A.sort_jobs[kLarge ? A.jobs_cap - 1 - h : h];
+        const SortJob job = A.sort_jobs[h];
         ReadRec& R = rec[job.read];
         const NamState* closed = job.closed;
         const uint32_t NN = job.n;
@@ -1027,6 +1070,142 @@ __global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __
                 A.nams[noff + i] = closed[in_tile ? tile.idx[i] : job.keys[i].idx];
         __syncthreads();
         if (A.rescue_cycles && threadIdx.x == 0) A.rescue_cycles[8ull * job.note + 3] = (uint64_t)(clock64() - t0);
+    }
+}
+
+// ---- cluster sort of the rescued reads with more than kSortTile NAMs ------------------
+//
+// A cluster of kClusterCtas CTAs sorts one read's keys: each CTA holds T = P /
+// kClusterCtas of the P (next power of two) keys in its shared-memory tile, so up to
+// kClusterCtas * kSortTile keys are sorted without touching global memory.  Bitonic
+// stages whose partner distance is below T stay within a CTA (block barrier); the
+// few with larger distances compare and swap across the CTAs' tiles through
+// distributed shared memory (cluster barrier).  Each CTA needs only kSortTile keys of
+// shared memory, so the clusters run beside the NAM kernels of the other stream.
+constexpr int kClusterCtas = 8;
+
+__device__ __forceinline__ SortTile tile_of_rank(const SortTile& t, uint32_t rank) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    SortTile r;
+    r.k1 = cl.map_shared_rank(t.k1, rank);
+    r.k2 = cl.map_shared_rank(t.k2, rank);
+    r.k3 = cl.map_shared_rank(t.k3, rank);
+    r.idx = cl.map_shared_rank(t.idx, rank);
+    return r;
+}
+
+// key(tb[b]) < key(ta[a]) for entries of possibly different tiles
+__device__ __forceinline__ bool tiles_less(const SortTile& tb, uint32_t b, const SortTile& ta, uint32_t a) {
+    const uint64_t x = tb.k1[b], y = ta.k1[a];
+    if (x != y) return x < y;
+    const uint64_t x2 = tb.k2[b], y2 = ta.k2[a];
+    if (x2 != y2) return x2 < y2;
+    const uint64_t x3 = tb.k3[b], y3 = ta.k3[a];
+    if (x3 != y3) return x3 < y3;
+    return tb.idx[b] < ta.idx[a];
+}
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
+    k_sort_jobs_cluster(MapConfig C, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    namespace cg = cooperative_groups;
+    extern __shared__ __align__(16) uint8_t s_dyn[];   // kSortTile keys, one array per field
+    __shared__ uint64_t s_noff;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t rank = cl.block_rank();
+    SortTile tile;
+    tile.k1 = reinterpret_cast<uint64_t*>(s_dyn);
+    tile.k2 = tile.k1 + kSortTile;
+    tile.k3 = tile.k2 + kSortTile;
+    tile.idx = reinterpret_cast<uint32_t*>(tile.k3 + kSortTile);
+    const uint32_t n_jobs = *(volatile unsigned int*)&ctr->n_huge;
+    const uint32_t n_clusters = gridDim.x / kClusterCtas;
+    for (uint32_t h = blockIdx.x / kClusterCtas; h < n_jobs; h += n_clusters) {
+        const long long t0 = clock64();
+        const SortJob job = A.sort_jobs[A.jobs_cap - 1 - h];
+        const NamState* closed = job.closed;
+        const uint32_t NN = job.n;
+        const uint32_t P = next_pow2(NN);
+        const bool in_tiles = P <= kClusterCtas * kSortTile;
+        if (in_tiles) {
+            const uint32_t T = P / kClusterCtas;   // NN > kSortTile: T >= kSortTile / 4
+            const uint32_t e0 = rank * T;
+            for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
+                const uint32_t e = e0 + i;
+                NamKey k;
+                if (e < NN) {
+                    k = nam_key(closed[e], e, C.sort_mode);
+                } else {
+                    k.k1 = k.k2 = k.k3 = ~0ULL;
+                    k.idx = 0xFFFFFFFFu;
+                }
+                tile.put(i, k);
+            }
+            cl.sync();
+            for (uint32_t k = 2; k <= P; k <<= 1) {
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    if (j < T) {
+                        for (uint32_t q = threadIdx.x; q < T / 2; q += blockDim.x) {
+                            const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                            const uint32_t ixj = i | j;
+                            if (tile.less_at(ixj, i) == (((e0 + i) & k) == 0)) tile.swap(i, ixj);
+                        }
+                        if (j > 1) __syncthreads();
+                        else cl.sync();   // the next stage may cross CTAs
+                    } else {
+                        // pairs (i, i | j) across CTAs; this CTA takes an equal share
+                        for (uint32_t q = rank * (T / 2) + threadIdx.x; q < (rank + 1) * (T / 2); q += blockDim.x) {
+                            const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                            const uint32_t ixj = i | j;
+                            SortTile ta = tile_of_rank(tile, i / T), tb = tile_of_rank(tile, ixj / T);
+                            const uint32_t ia = i % T, ib = ixj % T;
+                            if (tiles_less(tb, ib, ta, ia) == ((i & k) == 0)) {
+                                const NamKey a = ta.get(ia), b = tb.get(ib);
+                                ta.put(ia, b);
+                                tb.put(ib, a);
+                            }
+                        }
+                        cl.sync();
+                    }
+                }
+            }
+        }
+        if (rank == 0) {
+            if (!in_tiles) {
+                // beyond the cluster's tiles (rare): the first CTA sorts through global memory
+                for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x)
+                    job.keys[i] = nam_key(closed[i], i, C.sort_mode);
+                __syncthreads();
+                block_sort_keys(job.keys, NN, tile, kSortTile);
+            }
+            if (threadIdx.x == 0) {
+                ReadRec& R = rec[job.read];
+                const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)NN);
+                if (noff + NN > A.nam_cap) {
+                    R.flags |= kReadFailed;
+                    atomicOr(&ctr->status, kStatusNamOverflow);
+                    s_noff = ~0ULL;
+                } else {
+                    R.nam_off = noff;
+                    R.n_nams = NN;
+                    s_noff = noff;
+                }
+            }
+        }
+        cl.sync();
+        const uint64_t noff = *cl.map_shared_rank(&s_noff, 0u);
+        if (noff != ~0ULL) {
+            if (in_tiles) {
+                const uint32_t T = P / kClusterCtas, e0 = rank * T;
+                for (uint32_t i = threadIdx.x; i < T && e0 + i < NN; i += blockDim.x)
+                    A.nams[noff + e0 + i] = closed[tile.idx[i]];
+            } else if (rank == 0) {
+                for (uint32_t i = threadIdx.x; i < NN; i += blockDim.x) A.nams[noff + i] = closed[job.keys[i].idx];
+            }
+        }
+        if (A.rescue_cycles && rank == 0 && threadIdx.x == 0)
+            A.rescue_cycles[8ull * job.note + 3] = (uint64_t)(clock64() - t0);
+        cl.sync();   // tiles and s_noff are reused by the next job
     }
 }
 
@@ -1128,15 +1307,22 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
-    k_nams_lane<<<grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * 5), 32 * kLaneWarps, 0, st>>>(C, n, rec,
+    k_nams_lane<<<grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSm), 32 * kLaneWarps, 0,
+                  st>>>(C, n, rec,
                                                                                                         A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_bucket_reads(uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    if (!n) return;
+    k_bucket_reads<<<grid_for(n, 256, (unsigned)device_sm_count() * 8), 256, 0, st>>>(n, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
 void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
     if (!n) return;
     // at most nam_kernel_warps(n) warps: one scratch slot each
-    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * kHeavyBlocksPerSm,
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * kHeavyGridPerSm,
                                                          (n + kHeavyWarps - 1) / kHeavyWarps);
     k_nams<<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
@@ -1145,30 +1331,28 @@ void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Co
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st) {
     if (!n_reads) return;
-    // persistent: as many blocks as are resident at once (at most one scratch slot per warp)
-    static int per_sm = 0;
-    if (!per_sm) GBSA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rescue, 32 * kWarpsPerBlock, 0));
+    // persistent, kRescueBlocksPerSm per SM (at most one scratch slot per warp)
     const unsigned blocks =
-        std::min<unsigned>(warp_grid(n_reads, kWarpsPerBlock), (unsigned)device_sm_count() * std::max(per_sm, 1));
+        std::min<unsigned>(warp_grid(n_reads, kWarpsPerBlock), (unsigned)device_sm_count() * kRescueBlocksPerSm);
     k_rescue<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
-    constexpr int kSmall = 256, kLarge = 1024;
-    constexpr size_t smem_small = kSortTile * 28, smem_large = kSortTileLarge * 28;
+    constexpr int kSmall = 256;
+    constexpr size_t smem = kSortTile * 28;
     static bool attr = false;
     if (!attr) {
-        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile, false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_small));
-        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kLarge, kSortTileLarge, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_large));
+        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
     const unsigned sms = (unsigned)device_sm_count();
-    k_sort_jobs<kLarge, kSortTileLarge, true><<<sms, kLarge, smem_large, st>>>(C, rec, A, ctr);
+    k_sort_jobs<kSmall, kSortTile><<<sms * 4, kSmall, smem, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
-    k_sort_jobs<kSmall, kSortTile, false><<<sms * 4, kSmall, smem_small, st>>>(C, rec, A, ctr);
+    // sms / 2 clusters of kClusterCtas CTAs
+    k_sort_jobs_cluster<<<std::max(1u, sms / 2) * kClusterCtas, 256, smem, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

@@ -212,6 +212,26 @@ def test_wide_strobe_mask_against_oracle():
     _compare_profile(p, g, reads)
 
 
+@pytest.mark.parametrize("mode", [abi.GBSA_SORT_SCORE, abi.GBSA_SORT_REF_MATE2])
+def test_tandem_repeat_rescue_against_oracle(mode):
+    """A genome with 5% short tandem repeats: hundreds of rescued reads end with more
+    than 256 NAMs (block sorts) and some with more than 2048 (cluster sorts)."""
+    import dataclasses
+    gp = dataclasses.replace(synth.genome_params("C2", scale=0.01, seed=41), str_frac=0.05)
+    g = synth.make_genome(gp)
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=3000, seed=42))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    opt = abi.map_options(rescue_level=2, sort_mode=mode)
+    x = native.Mapper(idx, opt).map_reads(reads)
+    y = o.map_reads(reads, opt, n_threads=8)
+    counts = np.diff(y[1].astype(np.int64))
+    assert (counts > 2048).sum() >= 5 and (counts > 256).sum() >= 100
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+    assert nams_equal(x[0], y[0])
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
