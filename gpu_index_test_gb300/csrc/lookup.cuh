@@ -22,10 +22,12 @@ __device__ __forceinline__ uint64_t get_hash(const IndexView& I, uint64_t pos) {
 // in order until one is >= key (buckets hold ~2 entries on average) and switches to
 // a binary search for long buckets; both give the reference's answer.  ex receives
 // the number of entries examined by the linear rule (for the byte count).
-__device__ __forceinline__ uint64_t index_find(const IndexView& I, uint64_t key, uint32_t* ex = nullptr) {
+__device__ __forceinline__ uint64_t index_find(const IndexView& I, uint64_t key, uint32_t* ex = nullptr,
+                                               uint64_t* bucket_end = nullptr) {
     const uint64_t top = key >> (64 - I.bits);
     const uint64_t a = __ldg(&I.starts[top]);
     const uint64_t b = __ldg(&I.starts[top + 1]);
+    if (bucket_end) *bucket_end = b;
     if (a >= b) {
         if (ex) *ex = 0;
         return kNotFound;
@@ -53,6 +55,17 @@ __device__ __forceinline__ uint64_t index_find(const IndexView& I, uint64_t key,
 
 __device__ __forceinline__ bool index_is_filtered(const IndexView& I, uint64_t pos) {   // index.hpp:91-93
     return get_hash(I, pos) == get_hash(I, pos + I.filter_cutoff);
+}
+
+// index_is_filtered for a position returned by index_find(key) whose bucket ends at
+// bucket_end: an entry at or past the bucket's end has other top bits, so it cannot
+// equal key, and the second load is needed only when pos + filter_cutoff is still
+// inside the bucket (past the table's end get_hash reads all ones).
+__device__ __forceinline__ bool index_is_filtered_in(const IndexView& I, uint64_t pos, uint64_t key,
+                                                     uint64_t bucket_end) {
+    const uint64_t p2 = pos + I.filter_cutoff;
+    if (p2 >= bucket_end) return p2 >= I.n && key == ~0ULL;
+    return __ldg(&I.rs[p2].hash) == key;
 }
 
 // StrobemerIndex::get_count (step2/index.hpp:115-147): length of the equal-hash run

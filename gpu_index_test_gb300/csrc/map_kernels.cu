@@ -133,13 +133,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
         for (uint32_t i = lane; i < nq2; i += 32) {
             const Query q = Q[i];
             uint32_t ex = 0;
-            const uint64_t pos = index_find(I, q.hash, &ex);
+            uint64_t bend = 0;
+            const uint64_t pos = index_find(I, q.hash, &ex, &bend);
             uint32_t nh = 0;
             bytes += 16 + 16ull * ex;
             if (pos != kNotFound) {
                 ++tot;
-                bytes += 16;
-                if (!index_is_filtered(I, pos)) {
+                bytes += 16;   // the reference reads hash[pos + filter_cutoff]
+                if (!index_is_filtered_in(I, pos, q.hash, bend)) {
                     ++good;
                     uint32_t run = 0;
                     nh = walk_hit_run(I, (int)q.start, (int)q.end, pos, [&](uint32_t, int, int) {}, &run);
@@ -204,8 +205,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
         }
         const uint64_t* qp = A.q_pos + R.q_off;
         for (uint32_t i = lane; i < nq2; i += 32) {
+            // queries that emitted hits in the first pass (found and not filtered)
+            const uint32_t next = i + 1 < nq2 ? aux[i + 1] : (uint32_t)H;
+            if (next == aux[i]) continue;
             const uint64_t pos = qp[i];
-            if (pos == kNotFound || index_is_filtered(I, pos)) continue;
             const uint32_t dir = i >= nq ? 1u : 0u;
             HitRec* out = A.hits + hoff + aux[i];
             uint32_t k = 0;
