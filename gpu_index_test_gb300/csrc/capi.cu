@@ -4,6 +4,7 @@
 #include <atomic>
 #include <climits>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -11,6 +12,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "index.h"
@@ -24,6 +26,92 @@ std::atomic<uint64_t> g_launches{0};
 static thread_local std::string t_last_error;
 
 void set_last_error(const std::string& msg) { t_last_error = msg; }
+
+namespace {
+
+// Process-wide pool for host_parallel_for: workers sleep on a condition variable;
+// a job is a function and a range handed out in chunks through an atomic counter.
+class HostPool {
+public:
+    static HostPool& get() {
+        static HostPool pool;
+        return pool;
+    }
+    void run(size_t n, const std::function<void(size_t, size_t)>& fn) {
+        std::lock_guard<std::mutex> one_job(job_mu_);   // one job at a time
+        const size_t chunk = std::max<size_t>(kMinChunk, n / (4 * (workers_.size() + 1)) + 1);
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            fn_ = &fn;
+            n_ = n;
+            chunk_ = chunk;
+            next_.store(0);
+            active_ = workers_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> g(mu_);
+        done_cv_.wait(g, [&] { return active_ == 0; });
+        fn_ = nullptr;
+    }
+    static constexpr size_t kMinChunk = 1 << 16;
+
+private:
+    HostPool() {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const unsigned nw = std::min(15u, hw > 1 ? hw - 1 : 0u);
+        for (unsigned i = 0; i < nw; ++i) workers_.emplace_back([this] { loop(); });
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+    void work() {
+        for (;;) {
+            const size_t b = next_.fetch_add(chunk_);
+            if (b >= n_) return;
+            (*fn_)(b, std::min(n_, b + chunk_));
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_.wait(g, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+            }
+            work();
+            std::lock_guard<std::mutex> g(mu_);
+            if (--active_ == 0) done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex mu_, job_mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t, size_t)>* fn_ = nullptr;
+    size_t n_ = 0, chunk_ = 1, active_ = 0;
+    std::atomic<size_t> next_{0};
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+}  // namespace
+
+void host_parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn) {
+    if (n <= HostPool::kMinChunk) {
+        if (n) fn(0, n);
+        return;
+    }
+    HostPool::get().run(n, fn);
+}
 
 int device_sm_count() {
     static std::mutex mu;
@@ -139,6 +227,12 @@ struct gbsa_mapper {
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
+    // second input / output slots and copy streams of the pipelined host entry point
+    gbsa::DeviceBuffer seqs1, offs1, lens1, out_nams1, out_frac1, out_resc1, out_off_h[2];
+    gbsa::PinnedBuffer h_seqs1, h_meta1;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t in_ready[2] = {}, in_copied[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
+    uint32_t pipe_chunks = 4;   // chunks a large gbsa_map_reads call is cut into
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
     int count_bytes = 0;
     int profile = 0;          // record per-stage CUDA events
@@ -530,33 +624,73 @@ int gbsa_get_count(const gbsa_index* idx, const uint64_t* positions, uint64_t n,
 }
 
 // Copies n reads (host) into one contiguous pinned staging area and then to the device.
+// Host staging buffers and device inputs of one slot of the host entry points.
+struct InSlot {
+    DeviceBuffer* seqs;
+    DeviceBuffer* offs;
+    DeviceBuffer* lens;
+    PinnedBuffer* meta;
+    PinnedBuffer* gather;
+};
+
+static InSlot in_slot(gbsa_mapper& m, int s) {
+    if (s == 0) return InSlot{&m.seqs, &m.offs, &m.lens, &m.h_meta, &m.h_seqs};
+    return InSlot{&m.seqs1, &m.offs1, &m.lens1, &m.h_meta1, &m.h_seqs1};
+}
+
+// Copies n reads to the device inputs of a slot.  Reads usually lie back to back:
+// the span from the first read's start to the last read's end is copied in one
+// transfer and the offsets are rebased to it (in parallel, checking that every read
+// lies inside the span); otherwise the reads are gathered into pinned staging first.
 static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
-                            uint32_t n, cudaStream_t st) {
-    uint64_t total = 0;
-    for (uint32_t i = 0; i < n; ++i) total += lengths[i];
-    mapper_reserve(m, n, total);
-    m.h_meta.resize(12ull * (n + 1));
-    uint64_t* ho = m.h_meta.as<uint64_t>();
+                            uint32_t n, cudaStream_t st, int slot = 0) {
+    const InSlot in = in_slot(m, slot);
+    const uint64_t lo = n ? offsets[0] : 0;
+    const uint64_t hi = n ? offsets[n - 1] + lengths[n - 1] : 0;
+    const bool span_ok = hi >= lo;
+    const uint64_t span = span_ok ? hi - lo : 0;
+    std::atomic<bool> inside{span_ok};
+    std::atomic<uint64_t> total{0};
+    in.meta->resize(12ull * (n + 1));
+    uint64_t* ho = in.meta->as<uint64_t>();
     uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
-    bool contiguous = true;
-    uint64_t acc = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        ho[i] = acc;
-        hl[i] = lengths[i];
-        contiguous &= offsets[i] == offsets[0] + acc;
-        acc += lengths[i];
+    host_parallel_for(n, [&](size_t b, size_t e) {
+        bool ok = true;
+        uint64_t t = 0;
+        for (size_t i = b; i < e; ++i) {
+            ok &= offsets[i] >= lo && offsets[i] + lengths[i] <= hi;
+            ho[i] = offsets[i] - lo;
+            hl[i] = lengths[i];
+            t += lengths[i];
+        }
+        if (!ok) inside.store(false);
+        total.fetch_add(t);
+    });
+    const bool direct = inside.load() && span <= 2 * total.load() + (1u << 20);   // no large gaps
+    const uint64_t bases = direct ? span : total.load();
+    mapper_reserve(m, n, bases);
+    in.seqs->resize(bases + 64);
+    in.offs->resize(8ull * (n + 1));
+    in.lens->resize(4ull * (n + 1));
+    if (direct) {
+        if (span) GBSA_CUDA(cudaMemcpyAsync(in.seqs->as<void>(), seqs + lo, span, cudaMemcpyHostToDevice, st));
+    } else {
+        // exclusive offsets of the gathered layout, then a parallel gather
+        uint64_t acc = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            ho[i] = acc;
+            acc += lengths[i];
+        }
+        in.gather->resize(acc + 1);
+        char* hs = in.gather->as<char>();
+        host_parallel_for(n, [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
+        });
+        if (acc) GBSA_CUDA(cudaMemcpyAsync(in.seqs->as<void>(), hs, acc, cudaMemcpyHostToDevice, st));
     }
-    if (contiguous && total) {
-        GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), seqs + offsets[0], total, cudaMemcpyHostToDevice, st));
-    } else if (total) {
-        m.h_seqs.resize(total);
-        char* hs = m.h_seqs.as<char>();
-        for (uint32_t i = 0; i < n; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
-        GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), hs, total, cudaMemcpyHostToDevice, st));
-    }
-    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
-    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
-    return total;
+    GBSA_CUDA(cudaMemcpyAsync(in.offs->as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(in.lens->as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
+    return total.load();
 }
 
 int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
@@ -654,6 +788,13 @@ void gbsa_mapper_free(gbsa_mapper* m) {
     if (m->st) cudaStreamSynchronize(m->st);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
+    if (m->copy_in) cudaStreamSynchronize(m->copy_in);
+    if (m->copy_out) cudaStreamSynchronize(m->copy_out);
+    for (int k = 0; k < 2; ++k)
+        for (cudaEvent_t e : {m->in_ready[k], m->in_copied[k], m->in_free[k], m->out_ready[k], m->out_free[k]})
+            if (e) cudaEventDestroy(e);
+    if (m->copy_in) cudaStreamDestroy(m->copy_in);
+    if (m->copy_out) cudaStreamDestroy(m->copy_out);
     if (m->fork_ev) cudaEventDestroy(m->fork_ev);
     if (m->join_ev) cudaEventDestroy(m->join_ev);
     if (m->side) cudaStreamDestroy(m->side);
@@ -664,32 +805,84 @@ void gbsa_mapper_free(gbsa_mapper* m) {
 int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths, uint32_t n_reads,
                    gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets, float* frac, uint8_t* rescued) {
     return guarded([&] {
+        // A large call is cut into chunks that are pipelined over two slots: the reads of
+        // chunk k+1 are copied in (copy_in stream) and the NAMs of chunk k-1 copied out
+        // (copy_out stream) while chunk k is mapped on the mapper's stream.
         cudaStream_t st = m->st;
-        uint64_t done_nams = 0;
         nam_offsets[0] = 0;
-        for (uint32_t b0 = 0; b0 < n_reads || (n_reads == 0 && b0 == 0); b0 += m->max_reads) {
-            const uint32_t n = std::min(m->max_reads, n_reads - b0);
-            if (n == 0) break;
-            stage_reads(*m, seqs, offsets + b0, lengths + b0, n, st);
+        if (n_reads == 0) return;
+        if (!m->copy_in) {
+            GBSA_CUDA(cudaStreamCreateWithFlags(&m->copy_in, cudaStreamNonBlocking));
+            GBSA_CUDA(cudaStreamCreateWithFlags(&m->copy_out, cudaStreamNonBlocking));
+            for (int s = 0; s < 2; ++s) {
+                for (cudaEvent_t* e :
+                     {&m->in_ready[s], &m->in_copied[s], &m->in_free[s], &m->out_ready[s], &m->out_free[s]})
+                    GBSA_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+                GBSA_CUDA(cudaEventRecord(m->in_free[s], st));
+                GBSA_CUDA(cudaEventRecord(m->in_copied[s], m->copy_in));
+                GBSA_CUDA(cudaEventRecord(m->out_free[s], m->copy_out));
+            }
+        }
+        constexpr uint32_t kMinChunk = 1u << 17;
+        const uint32_t chunks = std::max<uint32_t>(1, std::min<uint32_t>(m->pipe_chunks, n_reads / kMinChunk));
+        const uint32_t chunk = std::min((n_reads + chunks - 1) / chunks, m->max_reads);
+        const uint32_t n_chunks = (n_reads + chunk - 1) / chunk;
+        auto stage = [&](uint32_t k) {
+            const int s = (int)(k & 1);
+            const uint32_t b0 = k * chunk, n = std::min(chunk, n_reads - b0);
+            GBSA_CUDA(cudaEventSynchronize(m->in_copied[s]));               // staging of chunk k-2 sent
+            GBSA_CUDA(cudaStreamWaitEvent(m->copy_in, m->in_free[s], 0));   // chunk k-2 done with the slot
+            stage_reads(*m, seqs, offsets + b0, lengths + b0, n, m->copy_in, s);
+            GBSA_CUDA(cudaEventRecord(m->in_ready[s], m->copy_in));
+            GBSA_CUDA(cudaEventRecord(m->in_copied[s], m->copy_in));
+        };
+        uint64_t done_nams = 0;
+        stage(0);
+        for (uint32_t k = 0; k < n_chunks; ++k) {
+            const int s = (int)(k & 1);
+            const uint32_t b0 = k * chunk, n = std::min(chunk, n_reads - b0);
+            if (k + 1 < n_chunks) stage(k + 1);
+            const InSlot in = in_slot(*m, s);
+            GBSA_CUDA(cudaStreamWaitEvent(st, m->in_ready[s], 0));
             const uint64_t total =
-                run_pipeline(*m, m->seqs.as<uint8_t>(), m->offs.as<uint64_t>(), m->lens.as<uint32_t>(), n, false, st);
-            // offsets
-            GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, m->out_off.as<uint64_t>(), 8ull * (n + 1),
-                                      cudaMemcpyDeviceToHost, st));
-            m->out_nams.resize(sizeof(gbsa_nam) * (total + 1));
+                run_pipeline(*m, in.seqs->as<uint8_t>(), in.offs->as<uint64_t>(), in.lens->as<uint32_t>(), n, false, st);
+            GBSA_CUDA(cudaEventRecord(m->in_free[s], st));
+            // output slot s is free once chunk k-2's results have been copied out
+            GBSA_CUDA(cudaEventSynchronize(m->out_free[s]));
+            DeviceBuffer& o_nams = s ? m->out_nams1 : m->out_nams;
+            DeviceBuffer& o_frac = s ? m->out_frac1 : m->out_frac;
+            DeviceBuffer& o_resc = s ? m->out_resc1 : m->out_resc;
+            DeviceBuffer& o_off = m->out_off_h[s];
+            o_nams.resize(sizeof(gbsa_nam) * (total + 1));
+            o_frac.resize(4ull * (n + 1));
+            o_resc.resize(n + 1);
+            o_off.resize(8ull * (n + 1));
             launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(),
-                               m->out_nams.as<gbsa_nam>(), m->out_frac.as<float>(), m->out_resc.as<uint8_t>(), st);
-            if (frac) GBSA_CUDA(cudaMemcpyAsync(frac + b0, m->out_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, st));
+                               o_nams.as<gbsa_nam>(), o_frac.as<float>(), o_resc.as<uint8_t>(), st);
+            launch_offsets_add(m->out_off.as<uint64_t>(), o_off.as<uint64_t>(), n + 1, done_nams, st);
+            GBSA_CUDA(cudaEventRecord(m->out_ready[s], st));
+            GBSA_CUDA(cudaStreamWaitEvent(m->copy_out, m->out_ready[s], 0));
+            GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, o_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost,
+                                      m->copy_out));
+            if (frac)
+                GBSA_CUDA(cudaMemcpyAsync(frac + b0, o_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, m->copy_out));
             if (rescued)
-                GBSA_CUDA(cudaMemcpyAsync(rescued + b0, m->out_resc.as<void>(), n, cudaMemcpyDeviceToHost, st));
+                GBSA_CUDA(cudaMemcpyAsync(rescued + b0, o_resc.as<void>(), n, cudaMemcpyDeviceToHost, m->copy_out));
             if (done_nams + total <= nam_capacity && total)
-                GBSA_CUDA(cudaMemcpyAsync(nams + done_nams, m->out_nams.as<void>(), sizeof(gbsa_nam) * total,
-                                          cudaMemcpyDeviceToHost, st));
-            GBSA_CUDA(cudaStreamSynchronize(st));
-            for (uint32_t i = 0; i <= n; ++i) nam_offsets[b0 + i] += done_nams;
+                GBSA_CUDA(cudaMemcpyAsync(nams + done_nams, o_nams.as<void>(), sizeof(gbsa_nam) * total,
+                                          cudaMemcpyDeviceToHost, m->copy_out));
+            GBSA_CUDA(cudaEventRecord(m->out_free[s], m->copy_out));
             done_nams += total;
         }
+        GBSA_CUDA(cudaStreamSynchronize(m->copy_out));
         if (done_nams > nam_capacity) throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
+    });
+}
+
+int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks) {
+    return guarded([&] {
+        if (chunks == 0) throw Error(GBSA_ERR_PARAM, "chunks must be at least 1");
+        m->pipe_chunks = chunks;
     });
 }
 

@@ -123,6 +123,7 @@ void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, c
 void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st);
 void launch_get_count(const IndexView& I, const uint64_t* pos, uint64_t n, uint32_t* counts, cudaStream_t st);
 void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st);
+void launch_offsets_add(const uint64_t* in, uint64_t* out, uint64_t n, uint64_t base, cudaStream_t st);
 void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st);
 
 }  // namespace gbsa

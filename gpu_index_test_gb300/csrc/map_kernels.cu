@@ -1392,6 +1392,17 @@ void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st) {
     GBSA_LAUNCHED();
 }
 
+__global__ void k_offsets_add(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint64_t n, uint64_t base) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[i] + base;
+}
+
+void launch_offsets_add(const uint64_t* in, uint64_t* out, uint64_t n, uint64_t base, cudaStream_t st) {
+    if (!n) return;
+    k_offsets_add<<<grid_for(n, 256, 4096), 256, 0, st>>>(in, out, n, base);
+    GBSA_LAUNCHED();
+}
+
 void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st) {
     if (!n) return;
     k_read_counts<<<grid_for(n, 256, 1u << 16), 256, 0, st>>>(n, rec, what, out);

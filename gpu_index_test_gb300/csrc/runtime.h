@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -147,5 +148,10 @@ inline unsigned grid_for(size_t n, unsigned block, unsigned max_blocks = 1u << 3
 }
 
 int device_sm_count();
+
+// Runs fn(begin, end) over [0, n) in chunks on a process-wide pool of host threads
+// (the calling thread takes part); small ranges run inline.  For the per-read host
+// loops of the C-ABI (staging offsets, rebasing results).
+void host_parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn);
 
 }  // namespace gbsa

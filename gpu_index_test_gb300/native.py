@@ -67,6 +67,7 @@ def lib():
             "gbsa_randstrobes_query_noalloc": (i32, [P, vp, vp, vp, u32, vp, u64, vp, C.POINTER(u64), vp]),
             "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, vp]),
             "gbsa_mapper_nam_cycles": (i32, [vp, vp, u32, vp]),
+            "gbsa_mapper_set_pipeline": (i32, [vp, u32]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -246,6 +247,10 @@ class Mapper:
         _check(lib().gbsa_mapper_rescue_cycles(self.h, a.ctypes.data, cap, n))
         k = min(cap // 8, n[0])
         return a[: 8 * k].reshape(-1, 8), int(n[1])
+
+    def set_pipeline(self, chunks):
+        """Chunks a large map_reads call is cut into for overlapped transfers (1 = off)."""
+        _check(lib().gbsa_mapper_set_pipeline(self.h, chunks))
 
     def nam_cycles(self, cap=1 << 22):
         """Per read of the warp find_nams kernel: (cycles, hits, NAMs, merge cycles)."""

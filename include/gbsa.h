@@ -231,6 +231,11 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
                    uint32_t rescue_cutoff, gbsa_nam* nams, uint64_t nam_capacity,
                    uint64_t* nam_offsets, float* frac);
 
+/* gbsa_map_reads cuts a call of at least 2 x 131072 reads into up to `chunks`
+ * chunks (default 4) and overlaps the transfers of one chunk with the mapping of the
+ * next; 1 turns the overlap off.  No reference counterpart. */
+int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
+
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later
  * calls; gbsa_mapper_last_alg_bytes returns the count of the last batch.  No

@@ -232,6 +232,57 @@ def test_tandem_repeat_rescue_against_oracle(mode):
     assert nams_equal(x[0], y[0])
 
 
+def test_read_layouts_give_the_same_nams():
+    """map_reads copies the span of the read buffer when the reads lie inside it (in
+    any order) and gathers them otherwise; both layouts give the NAMs of the
+    back-to-back layout, read by read."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.003, seed=51))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=1500, seed=52))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    m = native.Mapper(idx)
+    base = m.map_reads(reads)
+    perm = np.random.default_rng(53).permutation(reads.n)
+    shuffled = synth.Reads(reads.seq, reads.offsets[perm].copy(), reads.lengths[perm].copy())
+    # the last read moved far behind the others (a copy of the same bases): gathered
+    gap = 4 * len(reads.seq) + 12345
+    o_last, l_last = int(reads.offsets[-1]), int(reads.lengths[-1])
+    far_seq = np.concatenate([reads.seq, np.full(gap, ord("N"), np.uint8), reads.seq[o_last:o_last + l_last]])
+    far_offs = reads.offsets.copy()
+    far_offs[-1] = len(reads.seq) + gap
+    far = synth.Reads(far_seq, far_offs, reads.lengths.copy())
+    for layout, order in ((shuffled, perm), (far, np.arange(reads.n))):
+        x = m.map_reads(layout)
+        for j, r in enumerate(order):
+            a = x[0][int(x[1][j]):int(x[1][j + 1])]
+            b = base[0][int(base[1][r]):int(base[1][r + 1])]
+            assert len(a) == len(b) and nams_equal(a, b)
+        assert (x[2] == base[2][order]).all() and (x[3] == base[3][order]).all()
+
+
+def test_pipelined_map_reads_matches_single_batch():
+    """A call of 300k reads is cut into chunks whose transfers overlap the mapping of
+    the next; the results equal those of one unpipelined batch, also when the first
+    NAM capacity is too small (the call reports the total and is retried)."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.02, seed=61))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=150_000, seed=62))
+    assert reads.n >= 2 * (1 << 17)   # at least two chunks
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    m = native.Mapper(idx)
+    m.set_pipeline(1)
+    a = m.map_reads(reads)
+    m.set_pipeline(3)
+    b = m.map_reads(reads, capacity=1024)
+    assert (a[1] == b[1]).all() and (a[2] == b[2]).all() and (a[3] == b[3]).all()
+    assert nams_equal(a[0], b[0])
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    sub = reads.subset(np.arange(0, reads.n, 97))
+    y = o.map_reads(sub, n_threads=8)
+    x = m.map_reads(sub)
+    assert (x[1] == y[1]).all() and nams_equal(x[0], y[0])
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
