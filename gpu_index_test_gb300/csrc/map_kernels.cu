@@ -57,7 +57,7 @@ __device__ __forceinline__ void emit_read_queries(const DevParams& P, const uint
     }
 }
 
-__global__ void __launch_bounds__(32 * kSeedWarps) k_seed_smem(DevParams P, const uint8_t* __restrict__ seqs,
+__global__ void __launch_bounds__(32 * kSeedWarps, 5) k_seed_smem(DevParams P, const uint8_t* __restrict__ seqs,
                                                                 const uint64_t* __restrict__ offs,
                                                                 const uint32_t* __restrict__ lens, uint32_t n,
                                                                 ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
@@ -318,6 +318,21 @@ struct LaneOpen {
 // the open list is full and the current query start has passed it, or at the end.
 // The read's NAMs are then insertion-sorted in place.  Reads that do not fit go to
 // the warp-cooperative kernel.
+__device__ __forceinline__ HitRec load_hit(const HitRec* __restrict__ hits, uint32_t i, uint32_t H) {
+    HitRec h;
+    if (i < H) {
+        h.ref_rc = __ldg(&hits[i].ref_rc);
+        h.qs = __ldg(&hits[i].qs);
+        h.qe = __ldg(&hits[i].qe);
+        h.rs = __ldg(&hits[i].rs);
+        h.re = __ldg(&hits[i].re);
+    } else {
+        h.ref_rc = 0;
+        h.qs = h.qe = h.rs = h.re = -1;
+    }
+    return h;
+}
+
 // Hit-count bucket of a read for the lane kernel: 8 wide up to 64 hits, 16 wide up
 // to 128, then one bucket up to kLaneMaxHits.
 __device__ __forceinline__ uint32_t lane_bucket(uint32_t H) {
@@ -379,8 +394,12 @@ __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint
         NamState* out = A.nams + noff;
         uint32_t n_open = 0, n_closed = 0, cur_dir = 0;
         bool overflow = false;
+        // the next two hits are loaded while one merges
+        HitRec nx0 = load_hit(hits, 0, H), nx1 = load_hit(hits, 1, H);
         for (uint32_t i = 0; i < H; ++i) {
-            const HitRec x = hits[i];
+            const HitRec x = nx0;
+            nx0 = nx1;
+            nx1 = load_hit(hits, i + 2, H);
             const uint32_t dir = x.ref_rc >> 31;
             if (dir != cur_dir) {   // the other orientation's NAMs can take no more hits
                 for (uint32_t o = 0; o < n_open; ++o) out[n_closed++] = S.get(o, t);
@@ -565,20 +584,6 @@ __device__ __forceinline__ bool soa_merge_hits(const OpenSoA& O, uint32_t nn, ui
     return true;
 }
 
-__device__ __forceinline__ HitRec load_hit(const HitRec* __restrict__ hits, uint32_t i, uint32_t H) {
-    HitRec h;
-    if (i < H) {
-        h.ref_rc = __ldg(&hits[i].ref_rc);
-        h.qs = __ldg(&hits[i].qs);
-        h.qe = __ldg(&hits[i].qe);
-        h.rs = __ldg(&hits[i].rs);
-        h.re = __ldg(&hits[i].re);
-    } else {
-        h.ref_rc = 0;
-        h.qs = h.qe = h.rs = h.re = -1;
-    }
-    return h;
-}
 
 // find_nams merge of one read's hits (in (orientation, query_start, position)
 // order) with the open list O (capacity cap); closed NAMs are appended to closed.

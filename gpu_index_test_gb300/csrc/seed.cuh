@@ -39,10 +39,12 @@ struct WinInfo {
 // (LSB-first 32-bit words; bases at or beyond L count as N).  Writes
 // nwords = ceil(L/32) + 2 words to each array.  Each lane codes 4 consecutive bases
 // per round of 128; 8 lanes then make a word with three xor-shuffles.
-__device__ __forceinline__ void warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
+// Returns whether the read holds an N (any base that is not A/C/G/T/U).
+__device__ __forceinline__ bool warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
     const uint32_t lane = lane_id();
     const uint32_t nw = (L + 31) / 32 + 2;
     const uint32_t sub = lane & 7;   // position of the lane's 4 bases within the word
+    bool has_n = false;
     for (uint32_t b0 = 0; b0 < nw * 32; b0 += 128) {
         uint32_t code8 = 0, nbits = 0;
 #pragma unroll
@@ -63,9 +65,13 @@ __device__ __forceinline__ void warp_pack_read(const uint8_t* seq, uint32_t L, u
         if (sub == 0 && wi < nw) {
             packed[wi] = v;
             nmask[wi] = nm;
+            const uint32_t b = wi * 32;   // N bits of bases inside the read
+            const uint32_t in = b >= L ? 0u : (L - b >= 32 ? 0xFFFFFFFFu : (1u << (L - b)) - 1);
+            has_n |= (nm & in) != 0;
         }
     }
     __syncwarp();
+    return __any_sync(0xFFFFFFFFu, has_n);
 }
 
 // n (<= 33) bits of an LSB-first u32 bitmask stream starting at bit p (two words
@@ -109,19 +115,28 @@ __device__ __forceinline__ uint64_t kmer_hash(const DevParams& P, const uint64_t
 // s-mer hash of position p at hw[p & 63].  The minimum is found on the high 32 bits
 // of the hashes; a unique high-word minimum is the unique minimum, and only windows
 // with a high-word tie (or an all-ones high word) compare the full 64-bit values.
+// kW: s-mers per window when known at compile time (0: P.W).  kClean: the sequence
+// holds no N, so every window below nwin is valid and only window 0 starts a run.
+template <int kW = 0, bool kClean = false>
 __device__ __forceinline__ uint32_t window_info(const DevParams& P, const uint32_t* nmask, uint64_t base, uint32_t w,
                                                 uint32_t nwin, const uint64_t* hw) {
     if (w >= nwin) return 0;
-    // the k-mer's N bits and, for w > 0, the base before it (N before: a new run)
-    const uint32_t s1 = w > 0 ? 1u : 0u;
-    const uint64_t nb = nbits33(nmask, base + w - s1, P.k + (int)s1);
-    if ((nb >> s1) != 0) return 0;
-    const bool first = s1 == 0 || (nb & 1u);
+    bool first;
+    if (kClean) {
+        first = w == 0;
+    } else {
+        // the k-mer's N bits and, for w > 0, the base before it (N before: a new run)
+        const uint32_t s1 = w > 0 ? 1u : 0u;
+        const uint64_t nb = nbits33(nmask, base + w - s1, P.k + (int)s1);
+        if ((nb >> s1) != 0) return 0;
+        first = s1 == 0 || (nb & 1u);
+    }
+    const int W = kW ? kW : P.W;
     const uint32_t* h32 = reinterpret_cast<const uint32_t*>(hw);
     uint32_t mh = h32[2 * (w & 63) + 1];
     uint32_t eq = 1;
 #pragma unroll 8
-    for (int d = 1; d < P.W; ++d) {
+    for (int d = 1; d < W; ++d) {
         const uint32_t v = h32[2 * ((w + d) & 63) + 1];
         eq = v < mh ? 1u << d : (v == mh ? eq | 1u << d : eq);
         mh = v < mh ? v : mh;
@@ -133,7 +148,7 @@ __device__ __forceinline__ uint32_t window_info(const DevParams& P, const uint32
     } else {
         uint64_t mv = hw[w & 63];
         lo = ro = 0;
-        for (int d = 1; d < P.W; ++d) {
+        for (int d = 1; d < W; ++d) {
             const uint64_t v = hw[(w + d) & 63];
             if (v < mv) {
                 mv = v;
@@ -172,7 +187,7 @@ __device__ __forceinline__ uint32_t win_step(uint32_t m, uint32_t inf, uint32_t 
 // counting from 0.  Window w_begin must be determined, invalid, or window 0, so
 // that the state entering it never matters.  hbuf: 64 u64 of warp-private
 // scratch.  Returns the number of syncmers emitted.
-template <class Emit>
+template <int kW = 0, bool kClean = false, class Emit>
 __device__ uint32_t warp_syncmer_scan(const DevParams& P, const uint64_t* packed, const uint32_t* nmask, uint64_t base,
                                       uint32_t nwin, uint32_t w_begin, uint32_t w_end, uint32_t w_emit, uint64_t* hbuf,
                                       Emit&& emit) {
@@ -188,7 +203,7 @@ __device__ uint32_t warp_syncmer_scan(const DevParams& P, const uint64_t* packed
         const uint32_t w = c + lane;
         hbuf[(c + W1 + lane) & 63] = smer_hash(P, packed, base + c + W1 + lane);
         __syncwarp();
-        const uint32_t inf = (w < w_end) ? window_info(P, nmask, base, w, nwin, hbuf) : 0u;
+        const uint32_t inf = (w < w_end) ? window_info<kW, kClean>(P, nmask, base, w, nwin, hbuf) : 0u;
         const bool valid = inf & 1u;
         const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
         const uint32_t umask = __ballot_sync(0xFFFFFFFFu, valid && !win_determined(inf));
@@ -337,11 +352,17 @@ __device__ __forceinline__ uint32_t warp_read_syncmers(const DevParams& P, const
                                                        uint32_t* nm, uint64_t* hbuf, uint64_t* sh, uint32_t* sp,
                                                        uint32_t cap) {
     if (L < (uint32_t)P.k) return 0;
-    warp_pack_read(seq, L, pk, nm);
+    const bool has_n = warp_pack_read(seq, L, pk, nm);
     const uint32_t nwin = L - (uint32_t)P.k + 1;
-    const uint32_t n = warp_syncmer_scan(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, [&](uint32_t idx, uint32_t w) {
+    auto emit = [&](uint32_t idx, uint32_t w) {
         if (idx < cap) sp[idx] = w;
-    });
+    };
+    // reads without N (nearly all) skip the per-window N checks; the common window
+    // width (5 s-mers: k - s = 4) is unrolled at compile time
+    uint32_t n;
+    if (has_n) n = warp_syncmer_scan(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, emit);
+    else if (P.W == 5) n = warp_syncmer_scan<5, true>(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, emit);
+    else n = warp_syncmer_scan<0, true>(P, pk, nm, 0, nwin, 0, nwin, 0, hbuf, emit);
     if (n > cap) return 0xFFFFFFFFu;
     __syncwarp();
     for (uint32_t i = lane_id(); i < n; i += 32) sh[i] = kmer_hash(P, pk, sp[i]);
