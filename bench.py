@@ -260,10 +260,15 @@ def main():
             raise RuntimeError("NAM capacity too small")
         return tot
 
+    # random-gather peaks: a buffer the size of the index (larger than L2, within the
+    # GPU's TLB reach like the index) and one that fits L2
+    gather_peaks = (native.bench_gather(512 << 20)[1], native.bench_gather(16 << 20)[1]) if rank == 0 else (0.0, 0.0)
+
     # warm-up (first one also counts algorithmic bytes of the lookup stage)
     m.set_count_bytes(True)
     total_nams = step()
     alg_lookup = m.last_alg_bytes()
+    sectors_lookup = m.last_alg_sectors()
     counts = m.last_counts()
     m.set_count_bytes(False)
     for _ in range(max(0, args.warmup - 1)):
@@ -400,6 +405,18 @@ def main():
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": alg[dom], "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}}
+    # the lookup against the achievable random-gather bandwidth (sector form: 32 B per
+    # distinct sector the reference's probes touch), measured on this GPU before the
+    # timed region
+    lk_s = stage_ms.get("lookup", 0.0) / 1e3
+    gather_hbm, gather_l2 = gather_peaks
+    roofline["gather"] = {
+        "kernel": "lookup", "sectors_per_launch": int(sectors_lookup),
+        "achieved": round(sectors_lookup * 32 / lk_s / 1e9, 1) if lk_s > 0 else 0.0, "unit": "GB/s",
+        "peak_hbm_gather": round(gather_hbm, 1), "peak_l2_gather": round(gather_l2, 1),
+        "frac": round(sectors_lookup * 32 / lk_s / 1e9 / gather_hbm, 4) if lk_s > 0 and gather_hbm > 0 else None,
+        "peak_source": "gbsa_bench_gather: random 32 B sectors, 512 MB (HBM, index-sized) / 16 MB (L2) buffers",
+    }
 
     cpu = None
     exact = None

@@ -234,6 +234,7 @@ struct gbsa_mapper {
     cudaEvent_t in_ready[2] = {}, in_copied[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
     uint32_t pipe_chunks = 4;   // chunks a large gbsa_map_reads call is cut into
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
+    uint64_t alg_sectors = 0; // 32 B sectors of the lookup's gathers in the last batch (when counting)
     int count_bytes = 0;
     int profile = 0;          // record per-stage CUDA events
     cudaEvent_t ev[8] = {};
@@ -413,6 +414,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         }
         if (retry) continue;
         m.alg_bytes = h.alg_bytes;
+        m.alg_sectors = h.alg_sectors;
         m.last = h;
         // per-read NAM counts → offsets
         uint64_t* cnt = m.cnt.as<uint64_t>();
@@ -984,6 +986,7 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries, const u
 // the value of the last batch.
 void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on) { m->count_bytes = on; }
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m) { return m->alg_bytes; }
+uint64_t gbsa_mapper_last_alg_sectors(const gbsa_mapper* m) { return m->alg_sectors; }
 
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on) {
     return guarded([&] {

@@ -33,6 +33,7 @@ struct Counters {
     unsigned long long nam_used;
     unsigned long long scratch_used;
     unsigned long long alg_bytes;   // roofline numerator (see k_lookup)
+    unsigned long long alg_sectors; // distinct 32 B sectors of the lookup's gathers (see k_lookup)
     unsigned int n_rescue;        // rescued reads on the light end of the rescue list
     unsigned int n_long;
     unsigned int status;

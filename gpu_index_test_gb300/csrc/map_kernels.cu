@@ -117,8 +117,38 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_seed_long(DevParams P, 
     }
 }
 
+// Distinct 32 B sectors of [lo, hi) bytes.
+__device__ __forceinline__ uint64_t sector_span(uintptr_t lo, uintptr_t hi) {
+    return hi > lo ? ((hi - 1) >> 5) - (lo >> 5) + 1 : 0;
+}
+
+// Sector form of one query's gathers as the reference performs them: the bucket
+// bound pair, the entries examined in the bucket, and for a found key the filter
+// probe and the run walk up to the first entry of another hash (entries the search
+// already touched count once).
+__device__ __forceinline__ uint64_t lookup_sectors(const IndexView& I, uint64_t key, uint32_t ex, uint64_t pos,
+                                                   uint32_t run) {
+    const uint64_t top = key >> (64 - I.bits);
+    const uintptr_t sb = reinterpret_cast<uintptr_t>(I.starts + top);
+    uint64_t n = sector_span(sb, sb + 16);
+    const uint64_t a = I.starts[top];
+    uint64_t end = a + ex;   // entries [a, end) touched
+    if (pos != kNotFound) {
+        const uint64_t walk_end = pos + run + 1 < I.n ? pos + run + 1 : I.n;
+        end = walk_end > end ? walk_end : end;
+        const uint64_t probe = pos + I.filter_cutoff;
+        if (probe < I.n && (probe < a || probe >= end))
+            n += sector_span(reinterpret_cast<uintptr_t>(I.rs + probe), reinterpret_cast<uintptr_t>(I.rs + probe + 1));
+    }
+    n += sector_span(reinterpret_cast<uintptr_t>(I.rs + a), reinterpret_cast<uintptr_t>(I.rs + end));
+    return n;
+}
+
 constexpr uint32_t kRescueHeavyHits = 2000;   // estimated merge hits of a heavy rescued read
 
+// kCount: also count the reference's algorithmic bytes and gather sectors (a
+// separate instance, so that the counting code costs the mapping kernel nothing).
+template <bool kCount>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
                                                                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
     const uint32_t lane = lane_id();
@@ -129,32 +159,36 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
         Query* Q = A.q + R.q_off;
         uint32_t* aux = A.q_aux + R.q_off;
         uint32_t tot = 0, good = 0;
-        uint64_t bytes = 0;
+        uint64_t bytes = 0, sectors = 0;
         for (uint32_t i = lane; i < nq2; i += 32) {
             const Query q = Q[i];
             uint32_t ex = 0;
             uint64_t bend = 0;
             const uint64_t pos = index_find(I, q.hash, &ex, &bend);
-            uint32_t nh = 0;
+            uint32_t nh = 0, run = 0;
             bytes += 16 + 16ull * ex;
             if (pos != kNotFound) {
                 ++tot;
                 bytes += 16;   // the reference reads hash[pos + filter_cutoff]
                 if (!index_is_filtered_in(I, pos, q.hash, bend)) {
                     ++good;
-                    uint32_t run = 0;
                     nh = walk_hit_run(I, (int)q.start, (int)q.end, pos, [&](uint32_t, int, int) {}, &run);
                     bytes += 16ull * run;
                 }
             }
+            if (kCount) sectors += lookup_sectors(I, q.hash, ex, pos, run);
             A.q_pos[R.q_off + i] = pos;
             aux[i] = nh;
         }
         tot = warp_sum(tot);
         good = warp_sum(good);
-        if (C.count_bytes) {
+        if (kCount) {
             bytes = warp_sum(bytes);
-            if (lane == 0) atomicAdd(&ctr->alg_bytes, (unsigned long long)bytes);
+            sectors = warp_sum(sectors);
+            if (lane == 0) {
+                atomicAdd(&ctr->alg_bytes, (unsigned long long)bytes);
+                atomicAdd(&ctr->alg_sectors, (unsigned long long)sectors);
+            }
         }
         // nonrepetitive_fraction (step2/nam.cu:892) and the rescue trigger: a double
         // comparison of the float ratio with 0.7, or no hits (step2/main.cu:3211)
@@ -1308,7 +1342,8 @@ void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* o
 void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st) {
     if (!n) return;
-    k_lookup<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
+    if (C.count_bytes) k_lookup<true><<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
+    else k_lookup<false><<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

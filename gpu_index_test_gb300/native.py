@@ -61,6 +61,8 @@ def lib():
             "gbsa_find_nams": (i32, [vp, vp, vp, u32, i32, u32, vp, u64, vp, vp]),
             "gbsa_mapper_set_count_bytes": (None, [vp, i32]),
             "gbsa_mapper_last_alg_bytes": (u64, [vp]),
+            "gbsa_mapper_last_alg_sectors": (u64, [vp]),
+            "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "gbsa_mapper_set_profile": (i32, [vp, i32]),
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
@@ -104,6 +106,13 @@ def params_make(canonical_read_length, k, s, l, u, q, max_dist):
     p = abi.Params()
     _check(lib().gbsa_params_make(canonical_read_length, k, s, l, u, q, max_dist, C.byref(p)))
     return p
+
+
+def bench_gather(buffer_bytes):
+    """Random 32 B gather bandwidth over a device buffer: (sectors/s, GB/s)."""
+    a, b = C.c_double(), C.c_double()
+    _check(lib().gbsa_bench_gather(buffer_bytes, C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def _u8(a):
@@ -227,6 +236,10 @@ class Mapper:
 
     def last_alg_bytes(self):
         return lib().gbsa_mapper_last_alg_bytes(self.h)
+
+    def last_alg_sectors(self):
+        """32 B sectors of the lookup's gathers in the last batch (with set_count_bytes)."""
+        return lib().gbsa_mapper_last_alg_sectors(self.h)
 
     STAGES = ("seed", "seed_long", "lookup", "nams", "nams_warp", "rescue", "rescue_sort")
 

@@ -243,6 +243,15 @@ int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
  * step2/main.cu:4743-4746). */
 void gbsa_mapper_set_count_bytes(gbsa_mapper* m, int on);
 uint64_t gbsa_mapper_last_alg_bytes(const gbsa_mapper* m);
+/* Distinct 32-byte sectors the reference's lookup would gather in the last batch
+ * (bucket bound pair, entries examined, filter probe, run walk), counted with the
+ * bytes.  No reference counterpart. */
+uint64_t gbsa_mapper_last_alg_sectors(const gbsa_mapper* m);
+/* Achievable random-gather bandwidth of the current GPU: random 32-byte sector reads
+ * over a device buffer of buffer_bytes (allocated and freed by the call); reports
+ * sectors per second and the corresponding GB/s.  Measurement utility for the
+ * lookup's roofline; no reference counterpart. */
+int gbsa_bench_gather(uint64_t buffer_bytes, double* sectors_per_s, double* gb_per_s);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
  * returns the last batch's milliseconds for: seeding, long-read seeding, lookup,
  * NAM merge + sort (lane per read), NAM merge + sort (warp per read), rescue,

@@ -283,6 +283,24 @@ def test_pipelined_map_reads_matches_single_batch():
     assert (x[1] == y[1]).all() and nams_equal(x[0], y[0])
 
 
+def test_sector_count_and_gather_bench():
+    """The lookup's sector form lies between one sector per query (the bucket bounds)
+    and one per 16 B counted plus two per query; the gather benchmark reports a
+    positive rate, higher for a buffer that fits L2."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.003, seed=71))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=2000, seed=72))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    m = native.Mapper(idx)
+    m.set_count_bytes(True)
+    m.map_reads(reads)
+    q = m.last_counts()["queries"]
+    b, sec = m.last_alg_bytes(), m.last_alg_sectors()
+    assert q > 0 and q <= sec <= b // 16 + 2 * q
+    hbm = native.bench_gather(1 << 30)[1]
+    l2 = native.bench_gather(16 << 20)[1]
+    assert hbm > 100 and l2 > hbm
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
