@@ -324,6 +324,24 @@ def main():
             "block_sort_large_us": dist(resc[resc[:, 5] > 2048, 3], mhz),
             "worst": worst.tolist(),
         }
+    # the next stage after the NAM sort: read-pair types (gpu_pre_cal_type) of the
+    # last batch's pairs (mates are interleaved), timed alone on the same stream
+    pair_types = None
+    if rank == 0 and n >= 2:
+        d_types = torch.empty(n // 2, dtype=torch.uint8, device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        classify = lambda: native.classify_pairs_device(d_nams.data_ptr(), d_noff.data_ptr(), n // 2,
+                                                          d_types.data_ptr(), 0, 0.5, 300.0, 100.0,
+                                                          stream.cuda_stream)
+        classify()
+        e0.record(stream)
+        for _ in range(5):
+            classify()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pair_types = {"ms": round(e0.elapsed_time(e1) / 5, 4),
+                      "counts": np.bincount(d_types.cpu().numpy(), minlength=5).tolist()}
     nam_profile = None
     if len(nam_cyc):
         worst = nam_cyc[np.argsort(nam_cyc[:, 0])[-3:]]
@@ -437,7 +455,8 @@ def main():
         "bit_exact_vs_cpu_sample": exact,
         "clocks": clocks,
         "gpu_launches": int(launches),
-        "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile, nam_profile=nam_profile),
+        "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile, nam_profile=nam_profile,
+                     pair_types=pair_types),
     }
     print(json.dumps(line))
     if world > 1:

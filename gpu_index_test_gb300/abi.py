@@ -25,6 +25,8 @@ GBSA_MAX_READ_LEN = 4096
 GBSA_SORT_SCORE = 0
 GBSA_SORT_REF_MATE2 = 1
 GBSA_SORT_REF_MATE1 = 2
+GBSA_PAIRS_INTERLEAVED = 0
+GBSA_PAIRS_HALVES = 1
 
 
 class Params(C.Structure):

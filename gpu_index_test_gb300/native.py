@@ -63,6 +63,7 @@ def lib():
             "gbsa_mapper_last_alg_bytes": (u64, [vp]),
             "gbsa_mapper_last_alg_sectors": (u64, [vp]),
             "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
             "gbsa_mapper_set_profile": (i32, [vp, i32]),
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
@@ -113,6 +114,13 @@ def bench_gather(buffer_bytes):
     a, b = C.c_double(), C.c_double()
     _check(lib().gbsa_bench_gather(buffer_bytes, C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def classify_pairs_device(d_nams, d_nam_offsets, n_pairs, d_types, layout=0, dropoff=0.5, mu=300.0, sigma=100.0,
+                          stream=None):
+    """Pair types (gpu_pre_cal_type) from device NAM lists; all pointers are device addresses."""
+    _check(lib().gbsa_classify_pairs_device(d_nams, d_nam_offsets, n_pairs, layout, dropoff, mu, sigma, d_types,
+                                            stream))
 
 
 def _u8(a):

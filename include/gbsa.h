@@ -112,6 +112,11 @@ typedef struct gbsa_index_info {
 #define GBSA_SORT_REF_MATE2   1  /* Nam::operator< (step2/my_struct.hpp:78-92) made total */
 #define GBSA_SORT_REF_MATE1   2  /* sort_nams_single2 (step2/main.cu:2271-2289) made total */
 
+/* Mate layouts of the NAM lists given to gbsa_classify_pairs_device: pair i is read
+ * ends (2i, 2i+1), or (i, i + n_pairs) as in the reference's global_nams. */
+#define GBSA_PAIRS_INTERLEAVED 0
+#define GBSA_PAIRS_HALVES 1
+
 typedef struct gbsa_map_options {
     int32_t  rescue_level;      /* R (step2/cmdline.hpp:56); rescue runs when R > 1 */
     uint32_t rescue_count_cap;  /* 1000 = CPU find_nams_rescue (step2/nam.cu:964); 100 = step2/main.cu:39 */
@@ -235,6 +240,19 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
  * chunks (default 4) and overlaps the transfers of one chunk with the mapping of the
  * next; 1 turns the overlap off.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
+
+/* Read-pair classification after the NAM sort (gpu_pre_cal_type,
+ * step2/main.cu:3552-3580): for each pair, 0 = no NAMs on either end, 1 = NAMs on
+ * mate 1 only, 2 = mate 2 only, 3 = both ends' top_dropoff (main.cu:889-898) below
+ * dropoff_threshold and their first NAMs a proper pair (is_proper_nam_pair,
+ * main.cu:870-887, with insert-size mean mu and deviation sigma; the reference passes
+ * a fresh estimate, mu = 300, sigma = 100), 4 = otherwise.  d_nams / d_nam_offsets
+ * are the sorted NAM lists of 2 * n_pairs read ends as gbsa_map_reads_device writes
+ * them; d_types receives n_pairs bytes.  All pointers are device memory; the kernel
+ * runs on `stream` (0: the default stream). */
+int gbsa_classify_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs,
+                               int layout, float dropoff_threshold, float mu, float sigma,
+                               uint8_t* d_types, void* stream);
 
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later

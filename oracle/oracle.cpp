@@ -839,6 +839,51 @@ int64_t oracle_find_nams_rescue(const oracle_index* idx, const gbsa_query_randst
 
 void oracle_sort_nams(gbsa_nam* nams, uint64_t n, int sort_mode) { sort_nams(nams, n, sort_mode); }
 
+// top_dropoff (step2/main.cu:889-898): second NAM's hits over the first's, 1 when the
+// first has at most 2 hits, 0 for a single NAM; the ratio is a float division.
+static float top_dropoff(const gbsa_nam* nams, uint64_t n) {
+    const gbsa_nam& n_max = nams[0];
+    if (n_max.n_hits <= 2) return 1.0f;
+    if (n > 1) return (float)nams[1].n_hits / n_max.n_hits;
+    return 0.0f;
+}
+
+// is_proper_nam_pair (step2/main.cu:870-887): same reference, opposite orientations,
+// and the diagonal starts ordered with the reverse mate downstream, closer than
+// mu + 10 sigma (an int difference compared with a float; the bound as one fused
+// multiply-add, as nvcc compiles the reference's expression by default).
+static bool is_proper_nam_pair(const gbsa_nam& a1, const gbsa_nam& a2, float mu, float sigma) {
+    if (a1.ref_id != a2.ref_id || a1.is_rc == a2.is_rc) return false;
+    const int a = std::max(0, a1.ref_start - a1.query_start);
+    const int b = std::max(0, a2.ref_start - a2.query_start);
+    const float limit = std::fma(10.0f, sigma, mu);   // nvcc contracts mu + 10 * sigma
+    const bool r1_r2 = a2.is_rc && (a <= b) && ((float)(b - a) < limit);
+    const bool r2_r1 = a1.is_rc && (b <= a) && ((float)(a - b) < limit);
+    return r1_r2 || r2_r1;
+}
+
+// gpu_pre_cal_type (step2/main.cu:3552-3580) over the NAM lists of 2 * n_pairs ends.
+int oracle_classify_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout,
+                          float dropoff_threshold, float mu, float sigma, uint8_t* types) {
+    for (uint32_t i = 0; i < n_pairs; ++i) {
+        const uint64_t r1 = layout == GBSA_PAIRS_HALVES ? i : 2ull * i;
+        const uint64_t r2 = layout == GBSA_PAIRS_HALVES ? (uint64_t)i + n_pairs : 2ull * i + 1;
+        const gbsa_nam* n1 = nams + offsets[r1];
+        const gbsa_nam* n2 = nams + offsets[r2];
+        const uint64_t c1 = offsets[r1 + 1] - offsets[r1], c2 = offsets[r2 + 1] - offsets[r2];
+        uint8_t t;
+        if (c1 == 0 && c2 == 0) t = 0;
+        else if (c2 == 0) t = 1;
+        else if (c1 == 0) t = 2;
+        else if (top_dropoff(n1, c1) < dropoff_threshold && top_dropoff(n2, c2) < dropoff_threshold &&
+                 is_proper_nam_pair(n1[0], n2[0], mu, sigma))
+            t = 3;
+        else t = 4;
+        types[i] = t;
+    }
+    return 0;
+}
+
 int oracle_map_reads(const oracle_index* h, const gbsa_map_options* opt, const char* seqs, const uint64_t* offsets,
                      const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity,
                      uint64_t* nam_offsets, float* frac, uint8_t* rescued, int n_threads) {

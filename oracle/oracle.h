@@ -58,6 +58,8 @@ int64_t oracle_find_nams_rescue(const oracle_index* idx, const gbsa_query_randst
                                 gbsa_nam* out, uint64_t cap);
 /* Sort NAMs in place in one of the GBSA_SORT_* orders. */
 void oracle_sort_nams(gbsa_nam* nams, uint64_t n, int sort_mode);
+int oracle_classify_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout,
+                          float dropoff_threshold, float mu, float sigma, uint8_t* types);
 
 /* Whole path for a batch of reads with n_threads host threads (0 = all cores).
  * Same contract as gbsa_map_reads.  Returns GBSA_OK or GBSA_ERR_CAPACITY. */

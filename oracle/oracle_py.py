@@ -57,6 +57,9 @@ def lib():
         L.oracle_find_nams_rescue.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64]
         L.oracle_sort_nams.restype = None
         L.oracle_sort_nams.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
+        L.oracle_classify_pairs.restype = C.c_int
+        L.oracle_classify_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_float,
+                                            C.c_float, C.c_void_p]
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -203,3 +206,13 @@ def sort_nams(nams, mode=abi.GBSA_SORT_SCORE):
     if len(a):
         lib().oracle_sort_nams(a.ctypes.data, len(a), mode)
     return a
+
+
+def classify_pairs(nams, offsets, n_pairs, layout=abi.GBSA_PAIRS_INTERLEAVED, dropoff=0.5, mu=300.0, sigma=100.0):
+    """gpu_pre_cal_type restated: pair types 0..4 for the sorted NAM lists of 2 * n_pairs ends."""
+    a = np.ascontiguousarray(nams)
+    o = np.ascontiguousarray(offsets, np.uint64)
+    out = np.zeros(max(1, n_pairs), np.uint8)
+    assert lib().oracle_classify_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, dropoff,
+                                       mu, sigma, out.ctypes.data) == 0
+    return out[:n_pairs]

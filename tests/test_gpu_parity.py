@@ -301,6 +301,37 @@ def test_sector_count_and_gather_bench():
     assert hbm > 100 and l2 > hbm
 
 
+@pytest.mark.parametrize("params", [(0.5, 300.0, 100.0), (0.3, 250.3, 37.7)])
+def test_pair_classification_against_oracle(params):
+    """Pair types of mapped read pairs on the GPU equal the oracle's, with mates
+    interleaved and with mate 1 lists first (the reference's layout)."""
+    import torch
+    thr, mu, sigma = params
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=81))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=3000, seed=82))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    nams, offs, _, _ = native.Mapper(idx).map_reads(reads)
+    n_pairs = reads.n // 2
+    counts = np.diff(offs.astype(np.int64))
+    per_end = [nams[int(offs[r]):int(offs[r + 1])] for r in range(reads.n)]
+    order_h = list(range(0, reads.n, 2)) + list(range(1, reads.n, 2))
+    offs_h = np.zeros(reads.n + 1, np.uint64)
+    offs_h[1:] = np.cumsum(counts[order_h])
+    nams_h = np.concatenate([per_end[r] for r in order_h])
+    dev = torch.device("cuda:0")
+    seen = set()
+    for layout, (nn, oo) in ((abi.GBSA_PAIRS_INTERLEAVED, (nams, offs)), (abi.GBSA_PAIRS_HALVES, (nams_h, offs_h))):
+        d_n = torch.from_numpy(np.ascontiguousarray(nn).view(np.uint8).copy()).to(dev)
+        d_o = torch.from_numpy(oo.astype(np.int64)).to(dev)
+        d_t = torch.zeros(n_pairs, dtype=torch.uint8, device=dev)
+        native.classify_pairs_device(d_n.data_ptr(), d_o.data_ptr(), n_pairs, d_t.data_ptr(), layout, thr, mu, sigma)
+        got = d_t.cpu().numpy()
+        ref = oracle_py.classify_pairs(nn, oo, n_pairs, layout, thr, mu, sigma)
+        assert (got == ref).all()
+        seen |= set(got.tolist())
+    assert {3, 4} <= seen
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))

@@ -69,3 +69,48 @@ def test_nams_match_reference(case):
         a = nams[int(offs[i]) : int(offs[i + 1])]
         b = c.ref_nams[int(c.ref_nam_offsets[i]) : int(c.ref_nam_offsets[i + 1])]
         assert nams_equal(a, b), i
+
+
+def _nam(ref_id, is_rc, qs, rs, n_hits):
+    n = np.zeros(1, abi.NAM)
+    n["ref_id"], n["is_rc"], n["query_start"], n["ref_start"], n["n_hits"] = ref_id, is_rc, qs, rs, n_hits
+    n["query_end"], n["ref_end"] = qs + 50, rs + 50
+    return n
+
+
+def test_pair_classification_cases():
+    """gpu_pre_cal_type restated: each type and the boundaries of its comparisons
+    (dropoff ratio exactly 0.5, diagonal distance exactly mu + 10 sigma = 1300)."""
+    fwd = lambda rs, h=5, ref=3: _nam(ref, 0, 0, rs, h)
+    rev = lambda rs, h=5, ref=3: _nam(ref, 1, 10, rs + 10, h)   # diagonal rs
+    cases = [
+        ([], [], 0),
+        ([fwd(1000)], [], 1),
+        ([], [rev(1100)], 2),
+        ([fwd(1000)], [rev(1190)], 3),                 # r1 ---> <--- r2, distance 190
+        ([fwd(1000)], [rev(2299)], 3),                 # distance 1299
+        ([fwd(1000)], [rev(2300)], 4),                 # distance 1300 is not below the bound
+        ([rev(1190)], [fwd(1000)], 3),                 # r2 ---> <--- r1
+        ([fwd(1000)], [fwd(1190)], 4),                 # same orientation
+        ([fwd(1000)], [rev(1190, ref=4)], 4),          # other reference
+        ([fwd(1000, h=2)], [rev(1190)], 4),            # top NAM with <= 2 hits: dropoff 1
+        ([fwd(1000, h=10), fwd(5000, h=5)], [rev(1190)], 4),   # dropoff exactly 0.5
+        ([fwd(1000, h=10), fwd(5000, h=4)], [rev(1190)], 3),   # dropoff 0.4
+        ([rev(1000)], [fwd(1190)], 4),                 # reverse mate upstream
+    ]
+    ends = []
+    for m1, m2, _ in cases:
+        ends += [m1, m2]
+    offs = np.zeros(len(ends) + 1, np.uint64)
+    offs[1:] = np.cumsum([len(e) for e in ends])
+    nams = np.concatenate([x for e in ends for x in e]) if offs[-1] else np.zeros(0, abi.NAM)
+    got = oracle_py.classify_pairs(nams, offs, len(cases), abi.GBSA_PAIRS_INTERLEAVED)
+    assert list(got) == [c[2] for c in cases]
+    # the same pairs with mate 1 lists first, then mate 2 lists
+    halves = [c[0] for c in cases] + [c[1] for c in cases]
+    offs_h = np.zeros(len(halves) + 1, np.uint64)
+    offs_h[1:] = np.cumsum([len(e) for e in halves])
+    nams_h = np.concatenate([x for e in halves for x in e])
+    got_h = oracle_py.classify_pairs(nams_h, offs_h, len(cases), abi.GBSA_PAIRS_HALVES)
+    assert list(got_h) == [c[2] for c in cases]
+
