@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-rates", default="50,500,1000,2000",
+                    help="request rates (req/s) of the served-form measurement; empty to skip")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     return ap.parse_args()
 
 
@@ -124,6 +127,106 @@ def ncu_traffic():
             return json.load(f)
     except (OSError, ValueError):
         return {}
+
+
+def serve_measure(idx, g, rates, seconds, scale):
+    """Served form: Poisson arrivals of requests of 1k-100k reads (log-uniform) of
+    100-250 bp pairs against the resident index; p50/p99 latency from each request's
+    scheduled arrival to its completion, every request checked bit-exact against one
+    plain-form map_reads of the whole request pool."""
+    import queue
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
+    import torch
+    from gpu_index_test_gb300 import abi, native, synth
+
+    pool = synth.make_reads(g, synth.ReadParams(seed=123, n_units=max(2000, int(1_000_000 * scale)), len_min=100,
+                                                len_max=250, paired_frac=1.0, insert_mean=400, insert_sd=50))
+    pm = native.Mapper(idx, max_reads=pool.n, max_bases=int(pool.lengths.sum()))
+    plain = pm.map_reads(pool)
+    pm.free()
+    max_reads = 100_000
+    srv = native.Server(idx, workers=4, max_reads=max_reads, max_bases=max_reads * 250)
+    n_slots, slot_nams = 32, max_reads * 42
+    plain_bytes = np.ascontiguousarray(plain[0]).view(np.uint8)
+    slots = [(torch.empty(slot_nams * 44, dtype=torch.uint8).pin_memory(),
+              torch.empty(max_reads + 1, dtype=torch.int64).pin_memory(),
+              torch.empty(max_reads, dtype=torch.float32).pin_memory(),
+              torch.empty(max_reads, dtype=torch.uint8).pin_memory()) for _ in range(n_slots)]
+    seq_ptr = pool.seq.ctypes.data
+    results = []
+    for rate in rates:
+        rng = np.random.default_rng(1000 + int(rate))
+        arrivals, t = [], 0.0
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > seconds:
+                break
+            n = int(np.exp(rng.uniform(np.log(1000), np.log(max_reads)))) // 2 * 2
+            n = min(n, pool.n // 2 * 2)
+            start = int(rng.integers(0, (pool.n - n) // 2 + 1)) * 2
+            arrivals.append((t, start, n))
+        free = queue.Queue()
+        for i in range(n_slots):
+            free.put(i)
+        meta = {}
+        t0 = time.perf_counter() + 0.05
+
+        def submitter():
+            for tag, (ta, start, n) in enumerate(arrivals):
+                dt = t0 + ta - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                slot = free.get()
+                offs = np.ascontiguousarray(pool.offsets[start:start + n])
+                lens = np.ascontiguousarray(pool.lengths[start:start + n])
+                meta[tag] = (slot, start, n, offs, lens)
+                b = slots[slot]
+                srv.submit(seq_ptr, offs.ctypes.data, lens.ctypes.data, n, b[0].data_ptr(), slot_nams, b[1].data_ptr(),
+                           b[2].data_ptr(), b[3].data_ptr(), tag)
+
+        def check(slot, start, n, tot):
+            # whole NAM records and offsets against the plain form (byte compare)
+            b = slots[slot]
+            a0, a1 = int(plain[1][start]), int(plain[1][start + n])
+            ok = tot == a1 - a0 and np.array_equal(b[0][: tot * 44].numpy(), plain_bytes[a0 * 44:a1 * 44]) and \
+                np.array_equal(b[1][: n + 1].numpy(), (plain[1][start:start + n + 1] - a0).astype(np.int64))
+            free.put(slot)
+            return ok
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat, reads_done, failed = [], 0, 0
+        checks = []
+        t_last = t0
+        with ThreadPoolExecutor(max_workers=8) as ex:
+            while len(lat) + failed < len(arrivals):
+                for tag, st, tot in srv.poll(wait_ms=20):
+                    now = time.perf_counter()
+                    slot, start, n, _, _ = meta[tag]
+                    if st != 0:
+                        failed += 1
+                        free.put(slot)
+                        continue
+                    lat.append(now - (t0 + arrivals[tag][0]))
+                    reads_done += n
+                    t_last = max(t_last, now)
+                    checks.append(ex.submit(check, slot, start, n, tot))
+            exact = all(c.result() for c in checks)
+        th.join()
+        lat_ms = np.sort(np.array(lat)) * 1e3
+        results.append({
+            "rate_req_s": rate, "requests": len(arrivals), "failed": failed,
+            "reads_per_s": round(reads_done / max(1e-9, t_last - t0), 1),
+            "p50_ms": round(float(lat_ms[len(lat_ms) // 2]), 2) if len(lat_ms) else None,
+            "p99_ms": round(float(lat_ms[min(len(lat_ms) - 1, int(len(lat_ms) * 0.99))]), 2) if len(lat_ms) else None,
+            "max_ms": round(float(lat_ms[-1]), 2) if len(lat_ms) else None,
+            "bit_exact_vs_plain": bool(exact and failed == 0),
+        })
+    srv.free()
+    return {"workers": 4, "max_reads_per_request": max_reads, "request_reads": "1k-100k log-uniform, 100-250 bp pairs",
+            "index": "the bench's C2 index", "rates": results}
 
 
 def cpu_baseline(g, reads, target_s, gpu_result=None):
@@ -436,6 +539,11 @@ def main():
         "peak_source": "gbsa_bench_gather: random 32 B sectors, 512 MB (HBM, index-sized) / 16 MB (L2) buffers",
     }
 
+    served = None
+    rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
+    if rates and world == 1:
+        served = serve_measure(idx, g, rates, args.serve_seconds, args.scale)
+
     cpu = None
     exact = None
     if not args.no_cpu_baseline:
@@ -451,6 +559,7 @@ def main():
         "e2e": {"value": round(world * n / e2e_s, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": roofline,
+        "served": served,
         "cpu_baseline": cpu,
         "bit_exact_vs_cpu_sample": exact,
         "clocks": clocks,

@@ -233,6 +233,7 @@ struct gbsa_mapper {
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t in_ready[2] = {}, in_copied[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
     uint32_t pipe_chunks = 4;   // chunks a large gbsa_map_reads call is cut into
+    gbsa::Workspace ws;       // temporary device buffers of the prefix scans
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
     uint64_t alg_sectors = 0; // 32 B sectors of the lookup's gathers in the last batch (when counting)
     int count_bytes = 0;
@@ -333,7 +334,10 @@ static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
 static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
                              uint32_t n, bool seeded, cudaStream_t st) {
     const IndexView I = view_of(*m.idx);
-    Workspace ws;
+    // the mapper's own scan workspace: a per-call allocation would free device memory,
+    // and cudaFree waits for the whole device (other mappers' work included)
+    Workspace& ws = m.ws;
+    ws.reset();
     for (int attempt = 0; attempt < 8; ++attempt) {
         Counters* ctr = m.ctr.as<Counters>();
         GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));

@@ -64,6 +64,10 @@ def lib():
             "gbsa_mapper_last_alg_sectors": (u64, [vp]),
             "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
+            "gbsa_server_create": (i32, [vp, vp, u32, u32, u64, vp]),
+            "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
+            "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
+            "gbsa_server_free": (None, [vp]),
             "gbsa_mapper_set_profile": (i32, [vp, i32]),
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
@@ -333,3 +337,37 @@ class Mapper:
                 continue
             _check(rc)
             return nams[: int(offs[-1])], offs, frac[:n]
+
+
+class Server:
+    """The served form: requests mapped from a queue by a pool of mappers (gbsa_server_*)."""
+
+    def __init__(self, index, opt=None, workers=4, max_reads=100_000, max_bases=None):
+        self.index = index
+        self.opt = opt or abi.map_options()
+        h = C.c_void_p()
+        _check(lib().gbsa_server_create(index.h, C.byref(self.opt), workers, max_reads,
+                                        max_bases or max_reads * 256, C.byref(h)))
+        self.h = h
+
+    def submit(self, seq_ptr, offsets_ptr, lengths_ptr, n, nams_ptr, cap, nam_offsets_ptr, frac_ptr, resc_ptr, tag):
+        """All buffers are host pointers kept alive until poll reports `tag`."""
+        _check(lib().gbsa_server_submit(self.h, seq_ptr, offsets_ptr, lengths_ptr, n, nams_ptr, cap, nam_offsets_ptr,
+                                        frac_ptr, resc_ptr, tag))
+
+    def poll(self, cap=64, wait_ms=-1):
+        """Completed requests: list of (tag, status, nam_total)."""
+        tags = (C.c_uint64 * cap)()
+        st = (C.c_int * cap)()
+        tot = (C.c_uint64 * cap)()
+        k = lib().gbsa_server_poll(self.h, tags, st, tot, cap, wait_ms)
+        return [(int(tags[i]), int(st[i]), int(tot[i])) for i in range(k)]
+
+    def free(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().gbsa_server_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        self.free()
+

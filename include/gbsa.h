@@ -241,6 +241,27 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
  * next; 1 turns the overlap off.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
 
+/* ---- served form ------------------------------------------------------------- */
+/* A server keeps the index resident and maps requests from a queue on `workers`
+ * mappers (each with its own streams and device work areas for requests of up to
+ * max_reads_per_request reads / max_bases_per_request bases: the admission budget);
+ * requests overlap on the GPU and give the NAMs gbsa_map_reads gives.  Submit
+ * returns at once (GBSA_ERR_CAPACITY for a request above the maximum); the caller
+ * keeps a request's buffers alive until poll reports its tag.  Poll returns up to
+ * cap completed requests (tag, status, NAM total), waiting up to wait_ms for one
+ * (-1: until one completes or none is in flight).  No reference counterpart. */
+typedef struct gbsa_server gbsa_server;
+int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint32_t workers,
+                       uint32_t max_reads_per_request, uint64_t max_bases_per_request,
+                       gbsa_server** out);
+int gbsa_server_submit(gbsa_server* s, const char* seqs, const uint64_t* offsets,
+                       const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams,
+                       uint64_t nam_capacity, uint64_t* nam_offsets, float* frac,
+                       uint8_t* rescued, uint64_t tag);
+uint32_t gbsa_server_poll(gbsa_server* s, uint64_t* tags, int* status, uint64_t* nam_totals,
+                          uint32_t cap, int wait_ms);
+void gbsa_server_free(gbsa_server* s);
+
 /* Read-pair classification after the NAM sort (gpu_pre_cal_type,
  * step2/main.cu:3552-3580): for each pair, 0 = no NAMs on either end, 1 = NAMs on
  * mate 1 only, 2 = mate 2 only, 3 = both ends' top_dropoff (main.cu:889-898) below

@@ -332,6 +332,45 @@ def test_pair_classification_against_oracle(params):
     assert {3, 4} <= seen
 
 
+def test_server_requests_match_plain_form():
+    """Requests of uneven sizes served by three workers give, request by request, the
+    NAMs of one plain map_reads call over all reads; a request above the maximum is
+    refused."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=91))
+    pool = synth.make_reads(g, synth.ReadParams(seed=92, n_units=20_000, len_min=100, len_max=250, paired_frac=1.0,
+                                                insert_mean=400, insert_sd=50))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    plain = native.Mapper(idx).map_reads(pool)
+    srv = native.Server(idx, workers=3, max_reads=8192)
+    rng = np.random.default_rng(93)
+    reqs, bufs = [], {}
+    for tag in range(40):
+        n = int(rng.integers(1, 4096)) * 2
+        start = int(rng.integers(0, (pool.n - n) // 2)) * 2
+        offs = np.ascontiguousarray(pool.offsets[start:start + n])
+        lens = np.ascontiguousarray(pool.lengths[start:start + n])
+        cap = 64 * n
+        out = (np.zeros(cap, abi.NAM), np.zeros(n + 1, np.uint64), np.zeros(n, np.float32), np.zeros(n, np.uint8))
+        bufs[tag] = (offs, lens, out, start, n)
+        srv.submit(pool.seq.ctypes.data, offs.ctypes.data, lens.ctypes.data, n, out[0].ctypes.data, cap,
+                   out[1].ctypes.data, out[2].ctypes.data, out[3].ctypes.data, tag)
+    with pytest.raises(RuntimeError):
+        big = np.zeros(8193, np.uint64)
+        srv.submit(pool.seq.ctypes.data, big.ctypes.data, big.ctypes.data, 8193, 0, 0, 0, 0, 0, 999)
+    done = {}
+    while len(done) < 40:
+        for tag, st, tot in srv.poll(wait_ms=-1):
+            done[tag] = (st, tot)
+    srv.free()
+    for tag, (st, tot) in done.items():
+        assert st == 0
+        offs, lens, (nams, noff, frac, resc), start, n = bufs[tag]
+        a, b = int(plain[1][start]), int(plain[1][start + n])
+        assert tot == b - a and (noff == plain[1][start:start + n + 1] - a).all()
+        assert nams_equal(nams[:tot], plain[0][a:b])
+        assert (frac == plain[2][start:start + n]).all() and (resc == plain[3][start:start + n]).all()
+
+
 def test_launch_count_grows():
     before = native.launch_count()
     g = synth.make_genome(synth.GenomeParams(seed=9, total_len=100_000))
