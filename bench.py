@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--serve-rates", default="50,500,1000,2000",
                     help="request rates (req/s) of the served-form measurement; empty to skip")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
+    ap.add_argument("--no-fastq", dest="fastq", action="store_false", help="skip the FASTQ staging measurement")
     return ap.parse_args()
 
 
@@ -227,6 +228,91 @@ def serve_measure(idx, g, rates, seconds, scale):
     srv.free()
     return {"workers": 4, "max_reads_per_request": max_reads, "request_reads": "1k-100k log-uniform, 100-250 bp pairs",
             "index": "the bench's C2 index", "rates": results}
+
+
+def fastq_pipeline(m, reads, plain_nams, plain_offs, chunk_mb=48):
+    """Input staging: the reads written as two mate FASTQ files (in memory), parsed in
+    chunks by the library's parser into pinned buffers while the GPU maps the previous
+    chunk (gbsa_map_reads); reports the parse rate and the FASTQ-to-NAMs rate, and
+    checks every chunk's NAMs byte for byte against the plain run of the same reads."""
+    import threading
+
+    import torch
+    from gpu_index_test_gb300 import native
+
+    n = reads.n // 2 * 2
+    mates = []
+    for mate in (0, 1):
+        recs = []
+        for i in range(mate, n, 2):
+            o, l = int(reads.offsets[i]), int(reads.lengths[i])
+            s = reads.seq[o:o + l].tobytes()
+            recs.append(b"@r%d/%d\n%s\n+\n%s\n" % (i // 2, mate + 1, s, b"I" * l))
+        mates.append(b"".join(recs))
+    total_bytes = len(mates[0]) + len(mates[1])
+    t0 = time.perf_counter()
+    native.fastq_parse_pairs(mates[0], mates[1])
+    parse_s = time.perf_counter() - t0
+    chunk = chunk_mb << 20
+    slots = []
+    for _ in range(2):
+        seq_t = torch.empty(2 * chunk, dtype=torch.uint8).pin_memory()
+        off_t = torch.empty(chunk // 4 + 2, dtype=torch.int64).pin_memory()
+        len_t = torch.empty(chunk // 4 + 1, dtype=torch.int32).pin_memory()
+        slots.append((seq_t.numpy(), off_t.numpy().view(np.uint64), len_t.numpy().view(np.uint32)))
+    # every chunk's NAMs land in their own region of one pinned buffer (checked after timing)
+    cap = int(len(plain_nams) * 1.05) + (1 << 20)
+    h_all = torch.empty(cap * 44, dtype=torch.uint8).pin_memory()
+    h_off = torch.empty(n + 2, dtype=torch.int64).pin_memory()
+    L = native.lib()
+    plain_bytes = np.ascontiguousarray(plain_nams).view(np.uint8)
+    pos = [0, 0]
+    state = {}
+    views = [memoryview(mates[0]), memoryview(mates[1])]
+
+    def parse(slot):
+        end = [min(len(mates[j]), pos[j] + chunk) for j in (0, 1)]
+        final = end[0] == len(mates[0]) and end[1] == len(mates[1])
+        r, u1, u2 = native.fastq_parse_pairs(views[0][pos[0]:end[0]], views[1][pos[1]:end[1]], final=final,
+                                             out=slots[slot])
+        pos[0] += u1
+        pos[1] += u2
+        state[slot] = r
+
+    t0 = time.perf_counter()
+    parse(0)
+    done_reads, done_nams, slot, parts = 0, 0, 0, []
+    while state.get(slot) is not None and state[slot].n > 0:
+        r = state.pop(slot)
+        nxt = 1 - slot
+        th = None
+        if pos[0] < len(mates[0]) or pos[1] < len(mates[1]):
+            th = threading.Thread(target=parse, args=(nxt,))
+            th.start()
+        k = r.n
+        rc = L.gbsa_map_reads(m.h, r.seq.ctypes.data, r.offsets.ctypes.data, r.lengths.ctypes.data, k,
+                              h_all.data_ptr() + 44 * done_nams, cap - done_nams, h_off.data_ptr() + 8 * done_reads,
+                              None, None)
+        if rc != 0:
+            raise RuntimeError(f"gbsa_map_reads failed: {rc}")
+        tot = int(h_off[done_reads + k])
+        parts.append((done_reads, k, done_nams, tot))
+        done_reads += k
+        done_nams += tot
+        if th is not None:
+            th.join()
+        slot = nxt
+    pipe_s = time.perf_counter() - t0
+    got = h_all[: done_nams * 44].numpy()
+    exact = done_reads == n
+    for r0, k, a_got, tot in parts:
+        a0, a1 = int(plain_offs[r0]), int(plain_offs[r0 + k])
+        exact = exact and tot == a1 - a0 and np.array_equal(got[a_got * 44:(a_got + tot) * 44],
+                                                            plain_bytes[a0 * 44:a1 * 44])
+    return {"fastq_bytes": total_bytes, "reads": done_reads, "parse_gb_s": round(total_bytes / parse_s / 1e9, 2),
+            "parse_reads_per_s": round(n / parse_s, 1), "chunk_mb_per_file": chunk_mb,
+            "fastq_to_nams_reads_per_s": round(done_reads / pipe_s, 1),
+            "bit_exact_vs_plain": bool(exact)}
 
 
 def cpu_baseline(g, reads, target_s, gpu_result=None):
@@ -539,6 +625,11 @@ def main():
         "peak_source": "gbsa_bench_gather: random 32 B sectors, 512 MB (HBM, index-sized) / 16 MB (L2) buffers",
     }
 
+    staging = None
+    if world == 1 and args.fastq:
+        staging = fastq_pipeline(m, reads, h_nams[: tot_nams_e2e * 44].numpy().view(abi.NAM),
+                                 h_noff.numpy().view(np.uint64))
+
     served = None
     rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
     if rates and world == 1:
@@ -560,6 +651,7 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "roofline": roofline,
         "served": served,
+        "fastq_staging": staging,
         "cpu_baseline": cpu,
         "bit_exact_vs_cpu_sample": exact,
         "clocks": clocks,

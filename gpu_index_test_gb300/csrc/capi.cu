@@ -37,9 +37,9 @@ public:
         static HostPool pool;
         return pool;
     }
-    void run(size_t n, const std::function<void(size_t, size_t)>& fn) {
+    void run(size_t n, const std::function<void(size_t, size_t)>& fn, size_t min_chunk = kMinChunk) {
         std::lock_guard<std::mutex> one_job(job_mu_);   // one job at a time
-        const size_t chunk = std::max<size_t>(kMinChunk, n / (4 * (workers_.size() + 1)) + 1);
+        const size_t chunk = std::max<size_t>(min_chunk, n / (4 * (workers_.size() + 1)) + 1);
         {
             std::lock_guard<std::mutex> g(mu_);
             fn_ = &fn;
@@ -111,6 +111,16 @@ void host_parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn) 
         return;
     }
     HostPool::get().run(n, fn);
+}
+
+void host_parallel_tasks(size_t n, const std::function<void(size_t)>& fn) {
+    if (n <= 1) {
+        if (n) fn(0);
+        return;
+    }
+    HostPool::get().run(n, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) fn(i);
+    }, 1);
 }
 
 int device_sm_count() {

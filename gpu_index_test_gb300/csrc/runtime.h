@@ -154,4 +154,8 @@ int device_sm_count();
 // loops of the C-ABI (staging offsets, rebasing results).
 void host_parallel_for(size_t n, const std::function<void(size_t, size_t)>& fn);
 
+// Runs fn(i) for i in [0, n) as separate tasks on the same pool (one task per
+// thread at a time); for a few coarse tasks.
+void host_parallel_tasks(size_t n, const std::function<void(size_t)>& fn);
+
 }  // namespace gbsa

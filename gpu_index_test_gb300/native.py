@@ -68,6 +68,10 @@ def lib():
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
             "gbsa_server_free": (None, [vp]),
+            "gbsa_fastq_parse": (i32, [vp, u64, i32, vp, u64, vp, vp, u32, C.POINTER(u32), C.POINTER(u64),
+                                       C.POINTER(u64)]),
+            "gbsa_fastq_parse_pairs": (i32, [vp, u64, vp, u64, i32, vp, u64, vp, vp, u32, C.POINTER(u32),
+                                             C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
             "gbsa_mapper_set_profile": (i32, [vp, i32]),
             "gbsa_mapper_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_mapper_last_counts": (i32, [vp, vp]),
@@ -370,4 +374,46 @@ class Server:
 
     def __del__(self):
         self.free()
+
+
+def _fastq_out(total_len):
+    seqs = np.zeros(max(1, total_len), np.uint8)
+    cap_reads = total_len // 8 + 2
+    return seqs, np.zeros(cap_reads + 1, np.uint64), np.zeros(max(1, cap_reads), np.uint32), cap_reads
+
+
+def fastq_parse(buf, final=True):
+    """Complete FASTQ records of a chunk: (Reads, consumed bytes)."""
+    from .synth import Reads
+    b = np.frombuffer(buf, np.uint8) if isinstance(buf, (bytes, bytearray)) else np.ascontiguousarray(buf, np.uint8)
+    seqs, offs, lens, cap = _fastq_out(len(b))
+    n, nb, used = C.c_uint32(), C.c_uint64(), C.c_uint64()
+    _check(lib().gbsa_fastq_parse(b.ctypes.data if len(b) else None, len(b), 1 if final else 0, seqs.ctypes.data,
+                                  len(seqs), offs.ctypes.data, lens.ctypes.data, cap, C.byref(n), C.byref(nb),
+                                  C.byref(used)))
+    k = n.value
+    return Reads(seqs[: nb.value].copy(), offs[:k].copy(), lens[:k].copy()), used.value
+
+
+def fastq_parse_pairs(buf1, buf2, final=True, out=None):
+    """Complete pairs of two mate-file chunks, mates interleaved: (Reads, consumed1, consumed2).
+    out = (seqs u8, offsets u64, lengths u32) arrays to parse into (e.g. views of pinned
+    memory); the returned Reads then views them."""
+    from .synth import Reads
+    b1 = np.frombuffer(buf1, np.uint8) if isinstance(buf1, (bytes, bytearray)) else np.ascontiguousarray(buf1, np.uint8)
+    b2 = np.frombuffer(buf2, np.uint8) if isinstance(buf2, (bytes, bytearray)) else np.ascontiguousarray(buf2, np.uint8)
+    if out is None:
+        seqs, offs, lens, cap = _fastq_out(len(b1) + len(b2))
+    else:
+        seqs, offs, lens = out
+        cap = min(len(lens), len(offs) - 1)
+    n, nb, u1, u2 = C.c_uint32(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+    _check(lib().gbsa_fastq_parse_pairs(b1.ctypes.data if len(b1) else None, len(b1),
+                                        b2.ctypes.data if len(b2) else None, len(b2), 1 if final else 0,
+                                        seqs.ctypes.data, len(seqs), offs.ctypes.data, lens.ctypes.data, cap,
+                                        C.byref(n), C.byref(nb), C.byref(u1), C.byref(u2)))
+    k = n.value
+    if out is not None:
+        return Reads(seqs[: nb.value], offs[:k], lens[:k]), u1.value, u2.value
+    return Reads(seqs[: nb.value].copy(), offs[:k].copy(), lens[:k].copy()), u1.value, u2.value
 

@@ -37,6 +37,7 @@ extern "C" {
 #define GBSA_ERR_READ_TOO_LONG  6  /* a read exceeds GBSA_MAX_READ_LEN */
 #define GBSA_ERR_NO_DEVICE      7  /* no CUDA device visible */
 #define GBSA_ERR_DEVICE_STATUS  8  /* a kernel reported an internal limit */
+#define GBSA_ERR_FORMAT         9  /* malformed FASTQ input */
 
 /* Longest read (bases) accepted by the seeding kernels. */
 #define GBSA_MAX_READ_LEN 4096
@@ -240,6 +241,27 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
  * chunks (default 4) and overlaps the transfers of one chunk with the mapping of the
  * next; 1 turns the overlap off.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
+
+/* ---- input staging ----------------------------------------------------------- */
+/* Parses the complete 4-line FASTQ records of a chunk of a file (host threads) into
+ * the reads layout of gbsa_map_reads: sequence bytes back to back in seqs, offsets
+ * (n + 1 entries) and lengths (step2/main.cu:63-81, 4212-4240, 4404-4430 stage the
+ * same layout).  CR before LF and blank lines between records are accepted.  When
+ * `final` is 0, a record cut by the end of the chunk is left out and *consumed is
+ * where it starts (the caller passes the rest again with the next chunk); when 1,
+ * the chunk is the end of the file.  seq_capacity >= len and read_capacity >=
+ * len / 8 + 1 always suffice; otherwise GBSA_ERR_CAPACITY reports the needed counts
+ * in *n_reads / *n_bases.  Malformed input gives GBSA_ERR_FORMAT. */
+int gbsa_fastq_parse(const char* buf, uint64_t len, int final, char* seqs, uint64_t seq_capacity,
+                     uint64_t* offsets, uint32_t* lengths, uint32_t read_capacity,
+                     uint32_t* n_reads, uint64_t* n_bases, uint64_t* consumed);
+/* The same for chunks of two mate files: pairs interleaved (mate 1, mate 2), as many
+ * pairs as both chunks hold complete; files of different record counts give
+ * GBSA_ERR_FORMAT at the end. */
+int gbsa_fastq_parse_pairs(const char* buf1, uint64_t len1, const char* buf2, uint64_t len2,
+                           int final, char* seqs, uint64_t seq_capacity, uint64_t* offsets,
+                           uint32_t* lengths, uint32_t read_capacity, uint32_t* n_reads,
+                           uint64_t* n_bases, uint64_t* consumed1, uint64_t* consumed2);
 
 /* ---- served form ------------------------------------------------------------- */
 /* A server keeps the index resident and maps requests from a queue on `workers`
