@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbsa", choices=["gbsa", "reference"])
+    ap.add_argument("--config", default="C2", choices=["C1", "C2", "C3", "C4"],
+                    help="workload (C2 is the headline configuration)")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -49,11 +51,16 @@ def parse():
     return ap.parse_args()
 
 
-def workload(scale, rank):
+# read units per config at scale 1 (pairs count as one unit): C1 100k single-end
+# reads; C2 1M pairs; C3 ~2M reads half single-end, half in pairs; C4 5M pairs
+UNITS = {"C1": 100_000, "C2": 1_000_000, "C3": 1_333_333, "C4": 5_000_000}
+
+
+def workload(scale, rank, config="C2"):
     from gpu_index_test_gb300 import synth
 
-    gp = synth.genome_params("C2", scale=scale, seed=1)
-    rp = synth.read_params("C2", n_units=max(1000, int(1_000_000 * scale)), seed=11 + rank)
+    gp = synth.genome_params("C1" if config == "C3" else config, scale=scale, seed=1)
+    rp = synth.read_params(config, n_units=max(1000, int(UNITS[config] * scale)), seed=11 + rank)
     t0 = time.perf_counter()
     g = synth.make_genome(gp)
     reads = synth.make_reads(g, rp)
@@ -357,7 +364,7 @@ def run_reference(args):
     import __graft_entry__
 
     __graft_entry__.build()
-    g, reads, _, gp, rp = workload(args.scale, 0)
+    g, reads, _, gp, rp = workload(args.scale, 0, args.config)
     p = oracle_py.params_from_read_length(150)
     idx = oracle_py.Index.build(p, g)
     cores = os.cpu_count() or 1
@@ -388,14 +395,24 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+WORKLOADS = {
+    "C1": "C1 plain small: synthetic 5 Mbp single contig, 100k single-end 150 bp reads",
+    "C2": "C2 repeat-rich mid-size: synthetic 100 Mbp / 20 contigs (5% segmental duplications, STRs), "
+          "1M paired-end 2x150 bp pairs = 2M reads per step",
+    "C3": "C3 uneven lengths: the C1 genome, ~2M reads of 50-500 bp (log-uniform), half single-end, half paired",
+    "C4": "C4 human-scale: synthetic 3.1 Gbp / 24 contigs (~45% repeat families, duplications, STRs), "
+          "5M paired-end 2x150 bp pairs = 10M reads per step",
+}
+
+
 def config_of(gp, rp, reads, args):
     return {
-        "workload": "C2 repeat-rich mid-size: synthetic 100 Mbp / 20 contigs (5% segmental duplications, STRs), "
-                    "1M paired-end 2x150 bp pairs = 2M reads per step",
-        "genome_bp": gp.total_len, "contigs": gp.n_contigs, "reads_per_step": reads.n, "read_len": rp.len_min,
-        "paired": True, "params": "from_read_length(150): k=20 s=16 l=1 u=7 q=255 max_dist=80",
+        "workload": WORKLOADS[args.config],
+        "genome_bp": gp.total_len, "contigs": gp.n_contigs, "reads_per_step": reads.n,
+        "read_len": rp.len_min if rp.len_min == rp.len_max else f"{rp.len_min}-{rp.len_max}",
+        "paired": rp.paired_frac, "params": "from_read_length(150): k=20 s=16 l=1 u=7 q=255 max_dist=80",
         "rescue": "R=2, rescue_cutoff=2*filter_cutoff, count cap 1000", "nam_order": "score",
-        "l2": "inputs larger than L2 (2M reads = 300 MB of bases; index 320 MB + 64 MB bucket table)",
+        "l2": "reads and index sizes as listed; no L2 flush between steps (C2, C4: inputs larger than L2)",
         "scale": args.scale,
     }
 
@@ -420,7 +437,7 @@ def main():
     __graft_entry__.build()
     from gpu_index_test_gb300 import abi, native
 
-    g, reads, gen_s, gp, rp = workload(args.scale, rank)
+    g, reads, gen_s, gp, rp = workload(args.scale, rank, args.config)
     p = native.params_from_read_length(150)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -626,13 +643,13 @@ def main():
     }
 
     staging = None
-    if world == 1 and args.fastq:
+    if world == 1 and args.fastq and args.config == "C2":
         staging = fastq_pipeline(m, reads, h_nams[: tot_nams_e2e * 44].numpy().view(abi.NAM),
                                  h_noff.numpy().view(np.uint64))
 
     served = None
     rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
-    if rates and world == 1:
+    if rates and world == 1 and args.config == "C2":
         served = serve_measure(idx, g, rates, args.serve_seconds, args.scale)
 
     cpu = None
