@@ -531,6 +531,7 @@ int gbsa_index_load(const gbsa_params* p, const gbsa_ref_randstrobe* randstrobes
         ix->starts.resize(8 * nb);
         if (n) GBSA_CUDA(cudaMemcpy(ix->rs.as<void>(), randstrobes, 16 * n, cudaMemcpyHostToDevice));
         GBSA_CUDA(cudaMemcpy(ix->starts.as<void>(), start_indices, 8 * nb, cudaMemcpyHostToDevice));
+        make_compact_starts(*ix, 0);
         ix->info.size = n;
         ix->info.bits = bits;
         ix->info.filter_cutoff = filter_cutoff;

@@ -23,6 +23,7 @@ struct gbsa_index {
     int device = 0;
     gbsa::DeviceBuffer rs;       // gbsa_ref_randstrobe[n]
     gbsa::DeviceBuffer starts;   // uint64_t[2^bits + 1]
+    gbsa::DeviceBuffer starts32; // uint32_t[2^bits + 1] copy read by the kernels when n < 2^32
 };
 
 namespace gbsa {
@@ -31,6 +32,7 @@ namespace gbsa {
 struct IndexView {
     const gbsa_ref_randstrobe* rs;
     const uint64_t* starts;
+    const uint32_t* starts32;   // half-size table (half the L2 footprint), or null
     uint64_t n;
     int bits;
     uint32_t filter_cutoff;
@@ -38,9 +40,13 @@ struct IndexView {
 };
 
 inline IndexView view_of(const gbsa_index& ix) {
-    return IndexView{ix.rs.as<gbsa_ref_randstrobe>(), ix.starts.as<uint64_t>(), ix.n, ix.bits, ix.filter_cutoff,
+    return IndexView{ix.rs.as<gbsa_ref_randstrobe>(), ix.starts.as<uint64_t>(),
+                     ix.starts32.size() ? ix.starts32.as<uint32_t>() : nullptr, ix.n, ix.bits, ix.filter_cutoff,
                      ix.params.k};
 }
+
+// Builds the 32-bit copy of the bucket table when every start fits (n < 2^32).
+void make_compact_starts(gbsa_index& ix, cudaStream_t st);
 
 // Validates parameters like the reference constructors (step2/indexparameters.hpp:24-68).
 bool params_valid(const gbsa_params& p);

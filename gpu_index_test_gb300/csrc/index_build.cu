@@ -393,6 +393,22 @@ void build_index(gbsa_index& ix, const char* seqs, const uint64_t* offsets, cons
     finish_stats(ix, H, unique, f);
     ix.info.size = ix.n;
     ix.info.bits = ix.bits;
+    make_compact_starts(ix, st);
+}
+
+__global__ void k_narrow_starts(const uint64_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = (uint32_t)in[i];
+}
+
+void make_compact_starts(gbsa_index& ix, cudaStream_t st) {
+    if (ix.n >= (1ull << 32)) return;
+    const uint64_t nb = (1ULL << ix.bits) + 1;
+    ix.starts32.resize(4 * nb);
+    k_narrow_starts<<<grid_for(nb, 256, 1u << 16), 256, 0, st>>>(ix.starts.as<uint64_t>(), ix.starts32.as<uint32_t>(),
+                                                                 nb);
+    GBSA_LAUNCHED();
+    GBSA_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace gbsa

@@ -17,6 +17,11 @@ __device__ __forceinline__ uint64_t get_hash(const IndexView& I, uint64_t pos) {
     return pos < I.n ? __ldg(&I.rs[pos].hash) : ~0ULL;
 }
 
+// Entry i of the bucket table (the 32-bit copy when the index has one).
+__device__ __forceinline__ uint64_t bucket_start(const IndexView& I, uint64_t i) {
+    return I.starts32 ? (uint64_t)__ldg(&I.starts32[i]) : __ldg(&I.starts[i]);
+}
+
 // StrobemerIndex::find (step2/index.hpp:57-81): first entry of the key's bucket
 // whose hash equals the key, or kNotFound.  The in-bucket search examines entries
 // in order until one is >= key (buckets hold ~2 entries on average) and switches to
@@ -25,8 +30,8 @@ __device__ __forceinline__ uint64_t get_hash(const IndexView& I, uint64_t pos) {
 __device__ __forceinline__ uint64_t index_find(const IndexView& I, uint64_t key, uint32_t* ex = nullptr,
                                                uint64_t* bucket_end = nullptr) {
     const uint64_t top = key >> (64 - I.bits);
-    const uint64_t a = __ldg(&I.starts[top]);
-    const uint64_t b = __ldg(&I.starts[top + 1]);
+    const uint64_t a = bucket_start(I, top);
+    const uint64_t b = bucket_start(I, top + 1);
     if (bucket_end) *bucket_end = b;
     if (a >= b) {
         if (ex) *ex = 0;
@@ -72,7 +77,7 @@ __device__ __forceinline__ bool index_is_filtered_in(const IndexView& I, uint64_
 // starting at pos, within the bucket.
 __device__ __forceinline__ uint32_t index_get_count(const IndexView& I, uint64_t pos) {
     const uint64_t key = __ldg(&I.rs[pos].hash);
-    const uint64_t end = __ldg(&I.starts[(key >> (64 - I.bits)) + 1]);
+    const uint64_t end = bucket_start(I, (key >> (64 - I.bits)) + 1);
     if (end - pos < 8) {
         uint32_t c = 1;
         for (uint64_t x = pos + 1; x < end && __ldg(&I.rs[x].hash) == key; ++x) ++c;

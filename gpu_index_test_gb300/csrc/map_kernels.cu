@@ -129,9 +129,10 @@ __device__ __forceinline__ uint64_t sector_span(uintptr_t lo, uintptr_t hi) {
 __device__ __forceinline__ uint64_t lookup_sectors(const IndexView& I, uint64_t key, uint32_t ex, uint64_t pos,
                                                    uint32_t run) {
     const uint64_t top = key >> (64 - I.bits);
-    const uintptr_t sb = reinterpret_cast<uintptr_t>(I.starts + top);
-    uint64_t n = sector_span(sb, sb + 16);
-    const uint64_t a = I.starts[top];
+    const uintptr_t sb = I.starts32 ? reinterpret_cast<uintptr_t>(I.starts32 + top)
+                                    : reinterpret_cast<uintptr_t>(I.starts + top);
+    uint64_t n = sector_span(sb, sb + (I.starts32 ? 8 : 16));
+    const uint64_t a = bucket_start(I, top);
     uint64_t end = a + ex;   // entries [a, end) touched
     if (pos != kNotFound) {
         const uint64_t walk_end = pos + run + 1 < I.n ? pos + run + 1 : I.n;
