@@ -230,6 +230,9 @@ struct gbsa_mapper {
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;                           // rescue chain, beside the NAM kernels
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaStream_t side_lo = nullptr;                        // rescue chain of a batch on a caller's stream
+    cudaStream_t early = nullptr;                          // seeding + lookup of pipelined chunks
+    cudaEvent_t early_ev = nullptr;
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
@@ -237,12 +240,21 @@ struct gbsa_mapper {
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
-    // second input / output slots and copy streams of the pipelined host entry point
-    gbsa::DeviceBuffer seqs1, offs1, lens1, out_nams1, out_frac1, out_resc1, out_off_h[2];
-    gbsa::PinnedBuffer h_seqs1, h_meta1;
+    gbsa::PinnedBuffer h_status;   // counters + NAM total of the last enqueued batch
+    // pipelined host entry point: copy streams, the twin that maps every other chunk,
+    // events (reads copied in, batch done), two output slots that a batch's results wait
+    // in to be copied out, and NAMs per read seen so far (sizes the slots)
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
-    cudaEvent_t in_ready[2] = {}, in_copied[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
-    uint32_t pipe_chunks = 4;   // chunks a large gbsa_map_reads call is cut into
+    gbsa_mapper* twin = nullptr;
+    cudaEvent_t in_ready = nullptr, done_ev = nullptr;
+    struct OutSlot {
+        gbsa::DeviceBuffer nams, frac, resc, off, off_g;   // off: batch offsets, off_g: call offsets
+        uint64_t cap = 0;                                 // NAM records nams holds
+        cudaEvent_t free = nullptr;                       // copies out of the slot ended
+    } outs[2];
+    double nams_per_read = 16.0;
+    uint64_t retries = 0;   // batches run again after a work area grew
+    uint32_t pipe_chunks = 2;   // full chunks a large gbsa_map_reads call is cut into
     gbsa::Workspace ws;       // temporary device buffers of the prefix scans
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
     uint64_t alg_sectors = 0; // 32 B sectors of the lookup's gathers in the last batch (when counting)
@@ -337,110 +349,183 @@ static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
     b.resize(elem * cap);
 }
 
-// Runs seeding (unless the queries are already in place) → lookup → NAMs → rescue
-// for n reads whose bases/offsets/lengths are on the device; retries with larger
-// work areas when a bump allocator overflowed.  Leaves per-read NAM offsets in
-// m.out_off[0..n] and returns the NAM total.
-static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
-                             uint32_t n, bool seeded, cudaStream_t st) {
+// Enqueues one attempt at n reads whose bases/offsets/lengths are on the device:
+// seeding (unless the queries are already in place) → lookup → NAMs (main stream) and
+// rescue → sorts (side stream), then the per-read NAM offsets into m.out_off[0..n]; the
+// device counters and the NAM total are copied to m.h_status (pinned).  Nothing waits
+// on the host.
+static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
+                          uint32_t n, bool seeded, cudaStream_t st, cudaStream_t early = nullptr) {
+    cudaStream_t main_st = st;
+    if (early) {
+        GBSA_CUDA(cudaEventRecord(m.early_ev, st));
+        GBSA_CUDA(cudaStreamWaitEvent(early, m.early_ev, 0));
+        st = early;
+    }
     const IndexView I = view_of(*m.idx);
     // the mapper's own scan workspace: a per-call allocation would free device memory,
     // and cudaFree waits for the whole device (other mappers' work included)
     Workspace& ws = m.ws;
     ws.reset();
+    m.h_status.resize(sizeof(Counters) + 8);
+    Counters* ctr = m.ctr.as<Counters>();
+    GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
+    if (!seeded) {
+        GBSA_CUDA(cudaMemsetAsync(m.rec.as<void>(), 0, sizeof(ReadRec) * n, st));
+    } else {
+        // keep q_off / nq / nq2 written by the caller; clear the rest
+        launch_reset_recs(n, m.rec.as<ReadRec>(), st);
+    }
+    Arenas A = arenas_of(m);
+    if (A.rescue_cycles) GBSA_CUDA(cudaMemsetAsync(A.rescue_cycles, 0, m.resc_cycles.size(), st));
+    MapConfig C = m.cfg;
+    C.count_bytes = m.count_bytes;
+    auto mark = [&](int i) {
+        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[i], st));
+    };
+    mark(0);
+    if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+    mark(1);
+    if (!seeded)
+        launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr, m.long_scratch.as<uint8_t>(),
+                         m.long_warps, st);
+    mark(2);
+    launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    launch_bucket_reads(n, m.rec.as<ReadRec>(), A, ctr, st);
+    if (early) {
+        GBSA_CUDA(cudaEventRecord(m.early_ev, early));
+        GBSA_CUDA(cudaStreamWaitEvent(main_st, m.early_ev, 0));
+        st = main_st;
+    }
+    mark(3);
+    // The rescue chain works on the rescued reads only and the NAM kernels on the
+    // others: the rescue chain runs on the side stream (with its own scratch slots) so
+    // that its tail of reads with thousands of hits overlaps them.
+    // (at the main stream's priority: a caller's stream has the lowest)
+    cudaStream_t side = m.side;
+    if (st != m.st) {
+        int prio = 0, lo = 0, hi = 0;
+        GBSA_CUDA(cudaStreamGetPriority(st, &prio));
+        GBSA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        if (prio != hi) side = m.side_lo;
+    }
+    GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
+    GBSA_CUDA(cudaStreamWaitEvent(side, m.fork_ev, 0));
+    Arenas As = A;
+    As.slots = m.side_slots.as<uint8_t>();
+    launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, side);
+    if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[6], side));
+    if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, side);
+    if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[7], side));
+    GBSA_CUDA(cudaEventRecord(m.join_ev, side));
+    launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    mark(4);
+    launch_nams_warp(C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    mark(5);
+    GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
+    // per-read NAM counts → offsets (meaningless when an arena overflowed; the batch is
+    // then run again)
+    uint64_t* cnt = m.cnt.as<uint64_t>();
+    uint64_t* off = m.out_off.as<uint64_t>();
+    launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st);
+    scan_exclusive_u64(cnt, off, n, off + n, ws, st);
+    GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<void>(), ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<uint8_t>() + sizeof(Counters), off + n, 8, cudaMemcpyDeviceToHost, st));
+}
+
+// Reads the status of a batch that enqueue_batch ran and that has completed.  Throws for
+// a fatal status; grows the work areas that overflowed and returns false (the batch must
+// run again); otherwise records the counters and returns true.
+static bool check_batch(gbsa_mapper& m, bool seeded) {
+    const Counters h = *m.h_status.as<Counters>();
+    if (m.profile) {
+        // seed, long seed, lookup, lane NAMs, warp NAMs (main stream); rescue, its
+        // block sorts (side stream, from the fork after the lookup)
+        static const int from[7] = {0, 1, 2, 3, 4, 3, 6}, to[7] = {1, 2, 3, 4, 5, 6, 7};
+        for (int i = 0; i < 7; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[from[i]], m.ev[to[i]]));
+    }
+    if (h.status & kStatusReadTooLong)
+        throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
+    if (h.status & kStatusSyncmerOverflow) throw Error(GBSA_ERR_DEVICE_STATUS, "syncmer buffer overflow");
+    bool retry = false;
+    if (h.status & kStatusQueryOverflow) {
+        if (seeded) throw Error(GBSA_ERR_DEVICE_STATUS, "query arena overflow");
+        grow(m.q, m.q_cap, h.q_used, sizeof(Query));
+        m.qaux.release();
+        m.qaux.resize(4 * m.q_cap);
+        m.qpos.release();
+        m.qpos.resize(8 * m.q_cap);
+        retry = true;
+    }
+    if (h.status & kStatusHitOverflow) {
+        grow(m.hits, m.hit_cap, h.hit_used, sizeof(HitRec));
+        retry = true;
+    }
+    if (h.status & kStatusNamOverflow) {
+        grow(m.nams, m.nam_cap, h.nam_used, sizeof(NamState));
+        retry = true;
+    }
+    if (h.status & kStatusScratchOverflow) {
+        grow(m.ovf, m.ovf_cap, h.scratch_used, 1);
+        retry = true;
+    }
+    if (retry) {
+        ++m.retries;
+        return false;
+    }
+    m.alg_bytes = h.alg_bytes;
+    m.alg_sectors = h.alg_sectors;
+    m.last = h;
+    return true;
+}
+
+static uint64_t batch_total(gbsa_mapper& m) {
+    uint64_t t;
+    std::memcpy(&t, m.h_status.as<uint8_t>() + sizeof(Counters), 8);
+    return t;
+}
+
+// enqueue_batch + check_batch until the work areas are large enough: leaves per-read NAM
+// offsets in m.out_off[0..n] and returns the NAM total.
+static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
+                             uint32_t n, bool seeded, cudaStream_t st) {
     for (int attempt = 0; attempt < 8; ++attempt) {
-        Counters* ctr = m.ctr.as<Counters>();
-        GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
-        if (!seeded) {
-            GBSA_CUDA(cudaMemsetAsync(m.rec.as<void>(), 0, sizeof(ReadRec) * n, st));
-        } else {
-            // keep q_off / nq / nq2 written by the caller; clear the rest
-            launch_reset_recs(n, m.rec.as<ReadRec>(), st);
-        }
-        Arenas A = arenas_of(m);
-        if (A.rescue_cycles) GBSA_CUDA(cudaMemsetAsync(A.rescue_cycles, 0, m.resc_cycles.size(), st));
-        MapConfig C = m.cfg;
-        C.count_bytes = m.count_bytes;
-        auto mark = [&](int i) {
-            if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[i], st));
-        };
-        mark(0);
-        if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
-        mark(1);
-        if (!seeded)
-            launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr,
-                             m.long_scratch.as<uint8_t>(), m.long_warps, st);
-        mark(2);
-        launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
-        launch_bucket_reads(n, m.rec.as<ReadRec>(), A, ctr, st);
-        mark(3);
-        // The rescue chain works on the rescued reads only and the NAM kernels on the
-        // others: the rescue chain runs on the side stream (with its own scratch
-        // slots) so that its tail of reads with thousands of hits overlaps them.
-        GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
-        GBSA_CUDA(cudaStreamWaitEvent(m.side, m.fork_ev, 0));
-        Arenas As = A;
-        As.slots = m.side_slots.as<uint8_t>();
-        launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, m.side);
-        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[6], m.side));
-        if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, m.side);
-        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[7], m.side));
-        GBSA_CUDA(cudaEventRecord(m.join_ev, m.side));
-        launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
-        mark(4);
-        launch_nams_warp(C, n, m.rec.as<ReadRec>(), A, ctr, st);
-        mark(5);
-        GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
-        Counters h{};
-        GBSA_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+        enqueue_batch(m, d_seqs, d_offs, d_lens, n, seeded, st);
         GBSA_CUDA(cudaStreamSynchronize(st));
-        if (m.profile) {
-            // seed, long seed, lookup, lane NAMs, warp NAMs (main stream); rescue, its
-            // block sorts (side stream, from the fork after the lookup)
-            static const int from[7] = {0, 1, 2, 3, 4, 3, 6}, to[7] = {1, 2, 3, 4, 5, 6, 7};
-            for (int i = 0; i < 7; ++i) GBSA_CUDA(cudaEventElapsedTime(&m.stage_ms[i], m.ev[from[i]], m.ev[to[i]]));
-        }
-        if (h.status & kStatusReadTooLong)
-            throw Error(GBSA_ERR_READ_TOO_LONG, "a read is longer than GBSA_MAX_READ_LEN bases");
-        if (h.status & kStatusSyncmerOverflow)
-            throw Error(GBSA_ERR_DEVICE_STATUS, "syncmer buffer overflow");
-        bool retry = false;
-        if (h.status & kStatusQueryOverflow) {
-            if (seeded) throw Error(GBSA_ERR_DEVICE_STATUS, "query arena overflow");
-            grow(m.q, m.q_cap, h.q_used, sizeof(Query));
-            m.qaux.release();
-            m.qaux.resize(4 * m.q_cap);
-            m.qpos.release();
-            m.qpos.resize(8 * m.q_cap);
-            retry = true;
-        }
-        if (h.status & kStatusHitOverflow) {
-            grow(m.hits, m.hit_cap, h.hit_used, sizeof(HitRec));
-            retry = true;
-        }
-        if (h.status & kStatusNamOverflow) {
-            grow(m.nams, m.nam_cap, h.nam_used, sizeof(NamState));
-            retry = true;
-        }
-        if (h.status & kStatusScratchOverflow) {
-            grow(m.ovf, m.ovf_cap, h.scratch_used, 1);
-            retry = true;
-        }
-        if (retry) continue;
-        m.alg_bytes = h.alg_bytes;
-        m.alg_sectors = h.alg_sectors;
-        m.last = h;
-        // per-read NAM counts → offsets
-        uint64_t* cnt = m.cnt.as<uint64_t>();
-        uint64_t* off = m.out_off.as<uint64_t>();
-        launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st);
-        scan_exclusive_u64(cnt, off, n, off + n, ws, st);
-        uint64_t total = 0;
-        GBSA_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, st));
-        GBSA_CUDA(cudaStreamSynchronize(st));
-        return total;
+        if (check_batch(m, seeded)) return batch_total(m);
     }
     throw Error(GBSA_ERR_DEVICE_STATUS, "work areas kept overflowing");
+}
+
+// Chunks of a pipelined host call: `chunks` full chunks of at least 2^17 reads, with
+// the first one cut in half (the GPU waits for its reads alone, and the half chunk ends
+// early, so that the following chunks run staggered: one in its NAM phase beside the
+// next one's seeding) and the last full chunk cut into two quarters (the results of
+// the last chunk are copied out after all work ends).  Returns the chunk starts with
+// n_reads at the end.
+static std::vector<uint32_t> plan_chunks(uint32_t n_reads, uint32_t chunks, uint32_t max_reads) {
+    constexpr uint32_t kMinChunk = 1u << 17;
+    const uint32_t c = std::max<uint32_t>(1, std::min<uint32_t>(chunks, n_reads / kMinChunk));
+    const uint32_t full = std::min((n_reads + c - 1) / c, max_reads);
+    std::vector<uint32_t> sizes;
+    if (c >= 2 && full >= 2 * kMinChunk) {
+        const uint32_t head = full / 2, quarter = full / 4;
+        uint32_t mid = n_reads - head - 2 * quarter;
+        sizes.push_back(head);
+        while (mid) {
+            const uint32_t x = std::min(full, mid);
+            sizes.push_back(x);
+            mid -= x;
+        }
+        sizes.push_back(quarter);
+        sizes.push_back(quarter);
+    } else {
+        for (uint32_t b = 0; b < n_reads; b += full) sizes.push_back(std::min(full, n_reads - b));
+    }
+    std::vector<uint32_t> starts{0};
+    for (uint32_t x : sizes)
+        if (x) starts.push_back(starts.back() + x);
+    return starts;
 }
 
 }  // namespace gbsa
@@ -640,36 +725,20 @@ int gbsa_get_count(const gbsa_index* idx, const uint64_t* positions, uint64_t n,
     });
 }
 
-// Copies n reads (host) into one contiguous pinned staging area and then to the device.
-// Host staging buffers and device inputs of one slot of the host entry points.
-struct InSlot {
-    DeviceBuffer* seqs;
-    DeviceBuffer* offs;
-    DeviceBuffer* lens;
-    PinnedBuffer* meta;
-    PinnedBuffer* gather;
-};
-
-static InSlot in_slot(gbsa_mapper& m, int s) {
-    if (s == 0) return InSlot{&m.seqs, &m.offs, &m.lens, &m.h_meta, &m.h_seqs};
-    return InSlot{&m.seqs1, &m.offs1, &m.lens1, &m.h_meta1, &m.h_seqs1};
-}
-
-// Copies n reads to the device inputs of a slot.  Reads usually lie back to back:
+// Copies n reads (host) to the mapper's device inputs.  Reads usually lie back to back:
 // the span from the first read's start to the last read's end is copied in one
 // transfer and the offsets are rebased to it (in parallel, checking that every read
 // lies inside the span); otherwise the reads are gathered into pinned staging first.
 static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
-                            uint32_t n, cudaStream_t st, int slot = 0) {
-    const InSlot in = in_slot(m, slot);
+                            uint32_t n, cudaStream_t st) {
     const uint64_t lo = n ? offsets[0] : 0;
     const uint64_t hi = n ? offsets[n - 1] + lengths[n - 1] : 0;
     const bool span_ok = hi >= lo;
     const uint64_t span = span_ok ? hi - lo : 0;
     std::atomic<bool> inside{span_ok};
     std::atomic<uint64_t> total{0};
-    in.meta->resize(12ull * (n + 1));
-    uint64_t* ho = in.meta->as<uint64_t>();
+    m.h_meta.resize(12ull * (n + 1));
+    uint64_t* ho = m.h_meta.as<uint64_t>();
     uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
     host_parallel_for(n, [&](size_t b, size_t e) {
         bool ok = true;
@@ -686,11 +755,11 @@ static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* of
     const bool direct = inside.load() && span <= 2 * total.load() + (1u << 20);   // no large gaps
     const uint64_t bases = direct ? span : total.load();
     mapper_reserve(m, n, bases);
-    in.seqs->resize(bases + 64);
-    in.offs->resize(8ull * (n + 1));
-    in.lens->resize(4ull * (n + 1));
+    m.seqs.resize(bases + 64);
+    m.offs.resize(8ull * (n + 1));
+    m.lens.resize(4ull * (n + 1));
     if (direct) {
-        if (span) GBSA_CUDA(cudaMemcpyAsync(in.seqs->as<void>(), seqs + lo, span, cudaMemcpyHostToDevice, st));
+        if (span) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), seqs + lo, span, cudaMemcpyHostToDevice, st));
     } else {
         // exclusive offsets of the gathered layout, then a parallel gather
         uint64_t acc = 0;
@@ -698,15 +767,15 @@ static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* of
             ho[i] = acc;
             acc += lengths[i];
         }
-        in.gather->resize(acc + 1);
-        char* hs = in.gather->as<char>();
+        m.h_seqs.resize(acc + 1);
+        char* hs = m.h_seqs.as<char>();
         host_parallel_for(n, [&](size_t b, size_t e) {
             for (size_t i = b; i < e; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
         });
-        if (acc) GBSA_CUDA(cudaMemcpyAsync(in.seqs->as<void>(), hs, acc, cudaMemcpyHostToDevice, st));
+        if (acc) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), hs, acc, cudaMemcpyHostToDevice, st));
     }
-    GBSA_CUDA(cudaMemcpyAsync(in.offs->as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
-    GBSA_CUDA(cudaMemcpyAsync(in.lens->as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
     return total.load();
 }
 
@@ -790,8 +859,16 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
         m->cfg.sort_mode = opt->sort_mode;
         m->max_reads = std::max<uint32_t>(max_reads, 1);
         m->max_bases = std::max<uint64_t>(max_bases, 1);
-        GBSA_CUDA(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
-        GBSA_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        // the mapper's own streams run the NAM phase at the highest priority, the seeding
+        // and lookup of pipelined chunks (early) at the lowest: the block scheduler then
+        // finishes the older chunk first and fills its tails with the next one's seeding
+        int lo = 0, hi = 0;
+        GBSA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        GBSA_CUDA(cudaStreamCreateWithPriority(&m->st, cudaStreamNonBlocking, hi));
+        GBSA_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, hi));
+        GBSA_CUDA(cudaStreamCreateWithPriority(&m->side_lo, cudaStreamNonBlocking, lo));
+        GBSA_CUDA(cudaStreamCreateWithPriority(&m->early, cudaStreamNonBlocking, lo));
+        GBSA_CUDA(cudaEventCreateWithFlags(&m->early_ev, cudaEventDisableTiming));
         GBSA_CUDA(cudaEventCreateWithFlags(&m->fork_ev, cudaEventDisableTiming));
         GBSA_CUDA(cudaEventCreateWithFlags(&m->join_ev, cudaEventDisableTiming));
         mapper_reserve(*m, m->max_reads, m->max_bases);
@@ -801,19 +878,25 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
 
 void gbsa_mapper_free(gbsa_mapper* m) {
     if (!m) return;
+    gbsa_mapper_free(m->twin);
     if (m->side) cudaStreamSynchronize(m->side);
     if (m->st) cudaStreamSynchronize(m->st);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
     if (m->copy_in) cudaStreamSynchronize(m->copy_in);
     if (m->copy_out) cudaStreamSynchronize(m->copy_out);
-    for (int k = 0; k < 2; ++k)
-        for (cudaEvent_t e : {m->in_ready[k], m->in_copied[k], m->in_free[k], m->out_ready[k], m->out_free[k]})
-            if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {m->in_ready, m->done_ev, m->outs[0].free, m->outs[1].free})
+        if (e) cudaEventDestroy(e);
     if (m->copy_in) cudaStreamDestroy(m->copy_in);
     if (m->copy_out) cudaStreamDestroy(m->copy_out);
     if (m->fork_ev) cudaEventDestroy(m->fork_ev);
     if (m->join_ev) cudaEventDestroy(m->join_ev);
+    for (cudaStream_t x : {m->early, m->side_lo})
+        if (x) {
+            cudaStreamSynchronize(x);
+            cudaStreamDestroy(x);
+        }
+    if (m->early_ev) cudaEventDestroy(m->early_ev);
     if (m->side) cudaStreamDestroy(m->side);
     if (m->st) cudaStreamDestroy(m->st);
     delete m;
@@ -822,76 +905,140 @@ void gbsa_mapper_free(gbsa_mapper* m) {
 int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths, uint32_t n_reads,
                    gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets, float* frac, uint8_t* rescued) {
     return guarded([&] {
-        // A large call is cut into chunks that are pipelined over two slots: the reads of
-        // chunk k+1 are copied in (copy_in stream) and the NAMs of chunk k-1 copied out
-        // (copy_out stream) while chunk k is mapped on the mapper's stream.
-        cudaStream_t st = m->st;
+        // A large call is cut into chunks that alternate between the mapper and its twin
+        // (a second set of work areas and streams), so that chunk k+1 is mapped while
+        // chunk k finishes: the tail of one chunk (the rescue chain of a few reads in
+        // repeats) runs beside the start of the next, and no host synchronisation stands
+        // between them.  A chunk's reads are copied in on the copy_in stream; its results
+        // are copied out on copy_out once the host has read its status, by which time
+        // the next chunk is already running.
         nam_offsets[0] = 0;
         if (n_reads == 0) return;
         if (!m->copy_in) {
             GBSA_CUDA(cudaStreamCreateWithFlags(&m->copy_in, cudaStreamNonBlocking));
             GBSA_CUDA(cudaStreamCreateWithFlags(&m->copy_out, cudaStreamNonBlocking));
-            for (int s = 0; s < 2; ++s) {
-                for (cudaEvent_t* e :
-                     {&m->in_ready[s], &m->in_copied[s], &m->in_free[s], &m->out_ready[s], &m->out_free[s]})
-                    GBSA_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-                GBSA_CUDA(cudaEventRecord(m->in_free[s], st));
-                GBSA_CUDA(cudaEventRecord(m->in_copied[s], m->copy_in));
-                GBSA_CUDA(cudaEventRecord(m->out_free[s], m->copy_out));
-            }
         }
-        constexpr uint32_t kMinChunk = 1u << 17;
-        const uint32_t chunks = std::max<uint32_t>(1, std::min<uint32_t>(m->pipe_chunks, n_reads / kMinChunk));
-        const uint32_t chunk = std::min((n_reads + chunks - 1) / chunks, m->max_reads);
-        const uint32_t n_chunks = (n_reads + chunk - 1) / chunk;
-        auto stage = [&](uint32_t k) {
-            const int s = (int)(k & 1);
-            const uint32_t b0 = k * chunk, n = std::min(chunk, n_reads - b0);
-            GBSA_CUDA(cudaEventSynchronize(m->in_copied[s]));               // staging of chunk k-2 sent
-            GBSA_CUDA(cudaStreamWaitEvent(m->copy_in, m->in_free[s], 0));   // chunk k-2 done with the slot
-            stage_reads(*m, seqs, offsets + b0, lengths + b0, n, m->copy_in, s);
-            GBSA_CUDA(cudaEventRecord(m->in_ready[s], m->copy_in));
-            GBSA_CUDA(cudaEventRecord(m->in_copied[s], m->copy_in));
+        const std::vector<uint32_t> starts = plan_chunks(n_reads, m->pipe_chunks, m->max_reads);
+        const uint32_t n_chunks = (uint32_t)starts.size() - 1;
+        if (n_chunks > 1 && !m->twin) {
+            gbsa_mapper* t = nullptr;
+            const int rc = gbsa_mapper_create(m->idx, &m->opt, m->max_reads, m->max_bases, &t);
+            if (rc != GBSA_OK) throw Error(rc, t_last_error);
+            m->twin = t;
+        }
+        if (m->twin) {
+            m->twin->cfg = m->cfg;
+            m->twin->opt = m->opt;
+        }
+        gbsa_mapper* part[2] = {m, n_chunks > 1 ? m->twin : m};
+        for (gbsa_mapper* b : part)
+            for (cudaEvent_t* e : {&b->done_ev, &b->in_ready, &b->outs[0].free, &b->outs[1].free})
+                if (!*e) GBSA_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        // chunk k runs on part k & 1 and leaves its results in that part's slot (k >> 1) & 1
+        auto rows = [&](uint32_t k) { return starts[k + 1] - starts[k]; };
+        auto slot_of = [&](uint32_t k) -> gbsa_mapper::OutSlot& { return part[k & 1]->outs[(k >> 1) & 1]; };
+        auto gather = [&](uint32_t k) {
+            gbsa_mapper& b = *part[k & 1];
+            gbsa_mapper::OutSlot& o = slot_of(k);
+            launch_gather_nams(rows(k), b.rec.as<ReadRec>(), b.nams.as<NamState>(), b.out_off.as<uint64_t>(),
+                               o.nams.as<gbsa_nam>(), o.frac.as<float>(), o.resc.as<uint8_t>(), b.st, o.cap);
+        };
+        // copies chunk k's reads in and queues its mapping and the gather of its results
+        // into its slot on its part's streams
+        auto enqueue = [&](uint32_t k) {
+            gbsa_mapper& b = *part[k & 1];
+            gbsa_mapper::OutSlot& o = slot_of(k);
+            const uint32_t b0 = starts[k], n = rows(k);
+            // the part's previous chunk is done (the host read its status) and the slot's
+            // previous results have been copied out
+            GBSA_CUDA(cudaEventSynchronize(b.done_ev));
+            GBSA_CUDA(cudaEventSynchronize(o.free));
+            stage_reads(b, seqs, offsets + b0, lengths + b0, n, m->copy_in);
+            GBSA_CUDA(cudaEventRecord(b.in_ready, m->copy_in));
+            const uint64_t want = (uint64_t)(b.nams_per_read * 1.25 * n) + 1024;
+            if (o.cap < want) {
+                o.nams.release();
+                o.nams.resize(sizeof(gbsa_nam) * want);
+                o.cap = want;
+            }
+            o.frac.resize(4ull * (n + 1));
+            o.resc.resize(n + 1);
+            o.off.resize(8ull * (n + 1));
+            o.off_g.resize(8ull * (n + 1));
+            GBSA_CUDA(cudaStreamWaitEvent(b.st, b.in_ready, 0));
+            enqueue_batch(b, b.seqs.as<uint8_t>(), b.offs.as<uint64_t>(), b.lens.as<uint32_t>(), n, false, b.st,
+                          b.early);
+            gather(k);
+            launch_offsets_add(b.out_off.as<uint64_t>(), o.off.as<uint64_t>(), n, 0, b.st);
+            GBSA_CUDA(cudaEventRecord(b.done_ev, b.st));
         };
         uint64_t done_nams = 0;
-        stage(0);
-        for (uint32_t k = 0; k < n_chunks; ++k) {
-            const int s = (int)(k & 1);
-            const uint32_t b0 = k * chunk, n = std::min(chunk, n_reads - b0);
-            if (k + 1 < n_chunks) stage(k + 1);
-            const InSlot in = in_slot(*m, s);
-            GBSA_CUDA(cudaStreamWaitEvent(st, m->in_ready[s], 0));
-            const uint64_t total =
-                run_pipeline(*m, in.seqs->as<uint8_t>(), in.offs->as<uint64_t>(), in.lens->as<uint32_t>(), n, false, st);
-            GBSA_CUDA(cudaEventRecord(m->in_free[s], st));
-            // output slot s is free once chunk k-2's results have been copied out
-            GBSA_CUDA(cudaEventSynchronize(m->out_free[s]));
-            DeviceBuffer& o_nams = s ? m->out_nams1 : m->out_nams;
-            DeviceBuffer& o_frac = s ? m->out_frac1 : m->out_frac;
-            DeviceBuffer& o_resc = s ? m->out_resc1 : m->out_resc;
-            DeviceBuffer& o_off = m->out_off_h[s];
-            o_nams.resize(sizeof(gbsa_nam) * (total + 1));
-            o_frac.resize(4ull * (n + 1));
-            o_resc.resize(n + 1);
-            o_off.resize(8ull * (n + 1));
-            launch_gather_nams(n, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(),
-                               o_nams.as<gbsa_nam>(), o_frac.as<float>(), o_resc.as<uint8_t>(), st);
-            launch_offsets_add(m->out_off.as<uint64_t>(), o_off.as<uint64_t>(), n + 1, done_nams, st);
-            GBSA_CUDA(cudaEventRecord(m->out_ready[s], st));
-            GBSA_CUDA(cudaStreamWaitEvent(m->copy_out, m->out_ready[s], 0));
-            GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, o_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost,
+        // waits for chunk k, reads its status and copies its results out; false when a work
+        // area overflowed (it has been grown and the chunk must run again)
+        auto finish = [&](uint32_t k) {
+            gbsa_mapper& b = *part[k & 1];
+            gbsa_mapper::OutSlot& o = slot_of(k);
+            const uint32_t b0 = starts[k], n = rows(k);
+            GBSA_CUDA(cudaEventSynchronize(b.done_ev));
+            if (!check_batch(b, false)) return false;
+            const uint64_t total = batch_total(b);
+            b.nams_per_read = std::max(b.nams_per_read, (double)total / std::max<uint32_t>(n, 1));
+            if (total > o.cap) {
+                // more NAMs than the estimate: gather again into a larger slot (the part's
+                // work areas are intact, its next chunk is not queued yet)
+                o.nams.release();
+                o.nams.resize(sizeof(gbsa_nam) * (total + 1));
+                o.cap = total + 1;
+                gather(k);
+                GBSA_CUDA(cudaEventRecord(b.done_ev, b.st));
+            }
+            GBSA_CUDA(cudaStreamWaitEvent(m->copy_out, b.done_ev, 0));
+            launch_offsets_add(o.off.as<uint64_t>(), o.off_g.as<uint64_t>(), n, done_nams, m->copy_out);
+            GBSA_CUDA(cudaMemcpyAsync(nam_offsets + b0, o.off_g.as<void>(), 8ull * n, cudaMemcpyDeviceToHost,
                                       m->copy_out));
             if (frac)
-                GBSA_CUDA(cudaMemcpyAsync(frac + b0, o_frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, m->copy_out));
+                GBSA_CUDA(cudaMemcpyAsync(frac + b0, o.frac.as<void>(), 4ull * n, cudaMemcpyDeviceToHost, m->copy_out));
             if (rescued)
-                GBSA_CUDA(cudaMemcpyAsync(rescued + b0, o_resc.as<void>(), n, cudaMemcpyDeviceToHost, m->copy_out));
+                GBSA_CUDA(cudaMemcpyAsync(rescued + b0, o.resc.as<void>(), n, cudaMemcpyDeviceToHost, m->copy_out));
             if (done_nams + total <= nam_capacity && total)
-                GBSA_CUDA(cudaMemcpyAsync(nams + done_nams, o_nams.as<void>(), sizeof(gbsa_nam) * total,
+                GBSA_CUDA(cudaMemcpyAsync(nams + done_nams, o.nams.as<void>(), sizeof(gbsa_nam) * total,
                                           cudaMemcpyDeviceToHost, m->copy_out));
-            GBSA_CUDA(cudaEventRecord(m->out_free[s], m->copy_out));
+            GBSA_CUDA(cudaEventRecord(o.free, m->copy_out));
             done_nams += total;
+            return true;
+        };
+        // on an error, the work and copies in flight end before the call returns (they
+        // write into the caller's buffers)
+        struct Drain {
+            gbsa_mapper* const* part;
+            gbsa_mapper* m;
+            bool armed = true;
+            ~Drain() {
+                if (!armed) return;
+                for (int i = 0; i < 2; ++i)
+                    for (cudaStream_t x : {part[i]->early, part[i]->side, part[i]->st}) cudaStreamSynchronize(x);
+                cudaStreamSynchronize(m->copy_in);
+                cudaStreamSynchronize(m->copy_out);
+            }
+        } drain{part, m};
+        // two chunks in flight: chunk k+1 is queued before the host waits for chunk k
+        uint32_t queued = 0, finished = 0, retries = 0;
+        while (finished < n_chunks) {
+            while (queued < n_chunks && queued < finished + 2) enqueue(queued++);
+            if (finish(finished)) {
+                ++finished;
+                continue;
+            }
+            // a work area overflowed: let everything in flight end, then run the chunk again
+            if (++retries > 8) throw Error(GBSA_ERR_DEVICE_STATUS, "work areas kept overflowing");
+            for (gbsa_mapper* b : part)
+                for (cudaStream_t x : {b->early, b->side, b->st}) GBSA_CUDA(cudaStreamSynchronize(x));
+            GBSA_CUDA(cudaStreamSynchronize(m->copy_in));
+            queued = finished;
         }
         GBSA_CUDA(cudaStreamSynchronize(m->copy_out));
+        drain.armed = false;
+        nam_offsets[n_reads] = done_nams;
         if (done_nams > nam_capacity) throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
     });
 }
@@ -1021,6 +1168,8 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
     out[6] = m->last.n_big;
     return GBSA_OK;
 }
+
+uint64_t gbsa_mapper_retries(const gbsa_mapper* m) { return m->retries + (m->twin ? m->twin->retries : 0); }
 
 int gbsa_mapper_rescue_cycles(const gbsa_mapper* m, uint64_t* out, uint32_t cap, uint32_t* n_out) {
     return guarded([&] {

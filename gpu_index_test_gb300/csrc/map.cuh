@@ -118,7 +118,7 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
                    cudaStream_t st);
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
-                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st);
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap = ~0ull);
 void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
                            gbsa_query_randstrobe* out, cudaStream_t st);
 void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st);

@@ -1252,14 +1252,17 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
     }
 }
 
+// Records at or beyond out_cap are not written (the caller sized out from an estimate
+// and gathers again when the total turns out larger).
 __global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const NamState* __restrict__ arena,
-                              const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, float* frac,
-                              uint8_t* rescued) {
+                              const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, uint64_t out_cap,
+                              float* frac, uint8_t* rescued) {
     const uint32_t lane = lane_id();
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
         const ReadRec R = rec[r];
         const uint64_t o = out_off[r];
-        for (uint32_t j = lane; j < R.n_nams; j += 32) to_gbsa_nam(arena[R.nam_off + j], (int)j, out[o + j]);
+        for (uint32_t j = lane; j < R.n_nams; j += 32)
+            if (o + j < out_cap) to_gbsa_nam(arena[R.nam_off + j], (int)j, out[o + j]);
         if (lane == 0) {
             if (frac) frac[r] = R.frac;
             if (rescued) rescued[r] = (R.flags & kReadRescue) ? 1 : 0;
@@ -1401,10 +1404,10 @@ void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr,
 }
 
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
-                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st) {
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap) {
     if (!n) return;
-    k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out, frac,
-                                                                                rescued);
+    k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out, out_cap,
+                                                                                frac, rescued);
     GBSA_LAUNCHED();
 }
 

@@ -79,6 +79,7 @@ def lib():
             "gbsa_mapper_rescue_cycles": (i32, [vp, vp, u32, vp]),
             "gbsa_mapper_nam_cycles": (i32, [vp, vp, u32, vp]),
             "gbsa_mapper_set_pipeline": (i32, [vp, u32]),
+            "gbsa_mapper_retries": (u64, [vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -267,6 +268,10 @@ class Mapper:
         lib().gbsa_mapper_last_counts(self.h, a.ctypes.data)
         return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes", "warp_nam_reads"),
                         (int(x) for x in a)))
+
+    def retries(self):
+        """Batches run again after a work area grew, since the mapper was created."""
+        return int(lib().gbsa_mapper_retries(self.h))
 
     def rescue_cycles(self, cap=1 << 24):
         """Per rescued read: cycles (total, plan, merge, sort), hit bound, NAMs,

@@ -237,9 +237,11 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
                    uint32_t rescue_cutoff, gbsa_nam* nams, uint64_t nam_capacity,
                    uint64_t* nam_offsets, float* frac);
 
-/* gbsa_map_reads cuts a call of at least 2 x 131072 reads into up to `chunks`
- * chunks (default 4) and overlaps the transfers of one chunk with the mapping of the
- * next; 1 turns the overlap off.  No reference counterpart. */
+/* gbsa_map_reads cuts a call of at least 2 x 131072 reads into up to `chunks` full
+ * chunks (default 2; the first cut in half and, for chunks of 262144 reads or more,
+ * the last into two quarters) that alternate between the mapper's work areas and a
+ * second set, and overlaps the transfers of one chunk with the mapping of the next;
+ * 1 maps the call as one batch.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
 
 /* ---- input staging ----------------------------------------------------------- */
@@ -326,6 +328,10 @@ int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
  * [5] overflow scratch bytes, [6] reads merged by the warp-cooperative NAM kernel.
  * out must hold 7 values.  No reference counterpart. */
 int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
+/* Batches this mapper ran again because a work area (queries, hits, NAMs, overflow
+ * scratch) was too small and has grown, since it was created.  No reference
+ * counterpart. */
+uint64_t gbsa_mapper_retries(const gbsa_mapper* m);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the
  * merge and of the sort (the block sort, for reads with many NAMs), then the hit

@@ -283,6 +283,60 @@ def test_pipelined_map_reads_matches_single_batch():
     assert (x[1] == y[1]).all() and nams_equal(x[0], y[0])
 
 
+def _str_reads(g, n, seed, read_len=150):
+    """n reads of read_len bases that start inside short tandem repeats of the genome:
+    positions where the sequence repeats itself at a shift of 2-6 bases for at least
+    100 bases."""
+    seq = g.seq
+    inside = np.zeros(len(seq), bool)
+    for u in range(2, 7):
+        c = np.concatenate([[0], np.cumsum(seq[u:] == seq[:-u])])
+        ok = (c[100:] - c[:-100]) == 100
+        inside[: len(ok)] |= ok
+    starts = np.flatnonzero(inside[: len(seq) - read_len])
+    pick = np.random.default_rng(seed).choice(starts, n)
+    rs = np.ascontiguousarray(seq[pick[:, None] + np.arange(read_len)].ravel())
+    return synth.Reads(rs, np.arange(n, dtype=np.uint64) * read_len, np.full(n, read_len, np.uint32))
+
+
+def test_pipelined_map_reads_with_growing_work_areas():
+    """A call of 600k reads whose last 150k start inside short tandem repeats: the
+    pipelined call cuts it into a half chunk, a full one and two quarter chunks that
+    alternate between two sets of work areas; the tail chunks outgrow the work areas
+    sized for their bases, which grow while the next chunk is in flight, and the chunks
+    run again.  Results equal one batch's and the oracle's."""
+    import dataclasses
+    gp = dataclasses.replace(synth.genome_params("C2", scale=0.01, seed=63), str_frac=0.05)
+    g = synth.make_genome(gp)
+    normal = synth.make_reads(g, synth.read_params("C2", n_units=225_000, seed=64))
+    rep = _str_reads(g, 600_000 - normal.n, seed=65)
+    reads = synth.Reads(np.concatenate([normal.seq, rep.seq]),
+                        np.concatenate([normal.offsets, rep.offsets + np.uint64(len(normal.seq))]),
+                        np.concatenate([normal.lengths, rep.lengths]))
+    assert reads.n == 600_000 and rep.n >= 140_000
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    opt = abi.map_options(rescue_level=2)
+    m = native.Mapper(idx, opt)
+    m.set_pipeline(2)
+    x = m.map_reads(reads)
+    assert m.retries() > 0
+    one = native.Mapper(idx, opt)
+    one.set_pipeline(1)
+    y = one.map_reads(reads)
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+    assert nams_equal(x[0], y[0])
+    # a second call reuses the grown work areas
+    r0 = m.retries()
+    z = m.map_reads(reads)
+    assert m.retries() == r0 and (z[1] == y[1]).all() and nams_equal(z[0], y[0])
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    sub = reads.subset(np.arange(0, reads.n, 211))
+    w = o.map_reads(sub, opt, n_threads=8)
+    v = m.map_reads(sub)
+    assert (v[1] == w[1]).all() and (v[2] == w[2]).all() and nams_equal(v[0], w[0])
+
+
 def test_sector_count_and_gather_bench():
     """The lookup's sector form lies between one sector per query (the bucket bounds)
     and one per 16 B counted plus two per query; the gather benchmark reports a
