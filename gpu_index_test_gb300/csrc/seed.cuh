@@ -40,19 +40,48 @@ struct WinInfo {
 // nwords = ceil(L/32) + 2 words to each array.  Each lane codes 4 consecutive bases
 // per round of 128; 8 lanes then make a word with three xor-shuffles.
 // Returns whether the read holds an N (any base that is not A/C/G/T/U).
+//
+// A lane reads its 4 bases as one 32-bit word (two aligned loads and a funnel shift
+// when the read starts off a 4-byte boundary; only words that hold a base of the
+// read are loaded) and codes them at once: ((b >> 1) ^ (b >> 2)) & 3 is the 2-bit
+// code of A, C, G and T in either case, and a byte permute of "ACGT" by those codes
+// gives back the upper-case bases, so a word holding only A/C/G/T (either case)
+// is recognised with one compare.  Any other word (U, N, raw codes 0-3, other
+// bytes) takes the per-base path of nt4.
 __device__ __forceinline__ bool warp_pack_read(const uint8_t* seq, uint32_t L, uint64_t* packed, uint32_t* nmask) {
     const uint32_t lane = lane_id();
     const uint32_t nw = (L + 31) / 32 + 2;
     const uint32_t sub = lane & 7;   // position of the lane's 4 bases within the word
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(seq);
+    const uint32_t mis = (uint32_t)(a0 & 3);
+    const uint32_t* words = reinterpret_cast<const uint32_t*>(a0 - mis);
     bool has_n = false;
     for (uint32_t b0 = 0; b0 < nw * 32; b0 += 128) {
-        uint32_t code8 = 0, nbits = 0;
+        const uint32_t p0 = b0 + 4 * lane;   // the lane's first base
+        uint32_t code8 = 0, nbits = 0xFu;
+        if (p0 < L) {
+            const uint32_t wi = (p0 + mis) >> 2;   // aligned word holding base p0
+            const uint32_t lo = words[wi];
+            const uint32_t hi = (mis != 0 && (wi + 1) * 4 - mis < L) ? words[wi + 1] : 0u;
+            const uint32_t w = __funnelshift_r(lo, hi, 8 * mis);   // base p0 in the low byte
+            const uint32_t c4 = ((w >> 1) ^ (w >> 2)) & 0x03030303u;
+            const uint32_t sel = (c4 & 3u) | ((c4 >> 4) & 0x30u) | ((c4 >> 8) & 0x300u) | ((c4 >> 12) & 0x3000u);
+            const uint32_t nv = min(L - p0, 4u);   // bases of the read among the 4
+            const uint32_t vmask = nv == 4 ? 0xFFFFFFFFu : (1u << (8 * nv)) - 1;
+            if ((((w & 0xDFDFDFDFu) ^ __byte_perm(0x54474341u, 0u, sel)) & vmask) == 0) {
+                code8 = ((sel & 3u) << 6) | (((sel >> 4) & 3u) << 4) | (((sel >> 8) & 3u) << 2) | ((sel >> 12) & 3u);
+                code8 &= (0xFF00u >> (2 * nv)) & 0xFFu;   // bases beyond the read pack as 0
+                nbits = 0xFu & ~((1u << nv) - 1);
+            } else {
+                nbits = 0;
 #pragma unroll
-        for (uint32_t u = 0; u < 4; ++u) {
-            const uint32_t p = b0 + 4 * lane + u;
-            const uint32_t c = p < L ? nt4(seq[p]) : 4u;
-            code8 = (code8 << 2) | (c & 3u);   // an N packs as 0
-            nbits |= (c == 4u ? 1u : 0u) << u;
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const uint32_t p = p0 + u;
+                    const uint32_t c = p < L ? nt4(seq[p]) : 4u;
+                    code8 = (code8 << 2) | (c & 3u);   // an N packs as 0
+                    nbits |= (c == 4u ? 1u : 0u) << u;
+                }
+            }
         }
         uint64_t v = (uint64_t)code8 << (8 * (7 - sub));
         uint32_t nm = nbits << (4 * sub);
@@ -378,19 +407,22 @@ __device__ __forceinline__ uint32_t n_query_per_dir(const DevParams& P, uint32_t
 }
 
 // Writes the 2*nq query randstrobes of a read (forward, then reverse complement).
+// The two orientations take passes of their own: a pass that mixed them would run
+// both selection loops one after the other.
 __device__ __forceinline__ void warp_write_queries(const DevParams& P, const uint64_t* sh, const uint32_t* sp,
                                                    uint32_t n, uint32_t L, uint32_t nq, Query* out) {
     const uint32_t lane = lane_id();
-    for (uint32_t j = lane; j < 2 * nq; j += 32) {
+    for (uint32_t j = lane; j < nq; j += 32) {
         uint64_t h;
         uint32_t s1, s2;
-        if (j < nq) randstrobe_fwd(P, sh, sp, n, j, h, s1, s2);
-        else randstrobe_rev(P, sh, sp, n, L, j - nq, h, s1, s2);
-        Query q;
-        q.hash = h;
-        q.start = s1;
-        q.end = s2 + (uint32_t)P.k;
-        out[j] = q;
+        randstrobe_fwd(P, sh, sp, n, j, h, s1, s2);
+        out[j] = Query{h, s1, s2 + (uint32_t)P.k};
+    }
+    for (uint32_t j = lane; j < nq; j += 32) {
+        uint64_t h;
+        uint32_t s1, s2;
+        randstrobe_rev(P, sh, sp, n, L, j, h, s1, s2);
+        out[nq + j] = Query{h, s1, s2 + (uint32_t)P.k};
     }
 }
 

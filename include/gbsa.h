@@ -238,10 +238,10 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
                    uint64_t* nam_offsets, float* frac);
 
 /* gbsa_map_reads cuts a call of at least 2 x 131072 reads into up to `chunks` full
- * chunks (default 2; the first cut in half and, for chunks of 262144 reads or more,
- * the last into two quarters) that alternate between the mapper's work areas and a
- * second set, and overlaps the transfers of one chunk with the mapping of the next;
- * 1 maps the call as one batch.  No reference counterpart. */
+ * chunks (default 2; when a full chunk has 262144 reads or more, the first is cut in
+ * half and the last into two quarters) that alternate between the mapper's work areas
+ * and a second set, and overlaps the transfers of one chunk with the mapping of the
+ * next; 1 maps the call as one batch.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
 
 /* ---- input staging ----------------------------------------------------------- */

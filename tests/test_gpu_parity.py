@@ -232,6 +232,58 @@ def test_tandem_repeat_rescue_against_oracle(mode):
     assert nams_equal(x[0], y[0])
 
 
+def test_read_bytes_and_alignments_against_oracle():
+    """Reads of every start alignment (mod 4) and of lengths around the 4-base packing
+    units, with lowercase bases, U/u, N/n, raw codes 0-3 and other bytes mixed in:
+    query randstrobes read by read and NAMs equal the oracle's."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.003, seed=71))
+    base = synth.make_reads(g, synth.read_params("C2", n_units=1500, seed=72))
+    rng = np.random.default_rng(73)
+    p = native.params_from_read_length(150)
+    lens_choice = [p.k - 1, p.k, 31, 32, 33, 63, 64, 65, 127, 129, 150]
+    parts, offs, lens = [], [], []
+    pos = 0
+    for r in range(base.n):
+        o = int(base.offsets[r])
+        L = min(int(base.lengths[r]), lens_choice[r % len(lens_choice)])
+        x = base.seq[o:o + L].copy()
+        kind = r % 6
+        if kind == 1:    # lowercase runs
+            m = rng.random(L) < 0.4
+            x[m] = x[m] | 0x20
+        elif kind == 2:  # U / u for T
+            m = (x == ord("T")) & (rng.random(L) < 0.5)
+            x[m] = np.where(rng.random(m.sum()) < 0.5, ord("U"), ord("u"))
+        elif kind == 3:  # N / n
+            m = rng.random(L) < 0.03
+            x[m] = np.where(rng.random(m.sum()) < 0.5, ord("N"), ord("n"))
+        elif kind == 4:  # raw codes and other bytes
+            m = rng.random(L) < 0.02
+            x[m] = rng.choice(np.array([0, 1, 2, 3, ord("R"), ord("."), 0xFF, 0x20, 0x61 ^ 0x80], np.uint8), m.sum())
+        gap = int(rng.integers(0, 4))
+        parts.append(np.full(gap, ord("N"), np.uint8))
+        pos += gap
+        parts.append(x)
+        offs.append(pos)
+        lens.append(L)
+        pos += L
+    reads = synth.Reads(np.concatenate(parts), np.array(offs, np.uint64), np.array(lens, np.uint32))
+    assert len(set(np.array(offs) % 4)) == 4
+    q, qo = native.randstrobes_query(p, reads)
+    for r in range(reads.n):
+        o0 = int(reads.offsets[r])
+        ref = oracle_py.randstrobes_query(p, bytes(reads.seq[o0:o0 + int(reads.lengths[r])]))
+        got = q[int(qo[r]):int(qo[r + 1])]
+        assert len(got) == len(ref), r
+        for f in ("hash", "start", "end", "is_reverse"):
+            assert (got[f] == ref[f]).all(), (r, f)
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    x = native.Mapper(idx).map_reads(reads)
+    y = o.map_reads(reads, n_threads=8)
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and nams_equal(x[0], y[0])
+
+
 def test_read_layouts_give_the_same_nams():
     """map_reads copies the span of the read buffer when the reads lie inside it (in
     any order) and gathers them otherwise; both layouts give the NAMs of the
