@@ -342,7 +342,26 @@ struct LaneOpen {
         nh[o][t] = n.n_hits;
         ref[o][t] = n.ref_rc;
     }
+    // After its merge a lane's 8 * kLaneOpen words (every 32 * kLaneWarps-th word of
+    // the struct, from its thread index on) are free: they hold the sort entries
+    // (first key word, NAM index; three words each) of up to kEntries of its NAMs.
+    // Only the lane touches them, and the lanes of a warp hit 32 different banks.
+    static constexpr uint32_t kEntries = 8 * kLaneOpen / 3;
+    static constexpr uint32_t kStride = 32 * kLaneWarps;
+    __device__ uint32_t* words() { return reinterpret_cast<uint32_t*>(this); }
+    __device__ uint64_t key(uint32_t e, uint32_t t) {
+        const uint32_t* w = words() + 3 * e * kStride + t;
+        return ((uint64_t)w[kStride] << 32) | w[0];
+    }
+    __device__ uint32_t index(uint32_t e, uint32_t t) { return words()[(3 * e + 2) * kStride + t]; }
+    __device__ void set_entry(uint32_t e, uint32_t t, uint64_t k, uint32_t i) {
+        uint32_t* w = words() + 3 * e * kStride + t;
+        w[0] = (uint32_t)k;
+        w[kStride] = (uint32_t)(k >> 32);
+        w[2 * kStride] = i;
+    }
 };
+static_assert(sizeof(LaneOpen) == 8 * kLaneOpen * 32 * kLaneWarps * 4, "LaneOpen is 8 word arrays");
 
 // find_nams merge with one lane per read, for reads with at most kLaneMaxHits hits
 // whose open-NAM list stays within kLaneOpen (the common case: one locus chain plus
@@ -419,8 +438,10 @@ __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint
         ReadRec& R = rec[r];
         const uint32_t flags = R.flags;
         const uint32_t H = R.n_hits;
-        const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)H);
-        if (noff + H > A.nam_cap) {
+        // 2H slots: the NAMs as they close, then (for the sort through shared memory)
+        // the same NAMs in order
+        const uint64_t noff = atomicAdd(&ctr->nam_used, 2ull * H);
+        if (noff + 2ull * H > A.nam_cap) {
             R.flags = flags | kReadFailed;
             atomicOr(&ctr->status, kStatusNamOverflow);
             continue;
@@ -481,20 +502,55 @@ __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint
             continue;
         }
         for (uint32_t o = 0; o < n_open; ++o) out[n_closed++] = S.get(o, t);
-        // insertion sort by the NAM order
-        for (uint32_t i = 1; i < n_closed; ++i) {
-            const NamState x = out[i];
-            const NamKey kx = nam_key(x, 0, C.sort_mode);
-            uint32_t j = i;
-            while (j > 0) {
-                const NamState y = out[j - 1];
-                if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
-                out[j] = y;
-                --j;
+        // stable insertion sort by the NAM order
+        uint64_t first = noff;
+        if (n_closed <= LaneOpen::kEntries) {
+            // on (first key word, index) entries in shared memory, full keys only on a
+            // tie of the first word; then one pass writes the NAMs in order behind the
+            // unsorted ones (no NAM moves through memory while sorting)
+            for (uint32_t i = 0; i < n_closed; ++i) S.set_entry(i, t, nam_key(out[i], 0, C.sort_mode).k1, i);
+            for (uint32_t i = 1; i < n_closed; ++i) {
+                const uint64_t kx = S.key(i, t);
+                if (kx > S.key(i - 1, t)) continue;   // already in place
+                const uint32_t ix = S.index(i, t);
+                NamKey fx;
+                bool have_fx = false;
+                uint32_t j = i;
+                while (j > 0) {
+                    const uint64_t ky = S.key(j - 1, t);
+                    const uint32_t iy = S.index(j - 1, t);
+                    bool less = kx < ky;
+                    if (kx == ky) {
+                        if (!have_fx) {
+                            fx = nam_key(out[ix], 0, C.sort_mode);
+                            have_fx = true;
+                        }
+                        less = nam_key3_less(fx, nam_key(out[iy], 0, C.sort_mode));
+                    }
+                    if (!less) break;
+                    S.set_entry(j, t, ky, iy);
+                    --j;
+                }
+                S.set_entry(j, t, kx, ix);
             }
-            out[j] = x;
+            NamState* sorted = out + H;
+            for (uint32_t i = 0; i < n_closed; ++i) sorted[i] = out[S.index(i, t)];
+            first = noff + H;
+        } else {
+            for (uint32_t i = 1; i < n_closed; ++i) {
+                const NamState x = out[i];
+                const NamKey kx = nam_key(x, 0, C.sort_mode);
+                uint32_t j = i;
+                while (j > 0) {
+                    const NamState y = out[j - 1];
+                    if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
+                    out[j] = y;
+                    --j;
+                }
+                out[j] = x;
+            }
         }
-        R.nam_off = noff;
+        R.nam_off = first;
         R.n_nams = n_closed;
     }
 }
