@@ -384,13 +384,14 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
         if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[i], st));
     };
     mark(0);
-    if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+    if (!seeded) launch_seed_lookup(m.idx->dp, I, C, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(1);
     if (!seeded)
         launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr, m.long_scratch.as<uint8_t>(),
                          m.long_warps, st);
     mark(2);
-    launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    if (seeded) launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    else launch_lookup_long(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
     launch_bucket_reads(n, m.rec.as<ReadRec>(), A, ctr, st);
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, early));

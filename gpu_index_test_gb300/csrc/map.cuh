@@ -108,6 +108,13 @@ void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, 
 void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens,
                       ReadRec* rec, Arenas A, Counters* ctr, uint8_t* long_scratch, uint32_t long_warps,
                       cudaStream_t st);
+// Main path: seeding and lookup fused (a warp per read); reads too long for the
+// shared-memory buffers are seeded by launch_seed_long and looked up by launch_lookup_long.
+void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig& C, const uint8_t* seqs,
+                        const uint64_t* offs, const uint32_t* lens, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                        cudaStream_t st);
+void launch_lookup_long(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                        cudaStream_t st);
 void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
 void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,

@@ -149,119 +149,186 @@ constexpr uint32_t kRescueHeavyHits = 2000;   // estimated merge hits of a heavy
 
 // kCount: also count the reference's algorithmic bytes and gather sectors (a
 // separate instance, so that the counting code costs the mapping kernel nothing).
+// find / is_filtered / walk for the queries of read r (warp): per-query index
+// positions and hit counts, the nonrepetitive fraction and rescue decision, and for a
+// read that is not rescued its hits (query order, then run order) in the hit arena.
+// The query loop of find_nams (step2/nam.cu:748-790).
+template <bool kCount>
+__device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig& C, uint32_t r, ReadRec* __restrict__ rec,
+                                            const Arenas& A, Counters* ctr) {
+    const uint32_t lane = lane_id();
+    ReadRec& R = rec[r];
+    if (R.flags & kReadFailed) return;
+    const uint32_t nq = R.nq, nq2 = R.nq2;
+    Query* Q = A.q + R.q_off;
+    uint32_t* aux = A.q_aux + R.q_off;
+    uint32_t tot = 0, good = 0;
+    uint64_t bytes = 0, sectors = 0;
+    for (uint32_t i = lane; i < nq2; i += 32) {
+        const Query q = Q[i];
+        uint32_t ex = 0;
+        uint64_t bend = 0;
+        const uint64_t pos = index_find(I, q.hash, &ex, &bend);
+        uint32_t nh = 0, run = 0;
+        bytes += 16 + 16ull * ex;
+        if (pos != kNotFound) {
+            ++tot;
+            bytes += 16;   // the reference reads hash[pos + filter_cutoff]
+            if (!index_is_filtered_in(I, pos, q.hash, bend)) {
+                ++good;
+                nh = walk_hit_run(I, (int)q.start, (int)q.end, pos, [&](uint32_t, int, int) {}, &run);
+                bytes += 16ull * run;
+            }
+        }
+        if (kCount) sectors += lookup_sectors(I, q.hash, ex, pos, run);
+        A.q_pos[R.q_off + i] = pos;
+        aux[i] = nh;
+    }
+    tot = warp_sum(tot);
+    good = warp_sum(good);
+    if (kCount) {
+        bytes = warp_sum(bytes);
+        sectors = warp_sum(sectors);
+        if (lane == 0) {
+            atomicAdd(&ctr->alg_bytes, (unsigned long long)bytes);
+            atomicAdd(&ctr->alg_sectors, (unsigned long long)sectors);
+        }
+    }
+    // nonrepetitive_fraction (step2/nam.cu:892) and the rescue trigger: a double
+    // comparison of the float ratio with 0.7, or no hits (step2/main.cu:3211)
+    const float frac = tot > 0 ? ((float)good) / ((float)tot) : 1.0f;
+    const bool rescue = C.force_rescue || (C.rescue_level > 1 && (good == 0 || (double)frac < 0.7));
+    if (lane == 0) {
+        R.frac = frac;
+        R.n_found = tot;
+    }
+    if (rescue) {
+        // Reads inside short tandem repeats merge thousands of hits: their seeds'
+        // runs (up to the count cap) estimate the merge's hits; reads above
+        // kRescueHeavyHits go to the heavy end of the list, whose warps start first.
+        uint32_t w = 0;
+        if (good < tot) {
+            for (uint32_t i = lane; i < nq2; i += 32) {
+                const uint64_t pos = A.q_pos[R.q_off + i];
+                if (pos == kNotFound) continue;
+                const uint32_t c = index_get_count(I, pos);
+                w += c <= C.count_cap ? c : 0u;
+            }
+            w = warp_sum(w);
+        }
+        const bool heavy = w >= kRescueHeavyHits;
+        if (lane == 0) {
+            R.flags |= kReadRescue;
+            if (heavy) A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
+            else A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
+            R.n_hits = 0;
+        }
+        return;
+    }
+    // hit offsets in generation order (query order, then run order)
+    uint64_t running = 0;
+    for (uint32_t base = 0; base < nq2; base += 32) {
+        const uint32_t i = base + lane;
+        const uint32_t v = i < nq2 ? aux[i] : 0;
+        const uint32_t inc = warp_inclusive_sum(v);
+        if (i < nq2) aux[i] = (uint32_t)running + inc - v;
+        running += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    }
+    __syncwarp();
+    const uint64_t H = running;
+    const uint64_t hoff = warp_bump(&ctr->hit_used, H);
+    if (hoff + H > A.hit_cap) {
+        warp_fail(R, ctr, kStatusHitOverflow);
+        return;
+    }
+    const uint64_t* qp = A.q_pos + R.q_off;
+    for (uint32_t i = lane; i < nq2; i += 32) {
+        // queries that emitted hits in the first pass (found and not filtered)
+        const uint32_t next = i + 1 < nq2 ? aux[i + 1] : (uint32_t)H;
+        if (next == aux[i]) continue;
+        const uint64_t pos = qp[i];
+        const uint32_t dir = i >= nq ? 1u : 0u;
+        HitRec* out = A.hits + hoff + aux[i];
+        uint32_t k = 0;
+        const int qs = (int)Q[i].start, qe = (int)Q[i].end;
+        walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
+            HitRec h;
+            h.ref_rc = (dir << 31) | ref;
+            h.qs = qs;
+            h.qe = qe;
+            h.rs = rs;
+            h.re = re;
+            out[k++] = h;
+        });
+    }
+    if (lane == 0) {
+        R.hit_off = hoff;
+        R.n_hits = (uint32_t)H;
+    }
+}
+
 template <bool kCount>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
                                                                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
-    const uint32_t lane = lane_id();
+    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) lookup_read<kCount>(I, C, r, rec, A, ctr);
+}
+
+// The lookup of the reads seeded by k_seed_long (the long list).
+template <bool kCount>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup_long(IndexView I, MapConfig C,
+                                                                      ReadRec* __restrict__ rec, Arenas A,
+                                                                      Counters* ctr) {
+    const uint32_t n_long = *(volatile unsigned int*)&ctr->n_long;
+    for (uint32_t t = warp_global_id(); t < n_long; t += warp_count())
+        lookup_read<kCount>(I, C, A.long_list[t], rec, A, ctr);
+}
+
+// Seeding and lookup of a read by one warp (the main path): randstrobes_query, then
+// the query loop of find_nams on the queries just written.  Seeding is bound by
+// integer issue and the lookup by the latency of random index reads, so the warps of
+// an SM interleave the two: while some wait on gathers, others hash.  Reads that do
+// not fit the shared-memory buffers go to the long list (k_seed_long, then
+// k_lookup_long).
+// 6 blocks of 8 warps per SM (48 warps: the lookup's gathers need the warps in flight;
+// 40 registers) and per-warp buffers for reads up to 512 bases and 160 syncmers (21 KB
+// per block, leaving the rest of the SM's unified L1 to cache index entries); longer
+// reads take the long path.
+constexpr int kFusedBlocksPerSm = 6;
+constexpr uint32_t kFusedMaxLen = 512;
+constexpr uint32_t kFusedSyncmers = 160;
+
+template <bool kCount>
+__global__ void __launch_bounds__(32 * kSeedWarps, kFusedBlocksPerSm)
+    k_seed_lookup(DevParams P, IndexView I, MapConfig C, const uint8_t* __restrict__ seqs,
+                  const uint64_t* __restrict__ offs, const uint32_t* __restrict__ lens, uint32_t n,
+                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    __shared__ uint64_t s_pk[kSeedWarps][kFusedMaxLen / 32 + 4];
+    __shared__ uint32_t s_nm[kSeedWarps][kFusedMaxLen / 32 + 4];
+    __shared__ uint64_t s_hb[kSeedWarps][64];
+    __shared__ uint64_t s_sh[kSeedWarps][kFusedSyncmers];
+    __shared__ uint32_t s_sp[kSeedWarps][kFusedSyncmers];
+    const uint32_t w = threadIdx.x >> 5;
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+        const uint32_t L = lens[r];
         ReadRec& R = rec[r];
-        if (R.flags & kReadFailed) continue;
-        const uint32_t nq = R.nq, nq2 = R.nq2;
-        Query* Q = A.q + R.q_off;
-        uint32_t* aux = A.q_aux + R.q_off;
-        uint32_t tot = 0, good = 0;
-        uint64_t bytes = 0, sectors = 0;
-        for (uint32_t i = lane; i < nq2; i += 32) {
-            const Query q = Q[i];
-            uint32_t ex = 0;
-            uint64_t bend = 0;
-            const uint64_t pos = index_find(I, q.hash, &ex, &bend);
-            uint32_t nh = 0, run = 0;
-            bytes += 16 + 16ull * ex;
-            if (pos != kNotFound) {
-                ++tot;
-                bytes += 16;   // the reference reads hash[pos + filter_cutoff]
-                if (!index_is_filtered_in(I, pos, q.hash, bend)) {
-                    ++good;
-                    nh = walk_hit_run(I, (int)q.start, (int)q.end, pos, [&](uint32_t, int, int) {}, &run);
-                    bytes += 16ull * run;
-                }
-            }
-            if (kCount) sectors += lookup_sectors(I, q.hash, ex, pos, run);
-            A.q_pos[R.q_off + i] = pos;
-            aux[i] = nh;
+        if (L > GBSA_MAX_READ_LEN) {
+            warp_fail(R, ctr, kStatusReadTooLong);
+            continue;
         }
-        tot = warp_sum(tot);
-        good = warp_sum(good);
-        if (kCount) {
-            bytes = warp_sum(bytes);
-            sectors = warp_sum(sectors);
-            if (lane == 0) {
-                atomicAdd(&ctr->alg_bytes, (unsigned long long)bytes);
-                atomicAdd(&ctr->alg_sectors, (unsigned long long)sectors);
-            }
-        }
-        // nonrepetitive_fraction (step2/nam.cu:892) and the rescue trigger: a double
-        // comparison of the float ratio with 0.7, or no hits (step2/main.cu:3211)
-        const float frac = tot > 0 ? ((float)good) / ((float)tot) : 1.0f;
-        const bool rescue = C.force_rescue || (C.rescue_level > 1 && (good == 0 || (double)frac < 0.7));
-        if (lane == 0) {
-            R.frac = frac;
-            R.n_found = tot;
-        }
-        if (rescue) {
-            // Reads inside short tandem repeats merge thousands of hits: their seeds'
-            // runs (up to the count cap) estimate the merge's hits; reads above
-            // kRescueHeavyHits go to the heavy end of the list, whose warps start first.
-            uint32_t w = 0;
-            if (good < tot) {
-                for (uint32_t i = lane; i < nq2; i += 32) {
-                    const uint64_t pos = A.q_pos[R.q_off + i];
-                    if (pos == kNotFound) continue;
-                    const uint32_t c = index_get_count(I, pos);
-                    w += c <= C.count_cap ? c : 0u;
-                }
-                w = warp_sum(w);
-            }
-            const bool heavy = w >= kRescueHeavyHits;
-            if (lane == 0) {
-                R.flags |= kReadRescue;
-                if (heavy) A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
-                else A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
-                R.n_hits = 0;
+        uint32_t ns = 0xFFFFFFFFu;
+        if (L <= kFusedMaxLen)
+            ns = warp_read_syncmers(P, seqs + offs[r], L, s_pk[w], s_nm[w], s_hb[w], s_sh[w], s_sp[w], kFusedSyncmers);
+        if (ns == 0xFFFFFFFFu) {
+            if (lane_id() == 0) {
+                R.flags |= kReadLong;
+                A.long_list[atomicAdd(&ctr->n_long, 1u)] = r;
             }
             continue;
         }
-        // hit offsets in generation order (query order, then run order)
-        uint64_t running = 0;
-        for (uint32_t base = 0; base < nq2; base += 32) {
-            const uint32_t i = base + lane;
-            const uint32_t v = i < nq2 ? aux[i] : 0;
-            const uint32_t inc = warp_inclusive_sum(v);
-            if (i < nq2) aux[i] = (uint32_t)running + inc - v;
-            running += __shfl_sync(0xFFFFFFFFu, inc, 31);
-        }
+        emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
         __syncwarp();
-        const uint64_t H = running;
-        const uint64_t hoff = warp_bump(&ctr->hit_used, H);
-        if (hoff + H > A.hit_cap) {
-            warp_fail(R, ctr, kStatusHitOverflow);
-            continue;
-        }
-        const uint64_t* qp = A.q_pos + R.q_off;
-        for (uint32_t i = lane; i < nq2; i += 32) {
-            // queries that emitted hits in the first pass (found and not filtered)
-            const uint32_t next = i + 1 < nq2 ? aux[i + 1] : (uint32_t)H;
-            if (next == aux[i]) continue;
-            const uint64_t pos = qp[i];
-            const uint32_t dir = i >= nq ? 1u : 0u;
-            HitRec* out = A.hits + hoff + aux[i];
-            uint32_t k = 0;
-            const int qs = (int)Q[i].start, qe = (int)Q[i].end;
-            walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
-                HitRec h;
-                h.ref_rc = (dir << 31) | ref;
-                h.qs = qs;
-                h.qe = qe;
-                h.rs = rs;
-                h.re = re;
-                out[k++] = h;
-            });
-        }
-        if (lane == 0) {
-            R.hit_off = hoff;
-            R.n_hits = (uint32_t)H;
-        }
+        lookup_read<kCount>(I, C, r, rec, A, ctr);
+        __syncwarp();
     }
 }
 
@@ -1396,6 +1463,28 @@ void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* o
                       cudaStream_t st) {
     const unsigned blocks = std::max(1u, long_warps / kWarpsPerBlock);
     k_seed_long<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(P, seqs, offs, lens, rec, A, ctr, long_scratch);
+    GBSA_LAUNCHED();
+}
+
+void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig& C, const uint8_t* seqs,
+                        const uint64_t* offs, const uint32_t* lens, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                        cudaStream_t st) {
+    if (!n) return;
+    const unsigned grid = warp_grid(n, kSeedWarps);
+    if (C.count_bytes)
+        k_seed_lookup<true><<<grid, 32 * kSeedWarps, 0, st>>>(P, I, C, seqs, offs, lens, n, rec, A, ctr);
+    else k_seed_lookup<false><<<grid, 32 * kSeedWarps, 0, st>>>(P, I, C, seqs, offs, lens, n, rec, A, ctr);
+    GBSA_LAUNCHED();
+}
+
+void launch_lookup_long(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
+                        cudaStream_t st) {
+    if (!n) return;
+    // sized for n long reads (every read, for long-read parameter sets); warps beyond
+    // the long-list count exit at once
+    const unsigned blocks = warp_grid(n, kWarpsPerBlock);
+    if (C.count_bytes) k_lookup_long<true><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
+    else k_lookup_long<false><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

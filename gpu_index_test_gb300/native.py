@@ -258,7 +258,7 @@ class Mapper:
         """32 B sectors of the lookup's gathers in the last batch (with set_count_bytes)."""
         return lib().gbsa_mapper_last_alg_sectors(self.h)
 
-    STAGES = ("seed", "seed_long", "lookup", "nams", "nams_warp", "rescue", "rescue_sort")
+    STAGES = ("seed_lookup", "seed_long", "lookup_long", "nams", "nams_warp", "rescue", "rescue_sort")
 
     def set_profile(self, on=True):
         _check(lib().gbsa_mapper_set_profile(self.h, 1 if on else 0))

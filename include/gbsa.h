@@ -316,11 +316,11 @@ uint64_t gbsa_mapper_last_alg_sectors(const gbsa_mapper* m);
  * lookup's roofline; no reference counterpart. */
 int gbsa_bench_gather(uint64_t buffer_bytes, double* sectors_per_s, double* gb_per_s);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
- * returns the last batch's milliseconds for: seeding, long-read seeding, lookup,
- * NAM merge + sort (lane per read), NAM merge + sort (warp per read), rescue,
- * sorting of the rescued reads with many NAMs.  The last two run on a second
- * stream beside the two NAM stages and are timed from the end of the lookup.  No
- * reference counterpart. */
+ * returns the last batch's milliseconds for: seeding + lookup (one kernel, a warp
+ * per read), long-read seeding, long-read lookup + read bucketing, NAM merge + sort
+ * (lane per read), NAM merge + sort (warp per read), rescue, sorting of the rescued
+ * reads with many NAMs.  The last two run on a second stream beside the two NAM
+ * stages and are timed from the end of the lookup.  No reference counterpart. */
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
 /* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
