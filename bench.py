@@ -610,16 +610,17 @@ def main():
     # roofline of the dominant kernel on the critical path (the rescue chain runs on a
     # second stream beside the NAM kernels; its stage times include that overlap)
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
-    main_stages = ("seed_lookup", "lookup_long", "nams", "nams_warp")
+    fused = m.fused_lookup()
+    main_stages = ("seed_lookup", "lookup_long", "nams", "nams_warp") if fused else ("seed", "lookup", "nams", "nams_warp")
     dom = max(main_stages, key=lambda k: stage_ms.get(k, 0.0))
     q, hits, nams_n = counts["queries"], counts["hits"], counts["nams"]
     bases = int(reads.lengths.sum())
+    seed_b = bases + 16 * q                          # ASCII bases in, query randstrobes out
+    lookup_b = alg_lookup + 16 * q + 8 * q + 20 * hits  # probes + queries in + positions + hits out
     alg = {
-        # ASCII bases in, query randstrobes out; then the lookup's probes, the queries
-        # read back, positions and hits out
-        "seed_lookup": bases + 16 * q + alg_lookup + 16 * q + 8 * q + 20 * hits,
+        "seed_lookup": seed_b + lookup_b, "lookup_long": 0,   # one kernel (indexes up to 2 GiB)
+        "seed": seed_b, "lookup": lookup_b,                   # two kernels (larger indexes)
         "seed_long": 0,
-        "lookup_long": 0,
         "nams": 20 * hits + 32 * nams_n,                 # hits in, NAM records out
         "nams_warp": 0,
         "rescue": 0,
@@ -635,10 +636,11 @@ def main():
     # distinct sector the reference's probes touch), measured on this GPU before the
     # timed region; the lookup runs inside the fused seeding + lookup kernel, so the
     # rate is taken over that kernel's whole time (a lower bound for the gathers)
-    lk_s = stage_ms.get("seed_lookup", 0.0) / 1e3
+    lk_stage = "seed_lookup" if fused else "lookup"
+    lk_s = stage_ms.get(lk_stage, 0.0) / 1e3
     gather_hbm, gather_l2 = gather_peaks
     roofline["gather"] = {
-        "kernel": "seed_lookup", "sectors_per_launch": int(sectors_lookup),
+        "kernel": lk_stage, "sectors_per_launch": int(sectors_lookup),
         "achieved": round(sectors_lookup * 32 / lk_s / 1e9, 1) if lk_s > 0 else 0.0, "unit": "GB/s",
         "peak_hbm_gather": round(gather_hbm, 1), "peak_l2_gather": round(gather_l2, 1),
         "frac": round(sectors_lookup * 32 / lk_s / 1e9 / gather_hbm, 4) if lk_s > 0 and gather_hbm > 0 else None,
@@ -666,7 +668,9 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": dict(config_of(gp, rp, reads, args), index_entries=int(info.size), index_bits=int(info.bits),
                        filter_cutoff=int(info.filter_cutoff), index_build_gpu_s=round(build_s, 3),
-                       form="seeding and lookup fused (a warp per read), then NAM kernels on two streams"),
+                       form=("seeding and lookup fused (a warp per read)" if fused else
+                             "seeding and lookup as two kernels (index over 2 GiB)")
+                       + ", then NAM kernels on two streams"),
         "e2e": {"value": round(world * n / e2e_s, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": roofline,

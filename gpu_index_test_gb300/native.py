@@ -80,6 +80,8 @@ def lib():
             "gbsa_mapper_nam_cycles": (i32, [vp, vp, u32, vp]),
             "gbsa_mapper_set_pipeline": (i32, [vp, u32]),
             "gbsa_mapper_retries": (u64, [vp]),
+            "gbsa_mapper_fused_lookup": (i32, [vp]),
+            "gbsa_mapper_set_fuse_limit": (i32, [vp, u64]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -294,10 +296,20 @@ class Mapper:
         k = min(cap // 4, n[0])
         return a[: 4 * k].reshape(-1, 4)
 
+    STAGES_UNFUSED = ("seed", "seed_long", "lookup", "nams", "nams_warp", "rescue", "rescue_sort")
+
+    def set_fuse_limit(self, index_bytes):
+        """Largest index (entry bytes) seeded and looked up in one kernel; 0: never."""
+        _check(lib().gbsa_mapper_set_fuse_limit(self.h, int(index_bytes)))
+
+    def fused_lookup(self):
+        """Whether the last batch ran seeding and lookup as one kernel."""
+        return bool(lib().gbsa_mapper_fused_lookup(self.h))
+
     def stage_ms(self):
         a = np.zeros(7, np.float32)
         lib().gbsa_mapper_stage_ms(self.h, a.ctypes.data, 7)
-        return dict(zip(self.STAGES, a.tolist()))
+        return dict(zip(self.STAGES if self.fused_lookup() else self.STAGES_UNFUSED, a.tolist()))
 
     def map_reads(self, reads, capacity=None):
         n = reads.n

@@ -317,10 +317,12 @@ uint64_t gbsa_mapper_last_alg_sectors(const gbsa_mapper* m);
 int gbsa_bench_gather(uint64_t buffer_bytes, double* sectors_per_s, double* gb_per_s);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
  * returns the last batch's milliseconds for: seeding + lookup (one kernel, a warp
- * per read), long-read seeding, long-read lookup + read bucketing, NAM merge + sort
- * (lane per read), NAM merge + sort (warp per read), rescue, sorting of the rescued
- * reads with many NAMs.  The last two run on a second stream beside the two NAM
- * stages and are timed from the end of the lookup.  No reference counterpart. */
+ * per read; seeding alone when gbsa_mapper_fused_lookup is 0), long-read seeding,
+ * long-read lookup + read bucketing (the whole lookup + bucketing when not fused),
+ * NAM merge + sort (lane per read), NAM merge + sort (warp per read), rescue,
+ * sorting of the rescued reads with many NAMs.  The last two run on a second stream
+ * beside the two NAM stages and are timed from the end of the lookup.  No reference
+ * counterpart. */
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
 /* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
@@ -332,6 +334,15 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
  * scratch) was too small and has grown, since it was created.  No reference
  * counterpart. */
 uint64_t gbsa_mapper_retries(const gbsa_mapper* m);
+/* 1 when the last batch ran seeding and lookup as one kernel (indexes of up to 2 GiB
+ * of entries), 0 when it ran them as two kernels (larger indexes); selects the
+ * meaning of the first and third gbsa_mapper_stage_ms values.  No reference
+ * counterpart. */
+int gbsa_mapper_fused_lookup(const gbsa_mapper* m);
+/* Largest index (bytes of entries, 16 per entry) whose batches run seeding and lookup
+ * as one kernel; default 2 GiB.  0 runs them as two kernels for every index.  The
+ * results are the same either way.  No reference counterpart. */
+int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the
  * merge and of the sort (the block sort, for reads with many NAMs), then the hit

@@ -284,6 +284,26 @@ def test_read_bytes_and_alignments_against_oracle():
     assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and nams_equal(x[0], y[0])
 
 
+def test_two_kernel_seeding_and_lookup_matches_fused():
+    """Indexes over 2 GiB of entries run seeding and lookup as two kernels; forced
+    here on a small index, the NAMs equal those of the fused kernel (which ran), for
+    150 bp reads and for reads over the fused kernel's 512-base buffers."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=81))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    for rp in (synth.read_params("C2", n_units=20_000, seed=82),
+               synth.ReadParams(seed=83, n_units=3000, len_min=300, len_max=900, paired_frac=0.0)):
+        reads = synth.make_reads(g, rp)
+        m = native.Mapper(idx)
+        a = m.map_reads(reads)
+        assert m.fused_lookup()
+        m.set_fuse_limit(0)
+        b = m.map_reads(reads)
+        assert not m.fused_lookup()
+        assert (a[1] == b[1]).all() and (a[2] == b[2]).all() and (a[3] == b[3]).all()
+        assert nams_equal(a[0], b[0])
+
+
 def test_read_layouts_give_the_same_nams():
     """map_reads copies the span of the read buffer when the reads lie inside it (in
     any order) and gathers them otherwise; both layouts give the NAMs of the
