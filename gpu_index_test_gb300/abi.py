@@ -92,6 +92,9 @@ NAM = np.dtype(
     ]
 )
 assert REF_RANDSTROBE.itemsize == 16 and QUERY_RANDSTROBE.itemsize == 24 and NAM.itemsize == 44
+# gbsa_nam_pair: a scored pair of NAMs (indices into the mates' NAM lists, -1: absent)
+NAM_PAIR = np.dtype([("score", "<i4"), ("i1", "<i4"), ("i2", "<i4")])
+GBSA_NAM_PAIRS_TOP_K = 40
 
 # Fields of a NAM that results are compared on (nam_id and the two prev-hit
 # positions are internal to the merge).

@@ -64,6 +64,7 @@ def lib():
             "gbsa_mapper_last_alg_sectors": (u64, [vp]),
             "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
+            "gbsa_nam_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, u32, vp, vp, vp]),
             "gbsa_server_create": (i32, [vp, vp, u32, u32, u64, vp]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
@@ -132,6 +133,15 @@ def classify_pairs_device(d_nams, d_nam_offsets, n_pairs, d_types, layout=0, dro
     """Pair types (gpu_pre_cal_type) from device NAM lists; all pointers are device addresses."""
     _check(lib().gbsa_classify_pairs_device(d_nams, d_nam_offsets, n_pairs, layout, dropoff, mu, sigma, d_types,
                                             stream))
+
+
+def nam_pairs_device(d_nams, d_nam_offsets, n_pairs, d_pairs, d_counts, layout=0, mu=300.0, sigma=100.0,
+                     max_tries=20, stream=None):
+    """NAM-pair scoring (get_best_scoring_nam_pairs_sort3) from device NAM lists: mate 1
+    in GBSA_SORT_REF_MATE1 order, mate 2 in GBSA_SORT_REF_MATE2 order; max_tries records
+    per pair into d_pairs and their count into d_counts.  Device addresses."""
+    _check(lib().gbsa_nam_pairs_device(d_nams, d_nam_offsets, n_pairs, layout, mu, sigma, max_tries, d_pairs,
+                                       d_counts, stream))
 
 
 def _u8(a):

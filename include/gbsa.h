@@ -299,6 +299,36 @@ int gbsa_classify_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_off
                                int layout, float dropoff_threshold, float mu, float sigma,
                                uint8_t* d_types, void* stream);
 
+/* NamPair (step2/main.cu:959-966) with the two NAMs as indices into the mates' NAM
+ * lists (-1: no NAM on that end). */
+typedef struct gbsa_nam_pair {
+    int32_t score;   /* joint n_hits of a pair, or the one NAM's n_hits */
+    int32_t i1;      /* index into mate 1's NAM list, or -1 */
+    int32_t i2;      /* index into mate 2's NAM list, or -1 */
+} gbsa_nam_pair;
+
+#define GBSA_NAM_PAIRS_TOP_K 40   /* TOP_K of the reference's pair heap (main.cu:1428) */
+
+/* NAM-pair scoring of the reads pairs whose two ends both have NAMs
+ * (get_best_scoring_nam_pairs_sort3, step2/main.cu:1475-1716, as align_PE_part4 calls
+ * it, main.cu:2026-2061): per reference id below 3000, mate-1 NAMs on the forward
+ * strand paired with mate-2 NAMs on the reverse strand whose diagonals
+ * max(0, ref_start - query_start) lie within [d1, d1 + mu + 10 sigma), then the
+ * opposite strands within (d1 - (mu + 10 sigma), d1], mu and sigma truncated to
+ * integers; pairs kept in a top-40 heap by joint n_hits with the reference's pruning
+ * (half the best joint count); mate-1 NAMs in no pair (at most max_tries per reference
+ * id and strand, n_hits at least half the best) and mate-2 NAMs in no pair (through
+ * the heap) as single-end entries; the list sorted by the reference's comparator and
+ * cut to max_tries.  Mate 1's NAMs must be in GBSA_SORT_REF_MATE1 order and mate 2's
+ * in GBSA_SORT_REF_MATE2 order (gpu_sort_nams, main.cu:3449-3466).  The reference
+ * compares fields of an otherwise uninitialised Nam for an absent end; here that Nam
+ * is all zero with ref_start -1.  d_pairs receives max_tries records per pair (pair p
+ * from p * max_tries on), d_counts the number written (0 when an end has no NAMs).
+ * Device pointers; the kernel runs on `stream` (0: the default stream). */
+int gbsa_nam_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs, int layout,
+                          float mu, float sigma, uint32_t max_tries, gbsa_nam_pair* d_pairs, uint32_t* d_counts,
+                          void* stream);
+
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later
  * calls; gbsa_mapper_last_alg_bytes returns the count of the last batch.  No

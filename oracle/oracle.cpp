@@ -884,6 +884,211 @@ int oracle_classify_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_
     return 0;
 }
 
+}  // extern "C"
+
+// ---- NAM-pair scoring (step2/main.cu:1428-1716) -------------------------------
+//
+// The heap keeps the TOP_K pairs of highest score: a binary min-heap on score whose
+// sift-up stops at a parent of score <= the child's and whose sift-down moves to the
+// smaller child (the left one on a tie) while it is strictly smaller (main.cu:1430-1473).
+struct PairHeap {
+    gbsa_nam_pair h[GBSA_NAM_PAIRS_TOP_K];
+    int size = 0;
+    void add(const gbsa_nam_pair& p) {
+        if (size < GBSA_NAM_PAIRS_TOP_K) {
+            int i = size++;
+            h[i] = p;
+            while (i > 0) {
+                const int up = (i - 1) / 2;
+                if (h[up].score <= h[i].score) break;
+                std::swap(h[up], h[i]);
+                i = up;
+            }
+        } else if (p.score > h[0].score) {
+            h[0] = p;
+            int i = 0;
+            while (2 * i + 1 < size) {
+                int s = i;
+                const int l = 2 * i + 1, r = l + 1;
+                if (l < size && h[l].score < h[s].score) s = l;
+                if (r < size && h[r].score < h[s].score) s = r;
+                if (s == i) break;
+                std::swap(h[i], h[s]);
+                i = s;
+            }
+        }
+    }
+};
+
+static inline int nam_diag(const gbsa_nam& n) { return std::max(0, n.ref_start - n.query_start); }
+
+// The comparator of the final sort (main.cu:1674-1713): joint score desc, then mate 1's
+// NAM (score desc, forward first, query end, query start, ref end, ref start) and mate
+// 2's likewise; an absent end compares as an all-zero NAM with ref_start -1.
+static bool nam_pair_before(const gbsa_nam_pair& a, const gbsa_nam_pair& b, const gbsa_nam* n1, const gbsa_nam* n2) {
+    gbsa_nam none{};
+    none.ref_start = -1;
+    const gbsa_nam& a1 = a.i1 < 0 ? none : n1[a.i1];
+    const gbsa_nam& a2 = a.i2 < 0 ? none : n2[a.i2];
+    const gbsa_nam& b1 = b.i1 < 0 ? none : n1[b.i1];
+    const gbsa_nam& b2 = b.i2 < 0 ? none : n2[b.i2];
+    if (a.score != b.score) return a.score > b.score;
+    if (a1.score != b1.score) return a1.score > b1.score;
+    if (a1.is_rc != b1.is_rc) return !a1.is_rc;
+    if (a1.query_end != b1.query_end) return a1.query_end < b1.query_end;
+    if (a1.query_start != b1.query_start) return a1.query_start < b1.query_start;
+    if (a1.ref_end != b1.ref_end) return a1.ref_end < b1.ref_end;
+    if (a1.ref_start != b1.ref_start) return a1.ref_start < b1.ref_start;
+    if (a2.score != b2.score) return a2.score > b2.score;
+    if (a2.is_rc != b2.is_rc) return !a2.is_rc;
+    if (a2.query_end != b2.query_end) return a2.query_end < b2.query_end;
+    if (a2.query_start != b2.query_start) return a2.query_start < b2.query_start;
+    if (a2.ref_end != b2.ref_end) return a2.ref_end < b2.ref_end;
+    return a2.ref_start < b2.ref_start;
+}
+
+// quick_sort_iterative (main.cu:317-358): Lomuto partition around the last element,
+// ranges on an explicit stack (left part pushed before the right one).  Not stable;
+// the same steps give the same order of elements that compare equal.
+template <class Less>
+static void quicksort_stack(gbsa_nam_pair* d, int lo, int hi, Less less) {
+    if (lo > hi) return;
+    std::vector<int> st;
+    st.push_back(lo);
+    st.push_back(hi);
+    while (!st.empty()) {
+        hi = st.back();
+        st.pop_back();
+        lo = st.back();
+        st.pop_back();
+        const gbsa_nam_pair pivot = d[hi];
+        int i = lo - 1;
+        for (int j = lo; j < hi; ++j)
+            if (less(d[j], pivot)) std::swap(d[++i], d[j]);
+        std::swap(d[i + 1], d[hi]);
+        const int p = i + 1;
+        if (p - 1 > lo) {
+            st.push_back(lo);
+            st.push_back(p - 1);
+        }
+        if (p + 1 < hi) {
+            st.push_back(p + 1);
+            st.push_back(hi);
+        }
+    }
+}
+
+// Pairs of mate-1 NAMs [b1, e1) with mate-2 NAMs [b2, e2) of opposite strands, one
+// reference id at a time (ids below 3000, main.cu:1520-1570 and 1573-1623).  fwd1: mate 1
+// on the forward strand (mate 2's diagonal in [d1, d1 + span)), else on the reverse
+// strand (mate 2's diagonal in (d1 - span, d1]).
+static void pair_pass(const gbsa_nam* n1, int b1, int e1, const gbsa_nam* n2, int b2, int e2, bool fwd1, int span,
+                      PairHeap& heap, std::vector<uint8_t>& add1, std::vector<uint8_t>& add2, int& best) {
+    int p1 = b1, p2 = b2;
+    for (int ref = 0; ref < 3000; ++ref) {
+        while (p1 < e1 && n1[p1].ref_id < ref) ++p1;
+        while (p2 < e2 && n2[p2].ref_id < ref) ++p2;
+        int q1 = p1, q2 = p2;
+        while (q1 < e1 && n1[q1].ref_id == ref) ++q1;
+        while (q2 < e2 && n2[q2].ref_id == ref) ++q2;
+        if (p1 == e1 || p2 == e2) break;
+        int best2 = -1;
+        for (int j = p2; j < q2; ++j) best2 = std::max(best2, n2[j].n_hits);
+        for (int i = p1; i < q1; ++i) {
+            const int round_best = n1[i].n_hits + best2;
+            if (round_best < best / 2) break;
+            if (heap.size == GBSA_NAM_PAIRS_TOP_K && round_best < heap.h[0].score) break;
+            const int d1 = nam_diag(n1[i]);
+            // first mate-2 NAM of this reference whose diagonal enters the window
+            int lo = p2, hi = q2 - 1, at = q2;
+            while (lo <= hi) {
+                const int mid = (lo + hi) / 2;
+                const bool in = fwd1 ? nam_diag(n2[mid]) >= d1 : nam_diag(n2[mid]) > d1 - span;
+                if (in) {
+                    at = mid;
+                    hi = mid - 1;
+                } else {
+                    lo = mid + 1;
+                }
+            }
+            for (int j = at; j < q2; ++j) {
+                const int d2 = nam_diag(n2[j]);
+                if (fwd1 ? d2 >= d1 + span : d2 > d1) break;
+                const int joint = n1[i].n_hits + n2[j].n_hits;
+                if (joint < best / 2) continue;
+                heap.add(gbsa_nam_pair{joint, i, j});
+                add1[i] = add2[j] = 1;
+                best = std::max(best, joint);
+            }
+        }
+    }
+}
+
+extern "C" {
+
+int oracle_nam_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout, float mu,
+                     float sigma, uint32_t max_tries, gbsa_nam_pair* out, uint32_t* counts) {
+    const int imu = (int)mu, isigma = (int)sigma;
+    const int span = imu + 10 * isigma;
+    for (uint32_t p = 0; p < n_pairs; ++p) {
+        const uint64_t r1 = layout == GBSA_PAIRS_HALVES ? p : 2ull * p;
+        const uint64_t r2 = layout == GBSA_PAIRS_HALVES ? (uint64_t)p + n_pairs : 2ull * p + 1;
+        const int c1 = (int)(offsets[r1 + 1] - offsets[r1]), c2 = (int)(offsets[r2 + 1] - offsets[r2]);
+        counts[p] = 0;
+        if (c1 == 0 || c2 == 0) continue;
+        const gbsa_nam* n1 = nams + offsets[r1];
+        const gbsa_nam* n2 = nams + offsets[r2];
+        std::vector<uint8_t> add1((size_t)c1, 0), add2((size_t)c2, 0);
+        int mid1 = c1, mid2 = c2;   // first reverse-strand NAM of each end
+        for (int i = 0; i < c1; ++i)
+            if (n1[i].is_rc == 1) {
+                mid1 = i;
+                break;
+            }
+        for (int i = 0; i < c2; ++i)
+            if (n2[i].is_rc == 1) {
+                mid2 = i;
+                break;
+            }
+        PairHeap heap;
+        int best = 0;
+        pair_pass(n1, 0, mid1, n2, mid2, c2, true, span, heap, add1, add2, best);
+        pair_pass(n1, mid1, c1, n2, 0, mid2, false, span, heap, add1, add2, best);
+        std::vector<gbsa_nam_pair> list;
+        // mate-1 NAMs in no pair: at most max_tries per (reference id, strand)
+        int best1 = best;
+        if (best1 == 0)
+            for (int i = 0; i < c1; ++i) best1 = std::max(best1, n1[i].n_hits);
+        int run = 0, prev = n1[0].ref_id + 3000 * n1[0].is_rc;
+        for (int i = 0; i < c1; ++i) {
+            const int key = n1[i].ref_id + 3000 * n1[i].is_rc;
+            if (key == prev) ++run;
+            else {
+                run = 1;
+                prev = key;
+            }
+            if (run > (int)max_tries) continue;
+            if (n1[i].n_hits < best1 / 2 || add1[i]) continue;
+            list.push_back(gbsa_nam_pair{n1[i].n_hits, i, -1});
+        }
+        // mate-2 NAMs in no pair, through the heap
+        int best2 = best;
+        if (best2 == 0)
+            for (int i = 0; i < c2; ++i) best2 = std::max(best2, n2[i].n_hits);
+        for (int i = 0; i < c2; ++i) {
+            if (n2[i].n_hits < best2 / 2 || add2[i]) continue;
+            heap.add(gbsa_nam_pair{n2[i].n_hits, -1, i});
+        }
+        for (int i = 0; i < heap.size; ++i) list.push_back(heap.h[i]);
+        quicksort_stack(list.data(), 0, (int)list.size() - 1,
+                        [&](const gbsa_nam_pair& a, const gbsa_nam_pair& b) { return nam_pair_before(a, b, n1, n2); });
+        const uint32_t k = std::min<uint32_t>((uint32_t)list.size(), max_tries);
+        for (uint32_t i = 0; i < k; ++i) out[(size_t)p * max_tries + i] = list[i];
+        counts[p] = k;
+    }
+    return 0;
+}
+
 int oracle_map_reads(const oracle_index* h, const gbsa_map_options* opt, const char* seqs, const uint64_t* offsets,
                      const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity,
                      uint64_t* nam_offsets, float* frac, uint8_t* rescued, int n_threads) {

@@ -61,6 +61,11 @@ void oracle_sort_nams(gbsa_nam* nams, uint64_t n, int sort_mode);
 int oracle_classify_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout,
                           float dropoff_threshold, float mu, float sigma, uint8_t* types);
 
+/* get_best_scoring_nam_pairs_sort3 (step2/main.cu:1475-1716) per pair, cut to max_tries
+ * (main.cu:2061-2064); out holds max_tries records per pair, counts the number kept. */
+int oracle_nam_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout, float mu,
+                     float sigma, uint32_t max_tries, gbsa_nam_pair* out, uint32_t* counts);
+
 /* Whole path for a batch of reads with n_threads host threads (0 = all cores).
  * Same contract as gbsa_map_reads.  Returns GBSA_OK or GBSA_ERR_CAPACITY. */
 int oracle_map_reads(const oracle_index* idx, const gbsa_map_options* opt, const char* seqs,

@@ -60,6 +60,9 @@ def lib():
         L.oracle_classify_pairs.restype = C.c_int
         L.oracle_classify_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_float,
                                             C.c_float, C.c_void_p]
+        L.oracle_nam_pairs.restype = C.c_int
+        L.oracle_nam_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_float,
+                                       C.c_uint32, C.c_void_p, C.c_void_p]
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -216,3 +219,15 @@ def classify_pairs(nams, offsets, n_pairs, layout=abi.GBSA_PAIRS_INTERLEAVED, dr
     assert lib().oracle_classify_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, dropoff,
                                        mu, sigma, out.ctypes.data) == 0
     return out[:n_pairs]
+
+
+def nam_pairs(nams, offsets, n_pairs, layout=abi.GBSA_PAIRS_INTERLEAVED, mu=300.0, sigma=100.0, max_tries=20):
+    """get_best_scoring_nam_pairs_sort3 restated, cut to max_tries: (records of shape
+    (n_pairs, max_tries), counts)."""
+    a = np.ascontiguousarray(nams)
+    o = np.ascontiguousarray(offsets, np.uint64)
+    out = np.zeros((max(1, n_pairs), max_tries), abi.NAM_PAIR)
+    cnt = np.zeros(max(1, n_pairs), np.uint32)
+    assert lib().oracle_nam_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, mu, sigma,
+                                  max_tries, out.ctypes.data, cnt.ctypes.data) == 0
+    return out[:n_pairs], cnt[:n_pairs]

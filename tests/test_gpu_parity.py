@@ -458,6 +458,55 @@ def test_pair_classification_against_oracle(params):
     assert {3, 4} <= seen
 
 
+@pytest.mark.parametrize("str_frac", [0.0, 0.05])
+def test_nam_pair_scoring_against_oracle(str_frac):
+    """NAM-pair scoring on the GPU equals the oracle's for mapped read pairs, mate 1
+    sorted as sort_nams_single2 and mate 2 as Nam::operator<, in both mate layouts; on a
+    genome with tandem repeats some pairs have hundreds of NAMs and fill the heap."""
+    import dataclasses
+    import torch
+    gp = dataclasses.replace(synth.genome_params("C2", scale=0.01, seed=91), str_frac=str_frac)
+    g = synth.make_genome(gp)
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=4000, seed=92))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    n_pairs = reads.n // 2
+    mate1 = reads.subset(np.arange(0, reads.n, 2))
+    mate2 = reads.subset(np.arange(1, reads.n, 2))
+    a = native.Mapper(idx, abi.map_options(rescue_level=2, sort_mode=abi.GBSA_SORT_REF_MATE1)).map_reads(mate1)
+    b = native.Mapper(idx, abi.map_options(rescue_level=2, sort_mode=abi.GBSA_SORT_REF_MATE2)).map_reads(mate2)
+    c1, c2 = np.diff(a[1].astype(np.int64)), np.diff(b[1].astype(np.int64))
+    # halves: mate 1 lists, then mate 2 lists; interleaved: mate 1, mate 2 per pair
+    nams_h = np.concatenate([a[0], b[0]])
+    offs_h = np.concatenate([a[1], b[1][1:] + a[1][-1]]).astype(np.uint64)
+    ends = [a[0][int(a[1][i]):int(a[1][i + 1])] for i in range(n_pairs)]
+    ends2 = [b[0][int(b[1][i]):int(b[1][i + 1])] for i in range(n_pairs)]
+    inter = [x for i in range(n_pairs) for x in (ends[i], ends2[i])]
+    offs_i = np.zeros(reads.n + 1, np.uint64)
+    offs_i[1:] = np.cumsum([len(e) for e in inter])
+    nams_i = np.concatenate(inter)
+    dev = torch.device("cuda:0")
+    tries = 20
+    for layout, (nn, oo) in ((abi.GBSA_PAIRS_HALVES, (nams_h, offs_h)), (abi.GBSA_PAIRS_INTERLEAVED, (nams_i, offs_i))):
+        d_n = torch.from_numpy(np.ascontiguousarray(nn).view(np.uint8).copy()).to(dev)
+        d_o = torch.from_numpy(oo.astype(np.int64)).to(dev)
+        d_p = torch.zeros(n_pairs * tries * 3, dtype=torch.int32, device=dev)
+        d_c = torch.zeros(n_pairs, dtype=torch.int32, device=dev)
+        native.nam_pairs_device(d_n.data_ptr(), d_o.data_ptr(), n_pairs, d_p.data_ptr(), d_c.data_ptr(), layout,
+                                300.0, 100.0, tries)
+        got = d_p.cpu().numpy().view(abi.NAM_PAIR).reshape(n_pairs, tries)
+        got_c = d_c.cpu().numpy().astype(np.uint32)
+        ref, ref_c = oracle_py.nam_pairs(nn, oo, n_pairs, layout, 300.0, 100.0, tries)
+        assert (got_c == ref_c).all()
+        for p in range(n_pairs):
+            k = int(ref_c[p])
+            assert (got[p][:k] == ref[p][:k]).all(), p
+    both = (c1 > 0) & (c2 > 0)
+    assert both.sum() > n_pairs // 2 and (ref_c[both] > 0).all()
+    assert ((ref["i1"] >= 0) & (ref["i2"] >= 0)).any()
+    if str_frac > 0:
+        assert (np.maximum(c1, c2) > 200).any()
+
+
 def test_server_requests_match_plain_form():
     """Requests of uneven sizes served by three workers give, request by request, the
     NAMs of one plain map_reads call over all reads; a request above the maximum is

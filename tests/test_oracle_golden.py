@@ -114,3 +114,55 @@ def test_pair_classification_cases():
     got_h = oracle_py.classify_pairs(nams_h, offs_h, len(cases), abi.GBSA_PAIRS_HALVES)
     assert list(got_h) == [c[2] for c in cases]
 
+
+
+def test_nam_pair_scoring_cases():
+    """get_best_scoring_nam_pairs_sort3 restated, on hand-worked cases (mu 300, sigma
+    100: mate 2's diagonal within [d1, d1 + 1300) of a forward mate 1, within
+    (d1 - 1300, d1] of a reverse one): pairing and its window edges on both strands,
+    pruning at half the best joint count, single-end entries (max_tries per reference
+    and strand) and the cut to max_tries, an absent end ordered as an all-zero NAM, and
+    reference ids from 3000 on never paired."""
+    fwd = lambda rs, h=5, ref=3: _nam(ref, 0, 0, rs, h)
+    rev = lambda rs, h=5, ref=3: _nam(ref, 1, 10, rs + 10, h)   # diagonal rs
+    cases = [
+        ([fwd(1000)], [rev(1190, h=4)], 20, [(9, 0, 0)]),
+        ([fwd(1000)], [rev(2300, h=4)], 20, [(5, 0, -1), (4, -1, 0)]),    # window end: no pair
+        ([fwd(1000)], [rev(999, h=4)], 20, [(5, 0, -1), (4, -1, 0)]),     # below the window
+        ([rev(1190, h=6)], [fwd(1000, h=3)], 20, [(9, 0, 0)]),             # mate 1 reverse
+        ([fwd(1000, h=10), fwd(5000, h=2)], [rev(1100, h=10), rev(5100, h=2)], 20, [(20, 0, 0)]),
+        ([fwd(1000 * k) for k in range(1, 6)], [rev(90000, ref=4)], 3,
+         [(5, -1, 0), (5, 0, -1), (5, 1, -1)]),
+        ([fwd(1000, ref=3000)], [rev(1190, ref=3000)], 20, [(5, -1, 0), (5, 0, -1)]),
+        ([fwd(1000)], [], 20, []),
+    ]
+    for layout in (abi.GBSA_PAIRS_INTERLEAVED, abi.GBSA_PAIRS_HALVES):
+        for m1, m2, tries, want in cases:
+            ends = [m1, m2]
+            offs = np.zeros(3, np.uint64)
+            offs[1:] = np.cumsum([len(e) for e in ends])
+            nams = np.concatenate([x for e in ends for x in e])
+            out, cnt = oracle_py.nam_pairs(nams, offs, 1, layout, 300.0, 100.0, tries)
+            got = [tuple(int(v) for v in out[0][i]) for i in range(int(cnt[0]))]
+            assert got == want, (m1, m2, got)
+
+
+def test_nam_pair_heap_keeps_the_best_forty():
+    """More than 40 candidate pairs: the list holds the 40 best joint counts (the
+    heap), sorted by score."""
+    m1 = [_nam(3, 0, 0, 1000 + 10 * i, 40 - i // 2) for i in range(30)]
+    m2 = [_nam(3, 1, 10, 1100 + 10 * i + 10, 40 - i // 3) for i in range(30)]
+    import itertools
+    m2 = sorted(m2, key=lambda n: int(n["ref_start"][0] - n["query_start"][0]))
+    nams = np.concatenate(m1 + m2)
+    offs = np.array([0, len(m1), len(m1) + len(m2)], np.uint64)
+    out, cnt = oracle_py.nam_pairs(nams, offs, 1, abi.GBSA_PAIRS_INTERLEAVED, 300.0, 100.0, 64)
+    got = out[0][: int(cnt[0])]
+    paired = got[(got["i1"] >= 0) & (got["i2"] >= 0)]
+    assert len(paired) == abi.GBSA_NAM_PAIRS_TOP_K
+    assert (np.diff(got["score"]) <= 0).all()
+    # the heap's 40 are the 40 largest joint counts among all pairs in the window
+    joint = sorted((int(a["n_hits"][0]) + int(b["n_hits"][0]) for a, b in itertools.product(m1, m2)
+                    if 0 <= int(b["ref_start"][0] - b["query_start"][0]) - int(a["ref_start"][0]) < 1300),
+                   reverse=True)
+    assert sorted(paired["score"].tolist(), reverse=True) == joint[:40]
