@@ -229,7 +229,7 @@ struct gbsa_mapper {
     gbsa::MapConfig cfg{};
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;                           // rescue chain, beside the NAM kernels
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, rescue_ev = nullptr;
     cudaStream_t side_lo = nullptr;                        // rescue chain of a batch on a caller's stream
     cudaStream_t early = nullptr;                          // seeding + lookup of pipelined chunks
     cudaEvent_t early_ev = nullptr;
@@ -356,8 +356,18 @@ static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
 // rescue → sorts (side stream), then the per-read NAM offsets into m.out_off[0..n]; the
 // device counters and the NAM total are copied to m.h_status (pinned).  Nothing waits
 // on the host.
+// Where a batch's NAM records, fractions and rescue flags go, when the batch gathers
+// them itself.
+struct GatherTarget {
+    gbsa_nam* nams;
+    uint64_t cap;   // records nams holds (the gather writes no further)
+    float* frac;
+    uint8_t* resc;
+};
+
 static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
-                          uint32_t n, bool seeded, cudaStream_t st, cudaStream_t early = nullptr) {
+                          uint32_t n, bool seeded, cudaStream_t st, cudaStream_t early = nullptr,
+                          const GatherTarget* gt = nullptr) {
     cudaStream_t main_st = st;
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, st));
@@ -425,6 +435,7 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
     Arenas As = A;
     As.slots = m.side_slots.as<uint8_t>();
     launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, side);
+    GBSA_CUDA(cudaEventRecord(m.rescue_ev, side));
     if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[6], side));
     if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, side);
     if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[7], side));
@@ -433,13 +444,22 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
     mark(4);
     launch_nams_warp(C, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(5);
-    GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
-    // per-read NAM counts → offsets (meaningless when an arena overflowed; the batch is
-    // then run again)
+    // Every read's NAM count is known once the rescue kernel has ended (the sorts after
+    // it only order NAMs): per-read counts → offsets, and the records of the reads that
+    // were not rescued, while the side stream may still sort; the rescued reads' records
+    // after the join.  (Meaningless when an arena overflowed; the batch then runs again.)
+    GBSA_CUDA(cudaStreamWaitEvent(st, m.rescue_ev, 0));
     uint64_t* cnt = m.cnt.as<uint64_t>();
     uint64_t* off = m.out_off.as<uint64_t>();
     launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st);
     scan_exclusive_u64(cnt, off, n, off + n, ws, st);
+    if (gt)
+        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt->nams, gt->frac, gt->resc, st,
+                           gt->cap, 1);
+    GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
+    if (gt)
+        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt->nams, nullptr, nullptr, st,
+                           gt->cap, 2, &A, ctr);
     GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<void>(), ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
     GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<uint8_t>() + sizeof(Counters), off + n, 8, cudaMemcpyDeviceToHost, st));
 }
@@ -499,9 +519,9 @@ static uint64_t batch_total(gbsa_mapper& m) {
 // enqueue_batch + check_batch until the work areas are large enough: leaves per-read NAM
 // offsets in m.out_off[0..n] and returns the NAM total.
 static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
-                             uint32_t n, bool seeded, cudaStream_t st) {
+                             uint32_t n, bool seeded, cudaStream_t st, const GatherTarget* gt = nullptr) {
     for (int attempt = 0; attempt < 8; ++attempt) {
-        enqueue_batch(m, d_seqs, d_offs, d_lens, n, seeded, st);
+        enqueue_batch(m, d_seqs, d_offs, d_lens, n, seeded, st, nullptr, gt);
         GBSA_CUDA(cudaStreamSynchronize(st));
         if (check_batch(m, seeded)) return batch_total(m);
     }
@@ -882,6 +902,7 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
         GBSA_CUDA(cudaEventCreateWithFlags(&m->early_ev, cudaEventDisableTiming));
         GBSA_CUDA(cudaEventCreateWithFlags(&m->fork_ev, cudaEventDisableTiming));
         GBSA_CUDA(cudaEventCreateWithFlags(&m->join_ev, cudaEventDisableTiming));
+        GBSA_CUDA(cudaEventCreateWithFlags(&m->rescue_ev, cudaEventDisableTiming));
         mapper_reserve(*m, m->max_reads, m->max_bases);
         *out = m.release();
     });
@@ -902,6 +923,7 @@ void gbsa_mapper_free(gbsa_mapper* m) {
     if (m->copy_out) cudaStreamDestroy(m->copy_out);
     if (m->fork_ev) cudaEventDestroy(m->fork_ev);
     if (m->join_ev) cudaEventDestroy(m->join_ev);
+    if (m->rescue_ev) cudaEventDestroy(m->rescue_ev);
     for (cudaStream_t x : {m->early, m->side_lo})
         if (x) {
             cudaStreamSynchronize(x);
@@ -978,9 +1000,9 @@ int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, co
             o.off.resize(8ull * (n + 1));
             o.off_g.resize(8ull * (n + 1));
             GBSA_CUDA(cudaStreamWaitEvent(b.st, b.in_ready, 0));
+            const GatherTarget gt{o.nams.as<gbsa_nam>(), o.cap, o.frac.as<float>(), o.resc.as<uint8_t>()};
             enqueue_batch(b, b.seqs.as<uint8_t>(), b.offs.as<uint64_t>(), b.lens.as<uint32_t>(), n, false, b.st,
-                          b.early);
-            gather(k);
+                          b.early, &gt);
             launch_offsets_add(b.out_off.as<uint64_t>(), o.off.as<uint64_t>(), n, 0, b.st);
             GBSA_CUDA(cudaEventRecord(b.done_ev, b.st));
         };
@@ -1068,8 +1090,11 @@ int gbsa_map_reads_device(gbsa_mapper* m, const char* d_seqs, const uint64_t* d_
     return guarded([&] {
         cudaStream_t st = stream ? (cudaStream_t)stream : m->st;
         mapper_reserve(*m, n_reads, m->max_bases);
+        // the batch gathers its records into the caller's buffers itself (at most
+        // nam_capacity of them)
+        const GatherTarget gt{d_nams, nam_capacity, d_frac, d_rescued};
         const uint64_t total = run_pipeline(*m, reinterpret_cast<const uint8_t*>(d_seqs), d_offsets, d_lengths,
-                                            n_reads, false, st);
+                                            n_reads, false, st, &gt);
         if (nam_total) *nam_total = total;
         GBSA_CUDA(cudaMemcpyAsync(d_nam_offsets, m->out_off.as<void>(), 8ull * (n_reads + 1),
                                   cudaMemcpyDeviceToDevice, st));
@@ -1077,8 +1102,6 @@ int gbsa_map_reads_device(gbsa_mapper* m, const char* d_seqs, const uint64_t* d_
             GBSA_CUDA(cudaStreamSynchronize(st));
             throw Error(GBSA_ERR_CAPACITY, "NAM capacity too small");
         }
-        launch_gather_nams(n_reads, m->rec.as<ReadRec>(), m->nams.as<NamState>(), m->out_off.as<uint64_t>(), d_nams,
-                           d_frac, d_rescued, st);
     });
 }
 

@@ -124,8 +124,11 @@ void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Co
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
+// mode 0: every read; 1: the reads that were not rescued; 2: the rescued reads (A and
+// ctr give the rescue list; needed for mode 2 only).
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
-                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap = ~0ull);
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap = ~0ull,
+                        int mode = 0, const Arenas* A = nullptr, const Counters* ctr = nullptr);
 void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
                            gbsa_query_randstrobe* out, cudaStream_t st);
 void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st);

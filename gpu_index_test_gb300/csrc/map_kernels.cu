@@ -1041,8 +1041,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         note.set(6, walk);
         note.set(5, L.n_closed);
         if (L.n_closed > kWarpSortMax) {
-            // many NAMs: the block-per-read sort kernel orders them
+            // many NAMs: the block-per-read sort kernel orders them.  The count is known
+            // now (the sort only orders them), so the NAM offsets of the batch can be
+            // computed while the sorts run; the sort sets nam_off.
             if (lane == 0) {
+                R.n_nams = L.n_closed;
                 const uint32_t j = L.n_closed > kSortTile ? A.jobs_cap - 1 - atomicAdd(&ctr->n_huge, 1u)
                                                           : atomicAdd(&ctr->n_heavy, 1u);
                 SortJob job;
@@ -1221,6 +1224,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __
             const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)NN);
             if (noff + NN > A.nam_cap) {
                 R.flags |= kReadFailed;
+                R.n_nams = 0;   // the rescue kernel set the count ahead of the sort
                 atomicOr(&ctr->status, kStatusNamOverflow);
                 s_noff = ~0ULL;
             } else {
@@ -1349,6 +1353,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
                 const uint64_t noff = atomicAdd(&ctr->nam_used, (unsigned long long)NN);
                 if (noff + NN > A.nam_cap) {
                     R.flags |= kReadFailed;
+                    R.n_nams = 0;   // the rescue kernel set the count ahead of the sort
                     atomicOr(&ctr->status, kStatusNamOverflow);
                     s_noff = ~0ULL;
                 } else {
@@ -1377,14 +1382,29 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
 
 // Records at or beyond out_cap are not written (the caller sized out from an estimate
 // and gathers again when the total turns out larger).
+// mode 0: every read; 1: the reads that were not rescued (fractions and rescue flags
+// of every read), while the rescued reads' sorts may still run; 2: the rescued reads
+// (through the rescue list), after their sorts.
 __global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const NamState* __restrict__ arena,
                               const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, uint64_t out_cap,
-                              float* frac, uint8_t* rescued) {
+                              float* frac, uint8_t* rescued, int mode, Arenas A, const Counters* ctr) {
     const uint32_t lane = lane_id();
+    if (mode == 2) {
+        const uint32_t n_light = ctr->n_rescue, n_heavy = ctr->n_rescue_heavy;
+        for (uint32_t t = warp_global_id(); t < n_light + n_heavy; t += warp_count()) {
+            const uint32_t r = t < n_light ? A.rescue_list[t] : A.rescue_list[A.rescue_cap - 1 - (t - n_light)];
+            const ReadRec R = rec[r];
+            const uint64_t o = out_off[r];
+            for (uint32_t j = lane; j < R.n_nams; j += 32)
+                if (o + j < out_cap) to_gbsa_nam(arena[R.nam_off + j], (int)j, out[o + j]);
+        }
+        return;
+    }
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
         const ReadRec R = rec[r];
         const uint64_t o = out_off[r];
-        for (uint32_t j = lane; j < R.n_nams; j += 32)
+        const bool skip = mode == 1 && (R.flags & kReadRescue);
+        for (uint32_t j = lane; j < (skip ? 0u : R.n_nams); j += 32)
             if (o + j < out_cap) to_gbsa_nam(arena[R.nam_off + j], (int)j, out[o + j]);
         if (lane == 0) {
             if (frac) frac[r] = R.frac;
@@ -1549,10 +1569,12 @@ void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr,
 }
 
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
-                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap) {
+                        gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap, int mode,
+                        const Arenas* A, const Counters* ctr) {
     if (!n) return;
-    k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(n, rec, arena, out_off, out, out_cap,
-                                                                                frac, rescued);
+    const Arenas none{};
+    k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(
+        n, rec, arena, out_off, out, out_cap, frac, rescued, mode, A ? *A : none, ctr);
     GBSA_LAUNCHED();
 }
 
