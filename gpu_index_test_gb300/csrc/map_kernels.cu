@@ -1165,20 +1165,6 @@ __device__ void block_sort_keys(NamKey* keys, uint32_t n, SortTile tile, uint32_
     }
 }
 
-// Bitonic sort of the P (a power of two) keys held in the tile.
-__device__ void tile_sort(SortTile tile, uint32_t P) {
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t q = threadIdx.x; q < P / 2; q += blockDim.x) {
-                const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
-                const uint32_t ixj = i | j;
-                if (tile.less_at(ixj, i) == ((i & k) == 0)) tile.swap(i, ixj);
-            }
-            __syncthreads();
-        }
-    }
-}
-
 // Shared-memory tile of the block sort that moves only the first key word and the
 // NAM index: the other key words stay where they were loaded (indexed by NAM) and
 // are read only when the first words tie.  A compare-exchange then moves 12 bytes
@@ -1304,26 +1290,17 @@ __global__ void __launch_bounds__(kThreads) k_sort_jobs(MapConfig C, ReadRec* __
 // shared memory, so the clusters run beside the NAM kernels of the other stream.
 constexpr int kClusterCtas = 8;
 
-__device__ __forceinline__ SortTile tile_of_rank(const SortTile& t, uint32_t rank) {
+// Tie break of the index-moving cluster sort: NAM indices ib and ia whose first key
+// words are equal, by their second and third words (fixed, NAM e in CTA e / T at e % T)
+// and then the index.
+__device__ __forceinline__ bool cluster_tie_less(uint32_t ib, uint32_t ia, uint64_t* k2, uint64_t* k3, uint32_t T) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    SortTile r;
-    r.k1 = cl.map_shared_rank(t.k1, rank);
-    r.k2 = cl.map_shared_rank(t.k2, rank);
-    r.k3 = cl.map_shared_rank(t.k3, rank);
-    r.idx = cl.map_shared_rank(t.idx, rank);
-    return r;
-}
-
-// key(tb[b]) < key(ta[a]) for entries of possibly different tiles
-__device__ __forceinline__ bool tiles_less(const SortTile& tb, uint32_t b, const SortTile& ta, uint32_t a) {
-    const uint64_t x = tb.k1[b], y = ta.k1[a];
-    if (x != y) return x < y;
-    const uint64_t x2 = tb.k2[b], y2 = ta.k2[a];
-    if (x2 != y2) return x2 < y2;
-    const uint64_t x3 = tb.k3[b], y3 = ta.k3[a];
-    if (x3 != y3) return x3 < y3;
-    return tb.idx[b] < ta.idx[a];
+    const uint64_t b2 = *cl.map_shared_rank(k2 + ib % T, ib / T), a2 = *cl.map_shared_rank(k2 + ia % T, ia / T);
+    if (b2 != a2) return b2 < a2;
+    const uint64_t b3 = *cl.map_shared_rank(k3 + ib % T, ib / T), a3 = *cl.map_shared_rank(k3 + ia % T, ia / T);
+    if (b3 != a3) return b3 < a3;
+    return ib < ia;
 }
 
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
@@ -1348,6 +1325,9 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
         const uint32_t P = next_pow2(NN);
         const bool in_tiles = P <= kClusterCtas * kSortTile;
         if (in_tiles) {
+            // Each CTA's tile moves only the first key word (k1) and the NAM index (idx) of
+            // its T positions; the second and third words stay where they were loaded,
+            // by NAM index, and are read (possibly from another CTA) only on ties.
             const uint32_t T = P / kClusterCtas;   // NN > kSortTile: T >= kSortTile / 4
             const uint32_t e0 = rank * T;
             for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
@@ -1355,11 +1335,13 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
                 NamKey k;
                 if (e < NN) {
                     k = nam_key(closed[e], e, C.sort_mode);
-                } else {
+                } else {   // padding sorts last (a NAM's first key word is never all ones)
                     k.k1 = k.k2 = k.k3 = ~0ULL;
-                    k.idx = 0xFFFFFFFFu;
                 }
-                tile.put(i, k);
+                tile.k1[i] = k.k1;
+                tile.idx[i] = e;
+                tile.k2[i] = k.k2;
+                tile.k3[i] = k.k3;
             }
             cl.sync();
             for (uint32_t k = 2; k <= P; k <<= 1) {
@@ -1368,7 +1350,16 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
                         for (uint32_t q = threadIdx.x; q < T / 2; q += blockDim.x) {
                             const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
                             const uint32_t ixj = i | j;
-                            if (tile.less_at(ixj, i) == (((e0 + i) & k) == 0)) tile.swap(i, ixj);
+                            const uint64_t xb = tile.k1[ixj], xa = tile.k1[i];
+                            const bool less =
+                                xb != xa ? xb < xa : cluster_tie_less(tile.idx[ixj], tile.idx[i], tile.k2, tile.k3, T);
+                            if (less == (((e0 + i) & k) == 0)) {
+                                tile.k1[i] = xb;
+                                tile.k1[ixj] = xa;
+                                const uint32_t t = tile.idx[i];
+                                tile.idx[i] = tile.idx[ixj];
+                                tile.idx[ixj] = t;
+                            }
                         }
                         if (j > 1) __syncthreads();
                         else cl.sync();   // the next stage may cross CTAs
@@ -1377,12 +1368,18 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
                         for (uint32_t q = rank * (T / 2) + threadIdx.x; q < (rank + 1) * (T / 2); q += blockDim.x) {
                             const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
                             const uint32_t ixj = i | j;
-                            SortTile ta = tile_of_rank(tile, i / T), tb = tile_of_rank(tile, ixj / T);
-                            const uint32_t ia = i % T, ib = ixj % T;
-                            if (tiles_less(tb, ib, ta, ia) == ((i & k) == 0)) {
-                                const NamKey a = ta.get(ia), b = tb.get(ib);
-                                ta.put(ia, b);
-                                tb.put(ib, a);
+                            uint64_t* pa = cl.map_shared_rank(tile.k1 + i % T, i / T);
+                            uint64_t* pb = cl.map_shared_rank(tile.k1 + ixj % T, ixj / T);
+                            uint32_t* qa = cl.map_shared_rank(tile.idx + i % T, i / T);
+                            uint32_t* qb = cl.map_shared_rank(tile.idx + ixj % T, ixj / T);
+                            const uint64_t xa = *pa, xb = *pb;
+                            const bool less = xb != xa ? xb < xa : cluster_tie_less(*qb, *qa, tile.k2, tile.k3, T);
+                            if (less == ((i & k) == 0)) {
+                                *pa = xb;
+                                *pb = xa;
+                                const uint32_t t = *qa;
+                                *qa = *qb;
+                                *qb = t;
                             }
                         }
                         cl.sync();
