@@ -346,23 +346,74 @@ __device__ __forceinline__ uint8_t* warp_scratch(const Arenas& A, Counters* ctr,
 
 // Scores, sorts and writes the closed NAMs of a read to the NAM arena.  keys needs
 // room for next_pow2(n_closed) entries.
-__device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, NamKey* keys, ReadRec& R, const Arenas& A,
-                                 Counters* ctr) {
+// Warp bitonic sort of P (a power of two) entries that moves only the first key word
+// (k1) and the NAM index (ix); the second and third words stay by NAM index and are
+// read when the first words tie.
+__device__ void warp_sort_idx(uint64_t* k1, uint32_t* ix, const uint64_t* k2, const uint64_t* k3, uint32_t P) {
+    const uint32_t lane = lane_id();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t q = lane; q < P / 2; q += 32) {
+                const uint32_t i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                const uint32_t ixj = i | j;
+                const uint64_t xb = k1[ixj], xa = k1[i];
+                bool less;
+                if (xb != xa) {
+                    less = xb < xa;
+                } else {
+                    const uint32_t ib = ix[ixj], ia = ix[i];
+                    const uint64_t b2 = k2[ib], a2 = k2[ia], b3 = k3[ib], a3 = k3[ia];
+                    less = b2 != a2 ? b2 < a2 : (b3 != a3 ? b3 < a3 : ib < ia);
+                }
+                if (less == ((i & k) == 0)) {
+                    k1[i] = xb;
+                    k1[ixj] = xa;
+                    const uint32_t t = ix[i];
+                    ix[i] = ix[ixj];
+                    ix[ixj] = t;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Sorts a rescued read's NAMs (at most kWarpSortMax) with the warp in its shared
+// buffers sa / sb (4 KB each, free after the merge) and writes them to the NAM arena.
+__device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, uint32_t* sa, uint32_t* sb, ReadRec& R,
+                                 const Arenas& A, Counters* ctr) {
     const uint32_t lane = lane_id();
     const uint32_t NN = L.n_closed;
-    for (uint32_t t = lane; t < NN; t += 32) keys[t] = nam_key(L.closed[t], t, C.sort_mode);
+    const uint32_t P = next_pow2(NN);
+    uint64_t* k1 = reinterpret_cast<uint64_t*>(sa);       // P <= 256: 2 KB
+    uint32_t* ix = sa + 512;                              // 1 KB
+    uint64_t* k2 = reinterpret_cast<uint64_t*>(sb);       // 2 KB
+    uint64_t* k3 = k2 + 256;                              // 2 KB
+    for (uint32_t t = lane; t < P; t += 32) {
+        NamKey k;
+        if (t < NN) {
+            k = nam_key(L.closed[t], t, C.sort_mode);
+        } else {   // padding sorts last (a NAM's first key word is never all ones)
+            k.k1 = k.k2 = k.k3 = ~0ULL;
+        }
+        k1[t] = k.k1;
+        ix[t] = t;
+        k2[t] = k.k2;
+        k3[t] = k.k3;
+    }
     __syncwarp();
-    warp_sort_keys(keys, NN);
+    warp_sort_idx(k1, ix, k2, k3, P);
     const uint64_t noff = warp_bump(&ctr->nam_used, NN);
     if (noff + NN > A.nam_cap) {
         warp_fail(R, ctr, kStatusNamOverflow);
         return;
     }
-    for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = L.closed[keys[t].idx];
+    for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = L.closed[ix[t]];
     if (lane == 0) {
         R.nam_off = noff;
         R.n_nams = NN;
     }
+    __syncwarp();
 }
 
 constexpr uint32_t kLaneMaxHits = 160;
@@ -963,8 +1014,8 @@ constexpr uint32_t kRescueSmemHits = 1024;   // per-warp shared buffer for one q
 
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
                                                                  Arenas A, Counters* ctr) {
-    __shared__ uint32_t s_hrs[kWarpsPerBlock][kRescueSmemHits];
-    __shared__ uint32_t s_hpk[kWarpsPerBlock][kRescueSmemHits];
+    __shared__ __align__(16) uint32_t s_hrs[kWarpsPerBlock][kRescueSmemHits];
+    __shared__ __align__(16) uint32_t s_hpk[kWarpsPerBlock][kRescueSmemHits];
     __shared__ uint8_t s_tb[kWarpsPerBlock][kRescueSmemHits];
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_rescue_heavy;
@@ -1060,7 +1111,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
             continue;
         }
         const long long t_fin = clock64();
-        warp_finish_nams(C, L, keys, R, A, ctr);
+        static_assert(kWarpSortMax <= 256 && kRescueSmemHits >= 1024, "the sort entries fit the hit buffers");
+        warp_finish_nams(C, L, s_hrs[w], s_hpk[w], R, A, ctr);
         note.phase(3, t_fin);
         __syncwarp();
     }
