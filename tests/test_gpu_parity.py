@@ -409,6 +409,56 @@ def test_pipelined_map_reads_with_growing_work_areas():
     assert (v[1] == w[1]).all() and (v[2] == w[2]).all() and nams_equal(v[0], w[0])
 
 
+def test_errors_leave_the_mapper_usable():
+    """A read over GBSA_MAX_READ_LEN in a late chunk of a pipelined call, or in a
+    device-resident batch, fails the call with GBSA_ERR_READ_TOO_LONG; a device call with
+    too small a NAM capacity reports GBSA_ERR_CAPACITY and the total.  The same mapper
+    then maps the valid reads exactly as a fresh one."""
+    import torch
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=95))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=150_000, seed=96))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    want = native.Mapper(idx).map_reads(reads)
+    bad_len = abi.GBSA_MAX_READ_LEN + 1
+    seq = np.concatenate([reads.seq, np.full(bad_len, ord("A"), np.uint8)])
+    offs = reads.offsets.copy()
+    lens = reads.lengths.copy()
+    r = reads.n - 10   # in the last chunk
+    offs[r], lens[r] = len(reads.seq), bad_len
+    bad = synth.Reads(seq, offs, lens)
+    m = native.Mapper(idx)
+    m.set_pipeline(2)
+    with pytest.raises(native.GbsaError) as e:
+        m.map_reads(bad)
+    assert e.value.code == abi.GBSA_ERR_READ_TOO_LONG
+    got = m.map_reads(reads)
+    assert (got[1] == want[1]).all() and nams_equal(got[0], want[0])
+    # device-resident batch
+    dev = torch.device("cuda:0")
+    n = reads.n
+    d_seq = torch.from_numpy(bad.seq).to(dev)
+    d_off = torch.from_numpy(bad.offsets.view(np.int64)).to(dev)
+    d_len = torch.from_numpy(bad.lengths.view(np.int32)).to(dev)
+    cap = int(want[1][-1])
+    d_n = torch.empty(cap * 44, dtype=torch.uint8, device=dev)
+    d_o = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    with pytest.raises(native.GbsaError) as e:
+        m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_n.data_ptr(), cap, d_o.data_ptr())
+    assert e.value.code == abi.GBSA_ERR_READ_TOO_LONG
+    d_seq = torch.from_numpy(reads.seq).to(dev)
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).to(dev)
+    d_len = torch.from_numpy(reads.lengths.view(np.int32)).to(dev)
+    tot = m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_n.data_ptr(), cap // 2,
+                             d_o.data_ptr())
+    assert tot == cap
+    tot = m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_n.data_ptr(), cap,
+                             d_o.data_ptr())
+    torch.cuda.synchronize()
+    assert tot == cap
+    assert (d_o.cpu().numpy().view(np.uint64) == want[1]).all()
+    assert nams_equal(d_n.cpu().numpy().view(abi.NAM), want[0])
+
+
 def test_sector_count_and_gather_bench():
     """The lookup's sector form lies between one sector per query (the bucket bounds)
     and one per 16 B counted plus two per query; the gather benchmark reports a
