@@ -420,8 +420,10 @@ constexpr uint32_t kLaneMaxHits = 160;
 constexpr uint32_t kLaneOpen = 10;   // open NAMs a lane keeps in shared memory
 constexpr int kLaneWarps = 4;
 // The rescue chain runs beside the two NAM kernels on another stream; the persistent
-// grids are sized so that their shared memory fits one SM together: rescue 1 x 72 KB,
-// lane kernel 3 x 40 KB, warp kernel 4 x 32 KB.
+// grids are sized so that the rescue chain keeps room beside them: rescue 1 x 72 KB,
+// lane kernel 3 x 40 KB, then the warp kernel 5 x 32 KB (measured against 4, and against
+// 2-3 lane blocks: fewer main-stream blocks speed the rescue chain but slow the main
+// stream more).
 constexpr int kLaneBlocksPerSm = 3;
 constexpr int kRescueBlocksPerSm = 1;
 
@@ -833,7 +835,7 @@ __device__ __forceinline__ bool warp_find_nams(const HitRec* __restrict__ hits, 
 constexpr uint32_t kHeavyOpen = 256;   // open NAMs (and sort keys) a warp keeps in shared memory
 constexpr int kHeavyWarps = 4;
 constexpr int kHeavyBlocksPerSm = 5;   // register budget
-constexpr int kHeavyGridPerSm = 4;     // blocks launched per SM (32 KB each)
+constexpr int kHeavyGridPerSm = 5;     // blocks launched per SM (32 KB each)
 
 // find_nams for the reads the lane kernel passed on (many hits, or many NAMs open
 // at once): a warp per read.  The open list lives in shared memory (in global
