@@ -874,17 +874,45 @@ __global__ void __launch_bounds__(32 * kHeavyWarps, kHeavyBlocksPerSm)
         }
         const long long t_merge = clock64();
         __syncwarp();
-        NamKey* keys = NN <= kHeavyOpen ? reinterpret_cast<NamKey*>(s_open[w]) : reinterpret_cast<NamKey*>(closed + H);
-        for (uint32_t t = lane; t < NN; t += 32) keys[t] = nam_key(closed[t], t, C.sort_mode);
-        __syncwarp();
-        if (NN <= kHeavyOpen) warp_sort_keys(reinterpret_cast<NamKey*>(s_open[w]), NN);
-        else warp_sort_keys(reinterpret_cast<NamKey*>(closed + H), NN);
+        // sort: up to kHeavyOpen NAMs in the warp's shared open-list buffer (now free),
+        // moving only the first key word and the NAM index; more in global scratch
+        const bool small = NN <= kHeavyOpen;
+        uint32_t* order = nullptr;   // sorted NAM indices
+        NamKey* keys = reinterpret_cast<NamKey*>(closed + H);
+        if (small) {
+            static_assert(kHeavyOpen <= 256, "the sort entries fit the open-list buffer");
+            int32_t* so = s_open[w];
+            uint64_t* k1 = reinterpret_cast<uint64_t*>(so);         // 2 KB
+            uint32_t* ix = reinterpret_cast<uint32_t*>(so + 512);   // 1 KB
+            uint64_t* k2 = reinterpret_cast<uint64_t*>(so + 768);   // 2 KB
+            uint64_t* k3 = k2 + 256;                                // 2 KB
+            const uint32_t P = next_pow2(NN);
+            for (uint32_t t = lane; t < P; t += 32) {
+                NamKey k;
+                if (t < NN) {
+                    k = nam_key(closed[t], t, C.sort_mode);
+                } else {   // padding sorts last (a NAM's first key word is never all ones)
+                    k.k1 = k.k2 = k.k3 = ~0ULL;
+                }
+                k1[t] = k.k1;
+                ix[t] = t;
+                k2[t] = k.k2;
+                k3[t] = k.k3;
+            }
+            __syncwarp();
+            warp_sort_idx(k1, ix, k2, k3, P);
+            order = ix;
+        } else {
+            for (uint32_t t = lane; t < NN; t += 32) keys[t] = nam_key(closed[t], t, C.sort_mode);
+            __syncwarp();
+            warp_sort_keys(keys, NN);
+        }
         const uint64_t noff = warp_bump(&ctr->nam_used, NN);
         if (noff + NN > A.nam_cap) {
             warp_fail(R, ctr, kStatusNamOverflow);
             continue;
         }
-        for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = closed[keys[t].idx];
+        for (uint32_t t = lane; t < NN; t += 32) A.nams[noff + t] = closed[small ? order[t] : keys[t].idx];
         if (lane == 0) {
             R.nam_off = noff;
             R.n_nams = NN;
