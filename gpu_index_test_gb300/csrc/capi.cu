@@ -296,7 +296,7 @@ static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     }
     if (m.hit_cap < 2 * q_need) {
         m.hit_cap = 2 * q_need;
-        m.hits.resize(sizeof(HitRec) * m.hit_cap);
+        m.hits.resize(sizeof(HitPacked) * m.hit_cap);
     }
     if (m.nam_cap < q_need) {
         m.nam_cap = q_need;
@@ -322,7 +322,7 @@ static Arenas arenas_of(gbsa_mapper& m) {
     A.q_cap = m.q_cap;
     A.q_aux = m.qaux.as<uint32_t>();
     A.q_pos = m.qpos.as<uint64_t>();
-    A.hits = m.hits.as<HitRec>();
+    A.hits = m.hits.as<HitPacked>();
     A.hit_cap = m.hit_cap;
     A.nams = m.nams.as<NamState>();
     A.nam_cap = m.nam_cap;
@@ -489,7 +489,7 @@ static bool check_batch(gbsa_mapper& m, bool seeded) {
         retry = true;
     }
     if (h.status & kStatusHitOverflow) {
-        grow(m.hits, m.hit_cap, h.hit_used, sizeof(HitRec));
+        grow(m.hits, m.hit_cap, h.hit_used, sizeof(HitPacked));
         retry = true;
     }
     if (h.status & kStatusNamOverflow) {

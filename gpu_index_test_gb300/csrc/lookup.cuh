@@ -13,6 +13,24 @@ struct HitRec {
     int32_t qs, qe, rs, re;
 };
 
+// A hit as stored in the hit arena: 16 bytes, one vector load.  Query coordinates are
+// below GBSA_MAX_READ_LEN, so query start and end share a word.
+struct __align__(16) HitPacked {
+    uint32_t ref_rc;
+    uint32_t qse;    // query start | query end << 16
+    int32_t rs, re;
+};
+static_assert(GBSA_MAX_READ_LEN < 65536, "query coordinates fit 16 bits");
+
+__device__ __forceinline__ HitPacked pack_hit(uint32_t ref_rc, int qs, int qe, int rs, int re) {
+    HitPacked p;
+    p.ref_rc = ref_rc;
+    p.qse = (uint32_t)qs | ((uint32_t)qe << 16);
+    p.rs = rs;
+    p.re = re;
+    return p;
+}
+
 __device__ __forceinline__ uint64_t get_hash(const IndexView& I, uint64_t pos) {   // index.hpp:83-89
     return pos < I.n ? __ldg(&I.rs[pos].hash) : ~0ULL;
 }

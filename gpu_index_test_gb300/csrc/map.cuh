@@ -62,7 +62,7 @@ struct Arenas {
     uint64_t q_cap;
     uint32_t* q_aux;         // per query: hits emitted (lookup) / exclusive offset
     uint64_t* q_pos;         // per query: index position of its hash (or kNotFound)
-    HitRec* hits;
+    HitPacked* hits;
     uint64_t hit_cap;
     NamState* nams;          // per read, sorted (converted to Nam records on output)
     uint64_t nam_cap;

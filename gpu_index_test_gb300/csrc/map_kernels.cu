@@ -248,17 +248,11 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
         if (next == aux[i]) continue;
         const uint64_t pos = qp[i];
         const uint32_t dir = i >= nq ? 1u : 0u;
-        HitRec* out = A.hits + hoff + aux[i];
+        HitPacked* out = A.hits + hoff + aux[i];
         uint32_t k = 0;
         const int qs = (int)Q[i].start, qe = (int)Q[i].end;
         walk_hit_run(I, qs, qe, pos, [&](uint32_t ref, int rs, int re) {
-            HitRec h;
-            h.ref_rc = (dir << 31) | ref;
-            h.qs = qs;
-            h.qe = qe;
-            h.rs = rs;
-            h.re = re;
-            out[k++] = h;
+            out[k++] = pack_hit((dir << 31) | ref, qs, qe, rs, re);
         });
     }
     if (lane == 0) {
@@ -490,16 +484,17 @@ static_assert(sizeof(LaneOpen) == 8 * kLaneOpen * 32 * kLaneWarps * 4, "LaneOpen
 // creation order of its (orientation, ref id) that accepts it.  Open NAMs live in
 // shared memory; a NAM is closed (written to the read's slots in the NAM arena) when
 // the open list is full and the current query start has passed it, or at the end.
-// The read's NAMs are then insertion-sorted in place.  Reads that do not fit go to
-// the warp-cooperative kernel.
-__device__ __forceinline__ HitRec load_hit(const HitRec* __restrict__ hits, uint32_t i, uint32_t H) {
+// The read's NAMs are then sorted (through shared memory).  Reads that do not fit go
+// to the warp-cooperative kernel.
+__device__ __forceinline__ HitRec load_hit(const HitPacked* __restrict__ hits, uint32_t i, uint32_t H) {
     HitRec h;
     if (i < H) {
-        h.ref_rc = __ldg(&hits[i].ref_rc);
-        h.qs = __ldg(&hits[i].qs);
-        h.qe = __ldg(&hits[i].qe);
-        h.rs = __ldg(&hits[i].rs);
-        h.re = __ldg(&hits[i].re);
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(hits + i));
+        h.ref_rc = v.x;
+        h.qs = (int32_t)(v.y & 0xFFFFu);
+        h.qe = (int32_t)(v.y >> 16);
+        h.rs = (int32_t)v.z;
+        h.re = (int32_t)v.w;
     } else {
         h.ref_rc = 0;
         h.qs = h.qe = h.rs = h.re = -1;
@@ -566,7 +561,7 @@ __global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint
             atomicOr(&ctr->status, kStatusNamOverflow);
             continue;
         }
-        const HitRec* hits = A.hits + R.hit_off;
+        const HitPacked* hits = A.hits + R.hit_off;
         NamState* out = A.nams + noff;
         uint32_t n_open = 0, n_closed = 0, cur_dir = 0;
         bool overflow = false;
@@ -801,7 +796,7 @@ __device__ __forceinline__ bool soa_merge_hits(const OpenSoA& O, uint32_t nn, ui
 // Each query randstrobe's hits are loaded 32 at a time, one per lane, and the next
 // chunk is fetched while the current one merges.  Returns false when the open list
 // outgrew cap.
-__device__ __forceinline__ bool warp_find_nams(const HitRec* __restrict__ hits, uint32_t H, const OpenSoA& O,
+__device__ __forceinline__ bool warp_find_nams(const HitPacked* __restrict__ hits, uint32_t H, const OpenSoA& O,
                                                uint32_t cap, NamState* closed, uint32_t& n_closed) {
     const uint32_t lane = lane_id();
     uint32_t n_open = 0, cur_dir = 0;
@@ -855,7 +850,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps, kHeavyBlocksPerSm)
         if (R.flags & (kReadFailed | kReadRescue)) continue;
         const uint32_t H = R.n_hits;
         if (H == 0) continue;
-        const HitRec* hits = A.hits + R.hit_off;
+        const HitPacked* hits = A.hits + R.hit_off;
         const uint32_t P2 = next_pow2(H);
         const bool big = H > kHeavyOpen;
         uint8_t* sc = warp_scratch(A, ctr, 0, 32ull * H + (big ? 32ull * P2 : 0) + 64);

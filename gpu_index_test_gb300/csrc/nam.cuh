@@ -96,36 +96,6 @@ __device__ __forceinline__ void nam_close_passed(NamLists& L, int qs) {
     L.n_closed += done;
 }
 
-// Hit-major merge of the hits h[0..nh) of one query randstrobe (sorted by rs).
-__device__ __forceinline__ void nam_merge_hit_major(NamLists& L, const HitRec* h, uint32_t nh) {
-    const uint32_t lane = lane_id();
-    const uint32_t nn = L.n_open;   // NAMs made by this query cannot take its other hits
-    for (uint32_t j = 0; j < nh; ++j) {
-        const HitRec x = h[j];
-        int found = -1;
-        for (uint32_t base = 0; base < nn; base += 32) {
-            const uint32_t o = base + lane;
-            bool ok = false;
-            if (o < nn) {
-                const NamState& n = L.open[o];
-                ok = n.ref_rc == x.ref_rc && n.qprev < x.qs && x.qs <= n.qe && n.rprev < x.rs && x.rs <= n.re &&
-                     nam_takes(n, x);
-            }
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
-            if (m) {
-                found = (int)(base + __ffs(m) - 1);
-                break;
-            }
-        }
-        if (lane == 0) {
-            if (found >= 0) nam_add(L.open[found], x);
-            else L.open[L.n_open] = nam_from_hit(x);
-        }
-        if (found < 0) ++L.n_open;
-        __syncwarp();
-    }
-}
-
 // Hits of one query randstrobe in compact form: they share query_start, query_end
 // and orientation, so each hit is its ref_start and (ref id << 8 | ref span - k's
 // offset), i.e. the RefRandstrobe position and packed word.
