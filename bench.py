@@ -548,6 +548,48 @@ def main():
         torch.cuda.synchronize()
         pair_types = {"ms": round(e0.elapsed_time(e1) / 5, 4),
                       "counts": np.bincount(d_types.cpu().numpy(), minlength=5).tolist()}
+    # the first alignment step: seed extension (reverse_nam_if_needed + extend_seed_part)
+    # of each read's best NAM of the last batch, timed alone on the same stream
+    seed_ext, ext_in = None, None
+    if rank == 0 and total_nams > 0:
+        noff = d_noff.cpu().numpy()
+        cnt = np.diff(noff)
+        owners = np.nonzero(cnt > 0)[0].astype(np.uint32)
+        d_sel = torch.from_numpy(noff[:-1][cnt > 0].astype(np.int64)).to(dev)
+        d_best = d_nams[: int(noff[-1]) * 44].view(-1, 44).index_select(0, d_sel).contiguous()
+        d_own = torch.from_numpy(owners.view(np.int32)).to(dev)
+        d_ref = torch.from_numpy(g.seq).to(dev)
+        d_roff = torch.from_numpy(g.offsets.astype(np.uint64).view(np.int64)).to(dev)
+        d_rlen = torch.from_numpy(g.lengths.astype(np.uint64).view(np.int64)).to(dev)
+        n_ext = len(owners)
+        d_ext = torch.empty(n_ext * abi.SEED_ALIGNMENT.itemsize, dtype=torch.uint8, device=dev)
+        extend = lambda: native.extend_seeds_device(d_ref.data_ptr(), d_roff.data_ptr(), d_rlen.data_ptr(),
+                                                    len(g.lengths), d_seq.data_ptr(), d_off.data_ptr(),
+                                                    d_len.data_ptr(), n, d_best.data_ptr(), d_own.data_ptr(), n_ext,
+                                                    p.k, d_ext.data_ptr(), stream=stream.cuda_stream)
+        extend()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            extend()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_ext = e0.elapsed_time(e1) / 5
+        ext = d_ext.cpu().numpy().view(abi.SEED_ALIGNMENT)
+        # algorithmic bytes per NAM: the read and its projected reference window (L bytes
+        # each), the NAM (44 B), its read index (4 B) and the record out (36 B)
+        alg = int((2 * reads.lengths[owners].astype(np.int64) + 84).sum())
+        ext_peak, ext_peak_src = peaks()
+        achieved = alg / (ms_ext * 1e-3) / 1e9
+        seed_ext = {"nams": int(n_ext), "ms": round(ms_ext, 4), "nams_per_s": round(n_ext / (ms_ext * 1e-3), 1),
+                    "aligned_ungapped_frac": round(float(ext["done"].mean()), 4),
+                    "consistent_frac": round(float(ext["consistent"].mean()), 4),
+                    "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": round(ext_peak, 1),
+                                 "unit": "GB/s", "frac": round(achieved / ext_peak, 4), "peak_source": ext_peak_src,
+                                 "alg_bytes_per_launch": alg},
+                    "timing": "each call: the kernel and its 4-byte status read, 5 calls after one warm-up"}
+        ext_in = (d_best.cpu().numpy().view(abi.NAM).reshape(-1), owners, ext)
     nam_profile = None
     if len(nam_cyc):
         worst = nam_cyc[np.argsort(nam_cyc[:, 0])[-3:]]
@@ -661,6 +703,18 @@ def main():
     exact = None
     if not args.no_cpu_baseline:
         cpu, exact = cpu_baseline(g, reads, args.cpu_seconds, gpu_res)
+        if seed_ext is not None:
+            # the oracle on the first NAMs (one host thread), checked against the GPU records
+            from oracle import oracle_py
+            nb, ob, eb = ext_in
+            n_cpu = min(len(nb), 400000)
+            t0 = time.perf_counter()
+            ref_ext = oracle_py.extend_seeds(g.seq, g.offsets, g.lengths, reads.seq, reads.offsets, reads.lengths,
+                                             nb[:n_cpu], ob[:n_cpu], p.k)
+            cpu_s = time.perf_counter() - t0
+            seed_ext["cpu_baseline"] = {"value": round(n_cpu / cpu_s, 1), "unit": "NAMs/s", "cores": 1,
+                                        "kind": "port", "sample": f"the first {n_cpu} NAMs"}
+            seed_ext["bit_exact_vs_cpu_sample"] = bool((ref_ext == eb[:n_cpu]).all())
 
     line = {
         "metric": "reads/s seed+lookup+NAM", "value": round(value, 1), "unit": "reads/s", "n_gpus": world,
@@ -681,7 +735,7 @@ def main():
         "clocks": clocks,
         "gpu_launches": int(launches),
         "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile, nam_profile=nam_profile,
-                     pair_types=pair_types),
+                     pair_types=pair_types, seed_extension=seed_ext),
     }
     print(json.dumps(line))
     if world > 1:

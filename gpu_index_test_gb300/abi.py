@@ -96,6 +96,22 @@ assert REF_RANDSTROBE.itemsize == 16 and QUERY_RANDSTROBE.itemsize == 24 and NAM
 NAM_PAIR = np.dtype([("score", "<i4"), ("i1", "<i4"), ("i2", "<i4")])
 GBSA_NAM_PAIRS_TOP_K = 40
 
+# gbsa_align_params (AlignmentParameters, step2/aligner.hpp:11-18) and its command-line
+# defaults -A 2 -B 8 -O 12 -E 1 --end-bonus 10 (step2/cmdline.hpp:46-50).
+ALIGN_PARAMS = np.dtype([("match", "<i4"), ("mismatch", "<i4"), ("gap_open", "<i4"), ("gap_extend", "<i4"),
+                         ("end_bonus", "<i4")])
+DEFAULT_ALIGN = (2, 8, 12, 1, 10)
+
+# gbsa_seed_alignment: one NAM's seed extension.
+SEED_ALIGNMENT = np.dtype([("ref_id", "<i4"), ("ref_start", "<i4"), ("edit_distance", "<i4"), ("global_ed", "<i4"),
+                           ("score", "<i4"), ("length", "<i4"), ("query_start", "<i4"), ("query_end", "<i4"),
+                           ("is_rc", "u1"), ("done", "u1"), ("consistent", "u1"), ("_pad", "u1")])
+assert SEED_ALIGNMENT.itemsize == 36 and ALIGN_PARAMS.itemsize == 20
+
+
+def align_params(match=2, mismatch=8, gap_open=12, gap_extend=1, end_bonus=10):
+    return np.array([(match, mismatch, gap_open, gap_extend, end_bonus)], ALIGN_PARAMS)
+
 # Fields of a NAM that results are compared on (nam_id and the two prev-hit
 # positions are internal to the merge).
 NAM_COMPARED = ("ref_id", "query_start", "query_end", "ref_start", "ref_end", "n_hits", "score", "is_rc")

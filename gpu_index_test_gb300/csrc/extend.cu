@@ -1,0 +1,184 @@
+// extend.cu — seed extension of NAMs, the first step of the reference's alignment
+// kernels (align_PE_part1..4, step2/main.cu:1876-2165): reverse_nam_if_needed
+// (main.cu:759-793), then extend_seed_part (main.cu:582-643) with my_hamming_align
+// (main.cu:506-580).
+//
+// A thread per NAM.  The NAM's two k-mer checks come first.  Then one pass over the
+// read and its projected reference window counts the Hamming distance and runs the
+// best-segment scan together; the reference runs the scan only when the distance
+// admits the ungapped path, and its result is kept only then.  The reference's
+// distance loop stops once the count exceeds the limit, so its count is
+// min(mismatches, limit + 1).  The mismatches inside the best segment come from the
+// running mismatch count at the segment's two ends, so the read is walked once.
+#include "runtime.h"
+
+namespace gbsa {
+namespace {
+
+// revcomp_table (step2/main.cu:1832-1849): A/C/G/T/U in either case to the upper-case
+// complement, every other byte to 'N'.  c & 0xDF equals one of these letters only for
+// that letter in either case.  (The reference indexes its table with a signed char, so
+// bytes of 128 and above read outside it; here they give 'N'.)
+__device__ __forceinline__ uint8_t revcomp_base(uint8_t c) {
+    switch (c & 0xDF) {
+        case 'A': return 'T';
+        case 'C': return 'G';
+        case 'G': return 'C';
+        case 'T':
+        case 'U': return 'A';
+        default: return 'N';
+    }
+}
+
+// The read in one orientation: the reverse complement is read backwards through the
+// table, as the reference's rc copy (main.cu:1893-1900).
+struct ReadView {
+    const uint8_t* fwd;
+    int L;
+    bool rc;
+    __device__ __forceinline__ uint8_t at(int j) const {
+        return rc ? revcomp_base(__ldg(fwd + (L - 1 - j))) : __ldg(fwd + j);
+    }
+};
+
+__device__ __forceinline__ bool kmer_equal(const uint8_t* ref, const ReadView& q, int qpos, int k) {
+    for (int t = 0; t < k; ++t)
+        if (__ldg(ref + t) != q.at(qpos + t)) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(128)
+    k_extend_seeds(const uint8_t* __restrict__ ref_seqs, const uint64_t* __restrict__ ref_offs,
+                   const uint64_t* __restrict__ ref_lens, uint32_t n_refs, const uint8_t* __restrict__ read_seqs,
+                   const uint64_t* __restrict__ read_offs, const uint32_t* __restrict__ read_lens, uint32_t n_reads,
+                   const gbsa_nam* __restrict__ nams, const uint32_t* __restrict__ nam_reads, uint64_t n, int k,
+                   gbsa_align_params ap, gbsa_seed_alignment* __restrict__ out, unsigned int* bad) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        gbsa_nam nam = nams[i];
+        gbsa_seed_alignment o;
+        o.ref_id = o.ref_start = o.edit_distance = o.global_ed = o.score = o.length = 0;
+        o.query_start = o.query_end = 0;
+        o.is_rc = o.done = o.consistent = o._pad = 0;
+        const uint32_t r = nam_reads[i];
+        bool ok = r < n_reads && nam.ref_id >= 0 && (uint32_t)nam.ref_id < n_refs;
+        int L = 0, rlen = 0;
+        if (ok) {
+            L = (int)read_lens[r];
+            rlen = (int)ref_lens[nam.ref_id];
+            // every k-mer the checks compare then lies inside its sequence
+            ok = nam.query_start >= 0 && nam.query_end <= L && nam.query_end - nam.query_start >= k &&
+                 nam.ref_start >= 0 && nam.ref_end <= rlen && nam.ref_end - nam.ref_start >= k;
+        }
+        if (!ok) {
+            atomicAdd(bad, 1u);
+            out[i] = o;
+            continue;
+        }
+        const uint8_t* fwd = read_seqs + read_offs[r];
+        const uint8_t* ref = ref_seqs + ref_offs[nam.ref_id];
+        // reverse_nam_if_needed (step2/main.cu:759-793)
+        bool consistent = kmer_equal(ref + nam.ref_start, ReadView{fwd, L, nam.is_rc != 0}, nam.query_start, k) &&
+                          kmer_equal(ref + nam.ref_end - k, ReadView{fwd, L, nam.is_rc != 0}, nam.query_end - k, k);
+        if (!consistent) {
+            const int qs2 = L - nam.query_end, qe2 = L - nam.query_start;
+            const ReadView other{fwd, L, nam.is_rc == 0};
+            if (kmer_equal(ref + nam.ref_start, other, qs2, k) && kmer_equal(ref + nam.ref_end - k, other, qe2 - k, k)) {
+                nam.is_rc = nam.is_rc ? 0 : 1;
+                nam.query_start = qs2;
+                nam.query_end = qe2;
+                consistent = true;
+            }
+        }
+        o.ref_id = nam.ref_id;
+        o.query_start = nam.query_start;
+        o.query_end = nam.query_end;
+        o.is_rc = nam.is_rc;
+        o.consistent = consistent ? 1 : 0;
+        // extend_seed_part (step2/main.cu:582-643)
+        const int pstart = max(0, nam.ref_start - nam.query_start);
+        const int pend = min(nam.ref_end + L - nam.query_end, rlen);
+        if (pend - pstart == L && consistent) {
+            const ReadView q{fwd, L, nam.is_rc != 0};
+            const uint8_t* segm = ref + pstart;
+            const int limit_error = (int)(L * 0.05);
+            int total_mm = 0;
+            // my_hamming_align's scan (main.cu:518-538), with the mismatch count at the
+            // current segment start (cm_start) and at the best segment's ends
+            int start = 0, score = ap.end_bonus, best_start = 0, best_end = 0, best_score = 0;
+            int cm_start = 0, best_cm_start = 0, best_cm_end = 0;
+            for (int j = 0; j < L; ++j) {
+                const bool mm = q.at(j) != __ldg(segm + j);
+                total_mm += mm ? 1 : 0;
+                score += mm ? -ap.mismatch : ap.match;
+                if (score < 0) {
+                    start = j + 1;
+                    score = 0;
+                    cm_start = total_mm;
+                }
+                if (score > best_score) {
+                    best_start = start;
+                    best_score = score;
+                    best_end = j + 1;
+                    best_cm_start = cm_start;
+                    best_cm_end = total_mm;
+                }
+            }
+            if (score + ap.end_bonus > best_score) {
+                best_score = score + ap.end_bonus;
+                best_end = L;
+                best_start = start;
+                best_cm_start = cm_start;
+                best_cm_end = total_mm;
+            }
+            const int hamming_dist = min(total_mm, limit_error + 1);
+            if (hamming_dist >= 0 && ((float)hamming_dist / L) < 0.05) {
+                o.done = 1;
+                o.edit_distance = best_cm_end - best_cm_start;
+                o.global_ed = o.edit_distance + best_start + (L - best_end);
+                o.score = best_score;
+                o.ref_start = pstart + best_start;
+                o.length = best_end - best_start;
+            }
+        }
+        out[i] = o;
+    }
+}
+
+}  // namespace
+}  // namespace gbsa
+
+using namespace gbsa;
+
+extern "C" int gbsa_extend_seeds_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                                        const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                                        const uint64_t* d_read_offsets, const uint32_t* d_read_lengths,
+                                        uint32_t n_reads, const gbsa_nam* d_nams, const uint32_t* d_nam_reads,
+                                        uint64_t n_nams, int k, const gbsa_align_params* params,
+                                        gbsa_seed_alignment* d_out, void* stream) {
+    try {
+        if (!params) throw Error(GBSA_ERR_PARAM, "params must not be null");
+        if (k < 1) throw Error(GBSA_ERR_PARAM, "k must be at least 1");
+        if (n_nams == 0) return GBSA_OK;
+        cudaStream_t st = (cudaStream_t)stream;
+        DeviceBuffer bad(sizeof(unsigned int));
+        GBSA_CUDA(cudaMemsetAsync(bad.as<void>(), 0, sizeof(unsigned int), st));
+        k_extend_seeds<<<grid_for(n_nams, 128, (unsigned)device_sm_count() * 16), 128, 0, st>>>(
+            d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets, d_read_lengths, n_reads,
+            d_nams, d_nam_reads, n_nams, k, *params, d_out, bad.as<unsigned int>());
+        GBSA_LAUNCHED();
+        unsigned int h_bad = 0;
+        GBSA_CUDA(cudaMemcpyAsync(&h_bad, bad.as<void>(), sizeof h_bad, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        if (h_bad)
+            throw Error(GBSA_ERR_PARAM, std::to_string(h_bad) +
+                                            " NAM(s) name a read or contig out of range or leave their read or contig");
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}

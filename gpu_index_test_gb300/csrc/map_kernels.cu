@@ -9,6 +9,8 @@
 //                               (step2/nam.cu:515-539, 347-513) + NAM sort
 //   k_rescue                    find_nams_rescue (step2/nam.cu:927-985) + NAM sort
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include <cooperative_groups.h>
 
@@ -1643,9 +1645,8 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
-    k_nams_lane<<<grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSm), 32 * kLaneWarps, 0,
-                  st>>>(C, n, rec,
-                                                                                                        A, ctr);
+    const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSm);
+    k_nams_lane<<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
@@ -1677,12 +1678,22 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
     constexpr int kSmall = 256;
     constexpr size_t smem = kSortTile * 28;
-    static bool attr = false;
-    if (!attr) {
-        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-        GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
+    {
+        // the kernels' dynamic shared-memory limit, set once per device (mappers may
+        // launch from several threads at once)
+        static std::mutex mu;
+        static std::vector<char> done;
+        int dev = 0;
+        GBSA_CUDA(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> g(mu);
+        if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+        if (!done[dev]) {
+            GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+            done[dev] = 1;
+        }
     }
     const unsigned sms = (unsigned)device_sm_count();
     k_sort_jobs<kSmall, kSortTile><<<sms * 4, kSmall, smem, st>>>(C, rec, A, ctr);

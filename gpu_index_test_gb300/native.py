@@ -65,6 +65,7 @@ def lib():
             "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
             "gbsa_nam_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, u32, vp, vp, vp]),
+            "gbsa_extend_seeds_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, i32, vp, vp, vp]),
             "gbsa_server_create": (i32, [vp, vp, u32, u32, u64, vp]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
@@ -142,6 +143,17 @@ def nam_pairs_device(d_nams, d_nam_offsets, n_pairs, d_pairs, d_counts, layout=0
     per pair into d_pairs and their count into d_counts.  Device addresses."""
     _check(lib().gbsa_nam_pairs_device(d_nams, d_nam_offsets, n_pairs, layout, mu, sigma, max_tries, d_pairs,
                                        d_counts, stream))
+
+
+def extend_seeds_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets,
+                        d_read_lengths, n_reads, d_nams, d_nam_reads, n_nams, k, d_out, params=None, stream=None):
+    """Seed extension of NAMs (reverse_nam_if_needed + extend_seed_part): one
+    gbsa_seed_alignment per NAM into d_out.  Device addresses; params is an
+    abi.ALIGN_PARAMS record (host), the reference's defaults when None."""
+    p = abi.align_params() if params is None else np.ascontiguousarray(params, abi.ALIGN_PARAMS)
+    _check(lib().gbsa_extend_seeds_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs,
+                                          d_read_offsets, d_read_lengths, n_reads, d_nams, d_nam_reads, n_nams, k,
+                                          p.ctypes.data, d_out, stream))
 
 
 def _u8(a):

@@ -329,6 +329,56 @@ int gbsa_nam_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets,
                           float mu, float sigma, uint32_t max_tries, gbsa_nam_pair* d_pairs, uint32_t* d_counts,
                           void* stream);
 
+/* AlignmentParameters (step2/aligner.hpp:11-18): match is a score, the others are
+ * penalties (all nonnegative). */
+typedef struct gbsa_align_params {
+    int32_t match;
+    int32_t mismatch;
+    int32_t gap_open;
+    int32_t gap_extend;
+    int32_t end_bonus;
+} gbsa_align_params;
+
+/* One NAM's seed extension: GPUAlignment (step2/main.cu:418-444) plus the NAM's
+ * orientation and query interval after reverse_nam_if_needed and the done_align tag. */
+typedef struct gbsa_seed_alignment {
+    int32_t ref_id;         /* the NAM's contig */
+    int32_t ref_start;      /* alignment start on the reference */
+    int32_t edit_distance;  /* mismatches inside the aligned segment */
+    int32_t global_ed;      /* edit_distance + soft-clipped bases */
+    int32_t score;
+    int32_t length;         /* reference span of the aligned segment */
+    int32_t query_start;    /* the NAM after reverse_nam_if_needed */
+    int32_t query_end;
+    uint8_t is_rc;          /* the NAM's (and the alignment's) orientation after reverse_nam_if_needed */
+    uint8_t done;           /* done_align: 1 when the ungapped path aligned the NAM; 0 when a gapped
+                               aligner must (ref_start, edit_distance, global_ed, score and length
+                               are then zero) */
+    uint8_t consistent;     /* reverse_nam_if_needed's answer */
+    uint8_t _pad;
+} gbsa_seed_alignment;
+
+/* Seed extension of NAMs (the first alignment step of align_PE_part1..4): for NAM i,
+ * of read nam_reads[i], reverse_nam_if_needed (step2/main.cu:759-793: the k-mers at
+ * both NAM ends must match the reference, else the NAM is tried in the other
+ * orientation) and extend_seed_part (main.cu:582-643: when the NAM projected over the
+ * whole read fits the contig and is consistent, a Hamming distance below 5% of the
+ * read length admits my_hamming_align, main.cu:506-580, the best-scoring ungapped
+ * segment with end bonuses; otherwise the NAM is left to a gapped aligner).  The
+ * reference also builds a CIGAR for the ungapped segment and then drops it; none is
+ * returned.  Device pointers: contigs ref_seqs[ref_offsets[j] ..][ref_lengths[j]]
+ * (bytes as loaded), reads read_seqs[read_offsets[r] ..][read_lengths[r]] (bytes as
+ * given), NAMs as returned by the mapping entry points.  A NAM whose read or
+ * contig index is out of range, or whose coordinates leave its read or contig,
+ * fails the call (GBSA_ERR_PARAM) after the launch; the call synchronizes stream.
+ * No reference C entry point: the reference runs these steps inside its alignment
+ * kernels gpu_align_PE0..4 (main.cu:3583-3899). */
+int gbsa_extend_seeds_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                             const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                             const uint64_t* d_read_offsets, const uint32_t* d_read_lengths, uint32_t n_reads,
+                             const gbsa_nam* d_nams, const uint32_t* d_nam_reads, uint64_t n_nams, int k,
+                             const gbsa_align_params* params, gbsa_seed_alignment* d_out, void* stream);
+
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later
  * calls; gbsa_mapper_last_alg_bytes returns the count of the last batch.  No

@@ -33,6 +33,7 @@
 #include <limits>
 #include <thread>
 #include <unordered_map>
+#include <string>
 #include <vector>
 
 namespace {
@@ -1159,6 +1160,126 @@ int oracle_algorithmic_bytes(const oracle_index* h, const gbsa_map_options* opt,
     uint64_t tot = 0;
     for (auto x : per) tot += x;
     *bytes_out = tot;
+    return GBSA_OK;
+}
+
+}  // extern "C"
+
+// ---- seed extension (the first step of the alignment kernels) ------------------------
+
+// revcomp_table (step2/main.cu:1832-1849): A/C/G/T/U in either case to the upper-case
+// complement, every other byte to 'N'.
+static char revcomp_char(unsigned char c) {
+    switch (c) {
+        case 'A': case 'a': return 'T';
+        case 'C': case 'c': return 'G';
+        case 'G': case 'g': return 'C';
+        case 'T': case 't': case 'U': case 'u': return 'A';
+        default: return 'N';
+    }
+}
+
+// my_hamming_align (step2/main.cu:506-580): the best-scoring segment of an ungapped
+// alignment of query and ref (equal lengths n), with the end bonus at both ends; the
+// CIGAR it also builds is not kept by its caller.
+struct HammingAln {
+    int sw_score = 0, edit_distance = 0, ref_start = 0, ref_end = 0, query_start = 0, query_end = 0;
+};
+static HammingAln hamming_align(const char* query, const char* ref, int n, int match, int mismatch, int end_bonus) {
+    HammingAln a;
+    int start = 0, score = end_bonus, best_start = 0, best_end = 0, best_score = 0;
+    for (int i = 0; i < n; ++i) {
+        score += query[i] == ref[i] ? match : -mismatch;
+        if (score < 0) {
+            start = i + 1;
+            score = 0;
+        }
+        if (score > best_score) {
+            best_start = start;
+            best_score = score;
+            best_end = i + 1;
+        }
+    }
+    if (score + end_bonus > best_score) {
+        best_score = score + end_bonus;
+        best_end = n;
+        best_start = start;
+    }
+    int mismatches = 0;
+    for (int i = best_start; i < best_end; ++i) mismatches += query[i] == ref[i] ? 0 : 1;
+    a.sw_score = best_score;
+    a.edit_distance = mismatches;
+    a.ref_start = a.query_start = best_start;
+    a.ref_end = a.query_end = best_end;
+    return a;
+}
+
+static bool same_bytes(const char* a, const char* b, int n) { return std::memcmp(a, b, (size_t)n) == 0; }
+
+extern "C" {
+
+int oracle_extend_seeds(const char* ref_seqs, const uint64_t* ref_offsets, const uint64_t* ref_lengths,
+                        uint32_t n_refs, const char* read_seqs, const uint64_t* read_offsets,
+                        const uint32_t* read_lengths, uint32_t n_reads, const gbsa_nam* nams,
+                        const uint32_t* nam_reads, uint64_t n_nams, int k, const gbsa_align_params* ap,
+                        gbsa_seed_alignment* out) {
+    std::string rc;
+    for (uint64_t i = 0; i < n_nams; ++i) {
+        gbsa_nam nam = nams[i];
+        const uint32_t r = nam_reads[i];
+        if (r >= n_reads || nam.ref_id < 0 || (uint32_t)nam.ref_id >= n_refs) return GBSA_ERR_PARAM;
+        const int L = (int)read_lengths[r];
+        const int rlen = (int)ref_lengths[nam.ref_id];
+        if (nam.query_start < 0 || nam.query_end > L || nam.query_end - nam.query_start < k || nam.ref_start < 0 ||
+            nam.ref_end > rlen || nam.ref_end - nam.ref_start < k)
+            return GBSA_ERR_PARAM;
+        const char* fwd = read_seqs + read_offsets[r];
+        const char* ref = ref_seqs + ref_offsets[nam.ref_id];
+        rc.resize((size_t)L);
+        for (int j = 0; j < L; ++j) rc[(size_t)j] = revcomp_char((unsigned char)fwd[L - 1 - j]);
+        // reverse_nam_if_needed (step2/main.cu:759-793); the checks above keep every
+        // k-mer inside its sequence, so each substr is k bases long
+        const char* seq = nam.is_rc ? rc.data() : fwd;
+        const char* seq_rc = nam.is_rc ? fwd : rc.data();
+        bool consistent = same_bytes(ref + nam.ref_start, seq + nam.query_start, k) &&
+                          same_bytes(ref + nam.ref_end - k, seq + nam.query_end - k, k);
+        if (!consistent) {
+            const int qs2 = L - nam.query_end, qe2 = L - nam.query_start;
+            if (same_bytes(ref + nam.ref_start, seq_rc + qs2, k) && same_bytes(ref + nam.ref_end - k, seq_rc + qe2 - k, k)) {
+                nam.is_rc = nam.is_rc ? 0 : 1;
+                nam.query_start = qs2;
+                nam.query_end = qe2;
+                consistent = true;
+            }
+        }
+        // extend_seed_part (step2/main.cu:582-643)
+        gbsa_seed_alignment& o = out[i];
+        std::memset(&o, 0, sizeof o);
+        o.ref_id = nam.ref_id;
+        o.query_start = nam.query_start;
+        o.query_end = nam.query_end;
+        o.is_rc = nam.is_rc;
+        o.consistent = consistent ? 1 : 0;
+        const char* query = nam.is_rc ? rc.data() : fwd;
+        const int pstart = std::max(0, nam.ref_start - nam.query_start);
+        const int pend = std::min(nam.ref_end + L - nam.query_end, rlen);
+        if (pend - pstart == L && consistent) {
+            const char* segm = ref + pstart;
+            int hd = 0;
+            const int limit_error = (int)(L * 0.05);
+            for (int j = 0; j < L && hd <= limit_error; ++j)
+                if (query[j] != segm[j]) ++hd;
+            if (hd >= 0 && ((float)hd / L) < 0.05) {
+                const HammingAln a = hamming_align(query, segm, L, ap->match, ap->mismatch, ap->end_bonus);
+                o.done = 1;
+                o.edit_distance = a.edit_distance;
+                o.global_ed = a.edit_distance + a.query_start + (L - a.query_end);
+                o.score = a.sw_score;
+                o.ref_start = pstart + a.ref_start;
+                o.length = a.ref_end - a.ref_start;
+            }
+        }
+    }
     return GBSA_OK;
 }
 

@@ -66,6 +66,15 @@ int oracle_classify_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_
 int oracle_nam_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout, float mu,
                      float sigma, uint32_t max_tries, gbsa_nam_pair* out, uint32_t* counts);
 
+/* reverse_nam_if_needed + extend_seed_part (step2/main.cu:759-793, 582-643, 506-580)
+ * for each NAM; host pointers, same contract as gbsa_extend_seeds_device.  Returns
+ * GBSA_OK or GBSA_ERR_PARAM. */
+int oracle_extend_seeds(const char* ref_seqs, const uint64_t* ref_offsets, const uint64_t* ref_lengths,
+                        uint32_t n_refs, const char* read_seqs, const uint64_t* read_offsets,
+                        const uint32_t* read_lengths, uint32_t n_reads, const gbsa_nam* nams,
+                        const uint32_t* nam_reads, uint64_t n_nams, int k, const gbsa_align_params* ap,
+                        gbsa_seed_alignment* out);
+
 /* Whole path for a batch of reads with n_threads host threads (0 = all cores).
  * Same contract as gbsa_map_reads.  Returns GBSA_OK or GBSA_ERR_CAPACITY. */
 int oracle_map_reads(const oracle_index* idx, const gbsa_map_options* opt, const char* seqs,

@@ -63,6 +63,9 @@ def lib():
         L.oracle_nam_pairs.restype = C.c_int
         L.oracle_nam_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_float,
                                        C.c_uint32, C.c_void_p, C.c_void_p]
+        vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
+        L.oracle_extend_seeds.restype = C.c_int
+        L.oracle_extend_seeds.argtypes = [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, C.c_int, vp, vp]
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -231,3 +234,25 @@ def nam_pairs(nams, offsets, n_pairs, layout=abi.GBSA_PAIRS_INTERLEAVED, mu=300.
     assert lib().oracle_nam_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, mu, sigma,
                                   max_tries, out.ctypes.data, cnt.ctypes.data) == 0
     return out[:n_pairs], cnt[:n_pairs]
+
+
+def extend_seeds(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, nams, nam_reads, k,
+                 params=None):
+    """reverse_nam_if_needed + extend_seed_part restated: one abi.SEED_ALIGNMENT record
+    per NAM.  Raises ValueError for a NAM outside its read or contig."""
+    rs = np.ascontiguousarray(ref_seqs, np.uint8)
+    ro = np.ascontiguousarray(ref_offsets, np.uint64)
+    rl = np.ascontiguousarray(ref_lengths, np.uint64)
+    qs = np.ascontiguousarray(read_seqs, np.uint8)
+    qo = np.ascontiguousarray(read_offsets, np.uint64)
+    ql = np.ascontiguousarray(read_lengths, np.uint32)
+    a = np.ascontiguousarray(nams)
+    nr = np.ascontiguousarray(nam_reads, np.uint32)
+    p = abi.align_params() if params is None else np.ascontiguousarray(params, abi.ALIGN_PARAMS)
+    out = np.zeros(max(1, len(a)), abi.SEED_ALIGNMENT)
+    rc = lib().oracle_extend_seeds(rs.ctypes.data, ro.ctypes.data, rl.ctypes.data, len(rl), qs.ctypes.data,
+                                   qo.ctypes.data, ql.ctypes.data, len(ql), a.ctypes.data if len(a) else None,
+                                   nr.ctypes.data if len(nr) else None, len(a), k, p.ctypes.data, out.ctypes.data)
+    if rc != 0:
+        raise ValueError("a NAM names a read or contig out of range or leaves its read or contig")
+    return out[:len(a)]

@@ -1,0 +1,281 @@
+"""Seed extension of NAMs: reverse_nam_if_needed + extend_seed_part (step2/main.cu:759-793,
+582-643) with my_hamming_align (main.cu:506-580).
+
+The CPU tests check the oracle (C++) against a second, line-by-line Python restatement
+of the reference on small cases, including the edge cases the reference's code has:
+a NAM whose orientation is wrong (a false reverse hit), k-mers that match in neither
+orientation, a read overhanging its contig, the 5% Hamming limit on both sides, N and
+lower-case bases, and NAMs outside their read or contig.  The GPU tests compare
+gbsa_extend_seeds_device with the oracle on NAMs from the mapper and on altered ones."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "oracle"))
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), ".."))
+
+from gpu_index_test_gb300 import abi  # noqa: E402
+import oracle_py  # noqa: E402
+
+K = 20
+_RC = {ord(a): ord(b) for a, b in zip("ACGTUacgtu", "TGCAATGCAA")}
+
+
+def _revcomp(b: bytes) -> bytes:
+    """The reads' rc copy (main.cu:1893-1900) through revcomp_table (main.cu:1832-1849)."""
+    return bytes(_RC.get(c, ord("N")) for c in reversed(b))
+
+
+def _py_extend(ref: bytes, read: bytes, nam, k=K, match=2, mismatch=8, end_bonus=10):
+    """The reference's two functions restated in plain Python (small cases only)."""
+    L = len(read)
+    rc = _revcomp(read)
+    is_rc, qs, qe = int(nam["is_rc"]), int(nam["query_start"]), int(nam["query_end"])
+    rs, re_ = int(nam["ref_start"]), int(nam["ref_end"])
+    # reverse_nam_if_needed
+    seq, seq_rc = (rc, read) if is_rc else (read, rc)
+    ok = ref[rs:rs + k] == seq[qs:qs + k] and ref[re_ - k:re_] == seq[qe - k:qe]
+    if not ok:
+        qs2, qe2 = L - qe, L - qs
+        if ref[rs:rs + k] == seq_rc[qs2:qs2 + k] and ref[re_ - k:re_] == seq_rc[qe2 - k:qe2]:
+            is_rc, qs, qe, ok = 1 - is_rc, qs2, qe2, True
+    out = dict(ref_id=int(nam["ref_id"]), ref_start=0, edit_distance=0, global_ed=0, score=0, length=0,
+               query_start=qs, query_end=qe, is_rc=is_rc, done=0, consistent=int(ok))
+    # extend_seed_part
+    query = rc if is_rc else read
+    pstart = max(0, rs - qs)
+    pend = min(re_ + L - qe, len(ref))
+    if pend - pstart == L and ok:
+        segm = ref[pstart:pstart + L]
+        hd, limit, i = 0, int(L * 0.05), 0
+        while i < L and hd <= limit:
+            hd += query[i] != segm[i]
+            i += 1
+        if float(np.float32(hd) / np.float32(L)) < 0.05:   # (float) hd / size, compared in double
+            # my_hamming_align
+            start, score, best_start, best_end, best_score = 0, end_bonus, 0, 0, 0
+            for i in range(L):
+                score += match if query[i] == segm[i] else -mismatch
+                if score < 0:
+                    start, score = i + 1, 0
+                if score > best_score:
+                    best_start, best_score, best_end = start, score, i + 1
+            if score + end_bonus > best_score:
+                best_score, best_end, best_start = score + end_bonus, L, start
+            mm = sum(query[i] != segm[i] for i in range(best_start, best_end))
+            out.update(done=1, edit_distance=mm, global_ed=mm + best_start + (L - best_end), score=best_score,
+                       ref_start=pstart + best_start, length=best_end - best_start)
+    return out
+
+
+def _nam(qs, qe, rs, re_, is_rc=0, ref_id=0):
+    n = np.zeros(1, abi.NAM)
+    n["query_start"], n["query_end"], n["ref_start"], n["ref_end"] = qs, qe, rs, re_
+    n["is_rc"], n["ref_id"] = is_rc, ref_id
+    return n[0]
+
+
+def _oracle_one(ref: bytes, read: bytes, nam, **kw):
+    params = abi.align_params(**kw) if kw else None
+    return oracle_py.extend_seeds(np.frombuffer(ref, np.uint8), [0], [len(ref)], np.frombuffer(read, np.uint8), [0],
+                                  [len(read)], np.array([nam]), [0], K, params)[0]
+
+
+def _same(rec, py):
+    for f, v in py.items():
+        assert int(rec[f]) == v, (f, int(rec[f]), v)
+
+
+def _genome(n, seed):
+    return np.random.default_rng(seed).choice(np.frombuffer(b"ACGT", np.uint8), n).tobytes()
+
+
+def test_exact_and_single_mismatch_cases():
+    ref = _genome(400, 1)
+    read = ref[100:250]
+    got = _oracle_one(ref, read, _nam(10, 140, 110, 240))
+    assert got["done"] == 1 and got["consistent"] == 1
+    assert (got["score"], got["ref_start"], got["length"], got["edit_distance"]) == (150 * 2 + 20, 100, 150, 0)
+    # one mismatch in the middle costs match + mismatch; one at the last base is soft-clipped
+    mid = bytearray(read)
+    mid[75] = ord("A") if mid[75] != ord("A") else ord("C")
+    got = _oracle_one(ref, bytes(mid), _nam(10, 60, 110, 160))
+    assert (got["score"], got["edit_distance"], got["global_ed"]) == (149 * 2 - 8 + 20, 1, 1)
+    end = bytearray(read)
+    end[149] = ord("A") if end[149] != ord("A") else ord("C")
+    got = _oracle_one(ref, bytes(end), _nam(10, 60, 110, 160))
+    _same(got, _py_extend(ref, bytes(end), _nam(10, 60, 110, 160)))
+    assert got["done"] == 1
+
+
+def test_false_reverse_nam_is_flipped():
+    """A NAM given in the wrong orientation is turned around when its k-mers match
+    the other strand (main.cu:779-790)."""
+    ref = _genome(500, 2)
+    read = _revcomp(ref[200:350])             # the read comes from the reverse strand
+    nam = _nam(150 - 140, 150 - 10, 210, 340, is_rc=0)   # coordinates of the forward view, orientation wrong
+    got = _oracle_one(ref, read, nam)
+    _same(got, _py_extend(ref, read, nam))
+    assert got["is_rc"] == 1 and got["consistent"] == 1 and got["done"] == 1
+    assert (got["query_start"], got["query_end"]) == (10, 140) and got["ref_start"] == 200
+
+
+def test_inconsistent_and_overhanging_nams_are_left_to_a_gapped_aligner():
+    ref = _genome(500, 3)
+    read = ref[100:250]
+    other = _genome(150, 4)
+    got = _oracle_one(ref, other, _nam(10, 140, 110, 240))
+    assert (got["consistent"], got["done"]) == (0, 0)
+    # the read projected over the contig start: [pstart, pend) is shorter than the read
+    read0 = _genome(30, 5) + ref[0:120]
+    nam = _nam(30, 150, 0, 120)
+    got = _oracle_one(ref, read0, nam)
+    _same(got, _py_extend(ref, read0, nam))
+    assert got["consistent"] == 1 and got["done"] == 0
+
+
+@pytest.mark.parametrize("n_mm,done", [(4, 1), (5, 0), (9, 0)])
+def test_hamming_limit_of_five_percent(n_mm, done):
+    """L = 100: the limit is 5 mismatches, and 5/100 in float (0.0500000007) is not
+    below 0.05 in double, so 4 mismatches pass and 5 do not."""
+    ref = _genome(300, 6)
+    read = bytearray(ref[100:200])
+    for j in range(n_mm):
+        p = 30 + 7 * j
+        read[p] = ord("A") if read[p] != ord("A") else ord("G")
+    nam = _nam(0, 25, 100, 125)
+    got = _oracle_one(ref, bytes(read), nam)
+    _same(got, _py_extend(ref, bytes(read), nam))
+    assert got["done"] == done
+
+
+def test_n_and_lower_case_bases_compare_as_bytes():
+    ref = bytearray(_genome(300, 7))
+    ref[150] = ord("N")
+    read = bytearray(ref[100:250])
+    read[60] = ord("n")        # n against N: a mismatch (bytes differ)
+    read[10] = ord(read[10:11].decode().lower())
+    for nam in (_nam(70, 140, 170, 240), _nam(10, 80, 110, 180, is_rc=1)):
+        got = _oracle_one(bytes(ref), bytes(read), nam)
+        _same(got, _py_extend(bytes(ref), bytes(read), nam))
+
+
+def test_random_cases_against_the_python_restatement():
+    rng = np.random.default_rng(8)
+    ref = bytearray(_genome(3000, 9))
+    for p in rng.choice(3000, 15, replace=False):
+        ref[p] = ord("N")
+    ref = bytes(ref)
+    n_done = n_flip = 0
+    for t in range(300):
+        L = int(rng.integers(60, 260))
+        a = int(rng.integers(0, 3000 - L))
+        read = bytearray(ref[a:a + L])
+        for _ in range(int(rng.integers(0, 8))):
+            read[int(rng.integers(0, L))] = int(rng.choice(np.frombuffer(b"ACGTNacgt", np.uint8)))
+        strand = int(rng.integers(0, 2))
+        read = bytes(read) if strand == 0 else _revcomp(bytes(read))
+        # (qs, qe) in the view of the read that matches the reference (forward for
+        # strand 0, reverse complement for strand 1) against [a + qs, a + qe)
+        qs = int(rng.integers(0, L - K - 1))
+        qe = int(rng.integers(qs + K, L + 1))
+        shift = int(rng.integers(-2, 3)) if t % 5 == 0 else 0
+        rs = max(0, a + qs + shift)
+        re_ = min(len(ref), rs + (qe - qs))
+        if re_ - rs < K:
+            continue
+        if t % 4:
+            nam = _nam(qs, qe, rs, re_, is_rc=strand)
+        else:   # the other strand claimed, in its mirrored coordinates (a false reverse hit)
+            nam = _nam(L - qe, L - qs, rs, re_, is_rc=1 - strand)
+        got = _oracle_one(ref, read, nam)
+        py = _py_extend(ref, read, nam)
+        _same(got, py)
+        n_done += py["done"]
+        n_flip += py["is_rc"] != int(nam["is_rc"])
+    assert n_done > 50 and n_flip > 10
+
+
+def test_align_parameters_are_used():
+    ref = _genome(300, 10)
+    read = bytearray(ref[50:200])
+    read[20] = ord("A") if read[20] != ord("A") else ord("T")
+    nam = _nam(40, 100, 90, 150)
+    got = _oracle_one(ref, bytes(read), nam, match=1, mismatch=4, gap_open=6, gap_extend=1, end_bonus=5)
+    _same(got, _py_extend(ref, bytes(read), nam, match=1, mismatch=4, end_bonus=5))
+
+
+def test_nams_outside_their_read_or_contig_are_refused():
+    ref = _genome(300, 11)
+    read = ref[50:200]
+    for nam in (_nam(140, 160, 190, 210), _nam(10, 25, 60, 75), _nam(10, 60, 280, 330), _nam(10, 60, 60, 110, ref_id=1)):
+        with pytest.raises(ValueError):
+            _oracle_one(ref, read, nam)
+
+
+@pytest.mark.gpu
+def test_seed_extension_against_oracle():
+    """gbsa_extend_seeds_device equals the oracle on the best NAMs of mapped reads of
+    both orientations, on the same NAMs claiming the wrong orientation, and on reads
+    with N and lower-case bases; a NAM outside its contig fails the call, which stays
+    usable."""
+    import torch
+    from gpu_index_test_gb300 import native, synth
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=95))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=3000, seed=96))
+    seq = reads.seq.copy()
+    rng = np.random.default_rng(97)
+    seq[rng.choice(len(seq), len(seq) // 500, replace=False)] = ord("N")
+    low = rng.choice(len(seq), len(seq) // 200, replace=False)
+    seq[low] = np.frombuffer(bytes(seq[low]).lower(), np.uint8)
+    reads.seq = seq
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    nams, offs, _, _ = native.Mapper(idx, abi.map_options(rescue_level=2)).map_reads(reads)
+    sel, owner = [], []
+    for r in range(reads.n):
+        a, b = int(offs[r]), int(offs[r + 1])
+        for j in range(a, min(b, a + 3)):
+            sel.append(j)
+            owner.append(r)
+    nn = nams[np.array(sel)].copy()
+    owner = np.array(owner, np.uint32)
+    wrong = nn.copy()                          # the wrong orientation in the other strand's coordinates
+    L = reads.lengths[owner].astype(np.int32)
+    wrong["is_rc"] = 1 - wrong["is_rc"]
+    wrong["query_start"], wrong["query_end"] = L - nn["query_end"], L - nn["query_start"]
+    all_nams = np.concatenate([nn, wrong])
+    all_owner = np.concatenate([owner, owner])
+    k = native.params_from_read_length(150).k
+    ref = oracle_py.extend_seeds(g.seq, g.offsets, g.lengths, reads.seq, reads.offsets, reads.lengths, all_nams,
+                                 all_owner, k)
+    dev = torch.device("cuda:0")
+
+    def up(a, dt=None):
+        a = np.ascontiguousarray(a if dt is None else a.astype(dt))
+        return torch.from_numpy(a.view(np.uint8).copy()).to(dev)
+
+    d = [up(g.seq), up(g.offsets, np.uint64), up(g.lengths, np.uint64), up(reads.seq), up(reads.offsets, np.uint64),
+         up(reads.lengths, np.uint32), up(all_nams), up(all_owner, np.uint32)]
+    out = torch.zeros(len(all_nams) * abi.SEED_ALIGNMENT.itemsize, dtype=torch.uint8, device=dev)
+    native.extend_seeds_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), len(g.lengths), d[3].data_ptr(),
+                               d[4].data_ptr(), d[5].data_ptr(), reads.n, d[6].data_ptr(), d[7].data_ptr(),
+                               len(all_nams), k, out.data_ptr())
+    got = out.cpu().numpy().view(abi.SEED_ALIGNMENT)
+    assert (got == ref).all(), np.nonzero(got != ref)[0][:10]
+    half = len(nn)
+    assert ref["done"][:half].mean() > 0.5 and (ref["is_rc"][half:] == ref["is_rc"][:half]).mean() > 0.9
+    assert ((ref["done"] == 1) & (ref["edit_distance"] > 0)).any() and (ref["done"] == 0).any()
+    # a NAM past its contig's end fails the call; the next call works
+    bad = all_nams[:4].copy()
+    bad["ref_end"][2] = int(g.lengths[bad["ref_id"][2]]) + 5
+    d_bad = up(bad)
+    with pytest.raises(native.GbsaError):
+        native.extend_seeds_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), len(g.lengths),
+                                   d[3].data_ptr(), d[4].data_ptr(), d[5].data_ptr(), reads.n, d_bad.data_ptr(),
+                                   d[7].data_ptr(), 4, k, out.data_ptr())
+    native.extend_seeds_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), len(g.lengths), d[3].data_ptr(),
+                               d[4].data_ptr(), d[5].data_ptr(), reads.n, d[6].data_ptr(), d[7].data_ptr(),
+                               len(all_nams), k, out.data_ptr())
+    assert (out.cpu().numpy().view(abi.SEED_ALIGNMENT) == ref).all()
