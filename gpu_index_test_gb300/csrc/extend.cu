@@ -8,7 +8,8 @@
 // independent groups: the k-mer checks have no early exit, and the scan loads 8 bases of
 // both sequences before it scans them (8 measured faster than 4 or 16: more loads in
 // flight against more registers, fewer warps; 1.65 ms for 2M NAMs against 1.94 ms for
-// one base at a time; staging the warp's sequences in shared memory was slower).  The
+// one base at a time; staging the warp's sequences in shared memory was slower), and the
+// grid is one wave of resident blocks (1.55 ms).  The
 // NAM's two k-mer checks come first.  Then one pass over the read and its projected
 // reference window counts the Hamming distance and runs the best-segment scan together;
 // the reference runs the scan only when the distance admits the ungapped path, and its
@@ -191,9 +192,14 @@ extern "C" int gbsa_extend_seeds_device(const uint8_t* d_ref_seqs, const uint64_
         GBSA_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&bad), sizeof(unsigned int), st));
         unsigned int h_bad = 0;
         const cudaError_t e = [&] {
-            cudaError_t r = cudaMemsetAsync(bad, 0, sizeof(unsigned int), st);
+            // one wave of resident blocks (the loop strides over the NAMs)
+            int per_sm = 0;
+            cudaError_t r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_seeds, 128, 0);
             if (r != cudaSuccess) return r;
-            k_extend_seeds<<<grid_for(n_nams, 128, (unsigned)device_sm_count() * 16), 128, 0, st>>>(
+            const unsigned max_blocks = (unsigned)device_sm_count() * (unsigned)(per_sm > 0 ? per_sm : 1);
+            r = cudaMemsetAsync(bad, 0, sizeof(unsigned int), st);
+            if (r != cudaSuccess) return r;
+            k_extend_seeds<<<grid_for(n_nams, 128, max_blocks), 128, 0, st>>>(
                 d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets, d_read_lengths,
                 n_reads, d_nams, d_nam_reads, n_nams, k, *params, d_out, bad);
             g_launches.fetch_add(1, std::memory_order_relaxed);   // counted as GBSA_LAUNCHED, without a throw
