@@ -589,7 +589,26 @@ def main():
                                  "unit": "GB/s", "frac": round(achieved / ext_peak, 4), "peak_source": ext_peak_src,
                                  "alg_bytes_per_launch": alg},
                     "timing": "each call: the kernel and its 4-byte status read, 5 calls after one warm-up"}
-        ext_in = (d_best.cpu().numpy().view(abi.NAM).reshape(-1), owners, ext)
+        # mate rescue: each read's mate (mates are interleaved) from the read's best NAM
+        mates = (owners ^ 1).astype(np.uint32)
+        d_mates = torch.from_numpy(mates.view(np.int32)).to(dev)
+        d_resc_out = torch.empty(n_ext * abi.MATE_RESCUE.itemsize, dtype=torch.uint8, device=dev)
+        rescue = lambda: native.rescue_mates_device(d_ref.data_ptr(), d_roff.data_ptr(), d_rlen.data_ptr(),
+                                                    len(g.lengths), d_seq.data_ptr(), d_off.data_ptr(),
+                                                    d_len.data_ptr(), n, d_best.data_ptr(), d_mates.data_ptr(),
+                                                    n_ext, p.k, d_resc_out.data_ptr(), stream=stream.cuda_stream)
+        rescue()
+        e0.record(stream)
+        for _ in range(5):
+            rescue()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_resc = e0.elapsed_time(e1) / 5
+        mres = d_resc_out.cpu().numpy().view(abi.MATE_RESCUE)
+        seed_ext["mate_rescue"] = {"nams": int(n_ext), "ms": round(ms_resc, 4),
+                                   "nams_per_s": round(n_ext / (ms_resc * 1e-3), 1),
+                                   "mate_unaligned_frac": round(float(mres["is_unaligned"].mean()), 4)}
+        ext_in = (d_best.cpu().numpy().view(abi.NAM).reshape(-1), owners, ext, mates, mres)
     nam_profile = None
     if len(nam_cyc):
         worst = nam_cyc[np.argsort(nam_cyc[:, 0])[-3:]]
@@ -706,7 +725,7 @@ def main():
         if seed_ext is not None:
             # the oracle on the first NAMs (one host thread), checked against the GPU records
             from oracle import oracle_py
-            nb, ob, eb = ext_in
+            nb, ob, eb, mb, rb = ext_in
             n_cpu = min(len(nb), 400000)
             t0 = time.perf_counter()
             ref_ext = oracle_py.extend_seeds(g.seq, g.offsets, g.lengths, reads.seq, reads.offsets, reads.lengths,
@@ -715,6 +734,15 @@ def main():
             seed_ext["cpu_baseline"] = {"value": round(n_cpu / cpu_s, 1), "unit": "NAMs/s", "cores": 1,
                                         "kind": "port", "sample": f"the first {n_cpu} NAMs"}
             seed_ext["bit_exact_vs_cpu_sample"] = bool((ref_ext == eb[:n_cpu]).all())
+            n_cpu = min(len(nb), 100000)
+            t0 = time.perf_counter()
+            ref_resc = oracle_py.rescue_mates(g.seq, g.offsets, g.lengths, reads.seq, reads.offsets, reads.lengths,
+                                              nb[:n_cpu], mb[:n_cpu], p.k)
+            cpu_s = time.perf_counter() - t0
+            seed_ext["mate_rescue"]["cpu_baseline"] = {"value": round(n_cpu / cpu_s, 1), "unit": "NAMs/s",
+                                                       "cores": 1, "kind": "port",
+                                                       "sample": f"the first {n_cpu} NAMs"}
+            seed_ext["mate_rescue"]["bit_exact_vs_cpu_sample"] = bool((ref_resc == rb[:n_cpu]).all())
 
     line = {
         "metric": "reads/s seed+lookup+NAM", "value": round(value, 1), "unit": "reads/s", "n_gpus": world,

@@ -108,6 +108,11 @@ SEED_ALIGNMENT = np.dtype([("ref_id", "<i4"), ("ref_start", "<i4"), ("edit_dista
                            ("is_rc", "u1"), ("done", "u1"), ("consistent", "u1"), ("_pad", "u1")])
 assert SEED_ALIGNMENT.itemsize == 36 and ALIGN_PARAMS.itemsize == 20
 
+# gbsa_mate_rescue: one mate-rescue decision.
+MATE_RESCUE = np.dtype([("ref_id", "<i4"), ("window_start", "<i4"), ("window_end", "<i4"), ("edit_distance", "<i4"),
+                        ("is_rc", "u1"), ("done", "u1"), ("is_unaligned", "u1"), ("_pad", "u1")])
+assert MATE_RESCUE.itemsize == 20
+
 
 def align_params(match=2, mismatch=8, gap_open=12, gap_extend=1, end_bonus=10):
     return np.array([(match, mismatch, gap_open, gap_extend, end_bonus)], ALIGN_PARAMS)

@@ -170,6 +170,114 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// ---- mate rescue (rescue_mate_part with has_shared_substring) --------------------------
+
+// nt2int_mod8 (step2/main.cu:645-654) as nibbles of one word: the 2-bit code of a byte
+// from its value mod 8.
+__device__ __forceinline__ uint32_t code_mod8(uint8_t base) { return (0x20031000u >> ((base & 7) * 4)) & 0xFu; }
+
+constexpr int kMaxMateSubstrings = 64;   // sampled substrings of a mate (the reference keeps 50)
+constexpr int kRescueWarps = 8;
+
+// Hash of the sub bases at s (2 bits per base into 32 bits, as the reference's loop: a
+// substring of more than 16 bases keeps its last 16); rc: s is the end of a read walked
+// backwards through the complement table.
+__device__ __forceinline__ uint32_t substring_hash(const uint8_t* s, int sub, bool rc) {
+    uint32_t h = 0;
+    for (int j = 0; j < sub; ++j) h = (h << 2) | code_mod8(rc ? revcomp_base(__ldg(s - j)) : __ldg(s + j));
+    return h;
+}
+
+// A warp per NAM: the window where the mate lies (float arithmetic as the reference's:
+// the int offset converted to float, mu + 5 sigma as one fused multiply-add, truncation
+// back to int), then has_shared_substring (step2/main.cu:657-693).  The lanes hash the
+// mate's 2k/3-base substrings at multiples of k/3 into the warp's shared list, then take
+// the window's substring positions 32 at a time (consecutive positions, so the loads
+// coalesce) and compare each one's hash with the whole list (every lane reads the same
+// entry: a broadcast); the scan ends at the first group with a match, which gives the
+// reference's answer (a match at any position).  Both position sets stop one substring
+// short of the end, as the reference's loops.  Bound by the latency of the window's
+// loads and the list compares: 2M NAMs in about 8.5 ms (a thread per NAM with the list in
+// a per-thread array took 7.9 ms, its local arrays missing L1 on nearly every access;
+// with the list in shared memory 11 ms; unrolled hash and compare loops 9.4 ms).
+__global__ void __launch_bounds__(32 * kRescueWarps)
+    k_rescue_mates(const uint8_t* __restrict__ ref_seqs, const uint64_t* __restrict__ ref_offs,
+                   const uint64_t* __restrict__ ref_lens, uint32_t n_refs, const uint8_t* __restrict__ read_seqs,
+                   const uint64_t* __restrict__ read_offs, const uint32_t* __restrict__ read_lens, uint32_t n_reads,
+                   const gbsa_nam* __restrict__ nams, const uint32_t* __restrict__ mate_reads, uint64_t n, int k,
+                   float mu, float sigma, gbsa_mate_rescue* __restrict__ out, unsigned int* bad) {
+    __shared__ uint32_t s_list[kRescueWarps][kMaxMateSubstrings];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t* list = s_list[w];
+    const int sub = 2 * k / 3, step = k / 3;
+    const float spread = __fmaf_rn(5.0f, sigma, mu);
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const gbsa_nam nam = nams[i];
+        const uint32_t r = mate_reads[i];
+        gbsa_mate_rescue o;
+        o.ref_id = o.window_start = o.window_end = o.edit_distance = 0;
+        o.is_rc = o.done = o.is_unaligned = o._pad = 0;
+        bool ok = r < n_reads && nam.ref_id >= 0 && (uint32_t)nam.ref_id < n_refs;
+        const int L = ok ? (int)read_lens[r] : 0;
+        const int n_sub = L > sub ? (L - sub + step - 1) / step : 0;   // p = 0, step, ... with p + sub < L
+        if (n_sub > kMaxMateSubstrings) ok = false;
+        if (!ok) {
+            if (lane == 0) {
+                atomicAdd(bad, 1u);
+                out[i] = o;
+            }
+            continue;
+        }
+        const uint8_t* fwd = read_seqs + read_offs[r];
+        // rescue_mate_part (step2/main.cu:695-757)
+        const bool mate_fwd = nam.is_rc != 0;   // the mate in the orientation opposite to the NAM
+        int a, b;
+        if (mate_fwd) {
+            a = __float2int_rz(__fsub_rn(__int2float_rn(nam.ref_start - nam.query_start), spread));
+            b = nam.ref_start - nam.query_start + L / 2;
+        } else {
+            a = nam.ref_end + (L - nam.query_end) - L / 2;
+            b = __float2int_rz(__fadd_rn(__int2float_rn(nam.ref_end + (L - nam.query_end)), spread));
+        }
+        const int ref_len = (int)ref_lens[nam.ref_id];
+        const int ws = max(0, min(a, ref_len));
+        const int we = min(ref_len, max(0, b));
+        bool shared = false;
+        if (we >= ws + k) {
+            for (int t = (int)lane; t < n_sub; t += 32) {
+                const int q = t * step;   // the mate's substring [q, q + sub) in its orientation
+                list[t] = mate_fwd ? substring_hash(fwd + q, sub, false) : substring_hash(fwd + (L - 1 - q), sub, true);
+            }
+            __syncwarp();
+            const uint8_t* win = ref_seqs + ref_offs[nam.ref_id] + ws;
+            const int n_pos = we - ws - sub;   // positions p with p + sub < window length
+            for (int base = 0; base < n_pos && !shared; base += 32) {
+                const int p = base + (int)lane;
+                bool hit = false;
+                if (p < n_pos) {
+                    const uint32_t h = substring_hash(win + p, sub, false);
+                    for (int e = 0; e < n_sub; ++e) hit |= list[e] == h;
+                }
+                shared = __any_sync(0xFFFFFFFFu, hit);
+            }
+            __syncwarp();   // the next NAM rewrites the list
+        }
+        if (lane == 0) {
+            o.ref_id = nam.ref_id;
+            o.window_start = ws;
+            o.window_end = we;
+            o.is_rc = nam.is_rc;
+            if (!shared) {
+                o.done = 1;
+                o.is_unaligned = 1;
+                o.edit_distance = L;
+            }
+            out[i] = o;
+        }
+    }
+}
+
 }  // namespace
 }  // namespace gbsa
 
@@ -213,6 +321,54 @@ extern "C" int gbsa_extend_seeds_device(const uint8_t* d_ref_seqs, const uint64_
         if (h_bad)
             throw Error(GBSA_ERR_PARAM, std::to_string(h_bad) +
                                             " NAM(s) name a read or contig out of range or leave their read or contig");
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}
+
+extern "C" int gbsa_rescue_mates_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                                        const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                                        const uint64_t* d_read_offsets, const uint32_t* d_read_lengths,
+                                        uint32_t n_reads, const gbsa_nam* d_nams, const uint32_t* d_mate_reads,
+                                        uint64_t n_nams, int k, float mu, float sigma, gbsa_mate_rescue* d_out,
+                                        void* stream) {
+    try {
+        if (k < 3 || k > 32) throw Error(GBSA_ERR_PARAM, "k must be in [3, 32]");
+        if (n_nams == 0) return GBSA_OK;
+        cudaStream_t st = (cudaStream_t)stream;
+        unsigned int* bad = nullptr;
+        GBSA_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&bad), sizeof(unsigned int), st));
+        unsigned int h_bad = 0;
+        const cudaError_t e = [&] {
+            int per_sm = 0;
+            cudaError_t r =
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rescue_mates, 32 * kRescueWarps, 0);
+            if (r != cudaSuccess) return r;
+            const uint64_t want = (n_nams + kRescueWarps - 1) / kRescueWarps;   // a warp per NAM
+            const unsigned blocks = (unsigned)std::min<uint64_t>(
+                want, (uint64_t)device_sm_count() * (uint64_t)(per_sm > 0 ? per_sm : 1));
+            r = cudaMemsetAsync(bad, 0, sizeof(unsigned int), st);
+            if (r != cudaSuccess) return r;
+            k_rescue_mates<<<blocks, 32 * kRescueWarps, 0, st>>>(
+                d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets, d_read_lengths,
+                n_reads, d_nams, d_mate_reads, n_nams, k, mu, sigma, d_out, bad);
+            g_launches.fetch_add(1, std::memory_order_relaxed);   // counted as GBSA_LAUNCHED, without a throw
+            r = cudaGetLastError();
+            if (r != cudaSuccess) return r;
+            return cudaMemcpyAsync(&h_bad, bad, sizeof h_bad, cudaMemcpyDeviceToHost, st);
+        }();
+        GBSA_CUDA(cudaFreeAsync(bad, st));
+        GBSA_CUDA(e);
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        if (h_bad)
+            throw Error(GBSA_ERR_PARAM, std::to_string(h_bad) +
+                                            " NAM(s) name a contig or mate out of range or a mate with more than 64 "
+                                            "sampled substrings");
         return GBSA_OK;
     } catch (const Error& e) {
         set_last_error(e.what());

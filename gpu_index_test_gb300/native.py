@@ -66,6 +66,8 @@ def lib():
             "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
             "gbsa_nam_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, u32, vp, vp, vp]),
             "gbsa_extend_seeds_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, i32, vp, vp, vp]),
+            "gbsa_rescue_mates_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, i32, C.c_float,
+                                               C.c_float, vp, vp]),
             "gbsa_server_create": (i32, [vp, vp, u32, u32, u64, vp]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
@@ -154,6 +156,17 @@ def extend_seeds_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read
     _check(lib().gbsa_extend_seeds_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs,
                                           d_read_offsets, d_read_lengths, n_reads, d_nams, d_nam_reads, n_nams, k,
                                           p.ctypes.data, d_out, stream))
+
+
+def rescue_mates_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets,
+                        d_read_lengths, n_reads, d_nams, d_mate_reads, n_nams, k, d_out, mu=300.0, sigma=100.0,
+                        stream=None):
+    """Mate rescue (rescue_mate_part with has_shared_substring): one gbsa_mate_rescue per
+    NAM into d_out.  Device addresses; mu and sigma are the insert-size estimate (the
+    reference's defaults when not given)."""
+    _check(lib().gbsa_rescue_mates_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs,
+                                          d_read_offsets, d_read_lengths, n_reads, d_nams, d_mate_reads, n_nams, k,
+                                          mu, sigma, d_out, stream))
 
 
 def _u8(a):

@@ -379,6 +379,35 @@ int gbsa_extend_seeds_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_of
                              const gbsa_nam* d_nams, const uint32_t* d_nam_reads, uint64_t n_nams, int k,
                              const gbsa_align_params* params, gbsa_seed_alignment* d_out, void* stream);
 
+/* One mate-rescue decision: the reference window searched for the mate, and the
+ * alignment record rescue_mate_part writes. */
+typedef struct gbsa_mate_rescue {
+    int32_t ref_id;         /* the NAM's contig */
+    int32_t window_start;   /* the window [window_start, window_end) of the contig */
+    int32_t window_end;
+    int32_t edit_distance;  /* the mate's length when it is unaligned, else 0 */
+    uint8_t is_rc;          /* the NAM's orientation */
+    uint8_t done;           /* done_align: 1 when the mate is unaligned (window shorter than k, or
+                               no substring shared with the window); 0 when a gapped aligner must
+                               align the mate in the window */
+    uint8_t is_unaligned;
+    uint8_t _pad;
+} gbsa_mate_rescue;
+
+/* Mate rescue (rescue_mate_part, step2/main.cu:695-757, with has_shared_substring,
+ * main.cu:657-693): for NAM i of one read end and the other end's read mate_reads[i],
+ * the window where the mate lies for an insert of at most mu + 5 sigma (fr orientation,
+ * at most half a read of overlap), and whether the mate (in the orientation opposite to
+ * the NAM) shares a 2k/3-base substring, sampled every k/3 bases, with that window.
+ * Device pointers as gbsa_extend_seeds_device; k in [3, 32].  A NAM whose contig or mate index is out
+ * of range, or whose mate has more than 64 sampled substrings (the reference keeps 50 in
+ * a fixed shared array), fails the call (GBSA_ERR_PARAM); the call synchronizes stream. */
+int gbsa_rescue_mates_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                             const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                             const uint64_t* d_read_offsets, const uint32_t* d_read_lengths, uint32_t n_reads,
+                             const gbsa_nam* d_nams, const uint32_t* d_mate_reads, uint64_t n_nams, int k,
+                             float mu, float sigma, gbsa_mate_rescue* d_out, void* stream);
+
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later
  * calls; gbsa_mapper_last_alg_bytes returns the count of the last batch.  No

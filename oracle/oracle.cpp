@@ -1284,3 +1284,87 @@ int oracle_extend_seeds(const char* ref_seqs, const uint64_t* ref_offsets, const
 }
 
 }  // extern "C"
+
+// ---- mate rescue's shared-substring test ----------------------------------------------
+
+// nt2int_mod8 (step2/main.cu:645-654): the 2-bit code of a byte from its value mod 8
+// (A/a 0, C/c 1, G/g 2, T/t 3; other bytes whatever their value mod 8 selects).
+static uint32_t code_mod8(unsigned char base) {
+    static const uint8_t t[8] = {0, 0, 0, 1, 3, 0, 0, 2};
+    return t[base % 8];
+}
+
+// has_shared_substring (step2/main.cu:657-693): a 2k/3-base substring of the read starting
+// at a multiple of k/3 equals one of the reference segment's (each hashed 2 bits per base
+// into 32 bits; both loops stop one substring short of the end).
+static bool shared_substring(const char* read, int read_len, const char* ref, int ref_len, int k) {
+    const int sub = 2 * k / 3, step = k / 3;
+    std::vector<uint32_t> h0;
+    for (int i = 0; i + sub < read_len; i += step) {
+        uint32_t h = 0;
+        for (int j = 0; j < sub; ++j) h = (h << 2) | code_mod8((unsigned char)read[i + j]);
+        h0.push_back(h);
+    }
+    std::sort(h0.begin(), h0.end());
+    for (int i = 0; i + sub < ref_len; ++i) {
+        uint32_t h = 0;
+        for (int j = 0; j < sub; ++j) h = (h << 2) | code_mod8((unsigned char)ref[i + j]);
+        if (std::binary_search(h0.begin(), h0.end(), h)) return true;
+    }
+    return false;
+}
+
+extern "C" {
+
+int oracle_rescue_mates(const char* ref_seqs, const uint64_t* ref_offsets, const uint64_t* ref_lengths,
+                        uint32_t n_refs, const char* read_seqs, const uint64_t* read_offsets,
+                        const uint32_t* read_lengths, uint32_t n_reads, const gbsa_nam* nams,
+                        const uint32_t* mate_reads, uint64_t n_nams, int k, float mu, float sigma,
+                        gbsa_mate_rescue* out) {
+    if (k < 3 || k > 32) return GBSA_ERR_PARAM;
+    std::string rc;
+    const float spread = std::fmaf(5.0f, sigma, mu);   // mu + 5 * sigma, as one fused multiply-add
+    for (uint64_t i = 0; i < n_nams; ++i) {
+        const gbsa_nam& nam = nams[i];
+        const uint32_t r = mate_reads[i];
+        if (r >= n_reads || nam.ref_id < 0 || (uint32_t)nam.ref_id >= n_refs) return GBSA_ERR_PARAM;
+        const int L = (int)read_lengths[r];
+        const int sub = 2 * k / 3, step = k / 3;
+        if (L > sub && (L - sub + step - 1) / step > 64) return GBSA_ERR_PARAM;
+        const char* fwd = read_seqs + read_offsets[r];
+        // rescue_mate_part (step2/main.cu:695-757): the mate in the orientation opposite to
+        // the NAM, and its window (float arithmetic as the reference's)
+        int a, b;
+        const char* mate;
+        if (nam.is_rc) {
+            mate = fwd;
+            a = (int)((float)(nam.ref_start - nam.query_start) - spread);
+            b = nam.ref_start - nam.query_start + L / 2;
+        } else {
+            rc.resize((size_t)L);
+            for (int j = 0; j < L; ++j) rc[(size_t)j] = revcomp_char((unsigned char)fwd[L - 1 - j]);
+            mate = rc.data();
+            a = nam.ref_end + (L - nam.query_end) - L / 2;
+            b = (int)((float)(nam.ref_end + (L - nam.query_end)) + spread);
+        }
+        const int ref_len = (int)ref_lengths[nam.ref_id];
+        const int ws = std::max(0, std::min(a, ref_len));
+        const int we = std::min(ref_len, std::max(0, b));
+        gbsa_mate_rescue& o = out[i];
+        std::memset(&o, 0, sizeof o);
+        o.ref_id = nam.ref_id;
+        o.window_start = ws;
+        o.window_end = we;
+        o.is_rc = nam.is_rc;
+        const bool unaligned = we < ws + k || !shared_substring(mate, L, ref_seqs + ref_offsets[nam.ref_id] + ws,
+                                                                we - ws, k);
+        if (unaligned) {
+            o.done = 1;
+            o.is_unaligned = 1;
+            o.edit_distance = L;
+        }
+    }
+    return GBSA_OK;
+}
+
+}  // extern "C"

@@ -75,6 +75,14 @@ int oracle_extend_seeds(const char* ref_seqs, const uint64_t* ref_offsets, const
                         const uint32_t* nam_reads, uint64_t n_nams, int k, const gbsa_align_params* ap,
                         gbsa_seed_alignment* out);
 
+/* rescue_mate_part with has_shared_substring (step2/main.cu:695-757, 657-693) for each
+ * NAM; host pointers, same contract as gbsa_rescue_mates_device. */
+int oracle_rescue_mates(const char* ref_seqs, const uint64_t* ref_offsets, const uint64_t* ref_lengths,
+                        uint32_t n_refs, const char* read_seqs, const uint64_t* read_offsets,
+                        const uint32_t* read_lengths, uint32_t n_reads, const gbsa_nam* nams,
+                        const uint32_t* mate_reads, uint64_t n_nams, int k, float mu, float sigma,
+                        gbsa_mate_rescue* out);
+
 /* Whole path for a batch of reads with n_threads host threads (0 = all cores).
  * Same contract as gbsa_map_reads.  Returns GBSA_OK or GBSA_ERR_CAPACITY. */
 int oracle_map_reads(const oracle_index* idx, const gbsa_map_options* opt, const char* seqs,

@@ -66,6 +66,9 @@ def lib():
         vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
         L.oracle_extend_seeds.restype = C.c_int
         L.oracle_extend_seeds.argtypes = [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, C.c_int, vp, vp]
+        L.oracle_rescue_mates.restype = C.c_int
+        L.oracle_rescue_mates.argtypes = [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, C.c_int, C.c_float,
+                                          C.c_float, vp]
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -255,4 +258,25 @@ def extend_seeds(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, re
                                    nr.ctypes.data if len(nr) else None, len(a), k, p.ctypes.data, out.ctypes.data)
     if rc != 0:
         raise ValueError("a NAM names a read or contig out of range or leaves its read or contig")
+    return out[:len(a)]
+
+
+def rescue_mates(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, nams, mate_reads, k,
+                 mu=300.0, sigma=100.0):
+    """rescue_mate_part with has_shared_substring restated: one abi.MATE_RESCUE record per
+    NAM.  Raises ValueError for an out-of-range NAM or a mate with too many substrings."""
+    rs = np.ascontiguousarray(ref_seqs, np.uint8)
+    ro = np.ascontiguousarray(ref_offsets, np.uint64)
+    rl = np.ascontiguousarray(ref_lengths, np.uint64)
+    qs = np.ascontiguousarray(read_seqs, np.uint8)
+    qo = np.ascontiguousarray(read_offsets, np.uint64)
+    ql = np.ascontiguousarray(read_lengths, np.uint32)
+    a = np.ascontiguousarray(nams)
+    mr = np.ascontiguousarray(mate_reads, np.uint32)
+    out = np.zeros(max(1, len(a)), abi.MATE_RESCUE)
+    rc = lib().oracle_rescue_mates(rs.ctypes.data, ro.ctypes.data, rl.ctypes.data, len(rl), qs.ctypes.data,
+                                   qo.ctypes.data, ql.ctypes.data, len(ql), a.ctypes.data if len(a) else None,
+                                   mr.ctypes.data if len(mr) else None, len(a), k, mu, sigma, out.ctypes.data)
+    if rc != 0:
+        raise ValueError("a NAM names a contig or mate out of range, or its mate has too many substrings")
     return out[:len(a)]

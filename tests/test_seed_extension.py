@@ -279,3 +279,133 @@ def test_seed_extension_against_oracle():
                                d[4].data_ptr(), d[5].data_ptr(), reads.n, d[6].data_ptr(), d[7].data_ptr(),
                                len(all_nams), k, out.data_ptr())
     assert (out.cpu().numpy().view(abi.SEED_ALIGNMENT) == ref).all()
+
+
+# ---- mate rescue: rescue_mate_part with has_shared_substring (main.cu:695-757, 657-693) ----
+
+_MOD8 = [0, 0, 0, 1, 3, 0, 0, 2]   # nt2int_mod8 (main.cu:645-654)
+
+
+def _py_shared(read: bytes, ref: bytes, k):
+    sub, step = 2 * k // 3, k // 3
+
+    def h(s, i):
+        v = 0
+        for j in range(sub):
+            v = ((v << 2) | _MOD8[s[i + j] % 8]) & 0xFFFFFFFF
+        return v
+    h0 = {h(read, i) for i in range(0, max(0, len(read) - sub), step)}
+    return any(h(ref, i) in h0 for i in range(0, max(0, len(ref) - sub)))
+
+
+def _py_rescue(ref: bytes, mate: bytes, nam, k=K, mu=300.0, sigma=100.0):
+    L = len(mate)
+    spread = np.float32(5.0 * float(np.float32(sigma)) + float(np.float32(mu)))   # one fused multiply-add
+    qs, qe, rs, re_ = (int(nam[f]) for f in ("query_start", "query_end", "ref_start", "ref_end"))
+    if int(nam["is_rc"]):
+        seq = mate
+        a = int(np.float32(np.float32(rs - qs) - spread))
+        b = rs - qs + L // 2
+    else:
+        seq = _revcomp(mate)
+        a = re_ + (L - qe) - L // 2
+        b = int(np.float32(np.float32(re_ + (L - qe)) + spread))
+    ws, we = max(0, min(a, len(ref))), min(len(ref), max(0, b))
+    unaligned = we < ws + k or not _py_shared(seq, ref[ws:we], k)
+    return dict(ref_id=int(nam["ref_id"]), window_start=ws, window_end=we, edit_distance=L if unaligned else 0,
+                is_rc=int(nam["is_rc"]), done=int(unaligned), is_unaligned=int(unaligned))
+
+
+def _oracle_rescue(ref: bytes, mate: bytes, nam, **kw):
+    return oracle_py.rescue_mates(np.frombuffer(ref, np.uint8), [0], [len(ref)], np.frombuffer(mate, np.uint8), [0],
+                                  [len(mate)], np.array([nam]), [0], K, **kw)[0]
+
+
+def test_mate_rescue_random_cases():
+    rng = np.random.default_rng(20)
+    ref = bytearray(_genome(6000, 21))
+    for p in rng.choice(6000, 20, replace=False):
+        ref[p] = ord("N") if p % 2 else ord(chr(ref[p]).lower())
+    ref = bytes(ref)
+    seen = set()
+    for t in range(200):
+        L = int(rng.integers(60, 200))
+        a = int(rng.integers(0, 5000))
+        ins = int(rng.integers(L, 600))
+        mate = _revcomp(ref[a + ins - L:a + ins]) if a + ins <= len(ref) else _genome(L, t)
+        if t % 3 == 0:
+            mate = _genome(L, 1000 + t)           # a mate from elsewhere: usually nothing shared
+        qs = int(rng.integers(0, 40))
+        nam = _nam(qs, qs + 40, a + qs, a + qs + 40, is_rc=int(rng.integers(0, 2)))
+        got = _oracle_rescue(ref, mate, nam)
+        _same(got, _py_rescue(ref, mate, nam))
+        seen.add(int(got["done"]))
+    assert seen == {0, 1}
+
+
+def test_mate_rescue_window_clamps_and_float_positions():
+    """Windows clamp to the contig (shorter than k: unaligned), and positions past 2^24
+    go through float as in the reference (the window bound rounds to a float)."""
+    ref = _genome(3000, 22)
+    mate = ref[2800:2950]
+    for nam in (_nam(0, 40, 2950, 2990, is_rc=0), _nam(10, 50, 5, 45, is_rc=1), _nam(0, 40, 1000, 1040, is_rc=0)):
+        _same(_oracle_rescue(ref, mate, nam), _py_rescue(ref, mate, nam))
+    big = np.random.default_rng(23).choice(np.frombuffer(b"ACGT", np.uint8), 20_000_001).tobytes()
+    mate = _revcomp(big[19_000_300:19_000_450])
+    for nam in (_nam(3, 43, 19_000_003, 19_000_043, is_rc=0), _nam(7, 47, 17_777_778, 17_777_818, is_rc=1)):
+        got = _oracle_rescue(big, mate, nam)
+        _same(got, _py_rescue(big, mate, nam))
+    got = _oracle_rescue(big, mate, _nam(7, 47, 17_777_778, 17_777_818, is_rc=1))
+    # ref_start - query_start = 17_777_771 is odd, and floats between 2^24 and 2^25 are even
+    assert got["window_start"] == int(np.float32(np.float32(17_777_771) - np.float32(800)))
+    assert got["window_start"] != 17_777_771 - 800
+
+
+def test_mate_rescue_parameters_and_limits():
+    ref = _genome(3000, 24)
+    mate = _revcomp(ref[900:1050])
+    nam = _nam(0, 40, 600, 640, is_rc=0)
+    for mu, sigma in ((300.0, 100.0), (250.0, 33.3), (500.0, 80.0)):
+        _same(_oracle_rescue(ref, mate, nam, mu=mu, sigma=sigma), _py_rescue(ref, mate, nam, mu=mu, sigma=sigma))
+    with pytest.raises(ValueError):   # 82 sampled substrings in a 500-base mate
+        _oracle_rescue(ref, _genome(500, 25), nam)
+    with pytest.raises(ValueError):
+        _oracle_rescue(ref, mate, _nam(0, 40, 600, 640, ref_id=3))
+
+
+@pytest.mark.gpu
+def test_mate_rescue_against_oracle():
+    """gbsa_rescue_mates_device equals the oracle for each pair's mates rescued from the
+    other end's best NAM, and for mates paired with a read from elsewhere."""
+    import torch
+    from gpu_index_test_gb300 import native, synth
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=98))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=3000, seed=99))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    nams, offs, _, _ = native.Mapper(idx, abi.map_options(rescue_level=2)).map_reads(reads)
+    cnt = np.diff(offs.astype(np.int64))
+    ends = np.nonzero(cnt > 0)[0]
+    best = nams[offs[:-1][ends].astype(np.int64)]
+    mates = (ends ^ 1).astype(np.uint32)                 # mates are interleaved
+    other = np.random.default_rng(100).integers(0, reads.n, len(ends)).astype(np.uint32)
+    all_nams = np.concatenate([best, best])
+    all_mates = np.concatenate([mates, other])
+    k = native.params_from_read_length(150).k
+    ref = oracle_py.rescue_mates(g.seq, g.offsets, g.lengths, reads.seq, reads.offsets, reads.lengths, all_nams,
+                                 all_mates, k)
+    dev = torch.device("cuda:0")
+
+    def up(a, dt=None):
+        a = np.ascontiguousarray(a if dt is None else a.astype(dt))
+        return torch.from_numpy(a.view(np.uint8).copy()).to(dev)
+
+    d = [up(g.seq), up(g.offsets, np.uint64), up(g.lengths, np.uint64), up(reads.seq), up(reads.offsets, np.uint64),
+         up(reads.lengths, np.uint32), up(all_nams), up(all_mates, np.uint32)]
+    out = torch.zeros(len(all_nams) * abi.MATE_RESCUE.itemsize, dtype=torch.uint8, device=dev)
+    native.rescue_mates_device(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), len(g.lengths), d[3].data_ptr(),
+                               d[4].data_ptr(), d[5].data_ptr(), reads.n, d[6].data_ptr(), d[7].data_ptr(),
+                               len(all_nams), k, out.data_ptr())
+    got = out.cpu().numpy().view(abi.MATE_RESCUE)
+    assert (got == ref).all(), np.nonzero(got != ref)[0][:10]
+    half = len(best)
+    assert ref["done"][:half].mean() < 0.2 and ref["done"][half:].mean() > 0.5
