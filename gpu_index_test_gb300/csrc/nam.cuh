@@ -47,11 +47,6 @@ __device__ __forceinline__ NamState nam_from_hit(const HitRec& h) {
     return n;
 }
 
-// Extend-or-contain rule shared by both merges (step2/nam.cu:386-410, 167-192).
-__device__ __forceinline__ bool nam_takes(const NamState& n, const HitRec& h) {
-    return (h.qe > n.qe && h.re > n.re) || (h.qe <= n.qe && h.re <= n.re);
-}
-
 __device__ __forceinline__ void nam_add(NamState& n, const HitRec& h) {
     if (h.qe > n.qe && h.re > n.re) {
         n.qe = h.qe;
