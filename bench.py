@@ -119,6 +119,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, world, device=None):
+    """The largest of the ranks' values of x (one all-reduce MAX; the ranks map their own
+    shards of reads with no other exchange); x itself for one rank.  NCCL wants device
+    tensors, gloo host ones."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, seconds):
+    """Whole-job units per second: every rank processed units_per_rank in at most seconds."""
+    return world * units_per_rank / seconds
+
+
 def peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -615,12 +634,8 @@ def main():
         nam_profile = {"total_us": dist(nam_cyc[:, 0], mhz), "merge_us": dist(nam_cyc[:, 3], mhz),
                        "hits": dist(nam_cyc[:, 1]), "nams": dist(nam_cyc[:, 2]),
                        "worst_cycles_hits_nams": worst[:, :3].tolist()}
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
+    value = job_throughput(n, world, ms / 1e3)
 
     # device results of the last step, for the parity check in the CPU-baseline leg
     gpu_res = None
@@ -654,11 +669,7 @@ def main():
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, dev)
     tot_nams_e2e = int(h_noff[n].item())
     h2d = int(reads.seq.nbytes) + 12 * n
     d2h = 44 * tot_nams_e2e + 8 * (n + 1) + 4 * n + n
@@ -753,7 +764,7 @@ def main():
                        form=("seeding and lookup fused (a warp per read)" if fused else
                              "seeding and lookup as two kernels (index over 2 GiB)")
                        + ", then NAM kernels on two streams"),
-        "e2e": {"value": round(world * n / e2e_s, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": round(job_throughput(n, world, e2e_s), 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": roofline,
         "served": served,
