@@ -409,3 +409,28 @@ def test_mate_rescue_against_oracle():
     assert (got == ref).all(), np.nonzero(got != ref)[0][:10]
     half = len(best)
     assert ref["done"][:half].mean() < 0.2 and ref["done"][half:].mean() > 0.5
+
+
+@pytest.mark.parametrize("k", [9, 32])
+def test_other_k_values(k):
+    """k = 32 makes the rescue's substrings 21 bases (their 32-bit hashes keep the last
+    16), k = 9 makes them 6 bases; the extension's k-mer checks use k bases."""
+    rng = np.random.default_rng(30 + k)
+    ref = _genome(4000, 31 + k)
+    for t in range(40):
+        L = int(rng.integers(80, 180))
+        a = int(rng.integers(0, 3000))
+        read = bytearray(ref[a:a + L])
+        for _ in range(int(rng.integers(0, 4))):
+            read[int(rng.integers(0, L))] = ord("ACGT"[int(rng.integers(0, 4))])
+        read = bytes(read)
+        qs = int(rng.integers(0, L - k - 1))
+        nam = _nam(qs, qs + k + int(rng.integers(0, L - k - qs)), a + qs, 0, is_rc=int(rng.integers(0, 2)))
+        nam["ref_end"] = nam["ref_start"] + (nam["query_end"] - nam["query_start"])
+        got = oracle_py.extend_seeds(np.frombuffer(ref, np.uint8), [0], [len(ref)], np.frombuffer(read, np.uint8),
+                                     [0], [L], np.array([nam]), [0], k)[0]
+        _same(got, _py_extend(ref, read, nam, k=k))
+        mate = _revcomp(ref[a + 200:a + 200 + L]) if t % 2 else _genome(L, 500 + t)
+        got = oracle_py.rescue_mates(np.frombuffer(ref, np.uint8), [0], [len(ref)], np.frombuffer(mate, np.uint8),
+                                     [0], [L], np.array([nam]), [0], k)[0]
+        _same(got, _py_rescue(ref, mate, nam, k=k))
