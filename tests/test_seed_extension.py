@@ -434,3 +434,47 @@ def test_other_k_values(k):
         got = oracle_py.rescue_mates(np.frombuffer(ref, np.uint8), [0], [len(ref)], np.frombuffer(mate, np.uint8),
                                      [0], [L], np.array([nam]), [0], k)[0]
         _same(got, _py_rescue(ref, mate, nam, k=k))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [9, 32])
+def test_other_k_values_on_the_gpu(k):
+    """The two device entry points at k = 9 and k = 32 equal the oracle."""
+    import torch
+    from gpu_index_test_gb300 import native
+    rng = np.random.default_rng(60 + k)
+    ref = _genome(20000, 61 + k)
+    reads, nams, mates = [], [], []
+    for t in range(300):
+        L = int(rng.integers(80, 180))
+        a = int(rng.integers(0, 19000 - L))
+        read = bytearray(ref[a:a + L])
+        for _ in range(int(rng.integers(0, 4))):
+            read[int(rng.integers(0, L))] = ord("ACGT"[int(rng.integers(0, 4))])
+        reads.append(bytes(read) if t % 3 else _revcomp(bytes(read)))
+        qs = int(rng.integers(0, L - k - 1))
+        qe = qs + k + int(rng.integers(0, L - k - qs))
+        nams.append(_nam(qs, qe, a + qs, a + qe, is_rc=int(rng.integers(0, 2))))
+        mates.append((t + 1) % 300)
+    seq = np.frombuffer(b"".join(reads), np.uint8)
+    lens = np.array([len(r) for r in reads], np.uint32)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.uint64)
+    nn = np.array(nams)
+    own = np.arange(300, dtype=np.uint32)
+    mt = np.array(mates, np.uint32)
+    refa = np.frombuffer(ref, np.uint8)
+    want_e = oracle_py.extend_seeds(refa, [0], [len(ref)], seq, offs, lens, nn, own, k)
+    want_r = oracle_py.rescue_mates(refa, [0], [len(ref)], seq, offs, lens, nn, mt, k)
+    dev = torch.device("cuda:0")
+    up = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(dev)
+    d = [up(refa), up(np.array([0], np.uint64)), up(np.array([len(ref)], np.uint64)), up(seq), up(offs), up(lens),
+         up(nn), up(own), up(mt)]
+    e = torch.zeros(300 * abi.SEED_ALIGNMENT.itemsize, dtype=torch.uint8, device=dev)
+    r = torch.zeros(300 * abi.MATE_RESCUE.itemsize, dtype=torch.uint8, device=dev)
+    args = [d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), 1, d[3].data_ptr(), d[4].data_ptr(), d[5].data_ptr(),
+            300, d[6].data_ptr()]
+    native.extend_seeds_device(*args, d[7].data_ptr(), 300, k, e.data_ptr())
+    native.rescue_mates_device(*args, d[8].data_ptr(), 300, k, r.data_ptr())
+    assert (e.cpu().numpy().view(abi.SEED_ALIGNMENT) == want_e).all()
+    assert (r.cpu().numpy().view(abi.MATE_RESCUE) == want_r).all()
+    assert want_e["done"].any()
