@@ -1223,6 +1223,7 @@ int oracle_extend_seeds(const char* ref_seqs, const uint64_t* ref_offsets, const
                         const uint32_t* read_lengths, uint32_t n_reads, const gbsa_nam* nams,
                         const uint32_t* nam_reads, uint64_t n_nams, int k, const gbsa_align_params* ap,
                         gbsa_seed_alignment* out) {
+    if (k < 1) return GBSA_ERR_PARAM;
     std::string rc;
     for (uint64_t i = 0; i < n_nams; ++i) {
         gbsa_nam nam = nams[i];
