@@ -48,6 +48,8 @@ def parse():
                     help="request rates (req/s) of the served-form measurement; empty to skip")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--no-fastq", dest="fastq", action="store_false", help="skip the FASTQ staging measurement")
+    ap.add_argument("--other-configs", default="C1,C3,C4",
+                    help="configurations checked for parity (and timed) after the headline one; empty to skip")
     return ap.parse_args()
 
 
@@ -341,15 +343,61 @@ def fastq_pipeline(m, reads, plain_nams, plain_offs, chunk_mb=48):
             "bit_exact_vs_plain": bool(exact)}
 
 
-def cpu_baseline(g, reads, target_s, gpu_result=None):
-    """The oracle (CPU restatement of the reference path) on a bounded sample."""
-    from gpu_index_test_gb300 import abi
+def mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    return int(ln.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+# Genomes above this are not indexed on the host: the GPU's index is exported, checked
+# against the oracle without a host build (oracle_py.verify_index) and loaded into it.
+HOST_BUILD_MAX_BP = 500_000_000
+
+
+def oracle_index_for(g, gpu_index=None):
+    """The oracle's index of genome g: built on the host, or for a genome above
+    HOST_BUILD_MAX_BP the GPU's index after it passed the sort-free check.  Returns
+    (index or None, record of how it was obtained)."""
     from oracle import oracle_py
 
     p = oracle_py.params_from_read_length(150)
     t0 = time.perf_counter()
-    idx = oracle_py.Index.build(p, g)
-    build_s = time.perf_counter() - t0
+    if gpu_index is None or int(g.lengths.sum()) <= HOST_BUILD_MAX_BP:
+        idx = oracle_py.Index.build(p, g)
+        return idx, {"how": "built on the host by the oracle", "index_build_s": round(time.perf_counter() - t0, 2)}
+    info = gpu_index.info()
+    need = 2.2 * (16 * info.size + 8 * ((1 << info.bits) + 1)) / 1e9 + 8
+    if mem_available_gb() < need:
+        return None, {"how": f"skipped: host memory below {need:.0f} GB"}
+    rs, st = gpu_index.export()
+    t_exp = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    verdict, rep = oracle_py.verify_index(p, g, rs, st, info.bits, info.filter_cutoff)
+    rec = {"how": "GPU index exported and checked by the oracle without a host build (generated entries as a "
+                  "multiset, sorted order, bucket table, filter cutoff), then loaded into the oracle",
+           "export_s": round(t_exp, 2), "verify_s": round(time.perf_counter() - t0, 2), "verify": verdict,
+           "entries": int(info.size), "bits": int(info.bits)}
+    if verdict != "equal":
+        rec["report"] = rep
+        return None, rec
+    idx = oracle_py.Index.load(p, rs, st, info.bits, info.filter_cutoff)
+    del rs, st
+    return idx, rec
+
+
+def cpu_baseline(g, reads, target_s, gpu_result=None, gpu_index=None):
+    """The oracle (CPU restatement of the reference path) on a bounded sample."""
+    from gpu_index_test_gb300 import abi
+
+    idx, how = oracle_index_for(g, gpu_index)
+    if idx is None:
+        return {"index": how}, False
+    build_s = how.get("index_build_s")
     cores = os.cpu_count() or 1
     opt = abi.map_options()
     cal = reads.subset(np.arange(min(reads.n, 20000)))
@@ -363,14 +411,14 @@ def cpu_baseline(g, reads, target_s, gpu_result=None):
     dt = time.perf_counter() - t0
     exact = None
     if gpu_result is not None:
-        gn, go, gf, gr = gpu_result
+        gn, go, gf, gr = gpu_result(n) if callable(gpu_result) else gpu_result
         exact = bool((go[: n + 1] == offs).all() and (gf[:n] == frac).all() and (gr[:n] == resc).all())
         if exact:
             k = int(offs[-1])
             exact = all((gn[f][:k] == nams[f]).all() for f in abi.NAM_COMPARED)
     return {"value": n / dt, "unit": "reads/s", "cores": cores, "kind": "port",
             "sample": f"first {n} of the {reads.n} reads, all {cores} host threads, {dt:.1f} s",
-            "index_build_s": round(build_s, 2)}, exact
+            "index_build_s": build_s, "index": how}, exact
 
 
 def run_reference(args):
@@ -412,6 +460,69 @@ def run_reference(args):
         "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def other_config(name, scale, cpu_seconds, steps=3):
+    """Device throughput and parity of another configuration: its genome and reads, the
+    GPU index, one warm-up and `steps` timed device batches (CUDA events), then the
+    oracle on a bounded sample of the same reads compared with the GPU's NAMs, offsets,
+    fractions and rescue flags (for a genome above HOST_BUILD_MAX_BP the oracle uses the
+    GPU's index after checking it without a host build)."""
+    import torch
+    from gpu_index_test_gb300 import abi, native
+
+    g, reads, gen_s, gp, rp = workload(scale, 0, name)
+    p = native.params_from_read_length(150)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = native.Index.build(p, g)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    info = idx.info()
+    n = reads.n
+    m = native.Mapper(idx, abi.map_options(), max_reads=n, max_bases=int(reads.lengths.sum()))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    d_seq = torch.from_numpy(reads.seq).to(dev)
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).to(dev)
+    d_len = torch.from_numpy(reads.lengths.view(np.int32)).to(dev)
+    cap = 30 * n
+    d_nams = torch.empty(cap * 44, dtype=torch.uint8, device=dev)
+    d_noff = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    d_frac = torch.empty(n, dtype=torch.float32, device=dev)
+    d_resc = torch.empty(n, dtype=torch.uint8, device=dev)
+
+    def step():
+        return m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_nams.data_ptr(), cap,
+                                  d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), stream.cuda_stream)
+
+    step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        total = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    fused = bool(m.fused_lookup())
+    noff = d_noff.cpu().numpy().view(np.uint64)
+
+    def first(k):
+        t = int(noff[k])
+        return (d_nams[: t * 44].cpu().numpy().view(abi.NAM), noff[: k + 1], d_frac[:k].cpu().numpy(),
+                d_resc[:k].cpu().numpy())
+
+    m.free()
+    del d_nams
+    torch.cuda.empty_cache()
+    cpu, exact = cpu_baseline(g, reads, cpu_seconds, first, gpu_index=idx)
+    idx.free()
+    torch.cuda.empty_cache()
+    return {"workload": WORKLOADS[name], "genome_bp": int(gp.total_len), "reads_per_batch": int(n),
+            "index_entries": int(info.size), "index_bits": int(info.bits), "index_build_gpu_s": round(build_s, 3),
+            "form": "seeding and lookup fused" if fused else "seeding and lookup as two kernels (index over 2 GiB)",
+            "device_reads_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 3), "nams": int(total),
+            "cpu_baseline": cpu, "bit_exact_vs_cpu_sample": exact}
 
 
 WORKLOADS = {
@@ -488,6 +599,7 @@ def main():
     # random-gather peaks: a buffer the size of the index (larger than L2, within the
     # GPU's TLB reach like the index) and one that fits L2
     gather_peaks = (native.bench_gather(512 << 20)[1], native.bench_gather(16 << 20)[1]) if rank == 0 else (0.0, 0.0)
+    gather_index = native.bench_gather_index(idx) if rank == 0 else (0.0, 0.0, 0.0)
 
     # warm-up (first one also counts algorithmic bytes of the lookup stage)
     m.set_count_bytes(True)
@@ -686,37 +798,57 @@ def main():
     main_stages = ("seed_lookup", "lookup_long", "nams", "nams_warp") if fused else ("seed", "lookup", "nams", "nams_warp")
     dom = max(main_stages, key=lambda k: stage_ms.get(k, 0.0))
     q, hits, nams_n = counts["queries"], counts["hits"], counts["nams"]
-    bases = int(reads.lengths.sum())
-    seed_b = bases + 16 * q                          # ASCII bases in, query randstrobes out
-    lookup_b = alg_lookup + 16 * q + 8 * q + 20 * hits  # probes + queries in + positions + hits out
+    packed = int(((reads.lengths.astype(np.int64) + 3) // 4).sum())
+    # Algorithmic bytes as the measurement plan defines them per read: the 2-bit packed
+    # read (ceil(L/4) B), the lookup's probes (bucket bound pair, entries examined,
+    # filter probe, run walk; counted live by the kernel's counting instance) and 44 B
+    # per output NAM.  Seeding + lookup carry the first two, the NAM stages the third.
     alg = {
-        "seed_lookup": seed_b + lookup_b, "lookup_long": 0,   # one kernel (indexes up to 2 GiB)
-        "seed": seed_b, "lookup": lookup_b,                   # two kernels (larger indexes)
+        "seed_lookup": packed + alg_lookup, "lookup_long": 0,   # one kernel (indexes up to 2 GiB)
+        "seed": packed, "lookup": alg_lookup,                   # two kernels (larger indexes)
         "seed_long": 0,
-        "nams": 20 * hits + 32 * nams_n,                 # hits in, NAM records out
-        "nams_warp": 0,
-        "rescue": 0,
-        "rescue_sort": 0,
+        "nams": 44 * nams_n, "nams_warp": 0, "rescue": 0, "rescue_sort": 0,
+    }
+    # Bytes the kernels pass between their own phases through HBM / L2 (not algorithmic):
+    # query records written and read back, index positions, per-query hit counts and
+    # offsets, hit records written (seeding + lookup) and read (NAM stages), NAM states
+    # written unsorted and sorted.
+    inter = {
+        "seed_lookup": 16 * q + 16 * q + 8 * q + 8 * q + 16 * hits,
+        "seed": 16 * q, "lookup": 16 * q + 8 * q + 8 * q + 16 * hits,
+        "nams": 16 * hits + 64 * nams_n,
     }
     peak, peak_kind = peaks()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
     tr = ncu_traffic().get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": tr, "alg_bytes_per_launch": alg[dom], "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}}
-    # the lookup against the achievable random-gather bandwidth (sector form: 32 B per
-    # distinct sector the reference's probes touch), measured on this GPU before the
-    # timed region; the lookup runs inside the fused seeding + lookup kernel, so the
-    # rate is taken over that kernel's whole time (a lower bound for the gathers)
+                "traffic": tr, "alg_bytes_per_launch": alg[dom],
+                "alg_bytes_terms": ({"packed_reads": packed, "lookup_probes": int(alg_lookup)}
+                                    if dom in ("seed_lookup", "seed", "lookup") else {"nams_44B": 44 * nams_n}),
+                "intermediate_bytes_per_launch": inter.get(dom),
+                "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}}
+    step_alg = packed + alg_lookup + 44 * nams_n
+    roofline["whole_step"] = {"alg_bytes": int(step_alg), "ms": round(ms, 3),
+                              "achieved": round(step_alg / (ms / 1e3) / 1e9, 1),
+                              "frac": round(step_alg / (ms / 1e3) / 1e9 / peak, 4)}
+    # the lookup against the achievable random-gather bandwidth of its own footprint:
+    # the dependent bucket-pair -> first-entry gather on this index's buffers, measured
+    # before the timed region (sector form: 32 B per distinct sector the reference's
+    # probes touch); inside the fused kernel the rate is taken over the whole kernel
+    # (seeding included), a lower bound for the gathers
     lk_stage = "seed_lookup" if fused else "lookup"
     lk_s = stage_ms.get(lk_stage, 0.0) / 1e3
+    g_probes, g_sectors, g_gbs = gather_index
     gather_hbm, gather_l2 = gather_peaks
+    lk_gbs = sectors_lookup * 32 / lk_s / 1e9 if lk_s > 0 else 0.0
     roofline["gather"] = {
-        "kernel": lk_stage, "sectors_per_launch": int(sectors_lookup),
-        "achieved": round(sectors_lookup * 32 / lk_s / 1e9, 1) if lk_s > 0 else 0.0, "unit": "GB/s",
-        "peak_hbm_gather": round(gather_hbm, 1), "peak_l2_gather": round(gather_l2, 1),
-        "frac": round(sectors_lookup * 32 / lk_s / 1e9 / gather_hbm, 4) if lk_s > 0 and gather_hbm > 0 else None,
-        "peak_source": "gbsa_bench_gather: random 32 B sectors, 512 MB (HBM, index-sized) / 16 MB (L2) buffers",
+        "kernel": lk_stage, "sectors_per_launch": int(sectors_lookup), "achieved": round(lk_gbs, 1), "unit": "GB/s",
+        "peak": round(g_gbs, 1), "frac": round(lk_gbs / g_gbs, 4) if g_gbs > 0 else None,
+        "peak_source": "gbsa_bench_gather_index: uniform random keys, bucket bound pair then the bucket's first "
+                       "entry (dependent) on this index's own tables, 8 probes in flight per thread",
+        "peak_probes_per_s": round(g_probes, 1),
+        "flat_buffer_gather_gbs": {"512MB": round(gather_hbm, 1), "16MB": round(gather_l2, 1)},
     }
 
     staging = None
@@ -755,6 +887,20 @@ def main():
                                                        "sample": f"the first {n_cpu} NAMs"}
             seed_ext["mate_rescue"]["bit_exact_vs_cpu_sample"] = bool((ref_resc == rb[:n_cpu]).all())
 
+    others = None
+    names = [x.strip() for x in args.other_configs.split(",") if x.strip() and x.strip() != args.config]
+    if names and world == 1 and not args.no_cpu_baseline:
+        # the headline configuration's buffers are no longer needed
+        m.free()
+        del d_nams, h_nams
+        torch.cuda.empty_cache()
+        others = {}
+        for nm in names:
+            try:
+                others[nm] = other_config(nm, args.scale, min(args.cpu_seconds, 8.0))
+            except Exception as e:   # recorded, not fatal: the headline line still prints
+                others[nm] = {"error": f"{type(e).__name__}: {e}"}
+
     line = {
         "metric": "reads/s seed+lookup+NAM", "value": round(value, 1), "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
@@ -771,6 +917,7 @@ def main():
         "fastq_staging": staging,
         "cpu_baseline": cpu,
         "bit_exact_vs_cpu_sample": exact,
+        "other_configs": others,
         "clocks": clocks,
         "gpu_launches": int(launches),
         "work": dict(counts, nams_per_step=int(total_nams), rescue_profile=rescue_profile, nam_profile=nam_profile,

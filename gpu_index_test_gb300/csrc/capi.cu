@@ -261,6 +261,7 @@ struct gbsa_mapper {
     uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
     uint64_t alg_sectors = 0; // 32 B sectors of the lookup's gathers in the last batch (when counting)
     int count_bytes = 0;
+    bool use_l2_window = true;   // hold the bucket table in L2 when it fits a window
     int profile = 0;          // record per-stage CUDA events
     cudaEvent_t ev[8] = {};
     float stage_ms[8] = {};
@@ -526,6 +527,49 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
         if (check_batch(m, seeded)) return batch_total(m);
     }
     throw Error(GBSA_ERR_DEVICE_STATUS, "work areas kept overflowing");
+}
+
+// L2 access-policy window over the index's bucket table (the 32-bit copy when there
+// is one: 32 MB for 2^23 buckets), read by every probe of the lookup: held persisting
+// in L2 so that the entry gathers do not evict it.  Used when the table fits the
+// device's largest window; the hit ratio is the part of the table the persisting L2
+// set-aside can hold.  The set-aside (cudaLimitPersistingL2CacheSize) is a limit of
+// this process's context: it is raised to the largest window of the live mappers and
+// returned to zero, with the persisting lines reset, when the last of them is freed.
+static std::mutex g_l2_mu;
+static std::vector<int> g_l2_users;   // per device: mappers holding a window
+
+static void l2_window_attach(gbsa_mapper& m, bool on) {
+    const bool had = m.cfg.l2_bytes != 0;
+    if (on == had) return;
+    int dev = 0;
+    GBSA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(g_l2_mu);
+    if ((int)g_l2_users.size() <= dev) g_l2_users.resize(dev + 1, 0);
+    if (!on) {
+        m.cfg.l2_base = nullptr;
+        m.cfg.l2_bytes = 0;
+        if (--g_l2_users[dev] == 0) {
+            GBSA_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0));
+            GBSA_CUDA(cudaCtxResetPersistingL2Cache());
+        }
+        return;
+    }
+    const gbsa_index& ix = *m.idx;
+    const void* base = ix.starts32.size() ? ix.starts32.as<void>() : ix.starts.as<void>();
+    const uint64_t bytes = ((1ull << ix.bits) + 1) * (ix.starts32.size() ? 4 : 8);
+    int max_window = 0, persist_max = 0;
+    GBSA_CUDA(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev));
+    GBSA_CUDA(cudaDeviceGetAttribute(&persist_max, cudaDevAttrMaxPersistingL2CacheSize, dev));
+    if (!m.use_l2_window || persist_max <= 0 || bytes > (uint64_t)max_window) return;
+    size_t cur = 0;
+    GBSA_CUDA(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize));
+    const size_t want = std::min<size_t>((size_t)persist_max, bytes);
+    if (cur < want) GBSA_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+    m.cfg.l2_base = base;
+    m.cfg.l2_bytes = bytes;
+    m.cfg.l2_hit_ratio = (float)std::min(1.0, (double)want / (double)bytes);
+    ++g_l2_users[dev];
 }
 
 // Chunks of a pipelined host call: `chunks` full chunks of at least 2^17 reads, with
@@ -888,6 +932,7 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
                                                        : 100u;   // step2/main.cu:4204
         m->cfg.count_cap = opt->rescue_count_cap;
         m->cfg.sort_mode = opt->sort_mode;
+        l2_window_attach(*m, true);
         m->max_reads = std::max<uint32_t>(max_reads, 1);
         m->max_bases = std::max<uint64_t>(max_bases, 1);
         // the mapper's own streams run the NAM phase at the highest priority, the seeding
@@ -913,6 +958,10 @@ void gbsa_mapper_free(gbsa_mapper* m) {
     gbsa_mapper_free(m->twin);
     if (m->side) cudaStreamSynchronize(m->side);
     if (m->st) cudaStreamSynchronize(m->st);
+    try {
+        l2_window_attach(*m, false);
+    } catch (const Error&) {
+    }
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
     if (m->copy_in) cudaStreamSynchronize(m->copy_in);
@@ -958,9 +1007,18 @@ int gbsa_map_reads(gbsa_mapper* m, const char* seqs, const uint64_t* offsets, co
             const int rc = gbsa_mapper_create(m->idx, &m->opt, m->max_reads, m->max_bases, &t);
             if (rc != GBSA_OK) throw Error(rc, t_last_error);
             m->twin = t;
+            if (!m->use_l2_window) {
+                l2_window_attach(*t, false);
+                t->use_l2_window = false;
+            }
         }
         if (m->twin) {
+            // the twin keeps its own L2 window registration (same window as m's)
+            const MapConfig own = m->twin->cfg;
             m->twin->cfg = m->cfg;
+            m->twin->cfg.l2_base = own.l2_base;
+            m->twin->cfg.l2_bytes = own.l2_bytes;
+            m->twin->cfg.l2_hit_ratio = own.l2_hit_ratio;
             m->twin->opt = m->opt;
             m->twin->fuse_index_bytes = m->fuse_index_bytes;
         }
@@ -1207,6 +1265,20 @@ int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out) {
 uint64_t gbsa_mapper_retries(const gbsa_mapper* m) { return m->retries + (m->twin ? m->twin->retries : 0); }
 
 int gbsa_mapper_fused_lookup(const gbsa_mapper* m) { return m->fused ? 1 : 0; }
+
+int gbsa_mapper_set_l2_window(gbsa_mapper* m, int on, uint64_t* window_bytes) {
+    return guarded([&] {
+        for (gbsa_mapper* x : {m, m->twin}) {
+            if (!x) continue;
+            GBSA_CUDA(cudaStreamSynchronize(x->st));
+            GBSA_CUDA(cudaStreamSynchronize(x->side));
+            l2_window_attach(*x, false);
+            x->use_l2_window = on != 0;
+            l2_window_attach(*x, true);
+        }
+        if (window_bytes) *window_bytes = m->cfg.l2_bytes;
+    });
+}
 
 int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes) {
     m->fuse_index_bytes = index_bytes;

@@ -89,6 +89,11 @@ struct MapConfig {
     int sort_mode;
     int count_bytes;    // accumulate algorithmic bytes
     int force_rescue;   // every read takes the rescue path (find_nams_rescue entry point)
+    // L2 access-policy window of the kernels that probe the index (the bucket table,
+    // marked persisting), or l2_bytes == 0 for none; host side only
+    const void* l2_base;
+    uint64_t l2_bytes;
+    float l2_hit_ratio;
 };
 
 // Reads shorter than this (and with at most kSmemSyncmers syncmers) are seeded

@@ -1597,6 +1597,31 @@ unsigned warp_grid(uint64_t items, int warps_per_block) {
 
 uint32_t nam_kernel_warps(uint32_t n_reads) { return warp_grid(n_reads, kWarpsPerBlock) * kWarpsPerBlock; }
 
+// Launches a kernel that probes the index, with the mapper's L2 access-policy window
+// (the bucket table held persisting in L2) as a launch attribute, so that only these
+// launches carry it and the caller's stream keeps its own attributes.
+template <class... Exp, class... Act>
+static void launch_probe(void (*kernel)(Exp...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                         const MapConfig& C, Act&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (C.l2_bytes) {
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(C.l2_base);
+        attr[0].val.accessPolicyWindow.num_bytes = C.l2_bytes;
+        attr[0].val.accessPolicyWindow.hitRatio = C.l2_hit_ratio;
+        attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    GBSA_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...));
+}
+
 void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens, uint32_t n,
                  ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
     if (!n) return;
@@ -1617,9 +1642,8 @@ void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig&
                         cudaStream_t st) {
     if (!n) return;
     const unsigned grid = warp_grid(n, kSeedWarps);
-    if (C.count_bytes)
-        k_seed_lookup<true><<<grid, 32 * kSeedWarps, 0, st>>>(P, I, C, seqs, offs, lens, n, rec, A, ctr);
-    else k_seed_lookup<false><<<grid, 32 * kSeedWarps, 0, st>>>(P, I, C, seqs, offs, lens, n, rec, A, ctr);
+    launch_probe(C.count_bytes ? k_seed_lookup<true> : k_seed_lookup<false>, grid, 32 * kSeedWarps, 0, st, C, P, I, C,
+                 seqs, offs, lens, n, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
@@ -1629,16 +1653,16 @@ void launch_lookup_long(const IndexView& I, const MapConfig& C, uint32_t n, Read
     // sized for n long reads (every read, for long-read parameter sets); warps beyond
     // the long-list count exit at once
     const unsigned blocks = warp_grid(n, kWarpsPerBlock);
-    if (C.count_bytes) k_lookup_long<true><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
-    else k_lookup_long<false><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
+    launch_probe(C.count_bytes ? k_lookup_long<true> : k_lookup_long<false>, blocks, 32 * kWarpsPerBlock, 0, st, C, I,
+                 C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
 void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st) {
     if (!n) return;
-    if (C.count_bytes) k_lookup<true><<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
-    else k_lookup<false><<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(I, C, n, rec, A, ctr);
+    launch_probe(C.count_bytes ? k_lookup<true> : k_lookup<false>, warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0,
+                 st, C, I, C, n, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 
@@ -1671,7 +1695,7 @@ void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, Rea
     // persistent, kRescueBlocksPerSm per SM (at most one scratch slot per warp)
     const unsigned blocks =
         std::min<unsigned>(warp_grid(n_reads, kWarpsPerBlock), (unsigned)device_sm_count() * kRescueBlocksPerSm);
-    k_rescue<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(I, C, rec, A, ctr);
+    launch_probe(k_rescue, blocks, 32 * kWarpsPerBlock, 0, st, C, I, C, rec, A, ctr);
     GBSA_LAUNCHED();
 }
 

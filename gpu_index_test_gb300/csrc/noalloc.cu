@@ -18,8 +18,9 @@
 // array's device address with cudaGetSymbolAddress and caches it; make that first
 // call before any stream capture.  All calls share the array and it keeps the last
 // call's contents: the status words are cleared at the start of every call, and
-// calls that overlap on the GPU (different streams, threads or graph nodes running
-// at the same time) race on it.
+// calls that overlap on the GPU (different streams or threads running at the same
+// time) race on it.  Every call waits for its stream twice (it reads the total and
+// the status words back to the host before returning).
 #include <mutex>
 
 #include "map.cuh"
@@ -119,8 +120,9 @@ __global__ void __launch_bounds__(1024) k_noalloc_scan(uint64_t* offsets, uint32
     const uint32_t t = threadIdx.x, lane = t & 31, wid = t >> 5;
     if (t == 0) s_carry = 0;
     __syncthreads();
-    for (uint32_t base = 0; base < n; base += 1024) {
-        const uint32_t i = base + t;
+    // 64-bit indices: with 32-bit ones a count near 2^32 would wrap and never end
+    for (uint64_t base = 0; base < n; base += 1024) {
+        const uint64_t i = base + t;
         const uint64_t v = i < n ? offsets[i] : 0;
         const uint64_t inc = warp_inclusive_sum(v);
         if (lane == 31) s_warp[wid] = inc;

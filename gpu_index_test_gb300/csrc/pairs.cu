@@ -299,13 +299,21 @@ extern "C" int gbsa_nam_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_n
         GBSA_CUDA(cudaMemcpyAsync(&total, d_nam_offsets + 2ull * n_pairs, 8, cudaMemcpyDeviceToHost, st));
         GBSA_CUDA(cudaStreamSynchronize(st));
         const uint64_t slots = total + (uint64_t)GBSA_NAM_PAIRS_TOP_K * n_pairs + 1;
-        DeviceBuffer flags(total + 1), lists(sizeof(gbsa_nam_pair) * slots), stacks(8 * slots);
+        // scratch in stream order (cudaMalloc / cudaFree would wait for the whole device,
+        // other callers' work included)
+        const size_t b_flags = (total + 1 + 255) & ~size_t(255);
+        const size_t b_lists = (sizeof(gbsa_nam_pair) * slots + 255) & ~size_t(255);
+        uint8_t* scratch = nullptr;
+        GBSA_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), b_flags + b_lists + 8 * slots, st));
         const int span = (int)mu + 10 * (int)sigma;
         k_nam_pairs<<<grid_for(n_pairs, 128, (unsigned)device_sm_count() * 16), 128, 0, st>>>(
-            d_nams, d_nam_offsets, n_pairs, layout, span, max_tries, flags.as<uint8_t>(),
-            lists.as<gbsa_nam_pair>(), stacks.as<int>(), d_pairs, d_counts);
+            d_nams, d_nam_offsets, n_pairs, layout, span, max_tries, scratch,
+            reinterpret_cast<gbsa_nam_pair*>(scratch + b_flags), reinterpret_cast<int*>(scratch + b_flags + b_lists),
+            d_pairs, d_counts);
+        const cudaError_t launch = cudaGetLastError();
+        GBSA_CUDA(cudaFreeAsync(scratch, st));
+        GBSA_CUDA(launch);
         GBSA_LAUNCHED();
-        GBSA_CUDA(cudaStreamSynchronize(st));   // the scratch is freed on return
         return GBSA_OK;
     } catch (const Error& e) {
         set_last_error(e.what());

@@ -68,7 +68,8 @@ struct gbsa_server {
                                           r.nam_offsets, r.frac, r.rescued);
             {
                 std::lock_guard<std::mutex> g(mu);
-                done.push_back(Done{r.tag, rc, r.nam_offsets[r.n_reads]});
+                // a failed call may not have written the offsets: report no NAMs
+                done.push_back(Done{r.tag, rc, rc == GBSA_OK ? r.nam_offsets[r.n_reads] : 0});
                 --in_flight;
             }
             cv_done.notify_all();

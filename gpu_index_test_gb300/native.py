@@ -63,6 +63,8 @@ def lib():
             "gbsa_mapper_last_alg_bytes": (u64, [vp]),
             "gbsa_mapper_last_alg_sectors": (u64, [vp]),
             "gbsa_bench_gather": (i32, [u64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "gbsa_bench_gather_index": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double)]),
             "gbsa_classify_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, C.c_float, vp, vp]),
             "gbsa_nam_pairs_device": (i32, [vp, vp, u32, i32, C.c_float, C.c_float, u32, vp, vp, vp]),
             "gbsa_extend_seeds_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, i32, vp, vp, vp]),
@@ -86,6 +88,7 @@ def lib():
             "gbsa_mapper_retries": (u64, [vp]),
             "gbsa_mapper_fused_lookup": (i32, [vp]),
             "gbsa_mapper_set_fuse_limit": (i32, [vp, u64]),
+            "gbsa_mapper_set_l2_window": (i32, [vp, i32, C.POINTER(u64)]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -129,6 +132,14 @@ def bench_gather(buffer_bytes):
     a, b = C.c_double(), C.c_double()
     _check(lib().gbsa_bench_gather(buffer_bytes, C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def bench_gather_index(index):
+    """The lookup's dependent gather pattern (bucket pair, then the bucket's first entry)
+    on the index's own buffers: (probes/s, sectors/s, GB/s)."""
+    a, b, c = C.c_double(), C.c_double(), C.c_double()
+    _check(lib().gbsa_bench_gather_index(index.h, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
 
 
 def classify_pairs_device(d_nams, d_nam_offsets, n_pairs, d_types, layout=0, dropoff=0.5, mu=300.0, sigma=100.0,
@@ -336,6 +347,12 @@ class Mapper:
     def set_fuse_limit(self, index_bytes):
         """Largest index (entry bytes) seeded and looked up in one kernel; 0: never."""
         _check(lib().gbsa_mapper_set_fuse_limit(self.h, int(index_bytes)))
+
+    def set_l2_window(self, on=True):
+        """Bucket table held in L2 (access-policy window); returns the window's bytes."""
+        b = C.c_uint64()
+        _check(lib().gbsa_mapper_set_l2_window(self.h, 1 if on else 0, C.byref(b)))
+        return b.value
 
     def fused_lookup(self):
         """Whether the last batch ran seeding and lookup as one kernel."""

@@ -190,7 +190,8 @@ int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_
  * device array of about 3.3 MB (64 warp slots for reads of up to GBSA_MAX_READ_LEN
  * bases), held by every GPU that loads the library until the process exits.  The
  * first call on a device looks up that array's address (make it before any stream
- * capture); calls that overlap on the GPU race on the array.  d_out_offsets has
+ * capture); calls that overlap on the GPU race on the array.  Each call waits for
+ * its stream before it returns (it reads the total back).  d_out_offsets has
  * n_reads + 1 entries and is always filled; *out_total receives the total; reads
  * longer than GBSA_MAX_READ_LEN give GBSA_ERR_READ_TOO_LONG and a total above
  * out_capacity gives GBSA_ERR_CAPACITY (nothing written to d_out). */
@@ -424,6 +425,13 @@ uint64_t gbsa_mapper_last_alg_sectors(const gbsa_mapper* m);
  * sectors per second and the corresponding GB/s.  Measurement utility for the
  * lookup's roofline; no reference counterpart. */
 int gbsa_bench_gather(uint64_t buffer_bytes, double* sectors_per_s, double* gb_per_s);
+/* The same measurement on the lookup's own footprint and access pattern: for uniform
+ * random keys, the bucket bound pair from idx's bucket table, then the bucket's first
+ * entry (a dependent load), 8 probes in flight per thread; reports probes per second,
+ * 32-byte sectors per second (the pair's sector plus the entry's, for a non-empty
+ * bucket) and the corresponding GB/s.  The random-gather ceiling of the lookup; no
+ * reference counterpart. */
+int gbsa_bench_gather_index(const gbsa_index* idx, double* probes_per_s, double* sectors_per_s, double* gb_per_s);
 /* Record CUDA events between the stages of later batches; gbsa_mapper_stage_ms
  * returns the last batch's milliseconds for: seeding + lookup (one kernel, a warp
  * per read; seeding alone when gbsa_mapper_fused_lookup is 0), long-read seeding,
@@ -452,6 +460,13 @@ int gbsa_mapper_fused_lookup(const gbsa_mapper* m);
  * as one kernel; default 2 GiB.  0 runs them as two kernels for every index.  The
  * results are the same either way.  No reference counterpart. */
 int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes);
+/* Hold the index's bucket table in L2 during the probing kernels (on = 1, the
+ * default) through an access-policy window marked persisting, when the table fits
+ * the device's largest window (the 32-bit table of up to 2^25 buckets); the
+ * process's persisting L2 set-aside is raised for it while such mappers live.
+ * *window_bytes (may be NULL) receives the window's size, 0 when none is used.  The
+ * results are the same either way.  No reference counterpart. */
+int gbsa_mapper_set_l2_window(gbsa_mapper* m, int on, uint64_t* window_bytes);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the
  * merge and of the sort (the block sort, for reads with many NAMs), then the hit

@@ -281,50 +281,17 @@ struct IndexCpu {
     }
 };
 
-/* index.cu:28-41 (count_randstrobes), 280-311 (assign_randstrobes with the
- * RandstrobeGenerator of randstrobes.cu:161-190), 143-244 (populate). */
-void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
-              uint32_t n_contigs, float f) {
-    const gbsa_params& p = idx.p;
-    std::vector<std::vector<Syncmer>> sms(n_contigs);
-    std::vector<uint64_t> counts(n_contigs), offs(n_contigs);
-    uint64_t total = 0;
-    for (uint32_t c = 0; c < n_contigs; ++c) {
-        canonical_syncmers(p, seqs + offsets[c], lengths[c], sms[c]);
-        const uint64_t n = sms[c].size();
-        counts[c] = n < p.w_min ? 0 : n - p.w_min;
-        offs[c] = total;
-        total += counts[c];
-    }
-    idx.info.tot_strobemer_count = total;
-    idx.rs.assign(total, gbsa_ref_randstrobe{0, 0, 0});
-    for (uint32_t c = 0; c < n_contigs; ++c) {
-        if (lengths[c] < p.w_max) continue;               /* index.cu:282-284 */
-        uint64_t o = offs[c];
-        const auto& v = sms[c];
-        for (unsigned j = 0; j + p.w_min < v.size(); ++j) {
-            const Strobe r = randstrobe_at(p, v, j);
-            uint32_t packed = (uint32_t)((uint64_t)c << 8);
-            packed = packed + (r.s2 - r.s1);
-            idx.rs[o++] = gbsa_ref_randstrobe{r.hash, r.s1, packed};
-        }
-    }
-    std::sort(idx.rs.begin(), idx.rs.end(), [](const gbsa_ref_randstrobe& a, const gbsa_ref_randstrobe& b) {
-        if (a.hash != b.hash) return a.hash < b.hash;
-        if (a.position != b.position) return a.position < b.position;
-        return a.packed < b.packed;
-    });
-
-    /* bucket table and repetition statistics, index.cu:176-243 */
-    const int bits = idx.bits;
+/* Bucket table and repetition statistics of a sorted entry array (index.cu:176-243):
+ * starts (2^bits + 1 entries), filter_cutoff and the counters of info. */
+void finish_index(const gbsa_ref_randstrobe* rs, uint64_t n, int bits, float f, std::vector<uint64_t>& st,
+                  uint32_t& filter_cutoff, gbsa_index_info& info) {
     const uint64_t nb = (1ULL << bits) + 1;
-    auto& st = idx.starts;
     st.clear();
     st.reserve(nb);
     std::vector<uint64_t> rep_counts;
     uint64_t once = 0, high = 0, mid = 0;
-    uint64_t unique = idx.rs.empty() ? 0 : 1;
-    uint64_t prev = idx.rs.empty() ? 0 : idx.rs[0].hash;
+    uint64_t unique = n == 0 ? 0 : 1;
+    uint64_t prev = n == 0 ? 0 : rs[0].hash;
     unsigned run = 0;
     auto close_run = [&](unsigned cnt) {
         if (cnt == 1) {
@@ -335,8 +302,8 @@ void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const ui
             rep_counts.push_back(cnt);
         }
     };
-    for (uint64_t pos = 0; pos < idx.rs.size(); ++pos) {
-        const uint64_t cur = idx.rs[pos].hash;
+    for (uint64_t pos = 0; pos < n; ++pos) {
+        const uint64_t cur = rs[pos].hash;
         if (cur == prev) {
             ++run;
             continue;
@@ -351,7 +318,7 @@ void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const ui
         prev = cur;
     }
     close_run(run);
-    while (st.size() < nb) st.push_back(idx.rs.size());
+    while (st.size() < nb) st.push_back(n);
 
     std::sort(rep_counts.begin(), rep_counts.end(), [](uint64_t a, uint64_t b) { return a > b; });
     const uint64_t index_cutoff = (uint64_t)((float)unique * f);   /* float product, index.cu:232 */
@@ -363,12 +330,56 @@ void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const ui
     } else {
         fc = 30;
     }
-    idx.filter_cutoff = fc;
-    idx.info.tot_occur_once = once;
-    idx.info.tot_high_ab = high;
-    idx.info.tot_mid_ab = mid;
-    idx.info.index_cutoff = index_cutoff;
-    idx.info.distinct_strobemers = unique;
+    filter_cutoff = fc;
+    info.tot_occur_once = once;
+    info.tot_high_ab = high;
+    info.tot_mid_ab = mid;
+    info.index_cutoff = index_cutoff;
+    info.distinct_strobemers = unique;
+}
+
+/* Entries of contig c (index.cu:280-311, assign_randstrobes with the RandstrobeGenerator
+ * of randstrobes.cu:161-190): fn(entry) for each, in generation order. */
+template <class Fn>
+void contig_entries(const gbsa_params& p, const char* seq, uint64_t len, uint32_t c, std::vector<Syncmer>& v,
+                    Fn&& fn) {
+    v.clear();
+    canonical_syncmers(p, seq, len, v);
+    if (len < p.w_max) return;                                  /* index.cu:282-284 */
+    for (unsigned j = 0; j + p.w_min < v.size(); ++j) {
+        const Strobe r = randstrobe_at(p, v, j);
+        uint32_t packed = (uint32_t)((uint64_t)c << 8);
+        packed = packed + (r.s2 - r.s1);
+        fn(gbsa_ref_randstrobe{r.hash, r.s1, packed});
+    }
+}
+
+/* index.cu:28-41 (count_randstrobes), 280-311 (assign_randstrobes with the
+ * RandstrobeGenerator of randstrobes.cu:161-190), 143-244 (populate). */
+void populate(IndexCpu& idx, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+              uint32_t n_contigs, float f) {
+    const gbsa_params& p = idx.p;
+    std::vector<Syncmer> sm;
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < n_contigs; ++c) {
+        sm.clear();
+        canonical_syncmers(p, seqs + offsets[c], lengths[c], sm);
+        const uint64_t n = sm.size();
+        total += n < p.w_min ? 0 : n - p.w_min;
+    }
+    idx.info.tot_strobemer_count = total;
+    idx.rs.clear();
+    idx.rs.reserve(total);
+    for (uint32_t c = 0; c < n_contigs; ++c)
+        contig_entries(p, seqs + offsets[c], lengths[c], c, sm, [&](const gbsa_ref_randstrobe& e) { idx.rs.push_back(e); });
+    /* contigs shorter than w_max count but assign nothing: their slots stay zero */
+    idx.rs.resize(total, gbsa_ref_randstrobe{0, 0, 0});
+    std::sort(idx.rs.begin(), idx.rs.end(), [](const gbsa_ref_randstrobe& a, const gbsa_ref_randstrobe& b) {
+        if (a.hash != b.hash) return a.hash < b.hash;
+        if (a.position != b.position) return a.position < b.position;
+        return a.packed < b.packed;
+    });
+    finish_index(idx.rs.data(), idx.rs.size(), idx.bits, f, idx.starts, idx.filter_cutoff, idx.info);
 }
 
 /* ---- nam.cu ------------------------------------------------------------------ */
@@ -781,6 +792,98 @@ oracle_index* oracle_index_load(const gbsa_params* p, const gbsa_ref_randstrobe*
     h->idx.info.bits = bits;
     h->idx.info.filter_cutoff = filter_cutoff;
     return h;
+}
+
+/* Checks an index built elsewhere (the GPU's, exported to host memory) against this
+ * restatement without building one: the entries the contigs generate (index.cu:280-311,
+ * generated per contig on n_threads threads) must be the given entries as a multiset
+ * (same count, and two order-independent 64-bit sums of a mix of every entry), the
+ * given entries must be sorted by (hash, position, packed), which orders a multiset
+ * uniquely, and the bucket table and filter cutoff recomputed from them must be the
+ * given ones.  Returns 0 when all hold, else the first failed check: 1 count, 2 order,
+ * 3 multiset digest, 4 bucket table, 5 filter cutoff.  report (5 values): expected
+ * count, given count, index of the first out-of-order entry (or UINT64_MAX), expected
+ * filter cutoff, first differing bucket (or UINT64_MAX). */
+int oracle_index_verify(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+                        uint32_t n_contigs, float f, const gbsa_ref_randstrobe* rs, uint64_t n,
+                        const uint64_t* starts, int bits, uint32_t filter_cutoff, int n_threads, uint64_t* report) {
+    auto mix = [](uint64_t x) {
+        x += 0x9E3779B97F4A7C15ULL;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+        return x ^ (x >> 31);
+    };
+    auto digest = [&](const gbsa_ref_randstrobe& e, uint64_t& s1, uint64_t& s2) {
+        const uint64_t a = mix(e.hash);
+        const uint64_t b = mix(a ^ (((uint64_t)e.position << 32) | e.packed));
+        s1 += b;
+        s2 += mix(b ^ 0xD6E8FEB86659FD93ULL);
+    };
+    for (int i = 0; i < 5; ++i) report[i] = 0;
+    report[1] = n;
+    report[2] = UINT64_MAX;
+    report[4] = UINT64_MAX;
+    /* expected entries, per contig in parallel */
+    const int nt = n_threads <= 0 ? (int)std::max(1u, std::thread::hardware_concurrency()) : n_threads;
+    std::atomic<uint32_t> next{0};
+    std::vector<uint64_t> cnt(nt, 0), d1(nt, 0), d2(nt, 0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) {
+        th.emplace_back([&, t]() {
+            std::vector<Syncmer> sm;
+            for (;;) {
+                const uint32_t c = next.fetch_add(1);
+                if (c >= n_contigs) break;
+                uint64_t emitted = 0;
+                contig_entries(*p, seqs + offsets[c], lengths[c], c, sm, [&](const gbsa_ref_randstrobe& e) {
+                    digest(e, d1[t], d2[t]);
+                    ++emitted;
+                });
+                const uint64_t ns = sm.size();
+                const uint64_t slots = ns < p->w_min ? 0 : ns - p->w_min;
+                /* slots the reference counts but does not assign stay zero entries */
+                for (uint64_t z = emitted; z < slots; ++z) digest(gbsa_ref_randstrobe{0, 0, 0}, d1[t], d2[t]);
+                cnt[t] += slots;
+            }
+        });
+    }
+    for (auto& x : th) x.join();
+    uint64_t want = 0, w1 = 0, w2 = 0;
+    for (int t = 0; t < nt; ++t) {
+        want += cnt[t];
+        w1 += d1[t];
+        w2 += d2[t];
+    }
+    report[0] = want;
+    if (want != n) return 1;
+    /* order and digest of the given entries */
+    uint64_t g1 = 0, g2 = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (i > 0) {
+            const gbsa_ref_randstrobe& a = rs[i - 1];
+            const gbsa_ref_randstrobe& b = rs[i];
+            const bool le = a.hash != b.hash ? a.hash < b.hash
+                                             : (a.position != b.position ? a.position < b.position : a.packed <= b.packed);
+            if (!le) {
+                report[2] = i;
+                return 2;
+            }
+        }
+        digest(rs[i], g1, g2);
+    }
+    if (g1 != w1 || g2 != w2) return 3;
+    std::vector<uint64_t> st;
+    uint32_t fc = 0;
+    gbsa_index_info info{};
+    finish_index(rs, n, bits, f, st, fc, info);
+    report[3] = fc;
+    for (uint64_t i = 0; i < st.size(); ++i)
+        if (st[i] != starts[i]) {
+            report[4] = i;
+            return 4;
+        }
+    if (fc != filter_cutoff) return 5;
+    return 0;
 }
 
 void oracle_index_free(oracle_index* idx) { delete idx; }

@@ -39,6 +39,11 @@ oracle_index* oracle_index_build(const gbsa_params* p, const char* seqs, const u
                                  const uint64_t* lengths, uint32_t n_contigs, int bits, float f);
 oracle_index* oracle_index_load(const gbsa_params* p, const gbsa_ref_randstrobe* rs, uint64_t n,
                                 const uint64_t* starts, int bits, uint32_t filter_cutoff);
+/* Checks an index built elsewhere against the restatement without building one
+ * (generated entries as a multiset, order, bucket table, filter cutoff); 0 = equal. */
+int oracle_index_verify(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint64_t* lengths,
+                        uint32_t n_contigs, float f, const gbsa_ref_randstrobe* rs, uint64_t n,
+                        const uint64_t* starts, int bits, uint32_t filter_cutoff, int n_threads, uint64_t* report);
 void oracle_index_free(oracle_index* idx);
 void oracle_index_info(const oracle_index* idx, gbsa_index_info* out);
 const gbsa_ref_randstrobe* oracle_index_randstrobes(const oracle_index* idx);

@@ -72,6 +72,8 @@ def lib():
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_index_verify.restype = C.c_int
+        L.oracle_index_verify.argtypes = [P, vp, vp, vp, u32, C.c_float, vp, u64, vp, C.c_int, u32, C.c_int, vp]
         L.oracle_algorithmic_bytes.restype = C.c_int
         L.oracle_algorithmic_bytes.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64), C.c_int]
@@ -108,6 +110,26 @@ def randstrobes_query(p, seq: bytes):
     n = lib().oracle_randstrobes_query(C.byref(p), buf.ctypes.data, len(seq), out.ctypes.data, cap)
     assert n >= 0
     return out[:n].copy()
+
+
+VERIFY_CHECKS = {0: "equal", 1: "entry count", 2: "entry order", 3: "entry multiset", 4: "bucket table",
+                 5: "filter cutoff"}
+
+
+def verify_index(p, genome, randstrobes, starts, bits, filter_cutoff, f=0.0002, n_threads=0):
+    """Checks an index built elsewhere (exported to host arrays) against the restatement
+    without building one: (first failed check or "equal", report dict)."""
+    rs = np.ascontiguousarray(randstrobes)
+    st = np.ascontiguousarray(starts, np.uint64)
+    rep = np.zeros(5, np.uint64)
+    rc = lib().oracle_index_verify(C.byref(p), genome.seq.ctypes.data,
+                                   np.ascontiguousarray(genome.offsets, np.uint64).ctypes.data,
+                                   np.ascontiguousarray(genome.lengths, np.uint64).ctypes.data, len(genome.lengths),
+                                   f, rs.ctypes.data if len(rs) else None, len(rs), st.ctypes.data, bits,
+                                   filter_cutoff, n_threads, rep.ctypes.data)
+    return VERIFY_CHECKS.get(rc, str(rc)), {"expected_entries": int(rep[0]), "entries": int(rep[1]),
+                                            "first_unordered": int(rep[2]), "expected_filter_cutoff": int(rep[3]),
+                                            "first_bucket_diff": int(rep[4])}
 
 
 class Index:

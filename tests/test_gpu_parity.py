@@ -284,6 +284,53 @@ def test_read_bytes_and_alignments_against_oracle():
     assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and nams_equal(x[0], y[0])
 
 
+def test_index_with_2_28_buckets_against_oracle():
+    """The human-scale bucket table (bits = 28, the value pick_bits gives a 3.1 Gbp
+    genome; 2^28 + 1 starts, a 1 GB 32-bit copy) forced on a 20 Mbp genome: the GPU
+    index equals the oracle's entry for entry and bucket for bucket, passes the
+    oracle's sort-free check, and both lookup forms (fused, and the two kernels that
+    indexes over 2 GiB use) give the oracle's NAMs."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.2, seed=91))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g, bits=28)
+    info = idx.info()
+    assert info.bits == 28
+    op = oracle_py.params_from_read_length(150)
+    o = oracle_py.Index.build(op, g, bits=28)
+    rs, st = idx.export()
+    assert len(st) == (1 << 28) + 1
+    assert (rs == o.randstrobes()).all() and (st == o.starts()).all()
+    assert info.filter_cutoff == o.info().filter_cutoff
+    assert oracle_py.verify_index(op, g, rs, st, 28, info.filter_cutoff)[0] == "equal"
+    del rs, st
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=15_000, seed=92))
+    y = o.map_reads(reads, n_threads=8)
+    m = native.Mapper(idx)
+    for fuse_limit in (None, 0):
+        if fuse_limit is not None:
+            m.set_fuse_limit(fuse_limit)
+        x = m.map_reads(reads)
+        assert bool(m.fused_lookup()) == (fuse_limit is None)
+        assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+        assert nams_equal(x[0], y[0])
+
+
+def test_l2_window_gives_the_same_nams():
+    """With the bucket table held in L2 through an access-policy window (the default
+    when the table fits one) and without it, the NAMs are the same."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.05, seed=93))
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=20_000, seed=94))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    m = native.Mapper(idx)
+    on = m.set_l2_window(True)
+    a = m.map_reads(reads)
+    assert m.set_l2_window(False) == 0
+    b = m.map_reads(reads)
+    assert on >= 0
+    assert (a[1] == b[1]).all() and (a[2] == b[2]).all() and (a[3] == b[3]).all()
+    assert nams_equal(a[0], b[0])
+
+
 def test_two_kernel_seeding_and_lookup_matches_fused():
     """Indexes over 2 GiB of entries run seeding and lookup as two kernels; forced
     here on a small index, the NAMs equal those of the fused kernel (which ran), for
@@ -475,6 +522,8 @@ def test_sector_count_and_gather_bench():
     hbm = native.bench_gather(1 << 30)[1]
     l2 = native.bench_gather(16 << 20)[1]
     assert hbm > 100 and l2 > hbm
+    probes, sectors, gbs = native.bench_gather_index(idx)
+    assert probes > 0 and probes <= sectors <= 2 * probes and gbs > 0
 
 
 @pytest.mark.parametrize("params", [(0.5, 300.0, 100.0), (0.3, 250.3, 37.7)])

@@ -166,3 +166,28 @@ def test_nam_pair_heap_keeps_the_best_forty():
                     if 0 <= int(b["ref_start"][0] - b["query_start"][0]) - int(a["ref_start"][0]) < 1300),
                    reverse=True)
     assert sorted(paired["score"].tolist(), reverse=True) == joint[:40]
+
+
+def test_index_verifier_accepts_the_oracle_index_and_finds_planted_faults(case):
+    """The sort-free index check (used on indexes too large to build on the host) accepts
+    the oracle's own index and names a planted fault: a changed entry, two swapped
+    entries, a moved bucket bound and another filter cutoff."""
+    c, p, idx = case
+    rs, st = idx.randstrobes(), idx.starts()
+    info = idx.info()
+    check = lambda r, s, fc=info.filter_cutoff: oracle_py.verify_index(p, c.genome, r, s, info.bits, fc)[0]
+    assert check(rs, st) == "equal"
+    if len(rs) < 3:
+        return
+    bad = rs.copy()
+    bad[len(bad) // 2]["position"] += 1
+    assert check(bad, st) in ("entry multiset", "entry order")
+    i = int(np.nonzero(rs["hash"][1:] != rs["hash"][:-1])[0][0])   # rs[i] < rs[i + 1]
+    bad = rs.copy()
+    bad[[i, i + 1]] = bad[[i + 1, i]]
+    assert check(bad, st) == "entry order"
+    bst = st.copy()
+    j = int(np.nonzero(bst[1:] > bst[:-1])[0][0]) + 1
+    bst[j] -= 1
+    assert check(rs, bst) == "bucket table"
+    assert check(rs, st, info.filter_cutoff + 1) == "filter cutoff"
