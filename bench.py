@@ -462,6 +462,109 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def batched_measure(idx, reads, items, d_seq, d_off, d_len, plain_out, plain_ms, plain_e2e_s, steps, small=10_000):
+    """The batched form beside the plain one on the same reads: device reads/s (the
+    graph per batch, inputs in HBM), e2e reads/s (host entry point, pinned buffers,
+    copies inside the timing), per-batch latency for small batches of `small` reads
+    (plain device entry point against the batched one), and a byte compare of the
+    batched form's NAMs, offsets, fractions and rescue flags with the plain form's."""
+    import torch
+    from gpu_index_test_gb300 import abi, native
+
+    dev = d_seq.device
+    stream = torch.cuda.current_stream(dev)
+    n = reads.n
+    cap = 30 * n
+    b = native.Batcher(idx, max_reads=n, max_bases=int(reads.lengths.sum()))
+    cfg = b.config().as_dict()
+    tuned = native.batch_config_default()[1]
+    d_items = torch.from_numpy(items.view(np.int32)).to(dev)
+    n_items = len(items) - 1
+    d_nams = torch.empty(cap * 44, dtype=torch.uint8, device=dev)
+    d_noff = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    d_frac = torch.empty(n, dtype=torch.float32, device=dev)
+    d_resc = torch.empty(n, dtype=torch.uint8, device=dev)
+
+    def step(k=n, k_items=n_items):
+        return b.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), k, d_nams.data_ptr(), cap,
+                                  d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), d_items.data_ptr(), k_items,
+                                  stream.cuda_stream)
+
+    for _ in range(3):
+        tot = step()
+    torch.cuda.synchronize()
+    p_nams, p_noff, p_frac, p_resc, p_tot = plain_out
+    exact = bool(tot == p_tot and torch.equal(d_nams[: tot * 44], p_nams[: tot * 44]) and torch.equal(d_noff, p_noff)
+                 and torch.equal(d_frac, p_frac) and torch.equal(d_resc, p_resc))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # e2e: host entry point, pinned reads in, NAMs / offsets / fractions / flags out
+    h_seq = torch.from_numpy(reads.seq).pin_memory()
+    h_nams = torch.empty(cap * 44, dtype=torch.uint8).pin_memory()
+    h_noff = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    h_frac = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_resc = torch.empty(n, dtype=torch.uint8).pin_memory()
+    L = native.lib()
+
+    def e2e():
+        rc = L.gbsa_batcher_map(b.h, h_seq.data_ptr(), reads.offsets.ctypes.data, reads.lengths.ctypes.data, n,
+                                items.ctypes.data, n_items, h_nams.data_ptr(), cap, h_noff.data_ptr(),
+                                h_frac.data_ptr(), h_resc.data_ptr())
+        if rc != 0:
+            raise RuntimeError(f"gbsa_batcher_map failed: {rc}")
+
+    e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / steps
+    e2e_exact = bool(int(h_noff[n]) == p_tot and torch.equal(h_noff, p_noff.cpu())
+                     and torch.equal(h_nams[: p_tot * 44], p_nams[: p_tot * 44].cpu()))
+    # small batches: the first `small` reads (whole items) through both device entry points
+    k_items = int(np.searchsorted(items, small, side="right")) - 1
+    k = int(items[k_items])
+    pm = native.Mapper(idx, max_reads=k, max_bases=int(reads.lengths[:k].sum()))
+
+    def small_plain():
+        return pm.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), k, d_nams.data_ptr(), cap,
+                                   d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), stream.cuda_stream)
+
+    lat = {}
+    for name, fn in (("plain", small_plain), ("batched", lambda: step(k, k_items))):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(50):
+            fn()
+        torch.cuda.synchronize()
+        lat[name] = (time.perf_counter() - t0) / 50
+    pm.free()
+    stats = b.stats()
+    b.free()
+    return {
+        "form": "one CUDA graph per batch; seeding + lookup one persistent kernel pulling work items (read pairs) "
+                "from a device queue; NAM phase kernels in the same graph",
+        "config": cfg, "config_source": "tuned.json (autotuner)" if tuned else "built-in",
+        "device_reads_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 3),
+        "vs_plain_device": round(plain_ms / ms, 3),
+        "e2e_reads_per_s": round(n / e2e_s, 1), "vs_plain_e2e": round(plain_e2e_s / e2e_s, 3),
+        "small_batches": {"reads": k, "plain_ms": round(lat["plain"] * 1e3, 3),
+                          "batched_ms": round(lat["batched"] * 1e3, 3),
+                          "plain_reads_per_s": round(k / lat["plain"], 1),
+                          "batched_reads_per_s": round(k / lat["batched"], 1),
+                          "vs_plain": round(lat["plain"] / lat["batched"], 3),
+                          "timing": "host wall clock per call (each call returns after its batch ends), 50 calls"},
+        "bit_exact_vs_plain": exact, "e2e_bit_exact_vs_plain": e2e_exact, "graph": stats,
+    }
+
+
 def other_config(name, scale, cpu_seconds, steps=3):
     """Device throughput and parity of another configuration: its genome and reads, the
     GPU index, one warm-up and `steps` timed device batches (CUDA events), then the
@@ -469,7 +572,7 @@ def other_config(name, scale, cpu_seconds, steps=3):
     fractions and rescue flags (for a genome above HOST_BUILD_MAX_BP the oracle uses the
     GPU's index after checking it without a host build)."""
     import torch
-    from gpu_index_test_gb300 import abi, native
+    from gpu_index_test_gb300 import abi, native, synth
 
     g, reads, gen_s, gp, rp = workload(scale, 0, name)
     p = native.params_from_read_length(150)
@@ -506,6 +609,32 @@ def other_config(name, scale, cpu_seconds, steps=3):
     ms = e0.elapsed_time(e1) / steps
     fused = bool(m.fused_lookup())
     noff = d_noff.cpu().numpy().view(np.uint64)
+    # the batched form on the same reads (work items: single-end reads and pairs)
+    items = synth.read_items(rp)
+    d_items = torch.from_numpy(items.view(np.int32)).to(dev)
+    b = native.Batcher(idx, max_reads=n, max_bases=int(reads.lengths.sum()))
+    b_nams = torch.empty(cap * 44, dtype=torch.uint8, device=dev)
+    b_noff = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    b_frac = torch.empty(n, dtype=torch.float32, device=dev)
+    b_resc = torch.empty(n, dtype=torch.uint8, device=dev)
+
+    def bstep():
+        return b.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, b_nams.data_ptr(), cap,
+                                  b_noff.data_ptr(), b_frac.data_ptr(), b_resc.data_ptr(), d_items.data_ptr(),
+                                  len(items) - 1, stream.cuda_stream)
+
+    bstep()
+    bstep()
+    e0.record(stream)
+    for _ in range(steps):
+        btot = bstep()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bms = e0.elapsed_time(e1) / steps
+    b_exact = bool(btot == total and torch.equal(b_nams[: total * 44], d_nams[: total * 44])
+                   and torch.equal(b_noff, d_noff) and torch.equal(b_frac, d_frac) and torch.equal(b_resc, d_resc))
+    b.free()
+    del b_nams, b_noff, b_frac, b_resc, d_items
 
     def first(k):
         t = int(noff[k])
@@ -513,15 +642,17 @@ def other_config(name, scale, cpu_seconds, steps=3):
                 d_resc[:k].cpu().numpy())
 
     m.free()
-    del d_nams
-    torch.cuda.empty_cache()
     cpu, exact = cpu_baseline(g, reads, cpu_seconds, first, gpu_index=idx)
     idx.free()
+    del d_nams, d_seq, d_off, d_len, d_noff, d_frac, d_resc
     torch.cuda.empty_cache()
     return {"workload": WORKLOADS[name], "genome_bp": int(gp.total_len), "reads_per_batch": int(n),
             "index_entries": int(info.size), "index_bits": int(info.bits), "index_build_gpu_s": round(build_s, 3),
             "form": "seeding and lookup fused" if fused else "seeding and lookup as two kernels (index over 2 GiB)",
             "device_reads_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 3), "nams": int(total),
+            "batched": {"device_reads_per_s": round(n / (bms / 1e3), 1), "ms_per_batch": round(bms, 3),
+                        "vs_plain_device": round(ms / bms, 3), "work_items": int(len(items) - 1),
+                        "bit_exact_vs_plain": b_exact},
             "cpu_baseline": cpu, "bit_exact_vs_cpu_sample": exact}
 
 
@@ -565,7 +696,7 @@ def main():
     import __graft_entry__
 
     __graft_entry__.build()
-    from gpu_index_test_gb300 import abi, native
+    from gpu_index_test_gb300 import abi, native, synth
 
     g, reads, gen_s, gp, rp = workload(args.scale, rank, args.config)
     p = native.params_from_read_length(150)
@@ -851,6 +982,13 @@ def main():
         "flat_buffer_gather_gbs": {"512MB": round(gather_hbm, 1), "16MB": round(gather_l2, 1)},
     }
 
+    batched = None
+    if rank == 0:
+        items = synth.read_items(rp)
+        tot_plain = int(d_noff[n].item())
+        batched = batched_measure(idx, reads, items, d_seq, d_off, d_len, (d_nams, d_noff, d_frac, d_resc, tot_plain),
+                                  ms, e2e_s, max(3, args.steps))
+
     staging = None
     if world == 1 and args.fastq and args.config == "C2":
         staging = fastq_pipeline(m, reads, h_nams[: tot_nams_e2e * 44].numpy().view(abi.NAM),
@@ -890,10 +1028,6 @@ def main():
     others = None
     names = [x.strip() for x in args.other_configs.split(",") if x.strip() and x.strip() != args.config]
     if names and world == 1 and not args.no_cpu_baseline:
-        # the headline configuration's buffers are no longer needed
-        m.free()
-        del d_nams, h_nams
-        torch.cuda.empty_cache()
         others = {}
         for nm in names:
             try:
@@ -913,6 +1047,7 @@ def main():
         "e2e": {"value": round(job_throughput(n, world, e2e_s), 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": roofline,
+        "batched": batched,
         "served": served,
         "fastq_staging": staging,
         "cpu_baseline": cpu,

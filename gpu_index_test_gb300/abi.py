@@ -71,6 +71,26 @@ class MapOptions(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    """gbsa_batch_config: shape of the batched form's kernels (see include/gbsa.h)."""
+    _fields_ = [
+        ("seed_variant", C.c_int32),
+        ("lane_max_hits", C.c_uint32),
+        ("sort_variant", C.c_int32),
+        ("chunk_reads", C.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+SEED_VARIANTS = 6   # shapes of the batched form's seeding + lookup kernel
+
+
+def batch_config(seed_variant=0, lane_max_hits=160, sort_variant=0, chunk_reads=1 << 19):
+    return BatchConfig(seed_variant, lane_max_hits, sort_variant, chunk_reads)
+
+
 REF_RANDSTROBE = np.dtype([("hash", "<u8"), ("position", "<u4"), ("packed", "<u4")])
 QUERY_RANDSTROBE = np.dtype(
     [("hash", "<u8"), ("start", "<u4"), ("end", "<u4"), ("is_reverse", "u1"), ("_pad", "u1", (7,))]

@@ -15,10 +15,8 @@
 #include <thread>
 #include <vector>
 
-#include "index.h"
-#include "map.cuh"
+#include "mapper.h"
 #include "prims.cuh"
-#include "runtime.h"
 
 namespace gbsa {
 
@@ -223,54 +221,11 @@ static void write_sti(const gbsa_index& ix, const std::vector<gbsa_ref_randstrob
 
 }  // namespace gbsa
 
-struct gbsa_mapper {
-    const gbsa_index* idx = nullptr;
-    gbsa_map_options opt{};
-    gbsa::MapConfig cfg{};
-    cudaStream_t st = nullptr;
-    cudaStream_t side = nullptr;                           // rescue chain, beside the NAM kernels
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, rescue_ev = nullptr;
-    cudaStream_t side_lo = nullptr;                        // rescue chain of a batch on a caller's stream
-    cudaStream_t early = nullptr;                          // seeding + lookup of pipelined chunks
-    cudaEvent_t early_ev = nullptr;
-    uint32_t max_reads = 0;
-    uint64_t max_bases = 0;
-    gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
-        out_off, out_nams, out_frac, out_resc, resc_cycles, nam_notes, jobs, side_slots, lane_lists;
-    uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
-    uint32_t long_warps = 0;
-    gbsa::PinnedBuffer h_seqs, h_meta, h_out;
-    gbsa::PinnedBuffer h_status;   // counters + NAM total of the last enqueued batch
-    // pipelined host entry point: copy streams, the twin that maps every other chunk,
-    // events (reads copied in, batch done), two output slots that a batch's results wait
-    // in to be copied out, and NAMs per read seen so far (sizes the slots)
-    cudaStream_t copy_in = nullptr, copy_out = nullptr;
-    gbsa_mapper* twin = nullptr;
-    cudaEvent_t in_ready = nullptr, done_ev = nullptr;
-    struct OutSlot {
-        gbsa::DeviceBuffer nams, frac, resc, off, off_g;   // off: batch offsets, off_g: call offsets
-        uint64_t cap = 0;                                 // NAM records nams holds
-        cudaEvent_t free = nullptr;                       // copies out of the slot ended
-    } outs[2];
-    double nams_per_read = 16.0;
-    uint64_t retries = 0;   // batches run again after a work area grew
-    bool fused = false;     // the last batch ran seeding and lookup as one kernel
-    uint64_t fuse_index_bytes = 2ull << 30;   // largest index (entry bytes) seeded and looked up in one kernel
-    uint32_t pipe_chunks = 2;   // full chunks a large gbsa_map_reads call is cut into
-    gbsa::Workspace ws;       // temporary device buffers of the prefix scans
-    uint64_t alg_bytes = 0;   // algorithmic bytes of the last batch (when counting)
-    uint64_t alg_sectors = 0; // 32 B sectors of the lookup's gathers in the last batch (when counting)
-    int count_bytes = 0;
-    bool use_l2_window = true;   // hold the bucket table in L2 when it fits a window
-    int profile = 0;          // record per-stage CUDA events
-    cudaEvent_t ev[8] = {};
-    float stage_ms[8] = {};
-    gbsa::Counters last{};    // device counters of the last batch
-};
+// struct gbsa_mapper: mapper.h
 
 namespace gbsa {
 
-static void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
+void mapper_reserve(gbsa_mapper& m, uint32_t n, uint64_t bases) {
     m.seqs.resize(bases + 64);
     m.offs.resize(8ull * (n + 1));
     m.lens.resize(4ull * (n + 1));
@@ -357,18 +312,16 @@ static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
 // rescue → sorts (side stream), then the per-read NAM offsets into m.out_off[0..n]; the
 // device counters and the NAM total are copied to m.h_status (pinned).  Nothing waits
 // on the host.
-// Where a batch's NAM records, fractions and rescue flags go, when the batch gathers
-// them itself.
-struct GatherTarget {
-    gbsa_nam* nams;
-    uint64_t cap;   // records nams holds (the gather writes no further)
-    float* frac;
-    uint8_t* resc;
-};
 
-static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens,
-                          uint32_t n, bool seeded, cudaStream_t st, cudaStream_t early = nullptr,
-                          const GatherTarget* gt = nullptr) {
+// Batched form (bm != nullptr): n is bm->cap, the read capacity of the work areas; the
+// batch itself (reads, count, work items, outputs) is read from bm->desc in device
+// memory by the kernels, so that the sequence can be captured once as a CUDA graph and
+// replayed for every batch that fits.  Seeding and lookup then run as one persistent
+// kernel pulling work items from a device queue, the records of the batch's reads are
+// cleared on the device, and the gather writes the desc's outputs.
+void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs, const uint32_t* d_lens, uint32_t n,
+                   bool seeded, cudaStream_t st, cudaStream_t early, const GatherTarget* gt, const BatchMode* bm) {
+    const BatchDesc* desc = bm ? bm->desc : nullptr;
     cudaStream_t main_st = st;
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, st));
@@ -383,7 +336,9 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
     m.h_status.resize(sizeof(Counters) + 8);
     Counters* ctr = m.ctr.as<Counters>();
     GBSA_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
-    if (!seeded) {
+    if (desc) {
+        launch_clear_recs(n, m.rec.as<ReadRec>(), desc, st);
+    } else if (!seeded) {
         GBSA_CUDA(cudaMemsetAsync(m.rec.as<void>(), 0, sizeof(ReadRec) * n, st));
     } else {
         // keep q_off / nq / nq2 written by the caller; clear the rest
@@ -401,19 +356,21 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
     // gathers from an entry array beyond the GPU's TLB reach (3.1 Gbp: 9.9 GB) run
     // faster in a lookup kernel of their own (measured: 56.1 ms fused against 22.7 +
     // 27.8 ms for 10M reads).
-    const bool fused = !seeded && I.n * sizeof(gbsa_ref_randstrobe) <= m.fuse_index_bytes;
+    // (the batched form always runs its one persistent seeding + lookup kernel)
+    const bool fused = desc || (!seeded && I.n * sizeof(gbsa_ref_randstrobe) <= m.fuse_index_bytes);
     m.fused = fused;
     mark(0);
-    if (fused) launch_seed_lookup(m.idx->dp, I, C, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
+    if (desc) launch_seed_lookup_queue(m.idx->dp, I, C, desc, m.rec.as<ReadRec>(), A, ctr, bm->variant, st);
+    else if (fused) launch_seed_lookup(m.idx->dp, I, C, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     else if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(1);
     if (!seeded)
         launch_seed_long(m.idx->dp, d_seqs, d_offs, d_lens, m.rec.as<ReadRec>(), A, ctr, m.long_scratch.as<uint8_t>(),
-                         m.long_warps, st);
+                         m.long_warps, st, desc);
     mark(2);
     if (fused) launch_lookup_long(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
     else launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
-    launch_bucket_reads(n, m.rec.as<ReadRec>(), A, ctr, st);
+    launch_bucket_reads(n, C.lane_max_hits, m.rec.as<ReadRec>(), A, ctr, st, desc);
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, early));
         GBSA_CUDA(cudaStreamWaitEvent(main_st, m.early_ev, 0));
@@ -452,15 +409,16 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
     GBSA_CUDA(cudaStreamWaitEvent(st, m.rescue_ev, 0));
     uint64_t* cnt = m.cnt.as<uint64_t>();
     uint64_t* off = m.out_off.as<uint64_t>();
-    launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st);
+    launch_read_counts(n, m.rec.as<ReadRec>(), 0, cnt, st, desc);
     scan_exclusive_u64(cnt, off, n, off + n, ws, st);
-    if (gt)
-        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt->nams, gt->frac, gt->resc, st,
-                           gt->cap, 1);
+    if (gt || desc)
+        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt ? gt->nams : nullptr,
+                           gt ? gt->frac : nullptr, gt ? gt->resc : nullptr, st, gt ? gt->cap : 0, 1, nullptr,
+                           nullptr, desc);
     GBSA_CUDA(cudaStreamWaitEvent(st, m.join_ev, 0));
-    if (gt)
-        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt->nams, nullptr, nullptr, st,
-                           gt->cap, 2, &A, ctr);
+    if (gt || desc)
+        launch_gather_nams(n, m.rec.as<ReadRec>(), m.nams.as<NamState>(), off, gt ? gt->nams : nullptr, nullptr,
+                           nullptr, st, gt ? gt->cap : 0, 2, &A, ctr, desc);
     GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<void>(), ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
     GBSA_CUDA(cudaMemcpyAsync(m.h_status.as<uint8_t>() + sizeof(Counters), off + n, 8, cudaMemcpyDeviceToHost, st));
 }
@@ -468,7 +426,7 @@ static void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t*
 // Reads the status of a batch that enqueue_batch ran and that has completed.  Throws for
 // a fatal status; grows the work areas that overflowed and returns false (the batch must
 // run again); otherwise records the counters and returns true.
-static bool check_batch(gbsa_mapper& m, bool seeded) {
+bool check_batch(gbsa_mapper& m, bool seeded) {
     const Counters h = *m.h_status.as<Counters>();
     if (m.profile) {
         // seed, long seed, lookup, lane NAMs, warp NAMs (main stream); rescue, its
@@ -511,7 +469,7 @@ static bool check_batch(gbsa_mapper& m, bool seeded) {
     return true;
 }
 
-static uint64_t batch_total(gbsa_mapper& m) {
+uint64_t batch_total(gbsa_mapper& m) {
     uint64_t t;
     std::memcpy(&t, m.h_status.as<uint8_t>() + sizeof(Counters), 8);
     return t;
@@ -539,7 +497,7 @@ static uint64_t run_pipeline(gbsa_mapper& m, const uint8_t* d_seqs, const uint64
 static std::mutex g_l2_mu;
 static std::vector<int> g_l2_users;   // per device: mappers holding a window
 
-static void l2_window_attach(gbsa_mapper& m, bool on) {
+void l2_window_attach(gbsa_mapper& m, bool on) {
     const bool had = m.cfg.l2_bytes != 0;
     if (on == had) return;
     int dev = 0;
@@ -601,6 +559,60 @@ static std::vector<uint32_t> plan_chunks(uint32_t n_reads, uint32_t chunks, uint
     for (uint32_t x : sizes)
         if (x) starts.push_back(starts.back() + x);
     return starts;
+}
+
+// Copies n reads (host) to the mapper's device inputs.  Reads usually lie back to back:
+// the span from the first read's start to the last read's end is copied in one
+// transfer and the offsets are rebased to it (in parallel, checking that every read
+// lies inside the span); otherwise the reads are gathered into pinned staging first.
+uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths, uint32_t n,
+                     cudaStream_t st) {
+    const uint64_t lo = n ? offsets[0] : 0;
+    const uint64_t hi = n ? offsets[n - 1] + lengths[n - 1] : 0;
+    const bool span_ok = hi >= lo;
+    const uint64_t span = span_ok ? hi - lo : 0;
+    std::atomic<bool> inside{span_ok};
+    std::atomic<uint64_t> total{0};
+    m.h_meta.resize(12ull * (n + 1));
+    uint64_t* ho = m.h_meta.as<uint64_t>();
+    uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
+    host_parallel_for(n, [&](size_t b, size_t e) {
+        bool ok = true;
+        uint64_t t = 0;
+        for (size_t i = b; i < e; ++i) {
+            ok &= offsets[i] >= lo && offsets[i] + lengths[i] <= hi;
+            ho[i] = offsets[i] - lo;
+            hl[i] = lengths[i];
+            t += lengths[i];
+        }
+        if (!ok) inside.store(false);
+        total.fetch_add(t);
+    });
+    const bool direct = inside.load() && span <= 2 * total.load() + (1u << 20);   // no large gaps
+    const uint64_t bases = direct ? span : total.load();
+    mapper_reserve(m, n, bases);
+    m.seqs.resize(bases + 64);
+    m.offs.resize(8ull * (n + 1));
+    m.lens.resize(4ull * (n + 1));
+    if (direct) {
+        if (span) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), seqs + lo, span, cudaMemcpyHostToDevice, st));
+    } else {
+        // exclusive offsets of the gathered layout, then a parallel gather
+        uint64_t acc = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            ho[i] = acc;
+            acc += lengths[i];
+        }
+        m.h_seqs.resize(acc + 1);
+        char* hs = m.h_seqs.as<char>();
+        host_parallel_for(n, [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
+        });
+        if (acc) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), hs, acc, cudaMemcpyHostToDevice, st));
+    }
+    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
+    return total.load();
 }
 
 }  // namespace gbsa
@@ -798,60 +810,6 @@ int gbsa_get_count(const gbsa_index* idx, const uint64_t* positions, uint64_t n,
         launch_get_count(view_of(*idx), dp.as<uint64_t>(), n, dc.as<uint32_t>(), 0);
         GBSA_CUDA(cudaMemcpy(counts, dc.as<void>(), 4 * n, cudaMemcpyDeviceToHost));
     });
-}
-
-// Copies n reads (host) to the mapper's device inputs.  Reads usually lie back to back:
-// the span from the first read's start to the last read's end is copied in one
-// transfer and the offsets are rebased to it (in parallel, checking that every read
-// lies inside the span); otherwise the reads are gathered into pinned staging first.
-static uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
-                            uint32_t n, cudaStream_t st) {
-    const uint64_t lo = n ? offsets[0] : 0;
-    const uint64_t hi = n ? offsets[n - 1] + lengths[n - 1] : 0;
-    const bool span_ok = hi >= lo;
-    const uint64_t span = span_ok ? hi - lo : 0;
-    std::atomic<bool> inside{span_ok};
-    std::atomic<uint64_t> total{0};
-    m.h_meta.resize(12ull * (n + 1));
-    uint64_t* ho = m.h_meta.as<uint64_t>();
-    uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
-    host_parallel_for(n, [&](size_t b, size_t e) {
-        bool ok = true;
-        uint64_t t = 0;
-        for (size_t i = b; i < e; ++i) {
-            ok &= offsets[i] >= lo && offsets[i] + lengths[i] <= hi;
-            ho[i] = offsets[i] - lo;
-            hl[i] = lengths[i];
-            t += lengths[i];
-        }
-        if (!ok) inside.store(false);
-        total.fetch_add(t);
-    });
-    const bool direct = inside.load() && span <= 2 * total.load() + (1u << 20);   // no large gaps
-    const uint64_t bases = direct ? span : total.load();
-    mapper_reserve(m, n, bases);
-    m.seqs.resize(bases + 64);
-    m.offs.resize(8ull * (n + 1));
-    m.lens.resize(4ull * (n + 1));
-    if (direct) {
-        if (span) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), seqs + lo, span, cudaMemcpyHostToDevice, st));
-    } else {
-        // exclusive offsets of the gathered layout, then a parallel gather
-        uint64_t acc = 0;
-        for (uint32_t i = 0; i < n; ++i) {
-            ho[i] = acc;
-            acc += lengths[i];
-        }
-        m.h_seqs.resize(acc + 1);
-        char* hs = m.h_seqs.as<char>();
-        host_parallel_for(n, [&](size_t b, size_t e) {
-            for (size_t i = b; i < e; ++i) std::memcpy(hs + ho[i], seqs + offsets[i], lengths[i]);
-        });
-        if (acc) GBSA_CUDA(cudaMemcpyAsync(m.seqs.as<void>(), hs, acc, cudaMemcpyHostToDevice, st));
-    }
-    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
-    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
-    return total.load();
 }
 
 int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,

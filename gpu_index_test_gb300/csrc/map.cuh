@@ -43,6 +43,26 @@ struct Counters {
     unsigned int n_huge;   // rescued reads whose NAMs the large-tile block sort orders
     unsigned int rescue_next;  // next rescue-list entry to take (k_rescue's work counter)
     unsigned int lane_cnt[16]; // reads per hit-count bucket of the lane NAM kernel
+    unsigned int queue_head;   // next work item of the batched form's seeding + lookup kernel
+};
+
+// A batch of the batched form, in device memory: the kernels of a captured batch graph
+// read the batch's reads, sizes and output buffers from here, so one graph serves
+// every batch that fits the work areas it was captured with.  Work item i is reads
+// [items[i], items[i + 1]) (a single-end read, or both mates of a pair); with items ==
+// nullptr every read is an item.
+struct BatchDesc {
+    const uint8_t* seqs;
+    const uint64_t* offs;
+    const uint32_t* lens;
+    const uint32_t* items;
+    uint32_t n_reads;
+    uint32_t n_items;
+    gbsa_nam* out;          // NAM records (at most out_cap are written)
+    uint64_t out_cap;
+    uint64_t* out_off;      // n_reads + 1 NAM offsets
+    float* frac;            // may be null
+    uint8_t* rescued;       // may be null
 };
 
 constexpr uint32_t kLaneBuckets = 13;   // hit-count buckets of the lane NAM kernel (<= 16)
@@ -94,7 +114,13 @@ struct MapConfig {
     const void* l2_base;
     uint64_t l2_bytes;
     float l2_hit_ratio;
+    // NAM phase shape: reads with at most lane_max_hits hits (<= kLaneMaxHitsCap) are
+    // merged by one lane each, heavier ones by a warp each; sort_variant picks the block
+    // size of the sort of rescued reads with many NAMs (0: 256 threads, 1: 512)
+    uint32_t lane_max_hits;
+    int sort_variant;
 };
+constexpr uint32_t kLaneMaxHitsCap = 160;
 
 // Reads shorter than this (and with at most kSmemSyncmers syncmers) are seeded
 // with shared-memory buffers; the rest by the scratch-memory kernel.
@@ -112,7 +138,22 @@ void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, 
                  ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens,
                       ReadRec* rec, Arenas A, Counters* ctr, uint8_t* long_scratch, uint32_t long_warps,
-                      cudaStream_t st);
+                      cudaStream_t st, const BatchDesc* desc = nullptr);
+// Batched form: seeding and lookup in one persistent kernel whose warps pull work items
+// (a read, or both mates of a pair) from a device queue (ctr->queue_head) until the
+// batch's items run out; desc gives the reads and their count.  variant selects the
+// kernel's shape (warps per block, resident blocks per SM, shared-memory read window);
+// see batch_variant().
+struct SeedVariant {
+    int warps;            // warps per block
+    int blocks_per_sm;    // resident blocks per SM (launch bound and grid)
+    uint32_t max_len;     // longest read seeded in shared memory
+    uint32_t syncmers;    // syncmer buffer per warp
+};
+constexpr int kSeedVariants = 6;
+SeedVariant seed_variant(int v);
+void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
+                              ReadRec* rec, Arenas A, Counters* ctr, int variant, cudaStream_t st);
 // Main path: seeding and lookup fused (a warp per read); reads too long for the
 // shared-memory buffers are seeded by launch_seed_long and looked up by launch_lookup_long.
 void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig& C, const uint8_t* seqs,
@@ -124,22 +165,31 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
                    cudaStream_t st);
 void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st);
-void launch_bucket_reads(uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
+void launch_bucket_reads(uint32_t n, uint32_t lane_max_hits, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st,
+                         const BatchDesc* desc = nullptr);
 void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st);
 void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st);
 // mode 0: every read; 1: the reads that were not rescued; 2: the rescued reads (A and
 // ctr give the rescue list; needed for mode 2 only).
+// With desc (batched form): n is the work areas' read capacity, the batch's read count,
+// output buffers and capacity come from desc, and mode 1 also copies the NAM offsets of
+// reads [0, desc->n_reads] (out_off[n] holding the total) to desc->out_off.
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
                         gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap = ~0ull,
-                        int mode = 0, const Arenas* A = nullptr, const Counters* ctr = nullptr);
+                        int mode = 0, const Arenas* A = nullptr, const Counters* ctr = nullptr,
+                        const BatchDesc* desc = nullptr);
 void launch_gather_queries(uint32_t n, const ReadRec* rec, const Query* arena, const uint64_t* out_off,
                            gbsa_query_randstrobe* out, cudaStream_t st);
 void launch_find(const IndexView& I, const uint64_t* hashes, uint64_t n, uint64_t* pos, cudaStream_t st);
 void launch_get_count(const IndexView& I, const uint64_t* pos, uint64_t n, uint32_t* counts, cudaStream_t st);
-void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st);
+// With desc: out[r] for r < n, 0 for the slots at or past desc->n_reads.
+void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st,
+                        const BatchDesc* desc = nullptr);
 void launch_offsets_add(const uint64_t* in, uint64_t* out, uint64_t n, uint64_t base, cudaStream_t st);
 void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st);
+// Zeroes the records of reads [0, desc->n_reads) (every field).
+void launch_clear_recs(uint32_t cap, ReadRec* rec, const BatchDesc* desc, cudaStream_t st);
 
 }  // namespace gbsa

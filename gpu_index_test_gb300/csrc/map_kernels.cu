@@ -97,7 +97,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_seed_long(DevParams P, 
                                                                     const uint64_t* __restrict__ offs,
                                                                     const uint32_t* __restrict__ lens,
                                                                     ReadRec* __restrict__ rec, Arenas A, Counters* ctr,
-                                                                    uint8_t* scratch) {
+                                                                    uint8_t* scratch, const BatchDesc* desc) {
+    if (desc) {
+        seqs = desc->seqs;
+        offs = desc->offs;
+        lens = desc->lens;
+    }
     const uint32_t n_long = *(volatile unsigned int*)&ctr->n_long;
     uint8_t* slot = scratch + (size_t)warp_global_id() * kLongSlotBytes;
     uint64_t* pk = reinterpret_cast<uint64_t*>(slot);
@@ -328,6 +333,61 @@ __global__ void __launch_bounds__(32 * kSeedWarps, kFusedBlocksPerSm)
     }
 }
 
+// The batched form's seeding + lookup: the body of k_seed_lookup, but each warp pulls
+// work items from a device queue (an atomic counter) until the batch's items run out,
+// so reads of uneven lengths and the two mates of a pair (one item) balance over the
+// persistent grid; the batch (reads, count, items) is read from desc in device memory.
+// The shape (warps per block, resident blocks per SM, shared-memory read window) is a
+// template of its own per variant, picked at run time.
+template <bool kCount, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
+__global__ void __launch_bounds__(32 * kWarps, kBlocks)
+    k_seed_lookup_q(DevParams P, IndexView I, MapConfig C, const BatchDesc* __restrict__ desc,
+                    ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    __shared__ uint64_t s_pk[kWarps][kMaxLen / 32 + 4];
+    __shared__ uint32_t s_nm[kWarps][kMaxLen / 32 + 4];
+    __shared__ uint64_t s_hb[kWarps][64];
+    __shared__ uint64_t s_sh[kWarps][kSyncmers];
+    __shared__ uint32_t s_sp[kWarps][kSyncmers];
+    const uint32_t w = threadIdx.x >> 5;
+    const uint8_t* __restrict__ seqs = desc->seqs;
+    const uint64_t* __restrict__ offs = desc->offs;
+    const uint32_t* __restrict__ lens = desc->lens;
+    const uint32_t* __restrict__ items = desc->items;
+    const uint32_t n_items = items ? desc->n_items : desc->n_reads;
+    for (;;) {
+        uint32_t it = 0;
+        if (lane_id() == 0) it = atomicAdd(&ctr->queue_head, 1u);
+        it = __shfl_sync(0xFFFFFFFFu, it, 0);
+        if (it >= n_items) break;
+        // item bounds outside [0, n_reads] are clamped (reads no item covers stay empty)
+        const uint32_t n_reads = desc->n_reads;
+        const uint32_t r0 = min(items ? items[it] : it, n_reads);
+        const uint32_t r1 = min(items ? items[it + 1] : it + 1, n_reads);
+        for (uint32_t r = r0; r < r1; ++r) {
+            const uint32_t L = lens[r];
+            ReadRec& R = rec[r];
+            if (L > GBSA_MAX_READ_LEN) {
+                warp_fail(R, ctr, kStatusReadTooLong);
+                continue;
+            }
+            uint32_t ns = 0xFFFFFFFFu;
+            if (L <= kMaxLen)
+                ns = warp_read_syncmers(P, seqs + offs[r], L, s_pk[w], s_nm[w], s_hb[w], s_sh[w], s_sp[w], kSyncmers);
+            if (ns == 0xFFFFFFFFu) {
+                if (lane_id() == 0) {
+                    R.flags |= kReadLong;
+                    A.long_list[atomicAdd(&ctr->n_long, 1u)] = r;
+                }
+                continue;
+            }
+            emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
+            __syncwarp();
+            lookup_read<kCount>(I, C, r, rec, A, ctr);
+            __syncwarp();
+        }
+    }
+}
+
 // Scratch of `bytes` for the calling warp: its own slot from byte `slot_off` on when
 // the request fits, else a bump allocation in the shared overflow arena (nullptr
 // when that is full too).
@@ -412,7 +472,7 @@ __device__ void warp_finish_nams(const MapConfig& C, const NamLists& L, uint32_t
     __syncwarp();
 }
 
-constexpr uint32_t kLaneMaxHits = 160;
+constexpr uint32_t kLaneMaxHits = kLaneMaxHitsCap;   // the lane kernel's hit-count buckets cover this
 constexpr uint32_t kLaneOpen = 10;   // open NAMs a lane keeps in shared memory
 constexpr int kLaneWarps = 4;
 // The rescue chain runs beside the two NAM kernels on another stream; the persistent
@@ -516,7 +576,9 @@ __device__ __forceinline__ uint32_t lane_bucket(uint32_t H) {
 // warp kernel's list, the others into lists by hit count, so that the lanes of a
 // warp of the lane kernel merge reads of similar size (a warp runs as long as its
 // longest read).  Appends are aggregated per warp and bucket.
-__global__ void k_bucket_reads(uint32_t n, const ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+__global__ void k_bucket_reads(uint32_t n, uint32_t lane_max, const ReadRec* __restrict__ rec, Arenas A,
+                               Counters* ctr, const BatchDesc* desc) {
+    if (desc) n = min(n, desc->n_reads);
     const uint32_t lane = lane_id();
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -525,7 +587,7 @@ __global__ void k_bucket_reads(uint32_t n, const ReadRec* __restrict__ rec, Aren
         if (r < n) {
             const uint32_t flags = rec[r].flags;
             const uint32_t H = rec[r].n_hits;
-            if (!(flags & (kReadFailed | kReadRescue)) && H > 0) key = H > kLaneMaxHits ? 16u : lane_bucket(H);
+            if (!(flags & (kReadFailed | kReadRescue)) && H > 0) key = H > lane_max ? 16u : lane_bucket(H);
         }
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
         const uint32_t leader = __ffs(peers) - 1;
@@ -1513,8 +1575,23 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256)
 // (through the rescue list), after their sorts.
 __global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const NamState* __restrict__ arena,
                               const uint64_t* __restrict__ out_off, gbsa_nam* __restrict__ out, uint64_t out_cap,
-                              float* frac, uint8_t* rescued, int mode, Arenas A, const Counters* ctr) {
+                              float* frac, uint8_t* rescued, int mode, Arenas A, const Counters* ctr,
+                              const BatchDesc* desc) {
     const uint32_t lane = lane_id();
+    uint64_t* copy_off = nullptr;
+    if (desc) {
+        const uint32_t cap = n;
+        n = min(n, desc->n_reads);
+        out = desc->out;
+        out_cap = desc->out_cap;
+        frac = mode == 2 ? nullptr : desc->frac;
+        rescued = mode == 2 ? nullptr : desc->rescued;
+        if (mode != 2) {
+            copy_off = desc->out_off;
+            // slots past the batch hold no NAMs: out_off[cap] is the batch's total
+            if (blockIdx.x == 0 && threadIdx.x == 0) copy_off[n] = out_off[cap];
+        }
+    }
     if (mode == 2) {
         const uint32_t n_light = ctr->n_rescue, n_heavy = ctr->n_rescue_heavy;
         for (uint32_t t = warp_global_id(); t < n_light + n_heavy; t += warp_count()) {
@@ -1535,6 +1612,7 @@ __global__ void k_gather_nams(uint32_t n, const ReadRec* __restrict__ rec, const
         if (lane == 0) {
             if (frac) frac[r] = R.frac;
             if (rescued) rescued[r] = (R.flags & kReadRescue) ? 1 : 0;
+            if (copy_off) copy_off[r] = o;
         }
     }
 }
@@ -1558,9 +1636,20 @@ __global__ void k_gather_queries(uint32_t n, const ReadRec* __restrict__ rec, co
     }
 }
 
-__global__ void k_read_counts(uint32_t n, const ReadRec* __restrict__ rec, int what, uint64_t* __restrict__ out) {
+__global__ void k_read_counts(uint32_t n, const ReadRec* __restrict__ rec, int what, uint64_t* __restrict__ out,
+                              const BatchDesc* desc) {
+    const uint32_t live = desc ? min(n, desc->n_reads) : n;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-        out[r] = what == 0 ? rec[r].n_nams : (uint64_t)rec[r].nq2;
+        out[r] = r >= live ? 0 : (what == 0 ? rec[r].n_nams : (uint64_t)rec[r].nq2);
+}
+
+__global__ void k_clear_recs(uint32_t cap, ReadRec* __restrict__ rec, const BatchDesc* desc) {
+    const uint32_t n = min(cap, desc->n_reads);
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(rec);
+    static_assert(sizeof(ReadRec) % 8 == 0, "ReadRec is a whole number of 8-byte words");
+    const uint64_t words = (uint64_t)n * (sizeof(ReadRec) / 8);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+        w[i] = 0ull;
 }
 
 __global__ void k_reset_recs(uint32_t n, ReadRec* __restrict__ rec) {
@@ -1631,9 +1720,46 @@ void launch_seed(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, 
 
 void launch_seed_long(const DevParams& P, const uint8_t* seqs, const uint64_t* offs, const uint32_t* lens,
                       ReadRec* rec, Arenas A, Counters* ctr, uint8_t* long_scratch, uint32_t long_warps,
-                      cudaStream_t st) {
+                      cudaStream_t st, const BatchDesc* desc) {
     const unsigned blocks = std::max(1u, long_warps / kWarpsPerBlock);
-    k_seed_long<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(P, seqs, offs, lens, rec, A, ctr, long_scratch);
+    k_seed_long<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(P, seqs, offs, lens, rec, A, ctr, long_scratch, desc);
+    GBSA_LAUNCHED();
+}
+
+// Shapes of the batched form's seeding + lookup kernel (the autotuner's choices).
+// Variant 0 is the plain form's fused kernel shape.
+SeedVariant seed_variant(int v) {
+    static const SeedVariant table[kSeedVariants] = {
+        {8, 6, 512, 160}, {8, 5, 512, 160}, {4, 12, 512, 160}, {8, 7, 256, 96}, {16, 3, 512, 160}, {8, 6, 256, 96},
+    };
+    return table[v < 0 || v >= kSeedVariants ? 0 : v];
+}
+
+template <bool kCount, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
+static void launch_q(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc, ReadRec* rec,
+                     Arenas A, Counters* ctr, cudaStream_t st) {
+    const unsigned grid = (unsigned)device_sm_count() * kBlocks;
+    launch_probe(k_seed_lookup_q<kCount, kWarps, kBlocks, kMaxLen, kSyncmers>, grid, 32 * kWarps, 0, st, C, P, I, C,
+                 desc, rec, A, ctr);
+}
+
+template <bool kCount>
+static void launch_q_variant(int v, const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
+                             ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+    switch (v) {
+        case 1: launch_q<kCount, 8, 5, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 2: launch_q<kCount, 4, 12, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 3: launch_q<kCount, 8, 7, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
+        case 4: launch_q<kCount, 16, 3, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 5: launch_q<kCount, 8, 6, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
+        default: launch_q<kCount, 8, 6, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+    }
+}
+
+void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
+                              ReadRec* rec, Arenas A, Counters* ctr, int variant, cudaStream_t st) {
+    if (C.count_bytes) launch_q_variant<true>(variant, P, I, C, desc, rec, A, ctr, st);
+    else launch_q_variant<false>(variant, P, I, C, desc, rec, A, ctr, st);
     GBSA_LAUNCHED();
 }
 
@@ -1674,9 +1800,12 @@ void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec,
     GBSA_LAUNCHED();
 }
 
-void launch_bucket_reads(uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
+void launch_bucket_reads(uint32_t n, uint32_t lane_max_hits, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st,
+                         const BatchDesc* desc) {
     if (!n) return;
-    k_bucket_reads<<<grid_for(n, 256, (unsigned)device_sm_count() * 8), 256, 0, st>>>(n, rec, A, ctr);
+    const uint32_t lane_max = lane_max_hits == 0 ? kLaneMaxHits : std::min(lane_max_hits, kLaneMaxHits);
+    k_bucket_reads<<<grid_for(n, 256, (unsigned)device_sm_count() * 8), 256, 0, st>>>(n, lane_max, rec, A, ctr,
+                                                                                      desc);
     GBSA_LAUNCHED();
 }
 
@@ -1714,13 +1843,16 @@ void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr,
         if (!done[dev]) {
             GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<kSmall, kSortTile>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs<2 * kSmall, kSortTile>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             GBSA_CUDA(cudaFuncSetAttribute(k_sort_jobs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
             done[dev] = 1;
         }
     }
     const unsigned sms = (unsigned)device_sm_count();
-    k_sort_jobs<kSmall, kSortTile><<<sms * 4, kSmall, smem, st>>>(C, rec, A, ctr);
+    if (C.sort_variant == 1) k_sort_jobs<2 * kSmall, kSortTile><<<sms * 3, 2 * kSmall, smem, st>>>(C, rec, A, ctr);
+    else k_sort_jobs<kSmall, kSortTile><<<sms * 4, kSmall, smem, st>>>(C, rec, A, ctr);
     GBSA_LAUNCHED();
     // sms / 2 clusters of kClusterCtas CTAs
     k_sort_jobs_cluster<<<std::max(1u, sms / 2) * kClusterCtas, 256, smem, st>>>(C, rec, A, ctr);
@@ -1729,11 +1861,11 @@ void launch_sort_jobs(const MapConfig& C, ReadRec* rec, Arenas A, Counters* ctr,
 
 void launch_gather_nams(uint32_t n, const ReadRec* rec, const NamState* arena, const uint64_t* out_off,
                         gbsa_nam* out, float* frac, uint8_t* rescued, cudaStream_t st, uint64_t out_cap, int mode,
-                        const Arenas* A, const Counters* ctr) {
+                        const Arenas* A, const Counters* ctr, const BatchDesc* desc) {
     if (!n) return;
     const Arenas none{};
     k_gather_nams<<<warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, st>>>(
-        n, rec, arena, out_off, out, out_cap, frac, rescued, mode, A ? *A : none, ctr);
+        n, rec, arena, out_off, out, out_cap, frac, rescued, mode, A ? *A : none, ctr, desc);
     GBSA_LAUNCHED();
 }
 
@@ -1762,6 +1894,12 @@ void launch_reset_recs(uint32_t n, ReadRec* rec, cudaStream_t st) {
     GBSA_LAUNCHED();
 }
 
+void launch_clear_recs(uint32_t cap, ReadRec* rec, const BatchDesc* desc, cudaStream_t st) {
+    if (!cap) return;
+    k_clear_recs<<<(unsigned)device_sm_count() * 4, 256, 0, st>>>(cap, rec, desc);
+    GBSA_LAUNCHED();
+}
+
 __global__ void k_offsets_add(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint64_t n, uint64_t base) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         out[i] = in[i] + base;
@@ -1773,9 +1911,10 @@ void launch_offsets_add(const uint64_t* in, uint64_t* out, uint64_t n, uint64_t 
     GBSA_LAUNCHED();
 }
 
-void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st) {
+void launch_read_counts(uint32_t n, const ReadRec* rec, int what, uint64_t* out, cudaStream_t st,
+                        const BatchDesc* desc) {
     if (!n) return;
-    k_read_counts<<<grid_for(n, 256, 1u << 16), 256, 0, st>>>(n, rec, what, out);
+    k_read_counts<<<grid_for(n, 256, 1u << 16), 256, 0, st>>>(n, rec, what, out, desc);
     GBSA_LAUNCHED();
 }
 

@@ -284,6 +284,21 @@ int gbsa_synth_reads_size(const gbsa_read_spec* sp, uint64_t* n_reads, uint64_t*
 
 /* Pass 2: writes the reads.  truth (may be NULL) receives per read
  * (contig, start of the source window, strand). */
+/* The unit layout of gbsa_synth_reads: items[u] = first read of unit u (a single-end
+ * read, or mate 1 of a pair, mate 2 following), items[n_units] = the read count. */
+int gbsa_synth_read_items(const gbsa_read_spec* sp, uint32_t* items) {
+    Rng shape(sp->seed ^ 0x5EED5ULL);
+    uint32_t nr = 0;
+    for (uint32_t u = 0; u < sp->n_units; ++u) {
+        if (sp->len_max > sp->len_min) shape.uniform();   /* the length draw */
+        const bool paired = shape.uniform() < sp->paired_frac;
+        items[u] = nr;
+        nr += paired ? 2 : 1;
+    }
+    items[sp->n_units] = nr;
+    return 0;
+}
+
 int gbsa_synth_reads(const gbsa_read_spec* sp, const char* genome, const uint64_t* lengths, uint32_t n_contigs,
                      char* out, uint64_t* offsets, uint32_t* out_lengths, uint64_t* truth) {
     Rng shape(sp->seed ^ 0x5EED5ULL);

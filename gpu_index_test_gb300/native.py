@@ -89,6 +89,15 @@ def lib():
             "gbsa_mapper_fused_lookup": (i32, [vp]),
             "gbsa_mapper_set_fuse_limit": (i32, [vp, u64]),
             "gbsa_mapper_set_l2_window": (i32, [vp, i32, C.POINTER(u64)]),
+            "gbsa_batch_config_default": (i32, [C.POINTER(abi.BatchConfig), C.POINTER(i32)]),
+            "gbsa_batcher_create": (i32, [vp, C.POINTER(abi.MapOptions), C.POINTER(abi.BatchConfig), u32, u64,
+                                          C.POINTER(vp)]),
+            "gbsa_batcher_free": (None, [vp]),
+            "gbsa_batcher_get_config": (i32, [vp, C.POINTER(abi.BatchConfig)]),
+            "gbsa_batcher_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+            "gbsa_batcher_map_device": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, u64, vp, vp, vp, C.POINTER(u64),
+                                              vp]),
+            "gbsa_batcher_map": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, u64, vp, vp, vp]),
         }
         for name, (res, args) in proto.items():
             f = getattr(L, name)
@@ -410,6 +419,81 @@ class Mapper:
                 continue
             _check(rc)
             return nams[: int(offs[-1])], offs, frac[:n]
+
+
+def batch_config_default():
+    """The committed tuned batched-form configuration: (config, loaded from the file)."""
+    c, f = abi.BatchConfig(), C.c_int()
+    _check(lib().gbsa_batch_config_default(C.byref(c), C.byref(f)))
+    return c, bool(f.value)
+
+
+class Batcher:
+    """The batched form: each batch one launch of a captured CUDA graph, seeding and
+    lookup in one persistent kernel pulling work items (a read, or both mates of a pair)
+    from a device queue."""
+
+    def __init__(self, index, opt=None, config=None, max_reads=1 << 20, max_bases=None):
+        self.index = index
+        self.opt = opt or abi.map_options()
+        h = C.c_void_p()
+        _check(lib().gbsa_batcher_create(index.h, C.byref(self.opt), C.byref(config) if config is not None else None,
+                                         max_reads, max_bases or max_reads * 160, C.byref(h)))
+        self.h = h
+
+    def free(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().gbsa_batcher_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def config(self):
+        c = abi.BatchConfig()
+        _check(lib().gbsa_batcher_get_config(self.h, C.byref(c)))
+        return c
+
+    def stats(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().gbsa_batcher_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"graph_launches": a.value, "captures": b.value, "eager_runs": c.value}
+
+    def map_reads(self, reads, items=None, capacity=None):
+        """Host entry point; items (n_items + 1 read starts) may be None."""
+        n = reads.n
+        cap = capacity or max(1024, 24 * n)
+        seq = _u8(reads.seq)
+        offs_in = np.ascontiguousarray(reads.offsets, np.uint64)
+        lens = np.ascontiguousarray(reads.lengths, np.uint32)
+        it = None if items is None else np.ascontiguousarray(items, np.uint32)
+        while True:
+            nams = np.zeros(cap, abi.NAM)
+            offs = np.zeros(n + 1, np.uint64)
+            frac = np.zeros(max(1, n), np.float32)
+            resc = np.zeros(max(1, n), np.uint8)
+            rc = lib().gbsa_batcher_map(self.h, seq.ctypes.data, offs_in.ctypes.data, lens.ctypes.data, n,
+                                        None if it is None else it.ctypes.data, 0 if it is None else len(it) - 1,
+                                        nams.ctypes.data, cap, offs.ctypes.data, frac.ctypes.data, resc.ctypes.data)
+            if rc == abi.GBSA_ERR_CAPACITY:
+                cap = int(offs[-1]) + 16
+                continue
+            _check(rc)
+            return nams[: int(offs[-1])], offs, frac[:n], resc[:n]
+
+    def map_reads_device(self, d_seq, d_offsets, d_lengths, n, d_nams, nam_capacity, d_nam_offsets, d_frac=None,
+                         d_rescued=None, d_items=None, n_items=0, stream=None):
+        """All buffers are device pointers (ints); returns the NAM total."""
+        tot = C.c_uint64()
+        rc = lib().gbsa_batcher_map_device(self.h, d_seq, d_offsets, d_lengths, n, d_items, n_items, d_nams,
+                                           nam_capacity, d_nam_offsets, d_frac, d_rescued, C.byref(tot), stream)
+        if rc == abi.GBSA_ERR_CAPACITY:
+            return tot.value
+        _check(rc)
+        return tot.value
 
 
 class Server:

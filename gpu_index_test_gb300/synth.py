@@ -88,6 +88,8 @@ def lib():
         L.gbsa_synth_genome.argtypes = [C.POINTER(GenomeSpec), C.c_void_p, C.c_void_p]
         L.gbsa_synth_reads_size.restype = C.c_int
         L.gbsa_synth_reads_size.argtypes = [C.POINTER(ReadSpec), C.c_void_p, C.c_void_p]
+        L.gbsa_synth_read_items.restype = C.c_int
+        L.gbsa_synth_read_items.argtypes = [C.POINTER(ReadSpec), C.c_void_p]
         L.gbsa_synth_reads.restype = C.c_int
         L.gbsa_synth_reads.argtypes = [
             C.POINTER(ReadSpec), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -215,6 +217,20 @@ def make_reads(genome: Genome, rp: ReadParams, with_truth=False) -> Reads:
         truth.ctypes.data if truth is not None else None,
     )
     return Reads(seq, offsets, lengths, truth)
+
+
+def read_items(rp: ReadParams) -> np.ndarray:
+    """Work items of make_reads(genome, rp): item u is reads [items[u], items[u + 1]), a
+    single-end read or the two mates of a pair (n_units + 1 entries)."""
+    s = ReadSpec()
+    s.seed = rp.seed
+    s.n_units = rp.n_units
+    s.len_min = rp.len_min
+    s.len_max = rp.len_max
+    s.paired_frac = rp.paired_frac
+    out = np.empty(rp.n_units + 1, np.uint32)
+    lib().gbsa_synth_read_items(C.byref(s), out.ctypes.data)
+    return out
 
 
 # ---- benchmark configurations -------------------------------------------------

@@ -245,6 +245,56 @@ int gbsa_find_nams(gbsa_mapper* m, const gbsa_query_randstrobe* queries,
  * next; 1 maps the call as one batch.  No reference counterpart. */
 int gbsa_mapper_set_pipeline(gbsa_mapper* m, uint32_t chunks);
 
+/* ---- batched form ------------------------------------------------------------ */
+/* Shape of the batched form's kernels, picked by the autotuner
+ * (gpu_index_test_gb300/autotune.py) and committed as gpu_index_test_gb300/tuned.json,
+ * which the library reads from its own directory.  The results do not depend on it. */
+typedef struct gbsa_batch_config {
+    int32_t  seed_variant;   /* persistent seeding + lookup kernel: 0 8 warps x 6 blocks/SM, reads up to
+                                512 bases in shared memory; 1 8 x 5; 2 4 x 12; 3 8 x 7, 256 bases;
+                                4 16 x 3; 5 8 x 6, 256 bases (longer reads take the long-read path) */
+    uint32_t lane_max_hits;  /* reads with at most this many hits (1-160) are merged by one lane,
+                                heavier ones by a warp */
+    int32_t  sort_variant;   /* block size of the sort of rescued reads with many NAMs: 0 256, 1 512 */
+    uint32_t chunk_reads;    /* reads per batch of the host entry point (two batches in flight) */
+} gbsa_batch_config;
+
+typedef struct gbsa_batcher gbsa_batcher;
+
+/* The committed tuned configuration (*from_file = 1), or the built-in one (0) when the
+ * file is absent or malformed.  No reference counterpart. */
+int gbsa_batch_config_default(gbsa_batch_config* out, int* from_file);
+
+/* The batched form of gbsa_map_reads (the reference's per-stage launch chain with a
+ * fixed batch, step2/main.cu:4458-4597, replaced): each batch is one launch of a CUDA
+ * graph captured over the batcher's work areas, whose kernels read the batch (reads,
+ * count, work items, outputs) from a device-resident descriptor.  Seeding and lookup
+ * are one persistent kernel whose warps pull work items from a device queue; a work
+ * item is reads [items[i], items[i+1]) (a single-end read, or the mates of a pair),
+ * or every read is an item when items is NULL.  The first batch on a set of work areas
+ * (and one that outgrows them) runs without the graph and captures it.  cfg NULL takes
+ * gbsa_batch_config_default.  max_reads / max_bases size the work areas (they grow). */
+int gbsa_batcher_create(const gbsa_index* idx, const gbsa_map_options* opt, const gbsa_batch_config* cfg,
+                        uint32_t max_reads, uint64_t max_bases, gbsa_batcher** out);
+void gbsa_batcher_free(gbsa_batcher* b);
+int gbsa_batcher_get_config(const gbsa_batcher* b, gbsa_batch_config* out);
+/* Graph launches, graph captures and batches run without a graph, since creation. */
+int gbsa_batcher_stats(const gbsa_batcher* b, uint64_t* graph_launches, uint64_t* captures, uint64_t* eager_runs);
+/* Device buffers, as gbsa_map_reads_device; d_items (device, n_items + 1 entries, from 0
+ * to n_reads, non-decreasing) may be NULL.  The batch runs after the work queued on
+ * stream so far and the call returns once it has ended (the NAM total is read back);
+ * stream then waits for it.  Results equal gbsa_map_reads'. */
+int gbsa_batcher_map_device(gbsa_batcher* b, const char* d_seqs, const uint64_t* d_offsets, const uint32_t* d_lengths,
+                            uint32_t n_reads, const uint32_t* d_items, uint32_t n_items, gbsa_nam* d_nams,
+                            uint64_t nam_capacity, uint64_t* d_nam_offsets, float* d_frac, uint8_t* d_rescued,
+                            uint64_t* nam_total, void* stream);
+/* Host buffers, as gbsa_map_reads; items (host) may be NULL.  The call is cut into
+ * batches of about chunk_reads reads at item boundaries that alternate between two
+ * sets of work areas, copies overlapping the other set's graph. */
+int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
+                     uint32_t n_reads, const uint32_t* items, uint32_t n_items, gbsa_nam* nams, uint64_t nam_capacity,
+                     uint64_t* nam_offsets, float* frac, uint8_t* rescued);
+
 /* ---- input staging ----------------------------------------------------------- */
 /* Parses the complete 4-line FASTQ records of a chunk of a file (host threads) into
  * the reads layout of gbsa_map_reads: sequence bytes back to back in seqs, offsets

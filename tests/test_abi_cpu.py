@@ -35,3 +35,22 @@ def test_params_and_errors_without_gpu():
     assert native.lib().gbsa_pick_bits(C.byref(p), 100_000_000) == 23
     assert native.lib().gbsa_pick_bits(C.byref(p), 3_100_000_000) == 28
     assert native.lib().gbsa_pick_bits(C.byref(p), 10) == 8
+
+
+def test_batch_config_layout_and_default_without_gpu():
+    """gbsa_batch_config is four 32-bit fields; the default is the committed tuned file
+    when it is present and well formed (no GPU needed to read it)."""
+    import json
+    import os
+
+    assert C.sizeof(abi.BatchConfig) == 16
+    cfg, from_file = native.batch_config_default()
+    path = os.path.join(os.path.dirname(native.GBSA_SO), "tuned.json")
+    if os.path.exists(path):
+        assert from_file
+        want = json.load(open(path))
+        for k in ("seed_variant", "lane_max_hits", "sort_variant", "chunk_reads"):
+            assert getattr(cfg, k) == want[k], k
+    else:
+        assert not from_file
+    assert 0 <= cfg.seed_variant < abi.SEED_VARIANTS and 1 <= cfg.lane_max_hits <= 160

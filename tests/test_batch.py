@@ -1,0 +1,113 @@
+"""The batched form (gbsa_batcher_*) against the plain form and the oracle (GB300 only).
+
+A batch runs as one launch of a CUDA graph captured over the batcher's work areas;
+seeding and lookup are one persistent kernel pulling work items (a read, or both
+mates of a pair) from a device queue.  Every comparison is bit-exact: NAM records,
+offsets, nonrepetitive fractions and rescue flags.
+"""
+import numpy as np
+import pytest
+
+from golden_cases import nams_equal
+from gpu_index_test_gb300 import abi, native, synth
+from oracle import oracle_py
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b):
+    return (a[1] == b[1]).all() and (a[2] == b[2]).all() and (a[3] == b[3]).all() and nams_equal(a[0], b[0])
+
+
+@pytest.fixture(scope="module")
+def c3():
+    """Uneven lengths (50-500 bp, log-uniform), half single-end, half pairs, on a 1 Mbp
+    genome with duplications and tandem repeats (rescued reads with many NAMs)."""
+    g = synth.make_genome(synth.GenomeParams(seed=101, total_len=1_000_000, n_contigs=3, dup_frac=0.05,
+                                             str_frac=0.01))
+    rp = synth.read_params("C3", n_units=12_000, seed=102)
+    reads = synth.make_reads(g, rp)
+    items = synth.read_items(rp)
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    return g, reads, items, idx, o
+
+
+def test_batched_form_matches_oracle_on_uneven_reads_and_pairs(c3):
+    g, reads, items, idx, o = c3
+    y = o.map_reads(reads, n_threads=8)
+    b = native.Batcher(idx, max_reads=reads.n)
+    x = b.map_reads(reads, items)
+    assert same(x, y)
+    # again (now a graph replay), and without items (every read its own work item)
+    assert same(b.map_reads(reads, items), y)
+    assert same(b.map_reads(reads), y)
+    st = b.stats()
+    assert st["graph_launches"] >= 2 and st["captures"] >= 1
+
+
+@pytest.mark.parametrize("variant", range(abi.SEED_VARIANTS))
+def test_every_tuned_variant_is_bit_exact(c3, variant):
+    """Each shape the autotuner may pick (seeding + lookup variant, lane / warp split of
+    the NAM merge, sort block size) gives the plain form's output."""
+    g, reads, items, idx, o = c3
+    ref = native.Mapper(idx).map_reads(reads)
+    for lane_max, sort_variant in ((160, 0), (64, 1), (96, 0)):
+        cfg = abi.batch_config(variant, lane_max, sort_variant, 4096)
+        b = native.Batcher(idx, config=cfg, max_reads=reads.n)
+        assert same(b.map_reads(reads, items), ref)   # several chunks of ~4096 reads, two sets of work areas
+        b.free()
+
+
+def test_batched_device_entry_point_and_graph_reuse(c3):
+    """The device entry point with work items in device memory: one graph serves
+    batches of different sizes (each its own slice of the reads), bit-exact with the
+    plain form's device entry point."""
+    torch = pytest.importorskip("torch")
+    g, reads, items, idx, o = c3
+    dev = torch.device("cuda:0")
+    b = native.Batcher(idx, max_reads=reads.n)
+    m = native.Mapper(idx, max_reads=reads.n)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    for lo_item, hi_item in ((0, len(items) - 1), (100, 2100), (5000, 5400), (0, len(items) - 1)):
+        r0, r1 = int(items[lo_item]), int(items[hi_item])
+        sub = reads.subset(np.arange(r0, r1))
+        it = (items[lo_item:hi_item + 1] - r0).astype(np.uint32)
+        n = sub.n
+        d_seq = torch.from_numpy(sub.seq).to(dev)
+        d_off = torch.from_numpy(sub.offsets.view(np.int64)).to(dev)
+        d_len = torch.from_numpy(sub.lengths.view(np.int32)).to(dev)
+        d_it = torch.from_numpy(it.view(np.int32)).to(dev)
+        cap = 60 * n + 1024
+        outs = []
+        for form in ("batched", "plain"):
+            d_nams = torch.zeros(cap * 44, dtype=torch.uint8, device=dev)
+            d_noff = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+            d_frac = torch.zeros(n, dtype=torch.float32, device=dev)
+            d_resc = torch.zeros(n, dtype=torch.uint8, device=dev)
+            if form == "batched":
+                tot = b.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_nams.data_ptr(),
+                                         cap, d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(),
+                                         d_it.data_ptr(), len(it) - 1, st)
+            else:
+                tot = m.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), n, d_nams.data_ptr(),
+                                         cap, d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), st)
+            torch.cuda.synchronize()
+            assert tot <= cap
+            outs.append((d_nams[: tot * 44].cpu().numpy().view(abi.NAM), d_noff.cpu().numpy().view(np.uint64),
+                         d_frac.cpu().numpy(), d_resc.cpu().numpy()))
+        assert same(outs[0], outs[1])
+    assert b.stats()["graph_launches"] >= 3
+
+
+def test_batched_form_grows_its_work_areas():
+    """Reads inside a tandem-repeat-rich genome outgrow small work areas: the batch runs
+    again with larger ones and is captured anew; the results equal the plain form's."""
+    g = synth.make_genome(synth.GenomeParams(seed=111, total_len=400_000, n_contigs=2, str_frac=0.05))
+    rp = synth.ReadParams(seed=112, n_units=6000, len_min=150, len_max=150, paired_frac=1.0)
+    reads = synth.make_reads(g, rp)
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    ref = native.Mapper(idx).map_reads(reads)
+    b = native.Batcher(idx, max_reads=1024, max_bases=1024 * 20)
+    for _ in range(2):
+        assert same(b.map_reads(reads, synth.read_items(rp)), ref)
