@@ -84,6 +84,16 @@ class BatchConfig(C.Structure):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    """gbsa_server_config."""
+    _fields_ = [
+        ("slots", C.c_uint32),
+        ("batch_reads", C.c_uint32),
+        ("batch_bases", C.c_uint64),
+        ("memory_budget", C.c_uint64),
+    ]
+
+
 SEED_VARIANTS = 6   # shapes of the batched form's seeding + lookup kernel
 
 

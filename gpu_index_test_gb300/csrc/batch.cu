@@ -260,6 +260,99 @@ uint64_t run_sync(gbsa_batcher& b, Lane& L, const BatchDesc& d) {
 }
 
 }  // namespace
+
+void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, int* status, uint64_t* totals) {
+    Lane& L = b.lanes[0];
+    lane_init(b, L);
+    // the batch's reads: offsets relative to the lowest read address of all requests
+    uint32_t n = 0;
+    uintptr_t base = UINTPTR_MAX;
+    for (uint32_t j = 0; j < k; ++j) {
+        n += rq[j].n_reads;
+        for (uint32_t i = 0; i < rq[j].n_reads; ++i)
+            base = std::min(base, reinterpret_cast<uintptr_t>(rq[j].seqs) + rq[j].offsets[i]);
+    }
+    if (n == 0) {
+        for (uint32_t j = 0; j < k; ++j) {
+            rq[j].nam_offsets[0] = 0;
+            status[j] = GBSA_OK;
+            totals[j] = 0;
+        }
+        return;
+    }
+    GBSA_CUDA(cudaEventSynchronize(L.done));
+    lane_reserve(b, L, n);
+    L.h_items.resize(12ull * (n + 1));   // the batch's offsets (u64) and lengths (u32)
+    uint64_t* offs = L.h_items.as<uint64_t>();
+    uint32_t* lens = reinterpret_cast<uint32_t*>(offs + n + 1);
+    std::vector<uint32_t> first(k + 1, 0);
+    for (uint32_t j = 0; j < k; ++j) first[j + 1] = first[j] + rq[j].n_reads;
+    host_parallel_tasks(k, [&](size_t j) {
+        const uintptr_t s0 = reinterpret_cast<uintptr_t>(rq[j].seqs);
+        for (uint32_t i = 0; i < rq[j].n_reads; ++i) {
+            offs[first[j] + i] = s0 + rq[j].offsets[i] - base;
+            lens[first[j] + i] = rq[j].lengths[i];
+        }
+    });
+    stage_reads(*L.m, reinterpret_cast<const char*>(base), offs, lens, n, b.copy_in);
+    GBSA_CUDA(cudaEventRecord(L.in_ready, b.copy_in));
+    GBSA_CUDA(cudaStreamWaitEvent(L.m->st, L.in_ready, 0));
+    const uint64_t want = (uint64_t)(L.nams_per_read * 1.25 * n) + 1024;
+    if (L.out_cap < want) {
+        L.out_nams.release();
+        L.out_nams.resize(sizeof(gbsa_nam) * want);
+        L.out_cap = want;
+    }
+    L.out_off.resize(8ull * (n + 1));
+    L.out_frac.resize(4ull * (n + 1));
+    L.out_resc.resize(n + 1);
+    BatchDesc d{};
+    d.seqs = L.m->seqs.as<uint8_t>();
+    d.offs = L.m->offs.as<uint64_t>();
+    d.lens = L.m->lens.as<uint32_t>();
+    d.items = nullptr;
+    d.n_reads = n;
+    d.n_items = n;
+    d.out = L.out_nams.as<gbsa_nam>();
+    d.out_cap = L.out_cap;
+    d.out_off = L.out_off.as<uint64_t>();
+    d.frac = L.out_frac.as<float>();
+    d.rescued = L.out_resc.as<uint8_t>();
+    uint64_t total = run_sync(b, L, d);
+    if (total > L.out_cap) {   // more NAMs than the estimate: again with room for them
+        L.out_nams.release();
+        L.out_nams.resize(sizeof(gbsa_nam) * (total + 1024));
+        L.out_cap = total + 1024;
+        d.out = L.out_nams.as<gbsa_nam>();
+        d.out_cap = L.out_cap;
+        total = run_sync(b, L, d);
+    }
+    L.nams_per_read = std::max(L.nams_per_read, (double)total / n);
+    cudaStream_t st = L.m->st;
+    L.h_desc.resize(sizeof(BatchDesc) + 8ull * (n + 1));
+    uint64_t* h_off = reinterpret_cast<uint64_t*>(L.h_desc.as<uint8_t>() + sizeof(BatchDesc));
+    GBSA_CUDA(cudaMemcpyAsync(h_off, L.out_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost, st));
+    GBSA_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t j = 0; j < k; ++j) {
+        const ServeRequest& r = rq[j];
+        const uint64_t a = h_off[first[j]], e = h_off[first[j + 1]];
+        for (uint32_t i = 0; i <= r.n_reads; ++i) r.nam_offsets[i] = h_off[first[j] + i] - a;
+        totals[j] = e - a;
+        status[j] = e - a <= r.nam_capacity ? GBSA_OK : GBSA_ERR_CAPACITY;
+        if (status[j] == GBSA_OK && e > a)
+            GBSA_CUDA(cudaMemcpyAsync(r.nams, L.out_nams.as<gbsa_nam>() + a, sizeof(gbsa_nam) * (e - a),
+                                      cudaMemcpyDeviceToHost, st));
+        if (r.frac && r.n_reads)
+            GBSA_CUDA(cudaMemcpyAsync(r.frac, L.out_frac.as<float>() + first[j], 4ull * r.n_reads,
+                                      cudaMemcpyDeviceToHost, st));
+        if (r.rescued && r.n_reads)
+            GBSA_CUDA(cudaMemcpyAsync(r.rescued, L.out_resc.as<uint8_t>() + first[j], r.n_reads,
+                                      cudaMemcpyDeviceToHost, st));
+    }
+    GBSA_CUDA(cudaStreamSynchronize(st));
+    GBSA_CUDA(cudaEventRecord(L.done, st));
+}
+
 }  // namespace gbsa
 
 using namespace gbsa;
@@ -415,8 +508,7 @@ int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets,
             const uint32_t r0 = item_start(i0), r1 = i1 < ni ? item_start(i1) : n_reads;
             const uint32_t n = r1 - r0;
             GBSA_CUDA(cudaEventSynchronize(L.done));
-            GBSA_CUDA(cudaEventSynchronize(L.out_free));
-            lane_reserve(*b, L, n);
+            lane_reserve(*b, L, std::max(n, std::min(b->cfg.chunk_reads + 64, b->max_reads)));
             stage_reads(*L.m, seqs, offsets + r0, lengths + r0, n, b->copy_in);
             if (items) {
                 L.h_items.resize(4ull * (i1 - i0 + 1));
@@ -429,8 +521,12 @@ int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets,
             }
             GBSA_CUDA(cudaEventRecord(L.in_ready, b->copy_in));
             GBSA_CUDA(cudaStreamWaitEvent(L.m->st, L.in_ready, 0));
+            // the lane's outputs are rewritten once the copies of its previous chunk's
+            // results have ended (a wait on the device; the host goes on staging)
+            GBSA_CUDA(cudaStreamWaitEvent(L.m->st, L.out_free, 0));
             const uint64_t want = (uint64_t)(L.nams_per_read * 1.25 * n) + 1024;
             if (L.out_cap < want) {
+                GBSA_CUDA(cudaEventSynchronize(L.out_free));   // the old buffer is still being read
                 L.out_nams.release();
                 L.out_nams.resize(sizeof(gbsa_nam) * want);
                 L.out_cap = want;

@@ -356,11 +356,12 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     // gathers from an entry array beyond the GPU's TLB reach (3.1 Gbp: 9.9 GB) run
     // faster in a lookup kernel of their own (measured: 56.1 ms fused against 22.7 +
     // 27.8 ms for 10M reads).
-    // (the batched form always runs its one persistent seeding + lookup kernel)
-    const bool fused = desc || (!seeded && I.n * sizeof(gbsa_ref_randstrobe) <= m.fuse_index_bytes);
+    // (the batched form runs its persistent work-queue kernel, with the lookup fused
+    // under the same limit)
+    const bool fused = !seeded && I.n * sizeof(gbsa_ref_randstrobe) <= m.fuse_index_bytes;
     m.fused = fused;
     mark(0);
-    if (desc) launch_seed_lookup_queue(m.idx->dp, I, C, desc, m.rec.as<ReadRec>(), A, ctr, bm->variant, st);
+    if (desc) launch_seed_lookup_queue(m.idx->dp, I, C, desc, m.rec.as<ReadRec>(), A, ctr, bm->variant, fused, st);
     else if (fused) launch_seed_lookup(m.idx->dp, I, C, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     else if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(1);
@@ -369,7 +370,7 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
                          m.long_warps, st, desc);
     mark(2);
     if (fused) launch_lookup_long(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
-    else launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    else launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st, desc);
     launch_bucket_reads(n, C.lane_max_hits, m.rec.as<ReadRec>(), A, ctr, st, desc);
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, early));

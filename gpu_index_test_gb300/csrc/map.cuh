@@ -152,8 +152,9 @@ struct SeedVariant {
 };
 constexpr int kSeedVariants = 6;
 SeedVariant seed_variant(int v);
+// lookup false: seeding alone (the lookup then runs as launch_lookup with desc).
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
-                              ReadRec* rec, Arenas A, Counters* ctr, int variant, cudaStream_t st);
+                              ReadRec* rec, Arenas A, Counters* ctr, int variant, bool lookup, cudaStream_t st);
 // Main path: seeding and lookup fused (a warp per read); reads too long for the
 // shared-memory buffers are seeded by launch_seed_long and looked up by launch_lookup_long.
 void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig& C, const uint8_t* seqs,
@@ -162,7 +163,7 @@ void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig&
 void launch_lookup_long(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                         cudaStream_t st);
 void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
-                   cudaStream_t st);
+                   cudaStream_t st, const BatchDesc* desc = nullptr);
 void launch_nams(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st);
 void launch_bucket_reads(uint32_t n, uint32_t lane_max_hits, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st,

@@ -270,7 +270,9 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
 
 template <bool kCount>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, MapConfig C, uint32_t n,
-                                                                 ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+                                                                 ReadRec* __restrict__ rec, Arenas A, Counters* ctr,
+                                                                 const BatchDesc* desc) {
+    if (desc) n = min(n, desc->n_reads);   // batched form: n is the work areas' capacity
     for (uint32_t r = warp_global_id(); r < n; r += warp_count()) lookup_read<kCount>(I, C, r, rec, A, ctr);
 }
 
@@ -339,7 +341,9 @@ __global__ void __launch_bounds__(32 * kSeedWarps, kFusedBlocksPerSm)
 // persistent grid; the batch (reads, count, items) is read from desc in device memory.
 // The shape (warps per block, resident blocks per SM, shared-memory read window) is a
 // template of its own per variant, picked at run time.
-template <bool kCount, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
+// kLookup false: seeding alone (indexes whose entries exceed the fuse limit are looked
+// up by k_lookup afterwards, as in the plain form).
+template <bool kCount, bool kLookup, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
 __global__ void __launch_bounds__(32 * kWarps, kBlocks)
     k_seed_lookup_q(DevParams P, IndexView I, MapConfig C, const BatchDesc* __restrict__ desc,
                     ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
@@ -382,8 +386,10 @@ __global__ void __launch_bounds__(32 * kWarps, kBlocks)
             }
             emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
             __syncwarp();
-            lookup_read<kCount>(I, C, r, rec, A, ctr);
-            __syncwarp();
+            if (kLookup) {
+                lookup_read<kCount>(I, C, r, rec, A, ctr);
+                __syncwarp();
+            }
         }
     }
 }
@@ -1735,31 +1741,32 @@ SeedVariant seed_variant(int v) {
     return table[v < 0 || v >= kSeedVariants ? 0 : v];
 }
 
-template <bool kCount, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
+template <bool kCount, bool kLookup, int kWarps, int kBlocks, uint32_t kMaxLen, uint32_t kSyncmers>
 static void launch_q(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc, ReadRec* rec,
                      Arenas A, Counters* ctr, cudaStream_t st) {
     const unsigned grid = (unsigned)device_sm_count() * kBlocks;
-    launch_probe(k_seed_lookup_q<kCount, kWarps, kBlocks, kMaxLen, kSyncmers>, grid, 32 * kWarps, 0, st, C, P, I, C,
-                 desc, rec, A, ctr);
+    launch_probe(k_seed_lookup_q<kCount, kLookup, kWarps, kBlocks, kMaxLen, kSyncmers>, grid, 32 * kWarps, 0, st, C,
+                 P, I, C, desc, rec, A, ctr);
 }
 
-template <bool kCount>
+template <bool kCount, bool kLookup>
 static void launch_q_variant(int v, const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
                              ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
     switch (v) {
-        case 1: launch_q<kCount, 8, 5, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
-        case 2: launch_q<kCount, 4, 12, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
-        case 3: launch_q<kCount, 8, 7, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
-        case 4: launch_q<kCount, 16, 3, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
-        case 5: launch_q<kCount, 8, 6, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
-        default: launch_q<kCount, 8, 6, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 1: launch_q<kCount, kLookup, 8, 5, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 2: launch_q<kCount, kLookup, 4, 12, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 3: launch_q<kCount, kLookup, 8, 7, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
+        case 4: launch_q<kCount, kLookup, 16, 3, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
+        case 5: launch_q<kCount, kLookup, 8, 6, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
+        default: launch_q<kCount, kLookup, 8, 6, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
     }
 }
 
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
-                              ReadRec* rec, Arenas A, Counters* ctr, int variant, cudaStream_t st) {
-    if (C.count_bytes) launch_q_variant<true>(variant, P, I, C, desc, rec, A, ctr, st);
-    else launch_q_variant<false>(variant, P, I, C, desc, rec, A, ctr, st);
+                              ReadRec* rec, Arenas A, Counters* ctr, int variant, bool lookup, cudaStream_t st) {
+    if (!lookup) launch_q_variant<false, false>(variant, P, I, C, desc, rec, A, ctr, st);
+    else if (C.count_bytes) launch_q_variant<true, true>(variant, P, I, C, desc, rec, A, ctr, st);
+    else launch_q_variant<false, true>(variant, P, I, C, desc, rec, A, ctr, st);
     GBSA_LAUNCHED();
 }
 
@@ -1785,10 +1792,10 @@ void launch_lookup_long(const IndexView& I, const MapConfig& C, uint32_t n, Read
 }
 
 void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
-                   cudaStream_t st) {
+                   cudaStream_t st, const BatchDesc* desc) {
     if (!n) return;
     launch_probe(C.count_bytes ? k_lookup<true> : k_lookup<false>, warp_grid(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0,
-                 st, C, I, C, n, rec, A, ctr);
+                 st, C, I, C, n, rec, A, ctr, desc);
     GBSA_LAUNCHED();
 }
 

@@ -6,6 +6,8 @@
 #include "map.cuh"
 #include "runtime.h"
 
+struct gbsa_batcher;
+
 struct gbsa_mapper {
     const gbsa_index* idx = nullptr;
     gbsa_map_options opt{};
@@ -86,5 +88,25 @@ void l2_window_attach(gbsa_mapper& m, bool on);
 // their bases.
 uint64_t stage_reads(gbsa_mapper& m, const char* seqs, const uint64_t* offsets, const uint32_t* lengths, uint32_t n,
                      cudaStream_t st);
+
+// One request of the served form: host reads in, host results out (as gbsa_map_reads).
+struct ServeRequest {
+    const char* seqs;
+    const uint64_t* offsets;
+    const uint32_t* lengths;
+    uint32_t n_reads;
+    gbsa_nam* nams;
+    uint64_t nam_capacity;
+    uint64_t* nam_offsets;
+    float* frac;
+    uint8_t* rescued;
+};
+
+// Maps k requests as one batch of the batcher's first set of work areas (one graph
+// launch): their reads are staged back to back, and each request's NAMs, offsets,
+// fractions and flags are copied straight from the batch's device outputs into its
+// own buffers.  status[j] is GBSA_OK, or GBSA_ERR_CAPACITY when request j's NAMs do
+// not fit its nam_capacity (its offsets are still written); totals[j] its NAM count.
+void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, int* status, uint64_t* totals);
 
 }  // namespace gbsa

@@ -1,35 +1,36 @@
-// serve.cu — the served form: a request queue in front of a pool of mappers.
+// serve.cu — the served form: continuous batching of requests onto batch slots.
 //
-// A server keeps the index resident and owns `workers` mappers, each with its own
-// streams and device work areas sized for the largest request; those areas are the
-// admission budget (a request waits in the queue until a mapper is free).  Each
-// worker thread takes the next request and maps it with gbsa_map_reads on its own
-// mapper, so requests overlap on the GPU and every request's NAMs equal the plain
-// form's.  Callers submit host buffers (kept alive until the request completes) and
-// poll for completions.  No reference counterpart: the reference maps one file per
-// process (step2/main.cu:4100-4760).
+// A server keeps the index resident and owns `slots` batchers (the batched form: each
+// batch one launch of a captured CUDA graph), each with its own streams and device
+// work areas for batches of up to batch_reads reads / batch_bases bases.  The slots are
+// created against a device-memory budget (by default half the memory free when the
+// server is created): each slot's work areas are measured as it is created, and no
+// slot is added once the budget would be exceeded (at least one is).  A host thread
+// per slot takes, whenever its slot is free, every request waiting at the head of the
+// queue that still fits the slot (reads and bases), maps them as one batch, and copies
+// each request's NAMs, offsets, fractions and rescue flags straight from the batch's
+// device outputs into that request's buffers.  Requests that arrive while batches are
+// on the GPU are taken by the next slot to come free, so small requests share launches
+// and requests overlap on the device; each request's results equal gbsa_map_reads'
+// for its reads alone (a read's NAMs depend only on the read).  No reference
+// counterpart: the reference maps one file per process (step2/main.cu:4100-4760).
+#include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
 
-#include "index.h"
-#include "runtime.h"
+#include "mapper.h"
 
 namespace {
 
 struct Request {
-    const char* seqs;
-    const uint64_t* offsets;
-    const uint32_t* lengths;
-    uint32_t n_reads;
-    gbsa_nam* nams;
-    uint64_t nam_capacity;
-    uint64_t* nam_offsets;
-    float* frac;
-    uint8_t* rescued;
+    gbsa::ServeRequest r;
+    uint64_t bases;
     uint64_t tag;
+    std::chrono::steady_clock::time_point t_submit;
 };
 
 struct Done {
@@ -43,8 +44,10 @@ struct Done {
 struct gbsa_server {
     const gbsa_index* idx = nullptr;
     int device = 0;
-    uint32_t max_reads = 0;
-    std::vector<gbsa_mapper*> mappers;
+    gbsa_server_config cfg{};
+    std::vector<gbsa_batcher*> slots;
+    uint64_t slot_bytes = 0;      // device bytes one slot's work areas took at creation
+    uint64_t budget = 0;
     std::vector<std::thread> threads;
     std::mutex mu;
     std::condition_variable cv_req, cv_done;
@@ -52,25 +55,58 @@ struct gbsa_server {
     std::deque<Done> done;
     bool stop = false;
     uint64_t in_flight = 0;
+    uint64_t batches = 0, requests_batched = 0, max_requests_per_batch = 0;
 
-    void work(gbsa_mapper* m) {
+    void work(gbsa_batcher* b) {
         cudaSetDevice(device);
+        std::vector<Request> take;
+        std::vector<gbsa::ServeRequest> rq;
+        std::vector<int> st;
+        std::vector<uint64_t> tot;
         for (;;) {
-            Request r;
+            take.clear();
             {
                 std::unique_lock<std::mutex> g(mu);
                 cv_req.wait(g, [&] { return stop || !queue.empty(); });
                 if (queue.empty()) return;   // stopping
-                r = queue.front();
-                queue.pop_front();
+                // continuous batching: every request at the head of the queue that fits
+                uint64_t reads = 0, bases = 0;
+                while (!queue.empty()) {
+                    const Request& q = queue.front();
+                    if (!take.empty() && (reads + q.r.n_reads > cfg.batch_reads || bases + q.bases > cfg.batch_bases))
+                        break;
+                    reads += q.r.n_reads;
+                    bases += q.bases;
+                    take.push_back(q);
+                    queue.pop_front();
+                }
+                ++batches;
+                requests_batched += take.size();
+                max_requests_per_batch = std::max<uint64_t>(max_requests_per_batch, take.size());
             }
-            const int rc = gbsa_map_reads(m, r.seqs, r.offsets, r.lengths, r.n_reads, r.nams, r.nam_capacity,
-                                          r.nam_offsets, r.frac, r.rescued);
+            if (!queue.empty()) cv_req.notify_one();
+            rq.clear();
+            for (const Request& q : take) rq.push_back(q.r);
+            st.assign(take.size(), GBSA_OK);
+            tot.assign(take.size(), 0);
+            try {
+                gbsa::batcher_run_requests(*b, rq.data(), (uint32_t)rq.size(), st.data(), tot.data());
+            } catch (const gbsa::Error& e) {
+                gbsa::set_last_error(e.what());
+                st.assign(take.size(), e.code);
+                tot.assign(take.size(), 0);
+            } catch (const std::exception& e) {
+                gbsa::set_last_error(e.what());
+                st.assign(take.size(), GBSA_ERR_CUDA);
+                tot.assign(take.size(), 0);
+            }
             {
                 std::lock_guard<std::mutex> g(mu);
-                // a failed call may not have written the offsets: report no NAMs
-                done.push_back(Done{r.tag, rc, rc == GBSA_OK ? r.nam_offsets[r.n_reads] : 0});
-                --in_flight;
+                for (size_t j = 0; j < take.size(); ++j) {
+                    // a failed batch may not have written the offsets: report no NAMs
+                    done.push_back(Done{take[j].tag, st[j], st[j] == GBSA_ERR_CAPACITY || st[j] == GBSA_OK ? tot[j] : 0});
+                    --in_flight;
+                }
             }
             cv_done.notify_all();
         }
@@ -81,28 +117,45 @@ using namespace gbsa;
 
 extern "C" {
 
-int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint32_t workers,
-                       uint32_t max_reads_per_request, uint64_t max_bases_per_request, gbsa_server** out) {
+int gbsa_server_create_ex(const gbsa_index* idx, const gbsa_map_options* opt, const gbsa_server_config* cfg,
+                          gbsa_server** out) {
     try {
         *out = nullptr;
-        if (workers == 0 || workers > 64) throw Error(GBSA_ERR_PARAM, "workers must be in [1, 64]");
-        if (max_reads_per_request == 0) throw Error(GBSA_ERR_PARAM, "max_reads_per_request must be positive");
+        if (!idx || !opt || !cfg) throw Error(GBSA_ERR_PARAM, "null index, options or configuration");
+        if (cfg->slots == 0 || cfg->slots > 64) throw Error(GBSA_ERR_PARAM, "slots must be in [1, 64]");
+        if (cfg->batch_reads == 0) throw Error(GBSA_ERR_PARAM, "batch_reads must be positive");
         std::unique_ptr<gbsa_server> s(new gbsa_server());
         s->idx = idx;
         s->device = idx->device;
-        s->max_reads = max_reads_per_request;
+        s->cfg = *cfg;
+        if (s->cfg.batch_bases == 0) s->cfg.batch_bases = 500ull * cfg->batch_reads;
         GBSA_CUDA(cudaSetDevice(s->device));
-        for (uint32_t i = 0; i < workers; ++i) {
-            gbsa_mapper* m = nullptr;
-            const int rc = gbsa_mapper_create(idx, opt, max_reads_per_request, max_bases_per_request, &m);
+        size_t free0 = 0, total = 0;
+        GBSA_CUDA(cudaMemGetInfo(&free0, &total));
+        s->budget = cfg->memory_budget ? cfg->memory_budget : free0 / 2;
+        gbsa_batch_config bc{};
+        int from_file = 0;
+        if (gbsa_batch_config_default(&bc, &from_file) != GBSA_OK) throw Error(GBSA_ERR_PARAM, gbsa_last_error());
+        bc.chunk_reads = std::max<uint32_t>(bc.chunk_reads, s->cfg.batch_reads);
+        uint64_t used = 0;
+        for (uint32_t i = 0; i < s->cfg.slots; ++i) {
+            size_t f_before = 0, f_after = 0;
+            GBSA_CUDA(cudaMemGetInfo(&f_before, &total));
+            if (i > 0 && used + s->slot_bytes > s->budget) break;   // admission: the next slot would not fit
+            gbsa_batcher* b = nullptr;
+            const int rc = gbsa_batcher_create(idx, opt, &bc, s->cfg.batch_reads, s->cfg.batch_bases, &b);
             if (rc != GBSA_OK) {
-                for (gbsa_mapper* x : s->mappers) gbsa_mapper_free(x);
-                throw Error(rc, std::string("mapper for the server: ") + gbsa_last_error());
+                for (gbsa_batcher* x : s->slots) gbsa_batcher_free(x);
+                throw Error(rc, std::string("server slot: ") + gbsa_last_error());
             }
-            s->mappers.push_back(m);
+            GBSA_CUDA(cudaMemGetInfo(&f_after, &total));
+            const uint64_t took = f_before > f_after ? f_before - f_after : 0;
+            s->slot_bytes = std::max<uint64_t>(s->slot_bytes, took);
+            used += took;
+            s->slots.push_back(b);
         }
         gbsa_server* raw = s.get();
-        for (gbsa_mapper* m : s->mappers) s->threads.emplace_back([raw, m] { raw->work(m); });
+        for (gbsa_batcher* b : s->slots) s->threads.emplace_back([raw, b] { raw->work(b); });
         *out = s.release();
         return GBSA_OK;
     } catch (const Error& e) {
@@ -114,16 +167,49 @@ int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
     }
 }
 
+int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint32_t workers,
+                       uint32_t max_reads_per_request, uint64_t max_bases_per_request, gbsa_server** out) {
+    gbsa_server_config c{};
+    c.slots = workers;
+    c.batch_reads = max_reads_per_request;
+    c.batch_bases = max_bases_per_request;
+    c.memory_budget = 0;
+    if (workers == 0 || workers > 64) {
+        set_last_error("workers must be in [1, 64]");
+        return GBSA_ERR_PARAM;
+    }
+    return gbsa_server_create_ex(idx, opt, &c, out);
+}
+
+int gbsa_server_info(const gbsa_server* s, uint32_t* slots, uint64_t* slot_bytes, uint64_t* budget,
+                     uint64_t* batches, uint64_t* requests) {
+    gbsa_server* x = const_cast<gbsa_server*>(s);
+    std::lock_guard<std::mutex> g(x->mu);
+    if (slots) *slots = (uint32_t)s->slots.size();
+    if (slot_bytes) *slot_bytes = s->slot_bytes;
+    if (budget) *budget = s->budget;
+    if (batches) *batches = s->batches;
+    if (requests) *requests = s->requests_batched;
+    return GBSA_OK;
+}
+
 int gbsa_server_submit(gbsa_server* s, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
                        uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets, float* frac,
                        uint8_t* rescued, uint64_t tag) {
-    if (n_reads > s->max_reads) {
-        set_last_error("request larger than max_reads_per_request");
+    uint64_t bases = 0;
+    for (uint32_t i = 0; i < n_reads; ++i) bases += lengths[i];
+    if (n_reads > s->cfg.batch_reads || bases > s->cfg.batch_bases) {
+        set_last_error("request larger than a batch slot (batch_reads / batch_bases)");
         return GBSA_ERR_CAPACITY;
     }
     {
         std::lock_guard<std::mutex> g(s->mu);
-        s->queue.push_back(Request{seqs, offsets, lengths, n_reads, nams, nam_capacity, nam_offsets, frac, rescued, tag});
+        Request q;
+        q.r = ServeRequest{seqs, offsets, lengths, n_reads, nams, nam_capacity, nam_offsets, frac, rescued};
+        q.bases = bases;
+        q.tag = tag;
+        q.t_submit = std::chrono::steady_clock::now();
+        s->queue.push_back(q);
         ++s->in_flight;
     }
     s->cv_req.notify_one();
@@ -158,7 +244,7 @@ void gbsa_server_free(gbsa_server* s) {
     }
     s->cv_req.notify_all();
     for (auto& t : s->threads) t.join();
-    for (gbsa_mapper* m : s->mappers) gbsa_mapper_free(m);
+    for (gbsa_batcher* b : s->slots) gbsa_batcher_free(b);
     delete s;
 }
 

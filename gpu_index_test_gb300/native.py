@@ -71,6 +71,9 @@ def lib():
             "gbsa_rescue_mates_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, u64, i32, C.c_float,
                                                C.c_float, vp, vp]),
             "gbsa_server_create": (i32, [vp, vp, u32, u32, u64, vp]),
+            "gbsa_server_create_ex": (i32, [vp, vp, C.POINTER(abi.ServerConfig), vp]),
+            "gbsa_server_info": (i32, [vp, C.POINTER(u32), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64),
+                                       C.POINTER(u64)]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
             "gbsa_server_free": (None, [vp]),
@@ -497,15 +500,21 @@ class Batcher:
 
 
 class Server:
-    """The served form: requests mapped from a queue by a pool of mappers (gbsa_server_*)."""
+    """The served form (gbsa_server_*): continuous batching of queued requests onto batch
+    slots (batchers) created against a device-memory budget."""
 
-    def __init__(self, index, opt=None, workers=4, max_reads=100_000, max_bases=None):
+    def __init__(self, index, opt=None, workers=4, max_reads=100_000, max_bases=None, memory_budget=0):
         self.index = index
         self.opt = opt or abi.map_options()
+        cfg = abi.ServerConfig(workers, max_reads, max_bases or max_reads * 256, memory_budget)
         h = C.c_void_p()
-        _check(lib().gbsa_server_create(index.h, C.byref(self.opt), workers, max_reads,
-                                        max_bases or max_reads * 256, C.byref(h)))
+        _check(lib().gbsa_server_create_ex(index.h, C.byref(self.opt), C.byref(cfg), C.byref(h)))
         self.h = h
+
+    def info(self):
+        a, b, c, d, e = C.c_uint32(), C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().gbsa_server_info(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d), C.byref(e)))
+        return {"slots": a.value, "slot_bytes": b.value, "budget": c.value, "batches": d.value, "requests": e.value}
 
     def submit(self, seq_ptr, offsets_ptr, lengths_ptr, n, nams_ptr, cap, nam_offsets_ptr, frac_ptr, resc_ptr, tag):
         """All buffers are host pointers kept alive until poll reports `tag`."""

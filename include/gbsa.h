@@ -317,18 +317,39 @@ int gbsa_fastq_parse_pairs(const char* buf1, uint64_t len1, const char* buf2, ui
                            uint64_t* n_bases, uint64_t* consumed1, uint64_t* consumed2);
 
 /* ---- served form ------------------------------------------------------------- */
-/* A server keeps the index resident and maps requests from a queue on `workers`
- * mappers (each with its own streams and device work areas for requests of up to
- * max_reads_per_request reads / max_bases_per_request bases: the admission budget);
- * requests overlap on the GPU and give the NAMs gbsa_map_reads gives.  Submit
- * returns at once (GBSA_ERR_CAPACITY for a request above the maximum); the caller
- * keeps a request's buffers alive until poll reports its tag.  Poll returns up to
- * cap completed requests (tag, status, NAM total), waiting up to wait_ms for one
- * (-1: until one completes or none is in flight).  No reference counterpart. */
+/* A server keeps the index resident and maps requests with continuous batching: it
+ * owns up to `slots` batch slots (batchers of the batched form, each with its own
+ * streams and device work areas for batches of up to batch_reads reads and
+ * batch_bases bases), created against a device-memory budget (memory_budget bytes, 0:
+ * half the memory free at creation; a slot is not added once its measured footprint
+ * would exceed the budget, and at least one is).  Whenever a slot is free, its host
+ * thread takes every request waiting at the head of the queue that still fits the
+ * slot and maps them as one batch (one graph launch), so requests that arrive while
+ * others are on the GPU share launches and overlap on the device; each request's
+ * results are copied from the batch's device outputs into its own buffers and equal
+ * gbsa_map_reads' for its reads.  Submit returns at once (GBSA_ERR_CAPACITY for a
+ * request larger than a slot); the caller keeps a request's buffers alive until poll
+ * reports its tag.  Poll returns up to cap completed requests (tag, status, NAM
+ * total; a request whose NAMs exceed its nam_capacity completes with
+ * GBSA_ERR_CAPACITY, its offsets written), waiting up to wait_ms for one (-1: until
+ * one completes or none is in flight).  No reference counterpart. */
 typedef struct gbsa_server gbsa_server;
+typedef struct gbsa_server_config {
+    uint32_t slots;          /* batch slots at most (1-64) */
+    uint32_t batch_reads;    /* reads a batch holds (also the largest request) */
+    uint64_t batch_bases;    /* bases a batch holds (0: 500 per read) */
+    uint64_t memory_budget;  /* device bytes the slots may take (0: half the free memory) */
+} gbsa_server_config;
+int gbsa_server_create_ex(const gbsa_index* idx, const gbsa_map_options* opt, const gbsa_server_config* cfg,
+                          gbsa_server** out);
+/* gbsa_server_create_ex with slots = workers, batch_reads / batch_bases = the request
+ * maxima and the default budget. */
 int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint32_t workers,
                        uint32_t max_reads_per_request, uint64_t max_bases_per_request,
                        gbsa_server** out);
+/* Slots created, device bytes of one slot, the budget, and batches / requests mapped. */
+int gbsa_server_info(const gbsa_server* s, uint32_t* slots, uint64_t* slot_bytes, uint64_t* budget,
+                     uint64_t* batches, uint64_t* requests);
 int gbsa_server_submit(gbsa_server* s, const char* seqs, const uint64_t* offsets,
                        const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams,
                        uint64_t nam_capacity, uint64_t* nam_offsets, float* frac,

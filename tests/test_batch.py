@@ -111,3 +111,65 @@ def test_batched_form_grows_its_work_areas():
     b = native.Batcher(idx, max_reads=1024, max_bases=1024 * 20)
     for _ in range(2):
         assert same(b.map_reads(reads, synth.read_items(rp)), ref)
+
+
+def _serve(srv, pool, reqs):
+    bufs = {}
+    for tag, (start, n) in enumerate(reqs):
+        offs = np.ascontiguousarray(pool.offsets[start:start + n])
+        lens = np.ascontiguousarray(pool.lengths[start:start + n])
+        cap = 64 * n + 64
+        out = (np.zeros(cap, abi.NAM), np.zeros(n + 1, np.uint64), np.zeros(max(1, n), np.float32),
+               np.zeros(max(1, n), np.uint8))
+        bufs[tag] = (offs, lens, out)
+        srv.submit(pool.seq.ctypes.data, offs.ctypes.data, lens.ctypes.data, n, out[0].ctypes.data, cap,
+                   out[1].ctypes.data, out[2].ctypes.data, out[3].ctypes.data, tag)
+    done = {}
+    while len(done) < len(reqs):
+        for tag, st, tot in srv.poll(wait_ms=-1):
+            done[tag] = (st, tot)
+    return bufs, done
+
+
+def test_server_batches_requests_and_each_equals_alone():
+    """Small requests submitted together are mapped in shared batches (continuous
+    batching: fewer batches than requests) on two slots, and each request's NAMs,
+    offsets, fractions and flags equal those of the request mapped alone."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=121))
+    pool = synth.make_reads(g, synth.ReadParams(seed=122, n_units=20_000, len_min=100, len_max=250, paired_frac=1.0,
+                                                insert_mean=400, insert_sd=50))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    rng = np.random.default_rng(123)
+    reqs = []
+    for _ in range(80):
+        n = int(rng.integers(1, 400)) * 2
+        reqs.append((int(rng.integers(0, (pool.n - n) // 2)) * 2, n))
+    reqs.append((0, 0))   # an empty request
+    srv = native.Server(idx, workers=2, max_reads=16384)
+    bufs, done = _serve(srv, pool, reqs)
+    info = srv.info()
+    srv.free()
+    assert info["slots"] == 2 and info["requests"] == len(reqs) and info["batches"] < len(reqs)
+    m = native.Mapper(idx)
+    for tag, (start, n) in enumerate(reqs):
+        st, tot = done[tag]
+        assert st == 0
+        alone = m.map_reads(pool.subset(np.arange(start, start + n)))
+        offs, lens, (nams, noff, frac, resc) = bufs[tag]
+        assert tot == len(alone[0]) and (noff == alone[1]).all()
+        assert nams_equal(nams[:tot], alone[0])
+        assert (frac[:n] == alone[2]).all() and (resc[:n] == alone[3]).all()
+
+
+def test_server_memory_budget_limits_slots():
+    """Slots are created against the device-memory budget: a budget below one slot's
+    work areas leaves a single slot, which still serves every request."""
+    g = synth.make_genome(synth.genome_params("C2", scale=0.005, seed=124))
+    pool = synth.make_reads(g, synth.read_params("C2", n_units=2000, seed=125))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    srv = native.Server(idx, workers=6, max_reads=8192, memory_budget=1)
+    info = srv.info()
+    assert info["slots"] == 1 and info["slot_bytes"] > 0 and info["budget"] == 1
+    bufs, done = _serve(srv, pool, [(0, 1000), (1000, 2000), (3000, 1000)])
+    srv.free()
+    assert all(st == 0 for st, _ in done.values())
