@@ -158,7 +158,13 @@ def ncu_traffic():
         return {}
 
 
-def serve_measure(idx, g, rates, seconds, scale, index_name, slots=4, max_reads=100_000):
+# batch slots of the served form and reads per slot (a batch packs queued requests up to this)
+SERVE_SLOTS = 4
+SERVE_BATCH_READS = 100_000
+
+
+def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, max_reads=100_000,
+                  batch_reads=SERVE_BATCH_READS):
     """Served form: Poisson arrivals of requests of 1k-100k reads (log-uniform) of
     100-250 bp pairs against the resident index, continuous batching onto `slots` batch
     slots; p50/p99 latency from each request's scheduled arrival to its completion;
@@ -179,7 +185,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=4, max_reads=
     plain = pm.map_reads(pool)
     pm.free()
     npr = max(40, int(np.ceil(len(plain[0]) / pool.n * 3)))
-    srv = native.Server(idx, workers=slots, max_reads=max_reads, max_bases=max_reads * 250)
+    srv = native.Server(idx, workers=slots, max_reads=batch_reads, max_bases=batch_reads * 250)
     n_slots, slot_nams = 24, max_reads * npr
     plain_bytes = np.ascontiguousarray(plain[0]).view(np.uint8)
     bufs = [(torch.empty(slot_nams * 44, dtype=torch.uint8).pin_memory(),
@@ -270,7 +276,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=4, max_reads=
     sat = max(ok, key=lambda r: r["reads_per_s"]) if ok else None
     # the same requests' sizes, mapped one by one on 10k-read requests: p99 target is for them
     return {"index": index_name, "slots": info["slots"], "slot_bytes": info["slot_bytes"],
-            "memory_budget_bytes": info["budget"], "batch_reads": max_reads,
+            "memory_budget_bytes": info["budget"], "batch_reads": batch_reads,
             "request_reads": "1k-100k log-uniform, 100-250 bp pairs", "rates": results,
             "saturation": ({"rate_req_s": sat["rate_req_s"], "reads_per_s": sat["reads_per_s"], "p99_ms": sat["p99_ms"]}
                            if sat else None)}
@@ -439,16 +445,107 @@ def cpu_baseline(g, reads, target_s, gpu_result=None, gpu_index=None):
             "index_build_s": build_s, "index": how}, exact
 
 
+# Child process of the reference arm: the workload's reads as a case file of the
+# reference driver and the index as a .sti file (written by the oracle: the reference's
+# populate is commented out, so the reference only reads indexes).  Run apart so that
+# the arm's own process loads neither the data generator nor the oracle.
+_REF_PREP = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import bench
+from oracle import oracle_py
+out, config, scale = sys.argv[2], sys.argv[3], float(sys.argv[4])
+g, reads, _, gp, rp = bench.workload(scale, 0, config)
+p = oracle_py.params_from_read_length(150)
+oracle_py.Index.build(p, g).write_sti(out + "/index.sti")
+with open(out + "/case.bin", "wb") as f:
+    np.array([150, 2], np.int32).tofile(f)
+    np.array([reads.n], np.uint32).tofile(f)
+    reads.lengths.astype(np.uint32).tofile(f)
+    reads.seq.tofile(f)
+json.dump({"genome_bp": int(gp.total_len), "contigs": int(gp.n_contigs), "reads": int(reads.n),
+           "len_min": int(rp.len_min), "len_max": int(rp.len_max), "paired": float(rp.paired_frac)},
+          open(out + "/meta.json", "w"))
+"""
+
+
+def _ref_config(meta, args):
+    class _P:
+        pass
+
+    gp, rp = _P(), _P()
+    gp.total_len, gp.n_contigs = meta["genome_bp"], meta["contigs"]
+    rp.len_min, rp.len_max, rp.paired_frac = meta["len_min"], meta["len_max"], meta["paired"]
+
+    class _R:
+        n = meta["reads"]
+
+    return config_of(gp, rp, _R, args)
+
+
 def run_reference(args):
-    """--impl reference: the CPU restatement of the reference path on the host cores."""
+    """--impl reference: the reference's own CPU path (query randstrobes with its
+    SyncmerIterator / RandstrobeIterator, find_nams, find_nams_rescue; oracle/_ref/
+    ref_driver built from its sources, oracle/build_ref.sh) on all host cores, timed over
+    a bounded sample of the workload's reads; the CPU restatement when the reference's
+    sources are not at hand."""
+    import shutil
+    import tempfile
+
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from gpu_index_test_gb300 import abi
-    from oracle import oracle_py
     import __graft_entry__
 
     __graft_entry__.build()
+    ref = os.path.join(HERE, "oracle", "_ref", "ref_driver")
+    if not os.path.exists(ref):
+        return run_reference_port(args, "reference sources not staged on this host (oracle/stage_ref.sh)")
+    tmp = tempfile.mkdtemp(prefix="gbsa_ref_")
+    try:
+        subprocess.run([sys.executable, "-c", _REF_PREP, HERE, tmp, args.config, str(args.scale)], check=True)
+        meta = json.load(open(os.path.join(tmp, "meta.json")))
+        cores = os.cpu_count() or 1
+        case, sti = os.path.join(tmp, "case.bin"), os.path.join(tmp, "index.sti")
+
+        def drive(reps, max_reads):
+            r = subprocess.run([ref, "time", case, sti, str(cores), str(reps), str(max_reads)], check=True,
+                               stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            return json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+
+        cal = drive(1, 20000)
+        per_read = cal["seconds"] / max(1, cal["reads"])
+        step_budget = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+        n = int(min(meta["reads"], max(1000, step_budget / max(per_read, 1e-9))))
+        res = drive(args.warmup + args.steps, n)
+        times = res["rep_seconds"][args.warmup:] or res["rep_seconds"]
+        dt = sum(times) / len(times)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    v = n / dt
+    sample = (f"first {n} of {meta['reads']} reads per step, {cores} host threads (reads 256 at a time), "
+              f"mean of {len(times)} steps after {args.warmup} warm-up")
+    line = {
+        "impl": "reference", "metric": "reads/s seed+lookup+NAM", "value": v, "unit": "reads/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": _ref_config(meta, args),
+        "cpu_baseline": {"value": v, "unit": "reads/s", "cores": cores, "kind": "reference", "sample": sample,
+                         "code": "the reference's SyncmerIterator, RandstrobeIterator, StrobemerIndex::read/find, "
+                                 "find_nams, find_nams_rescue (step2/), built from its own sources by "
+                                 "oracle/build_ref.sh; index written by the oracle (.sti v2)"},
+        "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_reference_port(args, why):
+    """The CPU restatement of the reference path on the host cores (the reference's own
+    sources are not at hand on this host)."""
+    from gpu_index_test_gb300 import abi
+    from oracle import oracle_py
+
     g, reads, _, gp, rp = workload(args.scale, 0, args.config)
     p = oracle_py.params_from_read_length(150)
     idx = oracle_py.Index.build(p, g)
@@ -474,7 +571,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": config_of(gp, rp, reads, args),
         "cpu_baseline": {"value": v, "unit": "reads/s", "cores": cores, "kind": "port",
-                         "sample": f"first {n} of {reads.n} reads per step, {cores} host threads"},
+                         "sample": f"first {n} of {reads.n} reads per step, {cores} host threads",
+                         "why_port": why},
         "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

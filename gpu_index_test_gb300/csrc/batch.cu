@@ -261,6 +261,44 @@ uint64_t run_sync(gbsa_batcher& b, Lane& L, const BatchDesc& d) {
 
 }  // namespace
 
+void batcher_warm_up(gbsa_batcher& b, uint32_t max_reads, double nams_per_read) {
+    Lane& L = b.lanes[0];
+    lane_init(b, L);
+    lane_reserve(b, L, max_reads);
+    // every buffer a batch of max_reads reads needs, so that serving allocates nothing
+    // (cudaFree and cudaFreeHost wait for the whole device, other slots' work included)
+    L.h_items.resize(12ull * (max_reads + 1));
+    L.h_desc.resize(sizeof(BatchDesc) + 8ull * (max_reads + 1));
+    L.out_off.resize(8ull * (max_reads + 1));
+    L.out_frac.resize(4ull * (max_reads + 1));
+    L.out_resc.resize(max_reads + 1);
+    L.nams_per_read = std::max(L.nams_per_read, nams_per_read);
+    const uint64_t want = (uint64_t)(L.nams_per_read * 1.25 * max_reads) + 1024;
+    if (L.out_cap < want) {
+        L.out_nams.release();
+        L.out_nams.resize(sizeof(gbsa_nam) * want);
+        L.out_cap = want;
+    }
+    // one batch of pseudo-random 150 bp reads runs eagerly and captures the graph
+    const uint32_t n = std::min<uint32_t>(1024, max_reads), len = 150;
+    std::vector<char> seq((size_t)n * len);
+    uint64_t x = 0x9E3779B97F4A7C15ULL;
+    for (char& c : seq) {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        c = "ACGT"[x & 3];
+    }
+    std::vector<uint64_t> offs(n), noff(n + 1);
+    std::vector<uint32_t> lens(n, len);
+    for (uint32_t i = 0; i < n; ++i) offs[i] = (uint64_t)i * len;
+    std::vector<gbsa_nam> nams(64ull * n);
+    ServeRequest r{seq.data(), offs.data(), lens.data(), n, nams.data(), nams.size(), noff.data(), nullptr, nullptr};
+    int st = 0;
+    uint64_t tot = 0;
+    batcher_run_requests(b, &r, 1, &st, &tot);
+}
+
 void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, int* status, uint64_t* totals) {
     Lane& L = b.lanes[0];
     lane_init(b, L);

@@ -108,5 +108,9 @@ struct ServeRequest {
 // own buffers.  status[j] is GBSA_OK, or GBSA_ERR_CAPACITY when request j's NAMs do
 // not fit its nam_capacity (its offsets are still written); totals[j] its NAM count.
 void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, int* status, uint64_t* totals);
+// Sizes every buffer of the batcher's first set of work areas for batches of up to
+// max_reads reads (NAM outputs for nams_per_read NAMs per read) and captures its graph
+// with one batch of pseudo-random reads, so that later batches allocate nothing.
+void batcher_warm_up(gbsa_batcher& b, uint32_t max_reads, double nams_per_read);
 
 }  // namespace gbsa

@@ -148,6 +148,14 @@ int gbsa_server_create_ex(const gbsa_index* idx, const gbsa_map_options* opt, co
                 for (gbsa_batcher* x : s->slots) gbsa_batcher_free(x);
                 throw Error(rc, std::string("server slot: ") + gbsa_last_error());
             }
+            try {
+                // every buffer of a full batch, and the slot's graph, before any request
+                batcher_warm_up(*b, s->cfg.batch_reads, 40.0);
+            } catch (...) {
+                gbsa_batcher_free(b);
+                for (gbsa_batcher* x : s->slots) gbsa_batcher_free(x);
+                throw;
+            }
             GBSA_CUDA(cudaMemGetInfo(&f_after, &total));
             const uint64_t took = f_before > f_after ? f_before - f_after : 0;
             s->slot_bytes = std::max<uint64_t>(s->slot_bytes, took);

@@ -1,24 +1,27 @@
 #!/usr/bin/env bash
-# Builds oracle/_ref/ref_driver from the reference's own CPU sources where they lie
-# (never copied into this repository).  Test infrastructure: the binary runs the
-# reference's find_nams / find_nams_rescue / StrobemerIndex / syncmer code so that
-# the oracle restatement can be checked against it (tests/golden/make_golden.py).
+# Builds oracle/_ref/ref_driver from the reference's own CPU sources: where they lie in
+# the reference tree (never copied into this repository) on x86-64 hosts, or from the
+# staged copy of oracle/stage_ref.sh (baseline/_ref/src, git-ignored) on any host.  Test
+# and benchmark infrastructure: the binary runs the reference's find_nams /
+# find_nams_rescue / StrobemerIndex / syncmer code so that the oracle restatement can
+# be checked against it (tests/golden/make_golden.py) and the reference's CPU path can
+# be timed (bench.py --impl reference).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
-# Needs g++ and the CUDA headers (the reference headers include cuda_runtime.h).
-# The reference's nam.cu times its stages with x86 rdtsc, so this builds on x86-64
-# hosts only.
+# Usage: oracle/build_ref.sh [SOURCE_DIR]
+#   SOURCE_DIR: the reference's step2/ directory (default /root/reference/step2), or a
+#   staged copy.  Needs g++ and the CUDA headers (the reference headers include
+#   cuda_runtime.h).  The reference's nam.cu times its stages with x86 rdtsc, so an
+#   unstaged tree builds on x86-64 hosts only.
 set -euo pipefail
-REF="${1:-/root/reference}"
-SRC="$REF/step2"
+SRC="${1:-/root/reference/step2}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/nam.cu" ]; then
   echo "reference sources not found under $SRC" >&2
   exit 3
 fi
-if [ "$(uname -m)" != "x86_64" ]; then
-  echo "reference nam.cu uses x86 rdtsc; not buildable on $(uname -m)" >&2
+if [ "$(uname -m)" != "x86_64" ] && grep -q rdtsc "$SRC/nam.cu"; then
+  echo "reference nam.cu uses x86 rdtsc; stage it with oracle/stage_ref.sh to build on $(uname -m)" >&2
   exit 4
 fi
 mkdir -p "$OUT"
@@ -34,6 +37,16 @@ g++ -std=c++17 -w -O2 -I"$SRC" -I/usr/local/cuda/include -c "$SRC/indexparameter
 g++ -std=c++17 -w -O2 -I"$SRC" -c "$SRC/io.cpp" -o "$OUT/io.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/ref_driver.cu" -o "$OUT/ref_driver.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
-g++ -o "$OUT/ref_driver" "$OUT"/ref_driver.o "$OUT"/nam.o "$OUT"/index.o \
+g++ -pthread -o "$OUT/ref_driver" "$OUT"/ref_driver.o "$OUT"/nam.o "$OUT"/index.o \
   "$OUT"/randstrobes.o "$OUT"/indexparameters.o "$OUT"/io.o
 echo "built $OUT/ref_driver"
+# the reference-side binding (include/gbsa_shim.hpp) checked against the reference's own
+# find_nams: needs the library built first
+GBSA_DIR="$(cd "$HERE/../gpu_index_test_gb300" && pwd)"
+if [ -f "$GBSA_DIR/libgbsa.so" ]; then
+  g++ "${FLAGS[@]}" -I"$HERE/../include" -c "$HERE/shim_check.cu" -o "$OUT/shim_check.o"
+  g++ -pthread -o "$OUT/shim_check" "$OUT"/shim_check.o "$OUT"/nam.o "$OUT"/index.o "$OUT"/randstrobes.o \
+    "$OUT"/indexparameters.o "$OUT"/io.o -L"$GBSA_DIR" -lgbsa -Wl,-rpath,"$GBSA_DIR" \
+    -L/usr/local/cuda/lib64 -Wl,-rpath-link,/usr/local/cuda/lib64
+  echo "built $OUT/shim_check"
+fi
