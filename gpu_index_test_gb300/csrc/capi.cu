@@ -891,6 +891,16 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
                                                        : 100u;   // step2/main.cu:4204
         m->cfg.count_cap = opt->rescue_count_cap;
         m->cfg.sort_mode = opt->sort_mode;
+        {
+            // the NAM phase's shape from the committed autotuner result (the same kernels
+            // as the batched form's; results do not depend on it)
+            gbsa_batch_config bc{};
+            int from_file = 0;
+            if (gbsa_batch_config_default(&bc, &from_file) == GBSA_OK) {
+                m->cfg.lane_max_hits = bc.lane_max_hits;
+                m->cfg.sort_variant = bc.sort_variant;
+            }
+        }
         l2_window_attach(*m, true);
         m->max_reads = std::max<uint32_t>(max_reads, 1);
         m->max_bases = std::max<uint64_t>(max_bases, 1);

@@ -203,7 +203,9 @@ int gbsa_randstrobes_query_noalloc(const gbsa_params* p, const char* d_seqs,
 
 /* ---- NAM path ---------------------------------------------------------------- */
 /* A mapper owns the device work areas for batches of up to max_reads reads with up
- * to max_bases bases in total; both grow on demand. */
+ * to max_bases bases in total; both grow on demand.  The NAM phase's kernel shape (the
+ * split between one lane and one warp per read, the block size of the rescued reads'
+ * sort) is the one gbsa_batch_config_default gives. */
 int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt,
                        uint32_t max_reads, uint64_t max_bases, gbsa_mapper** out);
 void gbsa_mapper_free(gbsa_mapper* m);
