@@ -247,7 +247,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
 
         th = threading.Thread(target=submitter)
         th.start()
-        lat, reads_done, failed = [], 0, 0
+        lat, lat_n, reads_done, failed = [], [], 0, 0
         checks = []
         t_last = t0
         with ThreadPoolExecutor(max_workers=12) as ex:
@@ -260,6 +260,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
                         free.put(slot)
                         continue
                     lat.append(now - (t0 + arrivals[tag][0]))
+                    lat_n.append(n)
                     reads_done += n
                     t_last = max(t_last, now)
                     checks.append(ex.submit(check, slot, start, n, tot))
@@ -267,6 +268,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
         th.join()
         info1 = srv.info()
         lat_ms = np.sort(np.array(lat)) * 1e3
+        small = np.sort(np.array([x for x, k in zip(lat, lat_n) if k <= 10_000])) * 1e3
         n_req = len(arrivals)
         results.append({
             "rate_req_s": rate, "requests": n_req, "failed": failed,
@@ -275,6 +277,10 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
             "p50_ms": round(float(lat_ms[len(lat_ms) // 2]), 2) if len(lat_ms) else None,
             "p99_ms": round(float(lat_ms[min(len(lat_ms) - 1, int(len(lat_ms) * 0.99))]), 2) if len(lat_ms) else None,
             "max_ms": round(float(lat_ms[-1]), 2) if len(lat_ms) else None,
+            "requests_le_10k_reads": int(len(small)),
+            "p50_ms_le_10k_reads": round(float(small[len(small) // 2]), 2) if len(small) else None,
+            "p99_ms_le_10k_reads": round(float(small[min(len(small) - 1, int(len(small) * 0.99))]), 2)
+            if len(small) else None,
             "batches": info1["batches"] - info0["batches"],
             "requests_per_batch": round((info1["requests"] - info0["requests"])
                                         / max(1, info1["batches"] - info0["batches"]), 2),
@@ -284,12 +290,19 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     srv.free()
     ok = [r for r in results if r["p99_ms"] is not None and r["p99_ms"] < 20.0 and r["bit_exact_vs_plain"]]
     sat = max(ok, key=lambda r: r["reads_per_s"]) if ok else None
+    # the latency target is stated for requests of up to 10k reads
+    ok10 = [r for r in results if r["p99_ms_le_10k_reads"] is not None and r["p99_ms_le_10k_reads"] < 20.0
+            and r["bit_exact_vs_plain"]]
+    sat10 = max(ok10, key=lambda r: r["reads_per_s"]) if ok10 else None
     # the same requests' sizes, mapped one by one on 10k-read requests: p99 target is for them
     return {"index": index_name, "slots": info["slots"], "slot_bytes": info["slot_bytes"],
             "memory_budget_bytes": info["budget"], "batch_reads": batch_reads,
             "request_reads": "1k-100k log-uniform, 100-250 bp pairs", "rates": results,
             "saturation": ({"rate_req_s": sat["rate_req_s"], "reads_per_s": sat["reads_per_s"], "p99_ms": sat["p99_ms"]}
-                           if sat else None)}
+                           if sat else None),
+            "saturation_le_10k_reads": ({"rate_req_s": sat10["rate_req_s"], "reads_per_s": sat10["reads_per_s"],
+                                         "p99_ms_le_10k_reads": sat10["p99_ms_le_10k_reads"]} if sat10 else None),
+            "peak_reads_per_s": round(max(r["reads_per_s"] for r in results), 1) if results else None}
 
 
 def fastq_pipeline(m, reads, plain_nams, plain_offs, chunk_mb=48):

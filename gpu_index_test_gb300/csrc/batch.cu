@@ -24,8 +24,8 @@
 // from a gbsa_batch_config, by default the one the autotuner committed
 // (gpu_index_test_gb300/tuned.json, read next to the library).
 //
-// The host entry point cuts a call into chunks (aligned to work items) that alternate
-// between two sets of work areas, so that one chunk's copies overlap the other's graph.
+// The host entry point cuts a call into chunks (aligned to work items) that rotate over
+// three sets of work areas, so that one chunk's copies overlap the others' graphs.
 #include <dlfcn.h>
 
 #include <algorithm>
@@ -41,6 +41,10 @@
 
 namespace gbsa {
 namespace {
+
+// Sets of work areas of the host entry point: chunk k runs on set k % kLanes, so that
+// kLanes chunks are in flight (one's copies overlapping the others' graphs).
+constexpr uint32_t kLanes = 3;
 
 // One set of work areas with its captured graph.
 struct Lane {
@@ -152,7 +156,7 @@ struct gbsa_batcher {
     gbsa_batch_config cfg{};
     uint32_t max_reads = 0;
     uint64_t max_bases = 0;
-    gbsa::Lane lanes[2];
+    gbsa::Lane lanes[gbsa::kLanes];
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t caller_ev = nullptr;
     uint64_t graph_launches = 0, captures = 0, eager_runs = 0;
@@ -536,12 +540,12 @@ int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets,
             i = j;
         }
         const uint32_t n_chunks = (uint32_t)cuts.size() - 1;
-        if (n_chunks > 1) lane_init(*b, b->lanes[1]);
+        for (uint32_t i = 1; i < std::min<uint32_t>(n_chunks, kLanes); ++i) lane_init(*b, b->lanes[i]);
         uint64_t done_nams = 0;
-        // queues chunk k on lane k & 1: its reads (and items) in, its batch (the graph
+        // queues chunk k on lane k % kLanes: its reads (and items) in, its batch (the graph
         // when one is current)
         auto enqueue = [&](uint32_t k) {
-            Lane& L = b->lanes[k & 1];
+            Lane& L = b->lanes[k % kLanes];
             const uint32_t i0 = cuts[k], i1 = cuts[k + 1];
             const uint32_t r0 = item_start(i0), r1 = i1 < ni ? item_start(i1) : n_reads;
             const uint32_t n = r1 - r0;
@@ -596,7 +600,7 @@ int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets,
         std::vector<BatchDesc> descs(n_chunks);
         // waits for chunk k and copies its results out
         auto finish = [&](uint32_t k) {
-            Lane& L = b->lanes[k & 1];
+            Lane& L = b->lanes[k % kLanes];
             const uint32_t i0 = cuts[k], i1 = cuts[k + 1];
             const uint32_t r0 = item_start(i0), r1 = i1 < ni ? item_start(i1) : n_reads;
             const uint32_t n = r1 - r0;
@@ -655,7 +659,7 @@ int gbsa_batcher_map(gbsa_batcher* b, const char* seqs, const uint64_t* offsets,
         } drain{b};
         uint32_t queued = 0;
         for (uint32_t k = 0; k < n_chunks; ++k) {
-            while (queued < n_chunks && queued < k + 2) {
+            while (queued < n_chunks && queued < k + kLanes) {
                 descs[queued] = enqueue(queued);
                 ++queued;
             }

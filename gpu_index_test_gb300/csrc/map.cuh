@@ -43,7 +43,8 @@ struct Counters {
     unsigned int n_huge;   // rescued reads whose NAMs the large-tile block sort orders
     unsigned int rescue_next;  // next rescue-list entry to take (k_rescue's work counter)
     unsigned int lane_cnt[16]; // reads per hit-count bucket of the lane NAM kernel
-    unsigned int queue_head;   // next work item of the batched form's seeding + lookup kernel
+    unsigned int queue_head;   // next read (work item) of the seeding (+ lookup) kernel
+    unsigned int queue_head2;  // next read of the lookup kernel, when it runs on its own
 };
 
 // A batch of the batched form, in device memory: the kernels of a captured batch graph

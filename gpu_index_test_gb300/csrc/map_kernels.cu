@@ -33,6 +33,15 @@ __device__ __forceinline__ uint64_t warp_bump(unsigned long long* ctr, uint64_t 
     return __shfl_sync(0xFFFFFFFFu, off, 0);
 }
 
+// The next read for the calling warp from a device work counter: warps pull reads one
+// at a time, so reads of uneven cost (lengths, repeats) balance over a grid of resident
+// warps instead of each warp owning a fixed stride of them.
+__device__ __forceinline__ uint32_t warp_next(unsigned int* head) {
+    uint32_t r = 0;
+    if (lane_id() == 0) r = atomicAdd(head, 1u);
+    return __shfl_sync(0xFFFFFFFFu, r, 0);
+}
+
 __device__ __forceinline__ void warp_fail(ReadRec& rec, Counters* ctr, uint32_t bit) {
     if (lane_id() == 0) {
         rec.flags |= kReadFailed;
@@ -69,7 +78,7 @@ __global__ void __launch_bounds__(32 * kSeedWarps, 5) k_seed_smem(DevParams P, c
     __shared__ uint64_t s_sh[kSeedWarps][kSmemSyncmers];
     __shared__ uint32_t s_sp[kSeedWarps][kSmemSyncmers];
     const uint32_t w = threadIdx.x >> 5;
-    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+    for (uint32_t r = warp_next(&ctr->queue_head); r < n; r = warp_next(&ctr->queue_head)) {
         const uint32_t L = lens[r];
         ReadRec& R = rec[r];
         if (L > GBSA_MAX_READ_LEN) {
@@ -273,7 +282,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_lookup(IndexView I, Map
                                                                  ReadRec* __restrict__ rec, Arenas A, Counters* ctr,
                                                                  const BatchDesc* desc) {
     if (desc) n = min(n, desc->n_reads);   // batched form: n is the work areas' capacity
-    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) lookup_read<kCount>(I, C, r, rec, A, ctr);
+    for (uint32_t r = warp_next(&ctr->queue_head2); r < n; r = warp_next(&ctr->queue_head2))
+        lookup_read<kCount>(I, C, r, rec, A, ctr);
 }
 
 // The lookup of the reads seeded by k_seed_long (the long list).
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(32 * kSeedWarps, kFusedBlocksPerSm)
     __shared__ uint64_t s_sh[kSeedWarps][kFusedSyncmers];
     __shared__ uint32_t s_sp[kSeedWarps][kFusedSyncmers];
     const uint32_t w = threadIdx.x >> 5;
-    for (uint32_t r = warp_global_id(); r < n; r += warp_count()) {
+    for (uint32_t r = warp_next(&ctr->queue_head); r < n; r = warp_next(&ctr->queue_head)) {
         const uint32_t L = lens[r];
         ReadRec& R = rec[r];
         if (L > GBSA_MAX_READ_LEN) {
@@ -359,9 +369,7 @@ __global__ void __launch_bounds__(32 * kWarps, kBlocks)
     const uint32_t* __restrict__ items = desc->items;
     const uint32_t n_items = items ? desc->n_items : desc->n_reads;
     for (;;) {
-        uint32_t it = 0;
-        if (lane_id() == 0) it = atomicAdd(&ctr->queue_head, 1u);
-        it = __shfl_sync(0xFFFFFFFFu, it, 0);
+        const uint32_t it = warp_next(&ctr->queue_head);
         if (it >= n_items) break;
         // item bounds outside [0, n_reads] are clamped (reads no item covers stay empty)
         const uint32_t n_reads = desc->n_reads;
@@ -1774,7 +1782,8 @@ void launch_seed_lookup(const DevParams& P, const IndexView& I, const MapConfig&
                         const uint64_t* offs, const uint32_t* lens, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                         cudaStream_t st) {
     if (!n) return;
-    const unsigned grid = warp_grid(n, kSeedWarps);
+    // resident blocks only: the warps pull reads from the work counter until none is left
+    const unsigned grid = std::min<unsigned>(warp_grid(n, kSeedWarps), (unsigned)device_sm_count() * kFusedBlocksPerSm);
     launch_probe(C.count_bytes ? k_seed_lookup<true> : k_seed_lookup<false>, grid, 32 * kSeedWarps, 0, st, C, P, I, C,
                  seqs, offs, lens, n, rec, A, ctr);
     GBSA_LAUNCHED();
