@@ -48,6 +48,8 @@ def parse():
                     help="request rates (req/s) of the served-form measurement; empty to skip")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--no-fastq", dest="fastq", action="store_false", help="skip the FASTQ staging measurement")
+    ap.add_argument("--no-l2-window", dest="l2_window", action="store_false",
+                    help="map without the L2 access-policy window on the bucket table (for comparison)")
     ap.add_argument("--other-configs", default="C1,C3,C4",
                     help="configurations checked for parity (and timed) after the headline one; empty to skip")
     return ap.parse_args()
@@ -854,6 +856,7 @@ def main():
     info = idx.info()
     n = reads.n
     m = native.Mapper(idx, abi.map_options(), max_reads=n, max_bases=int(reads.lengths.sum()))
+    l2_window_bytes = m.set_l2_window(args.l2_window)
 
     dev = torch.device("cuda", local)
     d_seq = torch.from_numpy(reads.seq).to(dev)
@@ -1193,6 +1196,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": dict(config_of(gp, rp, reads, args), index_entries=int(info.size), index_bits=int(info.bits),
                        filter_cutoff=int(info.filter_cutoff), index_build_gpu_s=round(build_s, 3),
+                       l2_window_bytes=int(l2_window_bytes),
                        form=("seeding and lookup fused (a warp per read)" if fused else
                              "seeding and lookup as two kernels (index over 2 GiB)")
                        + ", then NAM kernels on two streams"),

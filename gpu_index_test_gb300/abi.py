@@ -143,6 +143,14 @@ MATE_RESCUE = np.dtype([("ref_id", "<i4"), ("window_start", "<i4"), ("window_end
                         ("is_rc", "u1"), ("done", "u1"), ("is_unaligned", "u1"), ("_pad", "u1")])
 assert MATE_RESCUE.itemsize == 20
 
+# gbsa_align_step / gbsa_pair_plan: the alignment orchestration's step lists
+GBSA_STEP_EXTEND, GBSA_STEP_RESCUE = 0, 1
+ALIGN_STEP = np.dtype([("pair", "<u4"), ("read", "<u4"), ("nam_read", "<u4"), ("nam", "<u4"), ("kind", "u1"),
+                       ("is_read1", "u1"), ("_pad", "u1", (2,))])
+PAIR_PLAN = np.dtype([("type", "u1"), ("mapq1", "u1"), ("mapq2", "u1"), ("_pad", "u1"), ("type4_loop_size", "<i4"),
+                      ("first_step", "<u4"), ("n_steps", "<u4")])
+assert ALIGN_STEP.itemsize == 20 and PAIR_PLAN.itemsize == 16
+
 
 def align_params(match=2, mismatch=8, gap_open=12, gap_extend=1, end_bonus=10):
     return np.array([(match, mismatch, gap_open, gap_extend, end_bonus)], ALIGN_PARAMS)

@@ -6,11 +6,12 @@ Sweeps, over the C-ABI (gbsa_batcher_*):
                  window (longest read seeded in shared memory: 512 or 256 bases)
   lane_max_hits  the NAM merge's split between one lane per read and one warp per read
   sort_variant   the block size of the sort of rescued reads with many NAMs
-on slices of the repeat-rich mid-size configuration (150 bp pairs) and of the uneven
-length configuration (50-500 bp, single-end and pairs mixed), timing each shape's graph
+on slices of the repeat-rich mid-size configuration (150 bp pairs), of the uneven length
+configuration (50-500 bp, single-end and pairs mixed) and of the human-scale one (repeat
+families, 150 bp pairs), timing each shape's graph
 launches with CUDA events and checking its output byte for byte against the plain
 form's; then the host entry point's chunk size on end-to-end reads/s.  The fastest
-shape (sum of the two slices' times relative to the best on each) is written to
+shape (sum of the slices' times relative to the best on each) is written to
 tuned.json next to the library, which gbsa_batcher_create reads; the whole sweep is
 written as a table to the path given by --table.
 
@@ -45,6 +46,11 @@ def _workloads(scale):
     g = synth.make_genome(gp)
     rp = synth.read_params("C3", n_units=max(2000, int(200_000 * scale)), seed=204)
     out.append(("C3 slice: 5 Mbp genome, 50-500 bp reads, half pairs", g, synth.make_reads(g, rp),
+                synth.read_items(rp)))
+    gp = synth.genome_params("C4", scale=0.05 * scale, seed=207)
+    g = synth.make_genome(gp)
+    rp = synth.read_params("C4", n_units=max(2000, int(150_000 * scale)), seed=208)
+    out.append(("C4 slice: 155 Mbp genome with 45% repeat families, 150 bp pairs", g, synth.make_reads(g, rp),
                 synth.read_items(rp)))
     return out
 

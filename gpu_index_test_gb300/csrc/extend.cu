@@ -378,3 +378,122 @@ extern "C" int gbsa_rescue_mates_device(const uint8_t* d_ref_seqs, const uint64_
         return GBSA_ERR_CUDA;
     }
 }
+
+// ---- the steps of the alignment orchestration ------------------------------------------
+//
+// Runs the step lists of gbsa_plan_pairs_device: every step's NAM goes through the seed
+// extension kernel on its own read (an extension step keeps the record; a rescue step
+// keeps only reverse_nam_if_needed's answer — orientation, query interval, consistency —
+// since the reference runs only that check before rescue_mate_part), then the rescue
+// steps' NAMs, in the orientation that check left them, through the mate rescue kernel.
+
+namespace gbsa {
+namespace {
+
+__global__ void k_gather_step_nams(const gbsa_nam* __restrict__ nams, const uint64_t* __restrict__ offs,
+                                   const gbsa_align_step* __restrict__ steps, uint64_t n, gbsa_nam* __restrict__ out,
+                                   uint32_t* __restrict__ out_reads) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        const gbsa_align_step st = steps[s];
+        out[s] = nams[offs[st.nam_read] + st.nam];
+        out_reads[s] = st.nam_read;
+    }
+}
+
+__global__ void k_rescue_list(const gbsa_align_step* __restrict__ steps, uint64_t n, const gbsa_nam* __restrict__ step_nams,
+                              gbsa_seed_alignment* __restrict__ ext, gbsa_nam* __restrict__ rnams,
+                              uint32_t* __restrict__ rmates, uint64_t* __restrict__ ridx, unsigned long long* count,
+                              gbsa_mate_rescue* __restrict__ resc) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        gbsa_mate_rescue none;
+        none.ref_id = none.window_start = none.window_end = none.edit_distance = 0;
+        none.is_rc = none.done = none.is_unaligned = none._pad = 0;
+        resc[s] = none;
+        const gbsa_align_step st = steps[s];
+        if (st.kind != GBSA_STEP_RESCUE) continue;
+        gbsa_seed_alignment e = ext[s];
+        gbsa_nam nm = step_nams[s];
+        nm.is_rc = e.is_rc;
+        nm.query_start = e.query_start;
+        nm.query_end = e.query_end;
+        // the reference only checks the orientation before the rescue: no alignment record
+        e.ref_start = e.edit_distance = e.global_ed = e.score = e.length = 0;
+        e.done = 0;
+        ext[s] = e;
+        const unsigned long long j = atomicAdd(count, 1ull);
+        rnams[j] = nm;
+        rmates[j] = st.read;
+        ridx[j] = s;
+    }
+}
+
+__global__ void k_scatter_rescues(const gbsa_mate_rescue* __restrict__ in, const uint64_t* __restrict__ idx, uint64_t n,
+                                  gbsa_mate_rescue* __restrict__ out) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
+        out[idx[j]] = in[j];
+}
+
+}  // namespace
+}  // namespace gbsa
+
+extern "C" int gbsa_run_align_steps_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                                           const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                                           const uint64_t* d_read_offsets, const uint32_t* d_read_lengths,
+                                           uint32_t n_reads, const gbsa_nam* d_nams, const uint64_t* d_nam_offsets,
+                                           const gbsa_align_step* d_steps, uint64_t n_steps, int k,
+                                           const gbsa_align_params* params, float mu, float sigma,
+                                           gbsa_seed_alignment* d_ext, gbsa_mate_rescue* d_resc, void* stream) {
+    try {
+        if (n_steps == 0) return GBSA_OK;
+        cudaStream_t st = (cudaStream_t)stream;
+        // scratch in stream order: the steps' NAMs and reads, the rescue list (NAMs, mates,
+        // step indices), its count and the rescue records
+        const size_t b_nams = (sizeof(gbsa_nam) * n_steps + 255) & ~size_t(255);
+        const size_t b_u32 = (4ull * n_steps + 255) & ~size_t(255);
+        const size_t b_u64 = (8ull * n_steps + 255) & ~size_t(255);
+        const size_t b_res = (sizeof(gbsa_mate_rescue) * n_steps + 255) & ~size_t(255);
+        uint8_t* sc = nullptr;
+        GBSA_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sc), 2 * b_nams + 2 * b_u32 + b_u64 + b_res + 256, st));
+        struct Free {
+            uint8_t* p;
+            cudaStream_t s;
+            ~Free() { cudaFreeAsync(p, s); }
+        } release{sc, st};
+        gbsa_nam* step_nams = reinterpret_cast<gbsa_nam*>(sc);
+        uint32_t* step_reads = reinterpret_cast<uint32_t*>(sc + b_nams);
+        gbsa_nam* rnams = reinterpret_cast<gbsa_nam*>(sc + b_nams + b_u32);
+        uint32_t* rmates = reinterpret_cast<uint32_t*>(sc + 2 * b_nams + b_u32);
+        uint64_t* ridx = reinterpret_cast<uint64_t*>(sc + 2 * b_nams + 2 * b_u32);
+        gbsa_mate_rescue* rout = reinterpret_cast<gbsa_mate_rescue*>(sc + 2 * b_nams + 2 * b_u32 + b_u64);
+        unsigned long long* count = reinterpret_cast<unsigned long long*>(sc + 2 * b_nams + 2 * b_u32 + b_u64 + b_res);
+        GBSA_CUDA(cudaMemsetAsync(count, 0, 8, st));
+        const unsigned grid = grid_for(n_steps, 256, (unsigned)device_sm_count() * 8);
+        k_gather_step_nams<<<grid, 256, 0, st>>>(d_nams, d_nam_offsets, d_steps, n_steps, step_nams, step_reads);
+        GBSA_LAUNCHED();
+        int rc = gbsa_extend_seeds_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets,
+                                          d_read_lengths, n_reads, step_nams, step_reads, n_steps, k, params, d_ext,
+                                          stream);
+        if (rc != GBSA_OK) throw Error(rc, gbsa_last_error());
+        k_rescue_list<<<grid, 256, 0, st>>>(d_steps, n_steps, step_nams, d_ext, rnams, rmates, ridx, count, d_resc);
+        GBSA_LAUNCHED();
+        unsigned long long n_resc = 0;
+        GBSA_CUDA(cudaMemcpyAsync(&n_resc, count, 8, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        if (n_resc) {
+            rc = gbsa_rescue_mates_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets,
+                                          d_read_lengths, n_reads, rnams, rmates, n_resc, k, mu, sigma, rout, stream);
+            if (rc != GBSA_OK) throw Error(rc, gbsa_last_error());
+            k_scatter_rescues<<<grid_for(n_resc, 256, (unsigned)device_sm_count() * 8), 256, 0, st>>>(rout, ridx, n_resc,
+                                                                                                    d_resc);
+            GBSA_LAUNCHED();
+        }
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}

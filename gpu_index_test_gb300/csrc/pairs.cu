@@ -7,6 +7,7 @@
 // fused multiply-add, as nvcc contracts the reference's expression.
 #include <cmath>
 
+#include "prims.cuh"
 #include "runtime.h"
 
 namespace gbsa {
@@ -335,6 +336,224 @@ extern "C" int gbsa_classify_pairs_device(const gbsa_nam* d_nams, const uint64_t
         k_classify_pairs<<<grid_for(n_pairs, 256, (unsigned)device_sm_count() * 8), 256, 0, (cudaStream_t)stream>>>(
             d_nams, d_nam_offsets, n_pairs, layout, dropoff_threshold, limit, d_types);
         GBSA_LAUNCHED();
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}
+
+// ---- alignment orchestration (align_PE_part0..4, step2/main.cu:1857-2165) ---------------
+//
+// A thread per read pair lists, in the order the reference's align_PE_part<type> runs
+// them, the seed extensions (extend_seed_part after reverse_nam_if_needed) and mate
+// rescues (rescue_mate_part of a NAM after reverse_nam_if_needed) of the pair, and
+// computes the pair's mapq for type 3 (get_mapq, main.cu:900-910).  Two passes: the
+// first counts each pair's steps, an exclusive scan places them, the second writes them.
+
+namespace gbsa {
+namespace {
+
+__device__ __forceinline__ void plan_push(gbsa_align_step* out, uint32_t& k, bool write, uint32_t pair, uint8_t kind,
+                                          bool is_read1, uint64_t read, uint64_t nam_read, uint32_t nam) {
+    if (write) {
+        gbsa_align_step s;
+        s.pair = pair;
+        s.read = (uint32_t)read;
+        s.nam_read = (uint32_t)nam_read;
+        s.nam = nam;
+        s.kind = kind;
+        s.is_read1 = is_read1 ? 1 : 0;
+        s._pad[0] = s._pad[1] = 0;
+        out[k] = s;
+    }
+    ++k;
+}
+
+// get_mapq (main.cu:900-910): the reference's float expression — min_matches is a float
+// rounded from the double n_hits / 10.0 (capped at 1), the log is logf of the float
+// score, the products are float in the reference's order — truncated to int, capped at
+// 60 and returned as uint8 (a negative value wraps, as the reference's return type makes
+// it).
+__device__ __forceinline__ uint8_t pair_mapq(const gbsa_nam* nams, uint64_t n) {
+    if (n <= 1) return 60;
+    const float s1 = nams[0].score, s2 = nams[1].score;
+    const double mm = nams[0].n_hits / 10.0;
+    const float min_matches = (float)(mm < 1.0 ? mm : 1.0);
+    const float f = __fmul_rn(__fmul_rn(__fmul_rn(40.0f, __fsub_rn(1.0f, __fdiv_rn(s2, s1))), min_matches), logf(s1));
+    const int uncapped = (int)f;
+    return (uint8_t)(uncapped < 60 ? uncapped : 60);
+}
+
+// rescue_read_part (main.cu:795-835): the NAMs of the mapped end in order while fewer than
+// max_tries were tried and n_hits / the first NAM's n_hits >= dropoff; each is extended on
+// its read, then its mate is rescued from it.
+__device__ void plan_rescue_read(gbsa_align_step* out, uint32_t& k, bool write, uint32_t p, const gbsa_nam* nams,
+                                 uint64_t n, uint64_t mapped, uint64_t mate, bool mapped_is_read1, uint32_t max_tries,
+                                 float dropoff) {
+    const int top = nams[0].n_hits;
+    uint32_t tries = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float d = (float)nams[i].n_hits / (float)top;
+        if (tries >= max_tries || d < dropoff) break;
+        plan_push(out, k, write, p, GBSA_STEP_EXTEND, mapped_is_read1, mapped, mapped, (uint32_t)i);
+        plan_push(out, k, write, p, GBSA_STEP_RESCUE, !mapped_is_read1, mate, mapped, (uint32_t)i);
+        ++tries;
+    }
+}
+
+template <bool kWrite>
+__global__ void k_plan_pairs(const gbsa_nam* __restrict__ nams, const uint64_t* __restrict__ offs, uint32_t n_pairs,
+                             int layout, const uint8_t* __restrict__ types, const gbsa_nam_pair* __restrict__ jp,
+                             const uint32_t* __restrict__ jcounts, uint32_t max_tries, float dropoff,
+                             uint64_t* __restrict__ counts, gbsa_pair_plan* __restrict__ plans,
+                             gbsa_align_step* __restrict__ steps, uint64_t step_cap, uint8_t* scratch,
+                             unsigned int* bad) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_pairs; p += gridDim.x * blockDim.x) {
+        const uint64_t e1 = layout == GBSA_PAIRS_HALVES ? p : 2ull * p;
+        const uint64_t e2 = layout == GBSA_PAIRS_HALVES ? (uint64_t)p + n_pairs : 2ull * p + 1;
+        const uint64_t o1 = offs[e1], c1 = offs[e1 + 1] - o1;
+        const uint64_t o2 = offs[e2], c2 = offs[e2 + 1] - o2;
+        const gbsa_nam* n1 = nams + o1;
+        const gbsa_nam* n2 = nams + o2;
+        const uint8_t type = types[p];
+        uint64_t first = 0;
+        gbsa_align_step* out = steps;
+        bool write = false;
+        if (kWrite) {
+            first = counts[p];
+            write = first + (counts[p + 1] - first) <= step_cap;
+            out = steps + first;
+        }
+        uint32_t k = 0;
+        gbsa_pair_plan plan;
+        plan.type = type;
+        plan.mapq1 = plan.mapq2 = 0;
+        plan._pad = 0;
+        plan.type4_loop_size = 0;
+        if (type == 1 && c1 > 0) {
+            plan_rescue_read(out, k, write, p, n1, c1, e1, e2, true, max_tries, dropoff);
+        } else if (type == 2 && c2 > 0) {
+            plan_rescue_read(out, k, write, p, n2, c2, e2, e1, false, max_tries, dropoff);
+        } else if (type == 3 && c1 > 0 && c2 > 0) {
+            plan_push(out, k, write, p, GBSA_STEP_EXTEND, true, e1, e1, 0);
+            plan_push(out, k, write, p, GBSA_STEP_EXTEND, false, e2, e2, 0);
+            plan.mapq1 = pair_mapq(n1, c1);
+            plan.mapq2 = pair_mapq(n2, c2);
+        } else if (type == 4 && c1 > 0 && c2 > 0) {
+            // per-NAM "aligned" flags in scratch indexed by the NAM's position in the batch
+            uint8_t* al1 = scratch + o1;
+            uint8_t* al2 = scratch + o2;
+            for (uint64_t i = 0; i < c1; ++i) al1[i] = 0;
+            for (uint64_t i = 0; i < c2; ++i) al2[i] = 0;
+            // the best-scoring NAM of each end first (the first of equal maxima)
+            uint32_t b1 = 0, b2 = 0;
+            for (uint32_t i = 0; i < c1; ++i)
+                if (n1[i].score > n1[b1].score) b1 = i;
+            for (uint32_t i = 0; i < c2; ++i)
+                if (n2[i].score > n2[b2].score) b2 = i;
+            plan_push(out, k, write, p, GBSA_STEP_EXTEND, true, e1, e1, b1);
+            al1[b1] = 1;
+            plan_push(out, k, write, p, GBSA_STEP_EXTEND, false, e2, e2, b2);
+            al2[b2] = 1;
+            const uint32_t nj = jcounts[p];
+            const gbsa_nam_pair* J = jp + (uint64_t)p * max_tries;
+            const double max_score = nj ? (double)J[0].score : 0.0;
+            uint32_t high = 0;
+            int loop = 0;
+            for (uint32_t i = 0; i < nj; ++i) {
+                const float d = (float)((double)J[i].score / max_score);
+                if (high >= max_tries || d < dropoff) break;
+                ++loop;
+                const int i1 = J[i].i1, i2 = J[i].i2;
+                if (i1 >= 0 && (uint64_t)i1 < c1) {
+                    if (!al1[i1]) {
+                        plan_push(out, k, write, p, GBSA_STEP_EXTEND, true, e1, e1, (uint32_t)i1);
+                        al1[i1] = 1;
+                    }
+                } else if (i2 >= 0 && (uint64_t)i2 < c2) {
+                    plan_push(out, k, write, p, GBSA_STEP_RESCUE, true, e1, e2, (uint32_t)i2);
+                } else if (bad) {
+                    atomicAdd(bad, 1u);   // a pair entry with neither NAM: not produced by the pair scoring
+                }
+                if (i2 >= 0 && (uint64_t)i2 < c2) {
+                    if (!al2[i2]) {
+                        plan_push(out, k, write, p, GBSA_STEP_EXTEND, false, e2, e2, (uint32_t)i2);
+                        al2[i2] = 1;
+                    }
+                } else if (i1 >= 0 && (uint64_t)i1 < c1) {
+                    plan_push(out, k, write, p, GBSA_STEP_RESCUE, false, e2, e1, (uint32_t)i1);
+                }
+                ++high;
+            }
+            plan.type4_loop_size = loop;
+        }
+        if (!kWrite) {
+            counts[p] = k;
+        } else {
+            plan.first_step = (uint32_t)first;
+            plan.n_steps = k;
+            plans[p] = plan;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace gbsa
+
+using namespace gbsa;
+
+extern "C" int gbsa_plan_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs,
+                                      int layout, const uint8_t* d_types, const gbsa_nam_pair* d_pairs,
+                                      const uint32_t* d_pair_counts, uint32_t max_tries, float dropoff,
+                                      gbsa_pair_plan* d_plans, gbsa_align_step* d_steps, uint64_t step_capacity,
+                                      uint64_t* n_steps, void* stream) {
+    try {
+        if (layout != GBSA_PAIRS_INTERLEAVED && layout != GBSA_PAIRS_HALVES)
+            throw Error(GBSA_ERR_PARAM, "layout must be GBSA_PAIRS_INTERLEAVED or GBSA_PAIRS_HALVES");
+        if (max_tries == 0) throw Error(GBSA_ERR_PARAM, "max_tries must be at least 1");
+        if (n_steps) *n_steps = 0;
+        if (n_pairs == 0) return GBSA_OK;
+        cudaStream_t st = (cudaStream_t)stream;
+        uint64_t total_nams = 0;
+        GBSA_CUDA(cudaMemcpyAsync(&total_nams, d_nam_offsets + 2ull * n_pairs, 8, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));
+        // scratch in stream order: step counts (then offsets) per pair, an "aligned" flag
+        // per NAM, the status word, the scan's partials
+        const size_t b_cnt = (8ull * (n_pairs + 1) + 255) & ~size_t(255);
+        const size_t b_flags = (total_nams + 1 + 255) & ~size_t(255);
+        uint8_t* scratch = nullptr;
+        GBSA_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), b_cnt + b_flags + 256, st));
+        uint64_t* counts = reinterpret_cast<uint64_t*>(scratch);
+        uint8_t* flags = scratch + b_cnt;
+        unsigned int* bad = reinterpret_cast<unsigned int*>(scratch + b_cnt + b_flags);
+        struct Free {
+            uint8_t* p;
+            cudaStream_t s;
+            ~Free() { cudaFreeAsync(p, s); }
+        } release{scratch, st};
+        GBSA_CUDA(cudaMemsetAsync(bad, 0, 4, st));
+        const unsigned grid = grid_for(n_pairs, 128, (unsigned)device_sm_count() * 16);
+        k_plan_pairs<false><<<grid, 128, 0, st>>>(d_nams, d_nam_offsets, n_pairs, layout, d_types, d_pairs, d_pair_counts,
+                                                   max_tries, dropoff, counts, nullptr, nullptr, 0, flags, nullptr);
+        GBSA_LAUNCHED();
+        Workspace ws;
+        scan_exclusive_u64(counts, counts, n_pairs, counts + n_pairs, ws, st);
+        k_plan_pairs<true><<<grid, 128, 0, st>>>(d_nams, d_nam_offsets, n_pairs, layout, d_types, d_pairs, d_pair_counts,
+                                                  max_tries, dropoff, counts, d_plans, d_steps, step_capacity, flags,
+                                                  bad);
+        GBSA_LAUNCHED();
+        uint64_t total = 0;
+        unsigned int h_bad = 0;
+        GBSA_CUDA(cudaMemcpyAsync(&total, counts + n_pairs, 8, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, st));
+        GBSA_CUDA(cudaStreamSynchronize(st));   // the scan's workspace is freed on return
+        if (n_steps) *n_steps = total;
+        if (h_bad) throw Error(GBSA_ERR_PARAM, "a NAM pair with neither NAM");
+        if (total > step_capacity) throw Error(GBSA_ERR_CAPACITY, "step capacity too small");
         return GBSA_OK;
     } catch (const Error& e) {
         set_last_error(e.what());

@@ -93,6 +93,10 @@ def lib():
             "gbsa_mapper_set_fuse_limit": (i32, [vp, u64]),
             "gbsa_mapper_set_l2_window": (i32, [vp, i32, C.POINTER(u64)]),
             "gbsa_batch_config_default": (i32, [C.POINTER(abi.BatchConfig), C.POINTER(i32)]),
+            "gbsa_plan_pairs_device": (i32, [vp, vp, u32, i32, vp, vp, vp, u32, C.c_float, vp, vp, u64,
+                                             C.POINTER(u64), vp]),
+            "gbsa_run_align_steps_device": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, vp, u64, i32, vp,
+                                                  C.c_float, C.c_float, vp, vp, vp]),
             "gbsa_batcher_create": (i32, [vp, C.POINTER(abi.MapOptions), C.POINTER(abi.BatchConfig), u32, u64,
                                           C.POINTER(vp)]),
             "gbsa_batcher_free": (None, [vp]),
@@ -190,6 +194,28 @@ def rescue_mates_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read
     _check(lib().gbsa_rescue_mates_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs,
                                           d_read_offsets, d_read_lengths, n_reads, d_nams, d_mate_reads, n_nams, k,
                                           mu, sigma, d_out, stream))
+
+
+def plan_pairs_device(d_nams, d_nam_offsets, n_pairs, d_types, d_pairs, d_pair_counts, d_plans, d_steps, step_cap,
+                      layout=0, max_tries=20, dropoff=0.5, stream=None):
+    """The alignment orchestration (align_PE_part0..4) as step lists: plans into d_plans,
+    steps into d_steps; returns the step count (raises GbsaError GBSA_ERR_CAPACITY when
+    above step_cap).  Device addresses."""
+    n = C.c_uint64()
+    _check(lib().gbsa_plan_pairs_device(d_nams, d_nam_offsets, n_pairs, layout, d_types, d_pairs, d_pair_counts,
+                                        max_tries, dropoff, d_plans, d_steps, step_cap, C.byref(n), stream))
+    return n.value
+
+
+def run_align_steps_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs, d_read_offsets,
+                           d_read_lengths, n_reads, d_nams, d_nam_offsets, d_steps, n_steps, k, d_ext, d_resc,
+                           params=None, mu=300.0, sigma=100.0, stream=None):
+    """Runs a plan's steps: seed extensions into d_ext, mate rescues into d_resc (one
+    record of each per step).  Device addresses."""
+    p = abi.align_params() if params is None else np.ascontiguousarray(params, abi.ALIGN_PARAMS)
+    _check(lib().gbsa_run_align_steps_device(d_ref_seqs, d_ref_offsets, d_ref_lengths, n_refs, d_read_seqs,
+                                             d_read_offsets, d_read_lengths, n_reads, d_nams, d_nam_offsets, d_steps,
+                                             n_steps, k, p.ctypes.data, mu, sigma, d_ext, d_resc, stream))
 
 
 def _u8(a):

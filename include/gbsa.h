@@ -403,6 +403,55 @@ int gbsa_nam_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets,
                           float mu, float sigma, uint32_t max_tries, gbsa_nam_pair* d_pairs, uint32_t* d_counts,
                           void* stream);
 
+/* One step of a read pair's alignment, in the order align_PE_part1..4 run them
+ * (step2/main.cu:1876-2165): kind GBSA_STEP_EXTEND is extend_seed_part of NAM `nam` of
+ * read end `nam_read` (after reverse_nam_if_needed) on that read; GBSA_STEP_RESCUE is
+ * rescue_mate_part of that NAM (after reverse_nam_if_needed on its own read) for the mate
+ * `read`.  is_read1 is the reference's is_read1 tag of the record the step writes. */
+#define GBSA_STEP_EXTEND 0
+#define GBSA_STEP_RESCUE 1
+typedef struct gbsa_align_step {
+    uint32_t pair;
+    uint32_t read;       /* the read extended (== nam_read), or the mate rescued */
+    uint32_t nam_read;   /* the read end whose NAM list holds the NAM */
+    uint32_t nam;        /* index of the NAM in that list */
+    uint8_t  kind;
+    uint8_t  is_read1;
+    uint8_t  _pad[2];
+} gbsa_align_step;
+
+/* A pair's plan: its type (as gbsa_classify_pairs_device), get_mapq of both ends for
+ * type 3 (step2/main.cu:900-910; 0 otherwise), the number of joint NAM pairs the type-4
+ * loop visited (type4_loop_size), and its steps [first_step, first_step + n_steps). */
+typedef struct gbsa_pair_plan {
+    uint8_t  type;
+    uint8_t  mapq1;
+    uint8_t  mapq2;
+    uint8_t  _pad;
+    int32_t  type4_loop_size;
+    uint32_t first_step;
+    uint32_t n_steps;
+} gbsa_pair_plan;
+
+/* The alignment orchestration of align_PE_part0..4 (step2/main.cu:1857-2165) as step
+ * lists: type 0 nothing; type 1 (2) rescue_read_part: mate 1's (2's) NAMs in order while
+ * fewer than max_tries were tried and n_hits / the first NAM's n_hits >= dropoff, each
+ * extended, then its mate rescued from it; type 3 both first NAMs extended and their
+ * mapq; type 4 the best-scoring NAM of each end extended (the first of equal maxima),
+ * then the joint NAM pairs d_pairs / d_pair_counts of gbsa_nam_pairs_device (max_tries
+ * records per pair) in order while fewer than max_tries were visited and score / the
+ * first pair's score >= dropoff: a present NAM not yet extended is extended, an absent one
+ * makes a rescue of that read from the other end's NAM.  d_types from
+ * gbsa_classify_pairs_device.  d_plans receives n_pairs records, d_steps the steps (pair
+ * after pair); *n_steps the step count (GBSA_ERR_CAPACITY when above step_capacity, with
+ * nothing but the count valid).  Device pointers; the call synchronizes stream.  The
+ * reference's insert-size estimate update of type 3 (main.cu:2002-2022) depends on the
+ * order in which its threads run, so it is not reproduced: mu and sigma stay fixed. */
+int gbsa_plan_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs, int layout,
+                           const uint8_t* d_types, const gbsa_nam_pair* d_pairs, const uint32_t* d_pair_counts,
+                           uint32_t max_tries, float dropoff, gbsa_pair_plan* d_plans, gbsa_align_step* d_steps,
+                           uint64_t step_capacity, uint64_t* n_steps, void* stream);
+
 /* AlignmentParameters (step2/aligner.hpp:11-18): match is a score, the others are
  * penalties (all nonnegative). */
 typedef struct gbsa_align_params {
@@ -481,6 +530,21 @@ int gbsa_rescue_mates_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_of
                              const uint64_t* d_read_offsets, const uint32_t* d_read_lengths, uint32_t n_reads,
                              const gbsa_nam* d_nams, const uint32_t* d_mate_reads, uint64_t n_nams, int k,
                              float mu, float sigma, gbsa_mate_rescue* d_out, void* stream);
+
+/* Runs the steps of gbsa_plan_pairs_device: d_ext[s] is the seed extension
+ * (gbsa_extend_seeds_device) of step s's NAM on its own read for an extension step; for
+ * a rescue step it holds only reverse_nam_if_needed's answer (ref_id, is_rc, query
+ * interval, consistent; the alignment fields zero and done 0), and d_resc[s] the mate
+ * rescue (gbsa_rescue_mates_device) of that NAM, in the orientation the check left it,
+ * for the mate step.read (all zero for an extension step).  d_nams / d_nam_offsets are the
+ * NAM lists the plan indexes; the other arguments as gbsa_extend_seeds_device and
+ * gbsa_rescue_mates_device.  Device pointers; the call synchronizes stream. */
+int gbsa_run_align_steps_device(const uint8_t* d_ref_seqs, const uint64_t* d_ref_offsets,
+                                const uint64_t* d_ref_lengths, uint32_t n_refs, const uint8_t* d_read_seqs,
+                                const uint64_t* d_read_offsets, const uint32_t* d_read_lengths, uint32_t n_reads,
+                                const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, const gbsa_align_step* d_steps,
+                                uint64_t n_steps, int k, const gbsa_align_params* params, float mu, float sigma,
+                                gbsa_seed_alignment* d_ext, gbsa_mate_rescue* d_resc, void* stream);
 
 /* ---- instrumentation ---------------------------------------------------------- */
 /* Count the algorithmic bytes of the lookup stage (roofline numerator) in later

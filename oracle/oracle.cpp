@@ -1193,6 +1193,119 @@ int oracle_nam_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_p
     return 0;
 }
 
+/* get_mapq (main.cu:900-910) in the reference's float arithmetic: min_matches a float
+ * rounded from n_hits / 10.0 (a double) capped at 1, the log a float log of the float
+ * score, the products float in the reference's order, truncated to int, capped at 60,
+ * returned as uint8 (negative values wrap). */
+static uint8_t pair_mapq(const gbsa_nam* nams, uint64_t n) {
+    if (n <= 1) return 60;
+    const float s1 = nams[0].score, s2 = nams[1].score;
+    const double mm = nams[0].n_hits / 10.0;
+    const float min_matches = (float)(mm < 1.0 ? mm : 1.0);
+    volatile float f = 40.0f * (1.0f - s2 / s1);   /* volatile: no contraction or reassociation */
+    f = f * min_matches;
+    f = f * std::log(s1);
+    const int uncapped = (int)f;
+    return (uint8_t)(uncapped < 60 ? uncapped : 60);
+}
+
+/* The alignment orchestration of align_PE_part0..4 (main.cu:1857-2165) as step lists
+ * (gbsa_plan_pairs_device's plans and steps).  Returns the step count (steps beyond
+ * step_cap are counted, not written). */
+int64_t oracle_plan_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout,
+                          const uint8_t* types, const gbsa_nam_pair* jp, const uint32_t* jcounts, uint32_t max_tries,
+                          float dropoff, gbsa_pair_plan* plans, gbsa_align_step* steps, uint64_t step_cap) {
+    uint64_t total = 0;
+    for (uint32_t p = 0; p < n_pairs; ++p) {
+        const uint64_t e1 = layout == GBSA_PAIRS_HALVES ? p : 2ull * p;
+        const uint64_t e2 = layout == GBSA_PAIRS_HALVES ? (uint64_t)p + n_pairs : 2ull * p + 1;
+        const uint64_t c1 = offsets[e1 + 1] - offsets[e1], c2 = offsets[e2 + 1] - offsets[e2];
+        const gbsa_nam* n1 = nams + offsets[e1];
+        const gbsa_nam* n2 = nams + offsets[e2];
+        gbsa_pair_plan plan{};
+        plan.type = types[p];
+        plan.first_step = (uint32_t)total;
+        uint64_t k = 0;
+        auto push = [&](uint8_t kind, bool is_read1, uint64_t read, uint64_t nam_read, uint32_t nam) {
+            if (total + k < step_cap) {
+                gbsa_align_step s{};
+                s.pair = p;
+                s.read = (uint32_t)read;
+                s.nam_read = (uint32_t)nam_read;
+                s.nam = nam;
+                s.kind = kind;
+                s.is_read1 = is_read1 ? 1 : 0;
+                steps[total + k] = s;
+            }
+            ++k;
+        };
+        /* rescue_read_part (main.cu:795-835) */
+        auto rescue_read = [&](const gbsa_nam* ns, uint64_t c, uint64_t mapped, uint64_t mate, bool mapped_is_read1) {
+            const int top = ns[0].n_hits;
+            uint32_t tries = 0;
+            for (uint64_t i = 0; i < c; ++i) {
+                const float d = (float)ns[i].n_hits / (float)top;
+                if (tries >= max_tries || d < dropoff) break;
+                push(GBSA_STEP_EXTEND, mapped_is_read1, mapped, mapped, (uint32_t)i);
+                push(GBSA_STEP_RESCUE, !mapped_is_read1, mate, mapped, (uint32_t)i);
+                ++tries;
+            }
+        };
+        if (plan.type == 1 && c1 > 0) {
+            rescue_read(n1, c1, e1, e2, true);
+        } else if (plan.type == 2 && c2 > 0) {
+            rescue_read(n2, c2, e2, e1, false);
+        } else if (plan.type == 3 && c1 > 0 && c2 > 0) {   /* align_PE_part3 */
+            push(GBSA_STEP_EXTEND, true, e1, e1, 0);
+            push(GBSA_STEP_EXTEND, false, e2, e2, 0);
+            plan.mapq1 = pair_mapq(n1, c1);
+            plan.mapq2 = pair_mapq(n2, c2);
+        } else if (plan.type == 4 && c1 > 0 && c2 > 0) {   /* align_PE_part4 */
+            std::vector<uint8_t> al1(c1, 0), al2(c2, 0);
+            uint32_t b1 = 0, b2 = 0;
+            for (uint32_t i = 0; i < c1; ++i)
+                if (n1[i].score > n1[b1].score) b1 = i;
+            for (uint32_t i = 0; i < c2; ++i)
+                if (n2[i].score > n2[b2].score) b2 = i;
+            push(GBSA_STEP_EXTEND, true, e1, e1, b1);
+            al1[b1] = 1;
+            push(GBSA_STEP_EXTEND, false, e2, e2, b2);
+            al2[b2] = 1;
+            const uint32_t nj = jcounts[p];
+            const gbsa_nam_pair* J = jp + (uint64_t)p * max_tries;
+            const double max_score = nj ? (double)J[0].score : 0.0;
+            uint32_t high = 0;
+            for (uint32_t i = 0; i < nj; ++i) {
+                const float d = (float)((float)J[i].score / max_score);
+                if (high >= max_tries || d < dropoff) break;
+                ++plan.type4_loop_size;
+                const int i1 = J[i].i1, i2 = J[i].i2;
+                if (i1 >= 0) {
+                    if (!al1[i1]) {
+                        push(GBSA_STEP_EXTEND, true, e1, e1, (uint32_t)i1);
+                        al1[i1] = 1;
+                    }
+                } else {
+                    push(GBSA_STEP_RESCUE, true, e1, e2, (uint32_t)i2);
+                }
+                if (i2 >= 0) {
+                    if (!al2[i2]) {
+                        push(GBSA_STEP_EXTEND, false, e2, e2, (uint32_t)i2);
+                        al2[i2] = 1;
+                    }
+                } else {
+                    push(GBSA_STEP_RESCUE, false, e2, e1, (uint32_t)i1);
+                }
+                ++high;
+            }
+        }
+        plan.n_steps = (uint32_t)k;
+        plans[p] = plan;
+        total += k;
+    }
+    return (int64_t)total;
+}
+
 int oracle_map_reads(const oracle_index* h, const gbsa_map_options* opt, const char* seqs, const uint64_t* offsets,
                      const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity,
                      uint64_t* nam_offsets, float* frac, uint8_t* rescued, int n_threads) {

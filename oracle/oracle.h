@@ -90,6 +90,9 @@ int oracle_rescue_mates(const char* ref_seqs, const uint64_t* ref_offsets, const
 
 /* Whole path for a batch of reads with n_threads host threads (0 = all cores).
  * Same contract as gbsa_map_reads.  Returns GBSA_OK or GBSA_ERR_CAPACITY. */
+int64_t oracle_plan_pairs(const gbsa_nam* nams, const uint64_t* offsets, uint32_t n_pairs, int layout,
+                          const uint8_t* types, const gbsa_nam_pair* jp, const uint32_t* jcounts, uint32_t max_tries,
+                          float dropoff, gbsa_pair_plan* plans, gbsa_align_step* steps, uint64_t step_cap);
 int oracle_map_reads(const oracle_index* idx, const gbsa_map_options* opt, const char* seqs,
                      const uint64_t* offsets, const uint32_t* lengths, uint32_t n_reads,
                      gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets,

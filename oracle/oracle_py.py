@@ -72,6 +72,8 @@ def lib():
         L.oracle_map_reads.restype = C.c_int
         L.oracle_map_reads.argtypes = [C.c_void_p, C.POINTER(abi.MapOptions), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_plan_pairs.restype = C.c_int64
+        L.oracle_plan_pairs.argtypes = [vp, vp, u32, C.c_int, vp, vp, vp, u32, C.c_float, vp, vp, u64]
         L.oracle_index_verify.restype = C.c_int
         L.oracle_index_verify.argtypes = [P, vp, vp, vp, u32, C.c_float, vp, u64, vp, C.c_int, u32, C.c_int, vp]
         L.oracle_algorithmic_bytes.restype = C.c_int
@@ -259,6 +261,47 @@ def nam_pairs(nams, offsets, n_pairs, layout=abi.GBSA_PAIRS_INTERLEAVED, mu=300.
     assert lib().oracle_nam_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, mu, sigma,
                                   max_tries, out.ctypes.data, cnt.ctypes.data) == 0
     return out[:n_pairs], cnt[:n_pairs]
+
+
+def plan_pairs(nams, offsets, n_pairs, types, pairs, pair_counts, layout=abi.GBSA_PAIRS_INTERLEAVED, max_tries=20,
+               dropoff=0.5):
+    """align_PE_part0..4's orchestration restated as step lists: (plans, steps)."""
+    a = np.ascontiguousarray(nams)
+    o = np.ascontiguousarray(offsets, np.uint64)
+    t = np.ascontiguousarray(types, np.uint8)
+    jp = np.ascontiguousarray(pairs, abi.NAM_PAIR)
+    jc = np.ascontiguousarray(pair_counts, np.uint32)
+    plans = np.zeros(max(1, n_pairs), abi.PAIR_PLAN)
+    cap = max(1, n_pairs * (2 + 2 * max_tries))
+    steps = np.zeros(cap, abi.ALIGN_STEP)
+    n = lib().oracle_plan_pairs(a.ctypes.data if len(a) else None, o.ctypes.data, n_pairs, layout, t.ctypes.data,
+                                jp.ctypes.data, jc.ctypes.data, max_tries, dropoff, plans.ctypes.data,
+                                steps.ctypes.data, cap)
+    assert 0 <= n <= cap
+    return plans[:n_pairs], steps[:n]
+
+
+def run_align_steps(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, nams, offsets, steps,
+                    k, mu=300.0, sigma=100.0):
+    """A plan's steps through the restated seed extension and mate rescue, as
+    gbsa_run_align_steps_device returns them: (extension records, rescue records)."""
+    offsets = np.asarray(offsets, np.uint64)
+    idx = (offsets[steps["nam_read"].astype(np.int64)] + steps["nam"].astype(np.uint64)).astype(np.int64)
+    step_nams = np.ascontiguousarray(np.asarray(nams)[idx]) if len(steps) else np.zeros(0, abi.NAM)
+    ext = extend_seeds(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, step_nams,
+                       steps["nam_read"], k)
+    resc = np.zeros(len(steps), abi.MATE_RESCUE)
+    r = np.nonzero(steps["kind"] == abi.GBSA_STEP_RESCUE)[0]
+    if len(r):
+        rn = step_nams[r].copy()
+        rn["is_rc"] = ext["is_rc"][r]
+        rn["query_start"] = ext["query_start"][r]
+        rn["query_end"] = ext["query_end"][r]
+        resc[r] = rescue_mates(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, rn,
+                               steps["read"][r], k, mu, sigma)
+        for f in ("ref_start", "edit_distance", "global_ed", "score", "length", "done"):
+            ext[f][r] = 0
+    return ext, resc
 
 
 def extend_seeds(ref_seqs, ref_offsets, ref_lengths, read_seqs, read_offsets, read_lengths, nams, nam_reads, k,
