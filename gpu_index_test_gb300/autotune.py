@@ -6,7 +6,10 @@ Sweeps, over the C-ABI (gbsa_batcher_*):
                  window (longest read seeded in shared memory: 512 or 256 bases)
   lane_max_hits  the NAM merge's split between one lane per read and one warp per read
   sort_variant   the block size of the sort of rescued reads with many NAMs
-on slices of the repeat-rich mid-size configuration (150 bp pairs), of the uneven length
+  lane_variant   the register budget of the lane-per-read NAM merge (96, 80 or 64)
+  warp_variant   the register budget of the warp-per-read NAM merge (96, 80 or 64)
+(the first three as a grid, then the two register budgets as a grid at the best of
+the first) on slices of the repeat-rich mid-size configuration (150 bp pairs), of the uneven length
 configuration (50-500 bp, single-end and pairs mixed) and of the human-scale one (repeat
 families, 150 bp pairs), timing each shape's graph
 launches with CUDA events and checking its output byte for byte against the plain
@@ -32,6 +35,7 @@ from ._build_paths import GBSA_SO
 
 LANE_MAX_HITS = (64, 96, 128, 160)
 SORT_VARIANTS = (0, 1)
+REG_VARIANTS = (0, 1, 2)
 CHUNKS = (1 << 17, 1 << 18, 1 << 19, 1 << 20)
 
 
@@ -94,10 +98,23 @@ def _same(a, b):
 
 
 def sweep(scale=1.0, reps=5, log=print):
+    """Shapes are (seed_variant, lane_max_hits, sort_variant, lane_variant, warp_variant)."""
+    grid = [(v, l, s, 0, 0) for v in range(abi.SEED_VARIANTS) for l in LANE_MAX_HITS for s in SORT_VARIANTS]
+    pick, rows, exact, score, plain_ms = _sweep(grid, scale, reps, log)
+    regs = [pick[:3] + (lv, wv) for lv in REG_VARIANTS for wv in REG_VARIANTS]
+    pick2, rows2, exact2, _, _ = _sweep(regs, scale, reps, log)
+    rows.update(rows2)
+    exact.update(exact2)
+    names = list(plain_ms)
+    best = {nm: min(rows[sh][nm] for sh in rows if exact[sh]) for nm in names}
+    score = {sh: sum(rows[sh][nm] / best[nm] for nm in names) for sh in rows if exact[sh]}
+    return min(score, key=score.get), rows, exact, score, plain_ms
+
+
+def _sweep(shapes, scale, reps, log):
     import torch
 
     p = native.params_from_read_length(150)
-    shapes = [(v, l, s) for v in range(abi.SEED_VARIANTS) for l in LANE_MAX_HITS for s in SORT_VARIANTS]
     rows = {sh: {} for sh in shapes}
     exact = {sh: True for sh in shapes}
     plain_ms = {}
@@ -113,7 +130,7 @@ def sweep(scale=1.0, reps=5, log=print):
         plain_ms[name], ref = _device_run(torch, idx, reads, items, plain, reps)
         m.free()
         for sh in shapes:
-            cfg = abi.batch_config(sh[0], sh[1], sh[2], 1 << 19)
+            cfg = abi.batch_config(sh[0], sh[1], sh[2], 1 << 19, sh[3], sh[4])
             b = native.Batcher(idx, config=cfg, max_reads=reads.n, max_bases=int(reads.lengths.sum()))
 
             def batched(d, n, cap, st, b=b):
@@ -126,7 +143,7 @@ def sweep(scale=1.0, reps=5, log=print):
             b.free()
             rows[sh][name] = ms
             exact[sh] &= _same(out, ref)
-            log(f"{name[:8]} variant={sh[0]} lane_max_hits={sh[1]} sort={sh[2]}: {ms:.3f} ms "
+            log(f"{name[:8]} variant={sh[0]} lane_max_hits={sh[1]} sort={sh[2]} regs={sh[3]},{sh[4]}: {ms:.3f} ms "
                 f"(plain {plain_ms[name]:.3f}) exact={exact[sh]}")
         idx.free()
     names = list(plain_ms)
@@ -155,7 +172,8 @@ def tune_chunks(pick, scale=1.0, log=print):
     L = native.lib()
     res = {}
     for ch in CHUNKS:
-        b = native.Batcher(idx, config=abi.batch_config(pick[0], pick[1], pick[2], ch), max_reads=min(n, 2 * ch),
+        b = native.Batcher(idx, config=abi.batch_config(pick[0], pick[1], pick[2], ch, pick[3], pick[4]),
+                           max_reads=min(n, 2 * ch),
                            max_bases=int(reads.lengths.sum()))
 
         def run():
@@ -188,7 +206,8 @@ def main():
     pick, rows, exact, score, plain_ms = sweep(args.scale)
     chunk, chunk_rates = tune_chunks(pick, args.scale)
     cfg = {"seed_variant": pick[0], "lane_max_hits": pick[1], "sort_variant": pick[2], "chunk_reads": chunk,
-           "device": torch.cuda.get_device_name(0), "tuned_s": round(time.time() - t0, 1)}
+           "lane_variant": pick[3], "warp_variant": pick[4], "device": torch.cuda.get_device_name(0),
+           "tuned_s": round(time.time() - t0, 1)}
     with open(args.out, "w") as f:
         json.dump(cfg, f, indent=1)
         f.write("\n")
@@ -196,12 +215,13 @@ def main():
     if args.table:
         names = list(plain_ms)
         with open(args.table, "w") as f:
-            f.write("| seed_variant | lane_max_hits | sort_variant | " + " | ".join(f"{n} ms" for n in names)
-                    + " | score | bit-exact |\n")
-            f.write("|---" * (5 + len(names)) + "|\n")
-            f.write("| plain form | | | " + " | ".join(f"{plain_ms[n]:.3f}" for n in names) + " | | |\n")
+            f.write("| seed_variant | lane_max_hits | sort_variant | lane_variant | warp_variant | "
+                    + " | ".join(f"{n} ms" for n in names) + " | score | bit-exact |\n")
+            f.write("|---" * (7 + len(names)) + "|\n")
+            f.write("| plain form | | | | | " + " | ".join(f"{plain_ms[n]:.3f}" for n in names) + " | | |\n")
             for sh in sorted(rows, key=lambda s: score.get(s, 1e9)):
-                f.write(f"| {sh[0]} | {sh[1]} | {sh[2]} | " + " | ".join(f"{rows[sh][n]:.3f}" for n in names)
+                f.write(f"| {sh[0]} | {sh[1]} | {sh[2]} | {sh[3]} | {sh[4]} | "
+                        + " | ".join(f"{rows[sh][n]:.3f}" for n in names)
                         + f" | {score.get(sh, float('nan')):.3f} | {exact[sh]} |\n")
             f.write("\n| chunk_reads | e2e reads/s |\n|---|---|\n")
             for ch, r in chunk_rates.items():

@@ -114,6 +114,8 @@ void check_config(const gbsa_batch_config& c) {
         throw Error(GBSA_ERR_PARAM, "lane_max_hits must be in [1, 160]");
     if (c.sort_variant < 0 || c.sort_variant > 1) throw Error(GBSA_ERR_PARAM, "sort_variant must be 0 or 1");
     if (c.chunk_reads < 1024) throw Error(GBSA_ERR_PARAM, "chunk_reads must be at least 1024");
+    if (c.lane_variant < 0 || c.lane_variant > 2) throw Error(GBSA_ERR_PARAM, "lane_variant must be 0, 1 or 2");
+    if (c.warp_variant < 0 || c.warp_variant > 2) throw Error(GBSA_ERR_PARAM, "warp_variant must be 0, 1 or 2");
 }
 
 // The committed autotuner result next to the library (gpu_index_test_gb300/tuned.json),
@@ -137,6 +139,9 @@ gbsa_batch_config tuned_config(int* from_file) {
     x.sort_variant = (int32_t)v;
     ok &= parse_flat_json(t, "chunk_reads", &v);
     x.chunk_reads = (uint32_t)v;
+    // the merge kernels' register budgets (a file written before they were tuned lacks them)
+    x.lane_variant = parse_flat_json(t, "lane_variant", &v) ? (int32_t)v : 0;
+    x.warp_variant = parse_flat_json(t, "warp_variant", &v) ? (int32_t)v : 0;
     if (!ok) return c;
     try {
         check_config(x);
@@ -173,6 +178,8 @@ void lane_init(gbsa_batcher& b, Lane& L) {
     L.m = m;
     L.m->cfg.lane_max_hits = b.cfg.lane_max_hits;
     L.m->cfg.sort_variant = b.cfg.sort_variant;
+    L.m->cfg.lane_variant = b.cfg.lane_variant;
+    L.m->cfg.warp_variant = b.cfg.warp_variant;
     L.desc.resize(sizeof(BatchDesc));
     L.h_desc.resize(sizeof(BatchDesc));
     for (cudaEvent_t* e : {&L.done, &L.in_ready, &L.out_free})

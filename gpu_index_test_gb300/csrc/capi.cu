@@ -899,6 +899,8 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
             if (gbsa_batch_config_default(&bc, &from_file) == GBSA_OK) {
                 m->cfg.lane_max_hits = bc.lane_max_hits;
                 m->cfg.sort_variant = bc.sort_variant;
+                m->cfg.lane_variant = bc.lane_variant;
+                m->cfg.warp_variant = bc.warp_variant;
             }
         }
         l2_window_attach(*m, true);

@@ -120,6 +120,10 @@ struct MapConfig {
     // size of the sort of rescued reads with many NAMs (0: 256 threads, 1: 512)
     uint32_t lane_max_hits;
     int sort_variant;
+    // register budgets of the NAM merge kernels (resident blocks they must fit):
+    // lane_variant 0 none, 1 six blocks, 2 eight; warp_variant 0 five, 1 six, 2 eight
+    int lane_variant;
+    int warp_variant;
 };
 constexpr uint32_t kLaneMaxHitsCap = 160;
 

@@ -614,7 +614,10 @@ __global__ void k_bucket_reads(uint32_t n, uint32_t lane_max, const ReadRec* __r
     }
 }
 
-__global__ void __launch_bounds__(32 * kLaneWarps) k_nams_lane(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
+// kMinBlocks: resident blocks the compiler must leave room for (0: no bound); a smaller
+// register budget leaves room on the SM for the rescued reads' sorts beside it.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks) k_nams_lane(MapConfig C, uint32_t n, ReadRec* __restrict__ rec,
                                                                Arenas A, Counters* ctr) {
     __shared__ LaneOpen S;
     __shared__ uint32_t s_cnt[kLaneBuckets];
@@ -916,7 +919,11 @@ constexpr int kHeavyGridPerSm = 5;     // blocks launched per SM (32 KB each)
 // warp's global scratch, which is only written until the sort.  The read's NAMs are
 // then sorted by key in shared memory (in scratch beyond kHeavyOpen NAMs) and
 // gathered to the NAM arena.
-__global__ void __launch_bounds__(32 * kHeavyWarps, kHeavyBlocksPerSm)
+// kMinBlocks: resident blocks the compiler must leave room for (its register budget);
+// the grid stays kHeavyGridPerSm blocks per SM, so a larger kMinBlocks leaves registers
+// free beside it for the rescued reads' sorts.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(32 * kHeavyWarps, kMinBlocks)
     k_nams(MapConfig C, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
     __shared__ __align__(16) int32_t s_open[kHeavyWarps][8 * kHeavyOpen];
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
@@ -1812,7 +1819,11 @@ void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec,
                  cudaStream_t st) {
     if (!n) return;
     const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSm);
-    k_nams_lane<<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+    switch (C.lane_variant) {
+        case 1: k_nams_lane<6><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr); break;
+        case 2: k_nams_lane<8><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr); break;
+        default: k_nams_lane<0><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr); break;
+    }
     GBSA_LAUNCHED();
 }
 
@@ -1830,7 +1841,11 @@ void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Co
     // at most nam_kernel_warps(n) warps: one scratch slot each
     const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * kHeavyGridPerSm,
                                                          (n + kHeavyWarps - 1) / kHeavyWarps);
-    k_nams<<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr);
+    switch (C.warp_variant) {
+        case 1: k_nams<6><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
+        case 2: k_nams<8><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
+        default: k_nams<kHeavyBlocksPerSm><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
+    }
     GBSA_LAUNCHED();
 }
 

@@ -258,7 +258,12 @@ typedef struct gbsa_batch_config {
     uint32_t lane_max_hits;  /* reads with at most this many hits (1-160) are merged by one lane,
                                 heavier ones by a warp */
     int32_t  sort_variant;   /* block size of the sort of rescued reads with many NAMs: 0 256, 1 512 */
-    uint32_t chunk_reads;    /* reads per batch of the host entry point (two batches in flight) */
+    uint32_t chunk_reads;    /* reads per batch of the host entry point (three batches in flight) */
+    int32_t  lane_variant;   /* register budget of the lane-per-read NAM merge: resident blocks it must fit,
+                                0 no bound (96 registers), 1 six (80), 2 eight (64) */
+    int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
+                                1 six (80), 2 eight (64); fewer registers leave room for the rescued reads'
+                                sorts beside it */
 } gbsa_batch_config;
 
 typedef struct gbsa_batcher gbsa_batcher;

@@ -38,19 +38,19 @@ def test_params_and_errors_without_gpu():
 
 
 def test_batch_config_layout_and_default_without_gpu():
-    """gbsa_batch_config is four 32-bit fields; the default is the committed tuned file
+    """gbsa_batch_config is six 32-bit fields; the default is the committed tuned file
     when it is present and well formed (no GPU needed to read it)."""
     import json
     import os
 
-    assert C.sizeof(abi.BatchConfig) == 16
+    assert C.sizeof(abi.BatchConfig) == 24
     cfg, from_file = native.batch_config_default()
     path = os.path.join(os.path.dirname(native.GBSA_SO), "tuned.json")
     if os.path.exists(path):
         assert from_file
         want = json.load(open(path))
-        for k in ("seed_variant", "lane_max_hits", "sort_variant", "chunk_reads"):
-            assert getattr(cfg, k) == want[k], k
+        for k in ("seed_variant", "lane_max_hits", "sort_variant", "chunk_reads", "lane_variant", "warp_variant"):
+            assert getattr(cfg, k) == want.get(k, 0), k
     else:
         assert not from_file
     assert 0 <= cfg.seed_variant < abi.SEED_VARIANTS and 1 <= cfg.lane_max_hits <= 160

@@ -49,13 +49,16 @@ def test_batched_form_matches_oracle_on_uneven_reads_and_pairs(c3):
 @pytest.mark.parametrize("variant", range(abi.SEED_VARIANTS))
 def test_every_tuned_variant_is_bit_exact(c3, variant):
     """Each shape the autotuner may pick (seeding + lookup variant, lane / warp split of
-    the NAM merge, sort block size) gives the plain form's output."""
+    the NAM merge, sort block size, register budgets of the two merges) gives the plain
+    form's output."""
     g, reads, items, idx, o = c3
     ref = native.Mapper(idx).map_reads(reads)
-    for lane_max, sort_variant in ((160, 0), (64, 1), (96, 0)):
-        cfg = abi.batch_config(variant, lane_max, sort_variant, 4096)
+    regs = ((0, 0), (1, 1), (2, 2))
+    for j, (lane_max, sort_variant) in enumerate(((160, 0), (64, 1), (96, 0))):
+        lv, wv = regs[(j + variant) % 3]
+        cfg = abi.batch_config(variant, lane_max, sort_variant, 4096, lv, wv)
         b = native.Batcher(idx, config=cfg, max_reads=reads.n)
-        assert same(b.map_reads(reads, items), ref)   # several chunks of ~4096 reads, two sets of work areas
+        assert same(b.map_reads(reads, items), ref)   # several chunks of ~4096 reads, three sets of work areas
         b.free()
 
 
