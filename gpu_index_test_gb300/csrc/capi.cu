@@ -1251,6 +1251,11 @@ int gbsa_mapper_set_l2_window(gbsa_mapper* m, int on, uint64_t* window_bytes) {
     });
 }
 
+int gbsa_mapper_set_rescue_block(gbsa_mapper* m, uint32_t hits) {
+    m->cfg.rescue_block_hits = hits;
+    return GBSA_OK;
+}
+
 int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes) {
     m->fuse_index_bytes = index_bytes;
     if (m->twin) m->twin->fuse_index_bytes = index_bytes;

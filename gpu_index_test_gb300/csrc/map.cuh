@@ -45,6 +45,7 @@ struct Counters {
     unsigned int lane_cnt[16]; // reads per hit-count bucket of the lane NAM kernel
     unsigned int queue_head;   // next read (work item) of the seeding (+ lookup) kernel
     unsigned int queue_head2;  // next read of the lookup kernel, when it runs on its own
+    unsigned int rescue_block_next;  // next heavy rescued read to take a block (k_rescue)
 };
 
 // A batch of the batched form, in device memory: the kernels of a captured batch graph
@@ -124,6 +125,10 @@ struct MapConfig {
     // lane_variant 0 none, 1 six blocks, 2 eight; warp_variant 0 five, 1 six, 2 eight
     int lane_variant;
     int warp_variant;
+    // rescued reads whose estimated merge hits (their seeds' runs up to the count cap)
+    // reach rescue_block_hits are merged by a whole block each, ahead of the others
+    // (0: every rescued read by one warp, those above kRescueHeavyHits first)
+    uint32_t rescue_block_hits;
 };
 constexpr uint32_t kLaneMaxHitsCap = 160;
 

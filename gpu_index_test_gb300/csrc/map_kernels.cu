@@ -221,7 +221,8 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
     if (rescue) {
         // Reads inside short tandem repeats merge thousands of hits: their seeds'
         // runs (up to the count cap) estimate the merge's hits; reads above
-        // kRescueHeavyHits go to the heavy end of the list, whose warps start first.
+        // kRescueHeavyHits (C.rescue_block_hits when set) go to the heavy end of the
+        // list, which the rescue kernel takes first.
         uint32_t w = 0;
         if (good < tot) {
             for (uint32_t i = lane; i < nq2; i += 32) {
@@ -232,7 +233,7 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
             }
             w = warp_sum(w);
         }
-        const bool heavy = w >= kRescueHeavyHits;
+        const bool heavy = w >= (C.rescue_block_hits ? C.rescue_block_hits : kRescueHeavyHits);
         if (lane == 0) {
             R.flags |= kReadRescue;
             if (heavy) A.rescue_list[A.rescue_cap - 1 - atomicAdd(&ctr->n_rescue_heavy, 1u)] = r;
@@ -1021,13 +1022,14 @@ struct RescuePlan {
     uint32_t maxrun;
 };
 
-__device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, const Query* const* Qd,
-                                     const uint64_t* const* Pd, const uint32_t* nqd, uint32_t Pq, uint64_t* buf) {
+// One orientation d of rescue_prepare: adds its taken prefix to plan.
+__device__ void rescue_prepare_dir(const IndexView& I, const MapConfig& C, const Query* const* Qd,
+                                   const uint64_t* const* Pd, const uint32_t* nqd, uint32_t Pq, uint64_t* buf, int d,
+                                   RescuePlan& plan) {
     const uint32_t lane = lane_id();
-    RescuePlan plan{};
     uint64_t* rk[2] = {buf, buf + Pq};
     uint64_t* tk[2] = {buf + 2 * Pq, buf + 3 * Pq};
-    for (int d = 0; d < 2; ++d) {
+    {
         uint32_t nd = 0;
         const uint32_t nq = nqd[d];
         for (uint32_t base = 0; base < nq; base += 32) {
@@ -1081,6 +1083,13 @@ __device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, con
         __syncwarp();
         warp_sort_u64(tk[d], stop);
     }
+}
+
+__device__ RescuePlan rescue_prepare(const IndexView& I, const MapConfig& C, const Query* const* Qd,
+                                     const uint64_t* const* Pd, const uint32_t* nqd, uint32_t Pq, uint64_t* buf) {
+    RescuePlan plan{};
+    rescue_prepare_dir(I, C, Qd, Pd, nqd, Pq, buf, 0, plan);
+    rescue_prepare_dir(I, C, Qd, Pd, nqd, Pq, buf, 1, plan);
     return plan;
 }
 
@@ -1122,19 +1131,190 @@ constexpr uint32_t kSortTile = 2048;      // keys per shared-memory tile of the 
 // end with more than kWarpSortMax NAMs leave the sort to k_sort_jobs.
 constexpr uint32_t kRescueSmemHits = 1024;   // per-warp shared buffer for one query's hits
 
+// Hands a rescued read's NAMs to the block sort (more than kWarpSortMax) and returns
+// true, or returns false (the caller's warp sorts them).
+__device__ __forceinline__ bool rescue_sort_job(const Arenas& A, Counters* ctr, ReadRec& R, const NamLists& L,
+                                                NamKey* keys, uint32_t r, uint32_t t) {
+    if (L.n_closed <= kWarpSortMax) return false;
+    // many NAMs: the block-per-read sort kernel orders them.  The count is known now
+    // (the sort only orders them), so the NAM offsets of the batch can be computed
+    // while the sorts run; the sort sets nam_off.
+    if (lane_id() == 0) {
+        R.n_nams = L.n_closed;
+        const uint32_t j = L.n_closed > kSortTile ? A.jobs_cap - 1 - atomicAdd(&ctr->n_huge, 1u)
+                                                  : atomicAdd(&ctr->n_heavy, 1u);
+        SortJob job;
+        job.closed = L.closed;
+        job.keys = keys;
+        job.n = L.n_closed;
+        job.read = r;
+        job.note = t;
+        job.pad = 0;
+        A.sort_jobs[j] = job;
+    }
+    return true;
+}
+
+// find_nams_rescue for one heavy read (entry t of the rescue list) with the whole
+// block: the two orientations' plans on warps 0 and 1, each query's hit run walked by
+// warp 0 and merged by block_close_merge_q.  The shared buffers of the block's warps
+// serve as one: the candidates (hrs), the query's hits (hpk: positions, then packed
+// words) and its taken flags (tb).
+__device__ void rescue_read_block(const IndexView& I, const MapConfig& C, ReadRec* __restrict__ rec,
+                                  const Arenas& A, Counters* ctr, uint32_t t, uint32_t* s_hrs, uint32_t* s_hpk,
+                                  uint8_t* s_tb) {
+    __shared__ uint8_t* s_sc;
+    __shared__ RescuePlan s_plan[2];
+    __shared__ uint32_t s_n;
+    __shared__ uint32_t s_bcnt[kBlockSeg / 32];
+    __shared__ uint32_t s_tot[3];
+    constexpr uint32_t kBlockHits = kWarpsPerBlock * kRescueSmemHits / 2;   // hits of one query in s_hpk
+    static_assert(kWarpsPerBlock * kRescueSmemHits >= kBlockSeg, "the candidates fit the shared buffers");
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+    const long long t0 = clock64();
+    const uint32_t r = A.rescue_list[A.rescue_cap - 1 - t];
+    ReadRec& R = rec[r];
+    const uint32_t nqd[2] = {R.nq, R.nq2 - R.nq};
+    const Query* Qd[2] = {A.q + R.q_off, A.q + R.q_off + R.nq};
+    const uint64_t* Pd[2] = {A.q_pos + R.q_off, A.q_pos + R.q_off + R.nq};
+    const uint32_t nqm = nqd[0] > nqd[1] ? nqd[0] : nqd[1];
+    const uint32_t Pq = next_pow2(nqm > 0 ? nqm : 1);
+    const uint64_t b1 = 4ull * 8 * Pq + 64;
+    if (w == 0) {
+        uint8_t* sc1 = warp_scratch(A, ctr, 0, b1);
+        if (!sc1) warp_fail(R, ctr, kStatusScratchOverflow);
+        if (lane == 0) s_sc = sc1;
+    }
+    __syncthreads();
+    uint64_t* buf = reinterpret_cast<uint64_t*>(s_sc);
+    __syncthreads();
+    if (!buf) return;
+    if (w < 2) {
+        RescuePlan p{};
+        rescue_prepare_dir(I, C, Qd, Pd, nqd, Pq, buf, (int)w, p);
+        if (lane == 0) s_plan[w] = p;
+    }
+    __syncthreads();
+    RescuePlan plan;
+    plan.m[0] = s_plan[0].m[0];
+    plan.m[1] = s_plan[1].m[1];
+    plan.bound = s_plan[0].bound + s_plan[1].bound;
+    plan.maxrun = s_plan[0].maxrun > s_plan[1].maxrun ? s_plan[0].maxrun : s_plan[1].maxrun;
+    const bool notes = A.rescue_cycles && threadIdx.x == 0;
+    uint64_t* note = A.rescue_cycles ? A.rescue_cycles + 8ull * t : nullptr;
+    if (notes) {
+        note[1] = (uint64_t)(clock64() - t0);
+        note[4] = plan.bound;
+        note[7] = plan.maxrun;
+    }
+    if (plan.bound == 0) {
+        if (threadIdx.x == 0) {
+            R.n_nams = 0;
+            if (notes) note[0] = (uint64_t)(clock64() - t0);
+        }
+        __syncthreads();
+        return;
+    }
+    const uint32_t H = (uint32_t)plan.bound;
+    const uint64_t P2 = next_pow2(H);
+    const bool big_run = plan.maxrun > kBlockHits;
+    // open, closed and spare lists (H each) and the sort keys; big runs' hits after them
+    const uint64_t b2 = 96ull * H + 32ull * P2 + (big_run ? 9ull * plan.maxrun + 64 : 0) + 256;
+    if (w == 0) {
+        uint8_t* sc2 = warp_scratch(A, ctr, (b1 + 255) & ~255ull, b2);
+        if (!sc2) warp_fail(R, ctr, kStatusScratchOverflow);
+        if (lane == 0) s_sc = sc2;
+    }
+    __syncthreads();
+    uint8_t* sc2 = s_sc;
+    __syncthreads();
+    if (!sc2) return;
+    NamLists L;
+    L.open = reinterpret_cast<NamState*>(sc2);
+    L.closed = L.open + H;
+    NamKey* keys = reinterpret_cast<NamKey*>(L.closed + H);
+    NamState* spare = reinterpret_cast<NamState*>(keys + P2);
+    uint32_t* hrs = s_hpk;
+    uint32_t* hpk = s_hpk + kBlockHits;
+    uint8_t* tb = s_tb;
+    if (big_run) {
+        hrs = reinterpret_cast<uint32_t*>(spare + H);
+        hpk = hrs + plan.maxrun;
+        tb = reinterpret_cast<uint8_t*>(hpk + plan.maxrun);
+    }
+    L.n_open = L.n_closed = 0;
+    L.cap = H;
+    const long long t_merge = clock64();
+    uint64_t walk_cycles = 0;
+    const uint64_t* tk[2] = {buf + 2 * Pq, buf + 3 * Pq};
+    for (int d = 0; d < 2; ++d) {
+        for (uint32_t j = 0; j < plan.m[d]; ++j) {
+            const uint32_t qi = (uint32_t)(tk[d][j] >> 32) & 0xFFFF;
+            const uint32_t cnt = (uint32_t)tk[d][j];
+            const Query q = Qd[d][qi];
+            QueryHits Q;
+            Q.rs = hrs;
+            Q.packed = hpk;
+            Q.qs = (int)q.start;
+            Q.qe = (int)q.end;
+            Q.dir = (uint32_t)d;
+            Q.k = I.k;
+            if (w == 0) {
+                const long long tw = clock64();
+                const uint32_t n = warp_walk_run_n(I, Q.qs, Q.qe, Pd[d][qi], cnt, hrs, hpk, plan.maxrun);
+                walk_cycles += (uint64_t)(clock64() - tw);
+                if (lane == 0) s_n = n;
+            }
+            __syncthreads();
+            Q.n = s_n;
+            block_close_merge_q(L, spare, Q, tb, s_hrs, s_bcnt, s_tot);
+        }
+        block_close_all(L);
+    }
+    if (notes) {
+        note[2] = (uint64_t)(clock64() - t_merge);
+        note[5] = L.n_closed;
+        note[6] = walk_cycles;
+    }
+    if (w == 0 && !rescue_sort_job(A, ctr, R, L, keys, r, t)) {
+        const long long t_fin = clock64();
+        warp_finish_nams(C, L, s_hrs, s_hpk, R, A, ctr);
+        if (notes) note[3] = (uint64_t)(clock64() - t_fin);
+    }
+    if (notes) note[0] = (uint64_t)(clock64() - t0);
+    __syncthreads();
+}
+
+// find_nams_rescue for the reads on the rescue list.  With C.rescue_block_hits set the
+// heavy end of the list (reads whose estimated merge hits reach it) is taken first, a
+// block per read, then the rest a warp per read; otherwise every read a warp, heavy
+// ones first.
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
                                                                  Arenas A, Counters* ctr) {
     __shared__ __align__(16) uint32_t s_hrs[kWarpsPerBlock][kRescueSmemHits];
     __shared__ __align__(16) uint32_t s_hpk[kWarpsPerBlock][kRescueSmemHits];
     __shared__ uint8_t s_tb[kWarpsPerBlock][kRescueSmemHits];
+    __shared__ uint32_t s_item;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_rescue_heavy;
     const uint32_t n_rescue = n_heavy + *(volatile unsigned int*)&ctr->n_rescue;
+    uint32_t first = 0;
+    if (C.rescue_block_hits) {
+        for (;;) {
+            if (threadIdx.x == 0) s_item = atomicAdd(&ctr->rescue_block_next, 1u);
+            __syncthreads();
+            const uint32_t t = s_item;
+            __syncthreads();
+            if (t >= n_heavy) break;
+            rescue_read_block(I, C, rec, A, ctr, t, &s_hrs[0][0], &s_hpk[0][0], &s_tb[0][0]);
+        }
+        first = n_heavy;
+    }
     // resident warps take reads in list order, heavy ones first
     for (;;) {
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(&ctr->rescue_next, 1u);
-        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0) + first;
         if (t >= n_rescue) break;
         const long long t_start = clock64();
         const uint32_t r = t < n_heavy ? A.rescue_list[A.rescue_cap - 1 - t] : A.rescue_list[t - n_heavy];
@@ -1201,25 +1381,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
         note.phase(2, t_merge);
         note.set(6, walk);
         note.set(5, L.n_closed);
-        if (L.n_closed > kWarpSortMax) {
-            // many NAMs: the block-per-read sort kernel orders them.  The count is known
-            // now (the sort only orders them), so the NAM offsets of the batch can be
-            // computed while the sorts run; the sort sets nam_off.
-            if (lane == 0) {
-                R.n_nams = L.n_closed;
-                const uint32_t j = L.n_closed > kSortTile ? A.jobs_cap - 1 - atomicAdd(&ctr->n_huge, 1u)
-                                                          : atomicAdd(&ctr->n_heavy, 1u);
-                SortJob job;
-                job.closed = L.closed;
-                job.keys = keys;
-                job.n = L.n_closed;
-                job.read = r;
-                job.note = t;
-                job.pad = 0;
-                A.sort_jobs[j] = job;
-            }
-            continue;
-        }
+        if (rescue_sort_job(A, ctr, R, L, keys, r, t)) continue;
         const long long t_fin = clock64();
         static_assert(kWarpSortMax <= 256 && kRescueSmemHits >= 1024, "the sort entries fit the hit buffers");
         warp_finish_nams(C, L, s_hrs[w], s_hpk[w], R, A, ctr);

@@ -112,6 +112,21 @@ struct QueryHits {
     }
 };
 
+// First untaken hit of the query at index from or later (hits sorted by rs) that NAM n
+// would take, or -1.
+__device__ __forceinline__ int nam_candidate_from(const NamState& n, const QueryHits& Q, const uint8_t* taken,
+                                                  uint32_t from) {
+    const uint32_t want = n.ref_rc & 0x7FFFFFFFu;
+    for (uint32_t j = from; j < Q.n; ++j) {
+        const int rs = (int)Q.rs[j];
+        if (rs > n.re) break;
+        if ((Q.packed[j] >> 8) != want || taken[j]) continue;
+        const int re = rs + (int)(Q.packed[j] & 0xFF) + Q.k;
+        if ((Q.qe > n.qe && re > n.re) || (Q.qe <= n.qe && re <= n.re)) return (int)j;
+    }
+    return -1;
+}
+
 // First untaken hit of the query (sorted by rs) that NAM n would take, or -1.
 __device__ __forceinline__ int nam_candidate_q(const NamState& n, const QueryHits& Q, const uint8_t* taken) {
     uint32_t lo = 0, hi = Q.n;
@@ -121,15 +136,7 @@ __device__ __forceinline__ int nam_candidate_q(const NamState& n, const QueryHit
         if ((int)Q.rs[mid] < from) lo = mid + 1;
         else hi = mid;
     }
-    const uint32_t want = n.ref_rc & 0x7FFFFFFFu;
-    for (uint32_t j = lo; j < Q.n; ++j) {
-        const int rs = (int)Q.rs[j];
-        if (rs > n.re) break;
-        if ((Q.packed[j] >> 8) != want || taken[j]) continue;
-        const int re = rs + (int)(Q.packed[j] & 0xFF) + Q.k;
-        if ((Q.qe > n.qe && re > n.re) || (Q.qe <= n.qe && re <= n.re)) return (int)j;
-    }
-    return -1;
+    return nam_candidate_from(n, Q, taken, lo);
 }
 
 // One query of the NAM-major merge (hits in compact form), in one pass over the open
@@ -201,6 +208,155 @@ __device__ __forceinline__ void nam_close_merge_q(NamLists& L, const QueryHits& 
     }
     L.n_open += added;
     __syncwarp();
+}
+
+// Block-cooperative form of nam_close_merge_q, for reads with thousands of open NAMs
+// (reads inside repeat families).  Same result; the open list is taken kBlockSeg NAMs
+// at a time in three phases:
+//   1. every warp, for its share of the segment's NAMs, finds the first hit each NAM
+//      accepts with no hit taken yet (the query's taken flags are clear) and notes
+//      which NAMs the query has passed;
+//   2. warp 0 walks the segment in open-list order, 32 NAMs at a time, and settles the
+//      clashes as nam_close_merge_q does: a NAM whose first choice an earlier NAM took
+//      scans on from the next hit (hits before its first choice it rejects whatever is
+//      taken);
+//   3. every warp applies its NAMs' hits and writes them, by the segment's running
+//      counts, to the other open list (NAMs staying, in order) or the closed list.
+// The untaken hits then open new NAMs in ref_start order.  Every thread of the block
+// calls it with the same arguments; L and spare are updated alike in every thread
+// (spare becomes the open list).  cand: kBlockSeg words, bcnt: kBlockSeg / 32 words,
+// tot: 3 words of shared memory; taken: Q.n bytes.
+constexpr uint32_t kBlockSeg = 8192;
+constexpr uint32_t kCandClose = 0xFFFFFFFEu;   // the query has passed the NAM
+constexpr uint32_t kCandNone = 0xFFFFFFFFu;    // the NAM takes no hit of the query
+
+__device__ inline void block_close_merge_q(NamLists& L, NamState*& spare, const QueryHits& Q, uint8_t* taken, uint32_t* cand,
+                                    uint32_t* bcnt, uint32_t* tot) {
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nh = Q.n;
+    for (uint32_t j = threadIdx.x; j < nh; j += blockDim.x) taken[j] = 0;
+    __syncthreads();
+    const uint32_t nn = L.n_open;
+    const uint32_t dirbit = Q.dir << 31;
+    uint32_t keep = 0, done = 0;
+    for (uint32_t seg = 0; seg < nn; seg += kBlockSeg) {
+        const uint32_t sn = nn - seg < kBlockSeg ? nn - seg : kBlockSeg;
+        const uint32_t nb = (sn + 31) >> 5;
+        // 1. first choices
+        for (uint32_t b = w; b < nb; b += nw) {
+            const uint32_t i = (b << 5) + lane;
+            const bool valid = i < sn;
+            bool close = false;
+            if (valid) {
+                const NamState m = L.open[seg + i];
+                uint32_t c = kCandNone;
+                close = m.qe < Q.qs;
+                if (close) {
+                    c = kCandClose;
+                } else if ((m.ref_rc & 0x80000000u) == dirbit) {
+                    const int x = nam_candidate_q(m, Q, taken);
+                    if (x >= 0) c = (uint32_t)x;
+                }
+                cand[i] = c;
+            }
+            const uint32_t ms = __ballot_sync(0xFFFFFFFFu, valid && !close);
+            const uint32_t mc = __ballot_sync(0xFFFFFFFFu, close);
+            if (lane == 0) bcnt[b] = (uint32_t)__popc(ms) | ((uint32_t)__popc(mc) << 16);
+        }
+        __syncthreads();
+        // 2. clashes, in open-list order; bcnt becomes the exclusive running counts
+        if (w == 0) {
+            uint32_t run_s = 0, run_c = 0;
+            uint32_t nxt = lane < sn ? cand[lane] : kCandNone;
+            for (uint32_t b = 0; b < nb; ++b) {
+                const uint32_t i = (b << 5) + lane;
+                uint32_t c = nxt;
+                if (i + 32 < sn) nxt = cand[i + 32];
+                bool pending = c < kCandClose;
+                for (;;) {
+                    if (pending && taken[c]) {
+                        const int x = nam_candidate_from(L.open[seg + i], Q, taken, c + 1);
+                        if (x < 0) {
+                            pending = false;
+                            c = kCandNone;
+                        } else {
+                            c = (uint32_t)x;
+                        }
+                    }
+                    const uint32_t key = pending ? c : 0xFFFFFFFFu;
+                    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+                    const bool clash = pending && (peers & lanemask_lt()) != 0;
+                    const uint32_t cm = __ballot_sync(0xFFFFFFFFu, clash);
+                    const uint32_t lim = cm ? (uint32_t)(__ffs(cm) - 1) : 32u;
+                    if (pending && lane < lim) {
+                        taken[c] = 1;
+                        pending = false;
+                    }
+                    __syncwarp();
+                    if (!cm) break;
+                }
+                if (i < sn) cand[i] = c;
+                const uint32_t v = bcnt[b];
+                __syncwarp();
+                if (lane == 0) bcnt[b] = run_s | (run_c << 16);
+                run_s += v & 0xFFFFu;
+                run_c += v >> 16;
+            }
+            if (lane == 0) {
+                tot[0] = run_s;
+                tot[1] = run_c;
+            }
+        }
+        __syncthreads();
+        // 3. apply and write
+        for (uint32_t b = w; b < nb; b += nw) {
+            const uint32_t i = (b << 5) + lane;
+            const bool valid = i < sn;
+            const uint32_t c = valid ? cand[i] : kCandNone;
+            const bool close = c == kCandClose;
+            const bool stay = valid && !close;
+            const uint32_t ms = __ballot_sync(0xFFFFFFFFu, stay);
+            const uint32_t mc = __ballot_sync(0xFFFFFFFFu, close);
+            const uint32_t pre = bcnt[b];
+            if (valid) {
+                NamState m = L.open[seg + i];
+                if (c < kCandClose) nam_add(m, Q.get(c));
+                if (stay) spare[keep + (pre & 0xFFFFu) + __popc(ms & lanemask_lt())] = m;
+                else L.closed[L.n_closed + done + (pre >> 16) + __popc(mc & lanemask_lt())] = m;
+            }
+        }
+        keep += tot[0];
+        done += tot[1];
+        __syncthreads();
+    }
+    // untaken hits open new NAMs, in ref_start order
+    if (w == 0) {
+        uint32_t added = 0;
+        for (uint32_t b = 0; b < nh; b += 32) {
+            const uint32_t j = b + lane;
+            const bool mk = j < nh && !taken[j];
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, mk);
+            if (mk) spare[keep + added + __popc(m & lanemask_lt())] = nam_from_hit(Q.get(j));
+            added += __popc(m);
+        }
+        if (lane == 0) tot[2] = added;
+    }
+    __syncthreads();
+    NamState* old = L.open;
+    L.open = spare;
+    spare = old;
+    L.n_open = keep + tot[2];
+    L.n_closed += done;
+    __syncthreads();
+}
+
+// Moves every open NAM to the closed list, in order (block-cooperative; every thread
+// updates its copy of L alike).
+__device__ inline void block_close_all(NamLists& L) {
+    for (uint32_t o = threadIdx.x; o < L.n_open; o += blockDim.x) L.closed[L.n_closed + o] = L.open[o];
+    L.n_closed += L.n_open;
+    L.n_open = 0;
+    __syncthreads();
 }
 
 // Warp-cooperative add_to_hits_per_ref (step2/nam.cu:45-62) for one query whose

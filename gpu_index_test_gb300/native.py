@@ -92,6 +92,7 @@ def lib():
             "gbsa_mapper_fused_lookup": (i32, [vp]),
             "gbsa_mapper_set_fuse_limit": (i32, [vp, u64]),
             "gbsa_mapper_set_l2_window": (i32, [vp, i32, C.POINTER(u64)]),
+            "gbsa_mapper_set_rescue_block": (i32, [vp, u32]),
             "gbsa_batch_config_default": (i32, [C.POINTER(abi.BatchConfig), C.POINTER(i32)]),
             "gbsa_plan_pairs_device": (i32, [vp, vp, u32, i32, vp, vp, vp, u32, C.c_float, vp, vp, u64,
                                              C.POINTER(u64), vp]),
@@ -391,6 +392,11 @@ class Mapper:
         b = C.c_uint64()
         _check(lib().gbsa_mapper_set_l2_window(self.h, 1 if on else 0, C.byref(b)))
         return b.value
+
+    def set_rescue_block(self, hits):
+        """Rescued reads with at least `hits` estimated merge hits are merged by a block
+        each (0: every rescued read by one warp)."""
+        _check(lib().gbsa_mapper_set_rescue_block(self.h, int(hits)))
 
     def fused_lookup(self):
         """Whether the last batch ran seeding and lookup as one kernel."""

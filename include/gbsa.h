@@ -609,6 +609,12 @@ int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes);
  * *window_bytes (may be NULL) receives the window's size, 0 when none is used.  The
  * results are the same either way.  No reference counterpart. */
 int gbsa_mapper_set_l2_window(gbsa_mapper* m, int on, uint64_t* window_bytes);
+/* Rescued reads whose estimated merge hits (the runs of their found seeds, up to the
+ * count cap) reach `hits` are merged by a whole thread block each, ahead of the other
+ * rescued reads, which a warp each merges; 0 merges every rescued read with one warp
+ * (those above 2000 estimated hits first).  Takes effect from the next batch; the
+ * results are the same either way.  No reference counterpart. */
+int gbsa_mapper_set_rescue_block(gbsa_mapper* m, uint32_t hits);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the
  * merge and of the sort (the block sort, for reads with many NAMs), then the hit

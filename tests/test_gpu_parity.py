@@ -232,6 +232,38 @@ def test_tandem_repeat_rescue_against_oracle(mode):
     assert nams_equal(x[0], y[0])
 
 
+@pytest.mark.parametrize("hits", [1, 3000])
+def test_block_rescue_merge_against_oracle(hits):
+    """Rescued reads merged by a whole block each (every rescued read with hits=1; the
+    heavy ones with 3000), against the oracle: reads of 5% short tandem repeats with
+    thousands of open NAMs, and the plain form's warp merge on the same reads."""
+    import dataclasses
+    gp = dataclasses.replace(synth.genome_params("C2", scale=0.01, seed=43), str_frac=0.05)
+    g = synth.make_genome(gp)
+    reads = synth.make_reads(g, synth.read_params("C2", n_units=3000, seed=44))
+    p = native.params_from_read_length(150)
+    idx = native.Index.build(p, g)
+    o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
+    opt = abi.map_options(rescue_level=2)
+    m = native.Mapper(idx, opt)
+    warp = m.map_reads(reads)
+    m.set_rescue_block(hits)
+    x = m.map_reads(reads)
+    y = o.map_reads(reads, opt, n_threads=8)
+    assert x[3].sum() >= 100
+    assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
+    assert nams_equal(x[0], y[0])
+    assert (warp[1] == x[1]).all() and nams_equal(warp[0], x[0])
+    # the find_nams_rescue entry point (every read rescued) through the block merge
+    m.set_rescue_block(1)
+    q, qoff = native.randstrobes_query(p, reads.subset(np.arange(0, reads.n, 7)))
+    cutoff = 2 * idx.info().filter_cutoff
+    rn, roffs, _ = m.find_nams(q, qoff, rescue=True, rescue_cutoff=cutoff)
+    for i in range(len(qoff) - 1):
+        orr = o.find_nams_rescue(q[int(qoff[i]):int(qoff[i + 1])], cutoff)
+        assert nams_equal(rn[int(roffs[i]):int(roffs[i + 1])], oracle_py.sort_nams(orr)), i
+
+
 def test_read_bytes_and_alignments_against_oracle():
     """Reads of every start alignment (mod 4) and of lengths around the 4-base packing
     units, with lowercase bases, U/u, N/n, raw codes 0-3 and other bytes mixed in:
