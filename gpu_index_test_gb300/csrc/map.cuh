@@ -131,6 +131,7 @@ struct MapConfig {
     uint32_t rescue_block_hits;
 };
 constexpr uint32_t kLaneMaxHitsCap = 160;
+constexpr uint32_t kRescueBlockHitsDefault = 4000;   // a new mapper's rescue_block_hits
 
 // Reads shorter than this (and with at most kSmemSyncmers syncmers) are seeded
 // with shared-memory buffers; the rest by the scratch-memory kernel.

@@ -1285,8 +1285,10 @@ __device__ void rescue_read_block(const IndexView& I, const MapConfig& C, ReadRe
     __syncthreads();
 }
 
-// find_nams_rescue for the reads on the rescue list.  With C.rescue_block_hits set the
-// heavy end of the list (reads whose estimated merge hits reach it) is taken first, a
+// find_nams_rescue for the reads on the rescue list.  With C.rescue_block_hits set and
+// no more rescued reads than the grid has warps (a small batch, whose heavy reads
+// would otherwise set the kernel's time while most warps idle), the heavy end of the
+// list (reads whose estimated merge hits reach rescue_block_hits) is taken first, a
 // block per read, then the rest a warp per read; otherwise every read a warp, heavy
 // ones first.
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, MapConfig C, ReadRec* __restrict__ rec,
@@ -1299,7 +1301,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_rescue(IndexView I, Map
     const uint32_t n_heavy = *(volatile unsigned int*)&ctr->n_rescue_heavy;
     const uint32_t n_rescue = n_heavy + *(volatile unsigned int*)&ctr->n_rescue;
     uint32_t first = 0;
-    if (C.rescue_block_hits) {
+    if (C.rescue_block_hits && n_rescue <= warp_count()) {
         for (;;) {
             if (threadIdx.x == 0) s_item = atomicAdd(&ctr->rescue_block_next, 1u);
             __syncthreads();

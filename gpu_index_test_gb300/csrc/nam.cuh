@@ -271,7 +271,7 @@ __device__ inline void block_close_merge_q(NamLists& L, NamState*& spare, const 
             for (uint32_t b = 0; b < nb; ++b) {
                 const uint32_t i = (b << 5) + lane;
                 uint32_t c = nxt;
-                if (i + 32 < sn) nxt = cand[i + 32];
+                nxt = i + 32 < sn ? cand[i + 32] : kCandNone;
                 bool pending = c < kCandClose;
                 for (;;) {
                     if (pending && taken[c]) {

@@ -610,10 +610,11 @@ int gbsa_mapper_set_fuse_limit(gbsa_mapper* m, uint64_t index_bytes);
  * results are the same either way.  No reference counterpart. */
 int gbsa_mapper_set_l2_window(gbsa_mapper* m, int on, uint64_t* window_bytes);
 /* Rescued reads whose estimated merge hits (the runs of their found seeds, up to the
- * count cap) reach `hits` are merged by a whole thread block each, ahead of the other
- * rescued reads, which a warp each merges; 0 merges every rescued read with one warp
- * (those above 2000 estimated hits first).  Takes effect from the next batch; the
- * results are the same either way.  No reference counterpart. */
+ * count cap) reach `hits` are taken first by the rescue kernel; in a batch with no more
+ * rescued reads than the kernel has warps (small batches), each of them is merged by a
+ * whole thread block, the others by a warp each.  0: every rescued read by one warp,
+ * those above 2000 estimated hits first.  Default 4000.  Takes effect from the next
+ * batch; the results are the same either way.  No reference counterpart. */
 int gbsa_mapper_set_rescue_block(gbsa_mapper* m, uint32_t hits);
 /* With profiling on: 8 values per rescued read of the last batch, in rescue-list
  * order: SM clock cycles in total (without a block sort), of the planning, of the

@@ -254,6 +254,13 @@ def test_block_rescue_merge_against_oracle(hits):
     assert (x[1] == y[1]).all() and (x[2] == y[2]).all() and (x[3] == y[3]).all()
     assert nams_equal(x[0], y[0])
     assert (warp[1] == x[1]).all() and nams_equal(warp[0], x[0])
+    # block merges take a batch with fewer rescued reads than the rescue kernel's warps
+    few = reads.subset(np.nonzero(x[3])[0][:500])
+    m.set_rescue_block(0)
+    a = m.map_reads(few)
+    m.set_rescue_block(hits)
+    b = m.map_reads(few)
+    assert (a[1] == b[1]).all() and nams_equal(a[0], b[0]) and (a[3] == b[3]).all()
     # the find_nams_rescue entry point (every read rescued) through the block merge
     m.set_rescue_block(1)
     q, qoff = native.randstrobes_query(p, reads.subset(np.arange(0, reads.n, 7)))
