@@ -246,6 +246,7 @@ def test_block_rescue_merge_against_oracle(hits):
     o = oracle_py.Index.build(oracle_py.params_from_read_length(150), g)
     opt = abi.map_options(rescue_level=2)
     m = native.Mapper(idx, opt)
+    m.set_rescue_block(0)
     warp = m.map_reads(reads)
     m.set_rescue_block(hits)
     x = m.map_reads(reads)
