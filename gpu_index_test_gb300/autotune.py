@@ -13,7 +13,8 @@ the first) on slices of the repeat-rich mid-size configuration (150 bp pairs), o
 configuration (50-500 bp, single-end and pairs mixed) and of the human-scale one (repeat
 families, 150 bp pairs), timing each shape's graph
 launches with CUDA events and checking its output byte for byte against the plain
-form's; then the host entry point's chunk size on end-to-end reads/s.  The fastest
+form's; then the host entry point's chunk size on end-to-end reads/s over the whole
+mid-size configuration (100 Mbp, 1M pairs).  The fastest
 shape (sum of the slices' times relative to the best on each) is written to
 tuned.json next to the library, which gbsa_batcher_create reads; the whole sweep is
 written as a table to the path given by --table.
@@ -36,7 +37,7 @@ from ._build_paths import GBSA_SO
 LANE_MAX_HITS = (64, 96, 128, 160)
 SORT_VARIANTS = (0, 1)
 REG_VARIANTS = (0, 1, 2)
-CHUNKS = (1 << 17, 1 << 18, 1 << 19, 1 << 20)
+CHUNKS = (1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 
 
 def _workloads(scale):
@@ -158,7 +159,9 @@ def tune_chunks(pick, scale=1.0, log=print):
     import torch
 
     p = native.params_from_read_length(150)
-    g = synth.make_genome(synth.genome_params("C2", scale=0.1 * scale, seed=205))
+    # the whole mid-size configuration (100 Mbp, 1M pairs): the copies and the index's
+    # cache behaviour both depend on the sizes
+    g = synth.make_genome(synth.genome_params("C2", scale=scale, seed=205))
     rp = synth.read_params("C2", n_units=max(4000, int(1_000_000 * scale)), seed=206)
     reads, items = synth.make_reads(g, rp), synth.read_items(rp)
     idx = native.Index.build(p, g)
