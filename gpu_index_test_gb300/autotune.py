@@ -6,7 +6,8 @@ Sweeps, over the C-ABI (gbsa_batcher_*):
                  window (longest read seeded in shared memory: 512 or 256 bases)
   lane_max_hits  the NAM merge's split between one lane per read and one warp per read
   sort_variant   the block size of the sort of rescued reads with many NAMs
-  lane_variant   the register budget of the lane-per-read NAM merge (96, 80 or 64)
+  lane_variant   the lane-per-read NAM merge: open NAMs in shared memory with a
+                 register budget of 96, 80 or 64, or open NAMs in registers
   warp_variant   the register budget of the warp-per-read NAM merge (96, 80 or 64)
 (the first three as a grid, then the two register budgets as a grid at the best of
 the first) on slices of the repeat-rich mid-size configuration (150 bp pairs), of the uneven length
@@ -37,6 +38,7 @@ from ._build_paths import GBSA_SO
 LANE_MAX_HITS = (64, 96, 128, 160)
 SORT_VARIANTS = (0, 1)
 REG_VARIANTS = (0, 1, 2)
+LANE_VARIANTS = (0, 1, 2, 3)   # 3: the open NAMs in registers
 CHUNKS = (1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 
 
@@ -102,7 +104,7 @@ def sweep(scale=1.0, reps=5, log=print):
     """Shapes are (seed_variant, lane_max_hits, sort_variant, lane_variant, warp_variant)."""
     grid = [(v, l, s, 0, 0) for v in range(abi.SEED_VARIANTS) for l in LANE_MAX_HITS for s in SORT_VARIANTS]
     pick, rows, exact, score, plain_ms = _sweep(grid, scale, reps, log)
-    regs = [pick[:3] + (lv, wv) for lv in REG_VARIANTS for wv in REG_VARIANTS]
+    regs = [pick[:3] + (lv, wv) for lv in LANE_VARIANTS for wv in REG_VARIANTS]
     pick2, rows2, exact2, _, _ = _sweep(regs, scale, reps, log)
     rows.update(rows2)
     exact.update(exact2)

@@ -752,6 +752,219 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks) k_nams_lane(MapCo
     }
 }
 
+// The lane-per-read merge with the open NAMs in registers (lane_variant 3).  Same rule
+// as k_nams_lane: each hit joins the first open NAM in creation order that accepts it,
+// else opens one; when all kLaneOpen slots are in use, NAMs the current query start has
+// passed are closed, and a read that still has no free slot goes to the warp kernel.
+// A slot keeps its place while open: creation order is a per-slot sequence number, a
+// closed NAM frees its slot (the read's NAMs are sorted by their full key at the end,
+// so the order they close in does not matter).  Every slot access is unrolled over the
+// kLaneOpen slots, so the lanes of a warp stay together through a hit whatever their
+// open lists hold; shared memory holds only the final sort's entries.
+constexpr uint32_t kLaneEntriesR = 20;   // NAMs of a read sorted in shared memory (more: in place, in HBM)
+constexpr int kLaneBlocksPerSmR = 3;
+
+struct LaneSlots {
+    // query start | query end << 12 | creation number << 24 (query coordinates are below
+    // GBSA_MAX_READ_LEN = 4096, creation numbers below kLaneMaxHitsCap + 1); creation
+    // number kFree: the slot is free
+    uint32_t qse[kLaneOpen];
+    uint32_t qpn[kLaneOpen];   // previous hit's query start | n_hits << 16
+    int32_t rs[kLaneOpen], re[kLaneOpen], rprev[kLaneOpen];
+    uint32_t ref[kLaneOpen];
+    static constexpr uint32_t kFree = 0xFFu;
+    __device__ __forceinline__ uint32_t seq(uint32_t o) const { return qse[o] >> 24; }
+    __device__ __forceinline__ int32_t qe(uint32_t o) const { return (int32_t)((qse[o] >> 12) & 0xFFFu); }
+    __device__ __forceinline__ void free_slot(uint32_t o) { qse[o] |= kFree << 24; }
+    __device__ __forceinline__ NamState get(uint32_t o) const {
+        NamState n;
+        n.qs = (int32_t)(qse[o] & 0xFFFu);
+        n.qe = qe(o);
+        n.qprev = (int32_t)(qpn[o] & 0xFFFFu);
+        n.n_hits = (int32_t)(qpn[o] >> 16);
+        n.rs = rs[o];
+        n.re = re[o];
+        n.rprev = rprev[o];
+        n.ref_rc = ref[o];
+        return n;
+    }
+};
+static_assert(GBSA_MAX_READ_LEN <= 4096 && kLaneMaxHitsCap < 255, "lane slot packing");
+
+struct LaneSortR {
+    uint32_t w[3 * kLaneEntriesR][32 * kLaneWarps];
+    static constexpr uint32_t kEntries = kLaneEntriesR;
+    __device__ uint64_t key(uint32_t e, uint32_t t) const {
+        return ((uint64_t)w[3 * e + 1][t] << 32) | w[3 * e][t];
+    }
+    __device__ uint32_t index(uint32_t e, uint32_t t) const { return w[3 * e + 2][t]; }
+    __device__ void set_entry(uint32_t e, uint32_t t, uint64_t k, uint32_t i) {
+        w[3 * e][t] = (uint32_t)k;
+        w[3 * e + 1][t] = (uint32_t)(k >> 32);
+        w[3 * e + 2][t] = i;
+    }
+};
+
+template <class Sort>
+__device__ __forceinline__ uint64_t lane_sort_nams(const MapConfig& C, Sort& S, uint32_t t, NamState* out,
+                                                   uint32_t n_closed, uint32_t H, uint64_t noff) {
+    // stable insertion sort by the NAM order (as k_nams_lane)
+    if (n_closed <= Sort::kEntries) {
+        for (uint32_t i = 0; i < n_closed; ++i) S.set_entry(i, t, nam_key(out[i], 0, C.sort_mode).k1, i);
+        for (uint32_t i = 1; i < n_closed; ++i) {
+            const uint64_t kx = S.key(i, t);
+            if (kx > S.key(i - 1, t)) continue;
+            const uint32_t ix = S.index(i, t);
+            NamKey fx;
+            bool have_fx = false;
+            uint32_t j = i;
+            while (j > 0) {
+                const uint64_t ky = S.key(j - 1, t);
+                const uint32_t iy = S.index(j - 1, t);
+                bool less = kx < ky;
+                if (kx == ky) {
+                    if (!have_fx) {
+                        fx = nam_key(out[ix], 0, C.sort_mode);
+                        have_fx = true;
+                    }
+                    less = nam_key3_less(fx, nam_key(out[iy], 0, C.sort_mode));
+                }
+                if (!less) break;
+                S.set_entry(j, t, ky, iy);
+                --j;
+            }
+            S.set_entry(j, t, kx, ix);
+        }
+        NamState* sorted = out + H;
+        for (uint32_t i = 0; i < n_closed; ++i) sorted[i] = out[S.index(i, t)];
+        return noff + H;
+    }
+    for (uint32_t i = 1; i < n_closed; ++i) {
+        const NamState x = out[i];
+        const NamKey kx = nam_key(x, 0, C.sort_mode);
+        uint32_t j = i;
+        while (j > 0) {
+            const NamState y = out[j - 1];
+            if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
+            out[j] = y;
+            --j;
+        }
+        out[j] = x;
+    }
+    return noff;
+}
+
+__global__ void __launch_bounds__(32 * kLaneWarps, kLaneBlocksPerSmR)
+    k_nams_lane_r(MapConfig C, uint32_t n, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
+    __shared__ LaneSortR S;
+    __shared__ uint32_t s_cnt[kLaneBuckets];
+    const uint32_t t = threadIdx.x;
+    if (t < kLaneBuckets) s_cnt[t] = *(volatile unsigned int*)&ctr->lane_cnt[t];
+    __syncthreads();
+    uint32_t total = 0;
+    for (uint32_t b = 0; b < kLaneBuckets; ++b) total += s_cnt[b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        uint32_t b = kLaneBuckets - 1, j = i;
+        while (j >= s_cnt[b]) j -= s_cnt[b--];
+        const uint32_t r = A.lane_lists[(size_t)b * A.lane_cap + j];
+        ReadRec& R = rec[r];
+        const uint32_t flags = R.flags;
+        const uint32_t H = R.n_hits;
+        const uint64_t noff = atomicAdd(&ctr->nam_used, 2ull * H);
+        if (noff + 2ull * H > A.nam_cap) {
+            R.flags = flags | kReadFailed;
+            atomicOr(&ctr->status, kStatusNamOverflow);
+            continue;
+        }
+        const HitPacked* hits = A.hits + R.hit_off;
+        NamState* out = A.nams + noff;
+        LaneSlots L;
+#pragma unroll
+        for (uint32_t o = 0; o < kLaneOpen; ++o) L.qse[o] = LaneSlots::kFree << 24;
+        uint32_t n_open = 0, n_closed = 0, cur_dir = 0, next_seq = 0;
+        bool overflow = false;
+        HitRec nx = load_hit(hits, 0, H);
+        for (uint32_t i = 0; i < H; ++i) {
+            const HitRec x = nx;
+            nx = load_hit(hits, i + 1, H);
+            const uint32_t dir = x.ref_rc >> 31;
+            if (dir != cur_dir) {   // the other orientation's NAMs can take no more hits
+#pragma unroll
+                for (uint32_t o = 0; o < kLaneOpen; ++o)
+                    if (L.seq(o) != LaneSlots::kFree) {
+                        out[n_closed++] = L.get(o);
+                        L.free_slot(o);
+                    }
+                n_open = 0;
+                cur_dir = dir;
+            }
+            // the accepting NAM created first (free slots have the largest number)
+            uint32_t best = kLaneOpen, bseq = LaneSlots::kFree;
+#pragma unroll
+            for (uint32_t o = 0; o < kLaneOpen; ++o) {
+                const int32_t sqe = L.qe(o);
+                const int32_t sqp = (int32_t)(L.qpn[o] & 0xFFFFu);
+                bool ok = L.ref[o] == x.ref_rc && sqp < x.qs && x.qs <= sqe && L.rprev[o] < x.rs && x.rs <= L.re[o];
+                ok = ok && ((x.qe > sqe && x.re > L.re[o]) || (x.qe <= sqe && x.re <= L.re[o]));
+                if (ok && L.seq(o) < bseq) {
+                    bseq = L.seq(o);
+                    best = o;
+                }
+            }
+            if (best < kLaneOpen) {
+#pragma unroll
+                for (uint32_t o = 0; o < kLaneOpen; ++o) {
+                    if (o != best) continue;
+                    if (x.qe > L.qe(o) && x.re > L.re[o]) {
+                        L.qse[o] = (L.qse[o] & 0xFF000FFFu) | ((uint32_t)x.qe << 12);
+                        L.re[o] = x.re;
+                    }
+                    L.qpn[o] = (uint32_t)x.qs | (((L.qpn[o] >> 16) + 1u) << 16);
+                    L.rprev[o] = x.rs;
+                }
+                continue;
+            }
+            if (n_open == kLaneOpen) {
+                // close NAMs the current query start has passed
+#pragma unroll
+                for (uint32_t o = 0; o < kLaneOpen; ++o)
+                    if (L.seq(o) != LaneSlots::kFree && L.qe(o) < x.qs) {
+                        out[n_closed++] = L.get(o);
+                        L.free_slot(o);
+                        --n_open;
+                    }
+                if (n_open == kLaneOpen) {
+                    overflow = true;
+                    break;
+                }
+            }
+            bool placed = false;
+#pragma unroll
+            for (uint32_t o = 0; o < kLaneOpen; ++o) {
+                if (placed || L.seq(o) != LaneSlots::kFree) continue;
+                L.qse[o] = (uint32_t)x.qs | ((uint32_t)x.qe << 12) | (next_seq << 24);
+                L.qpn[o] = (uint32_t)x.qs | (1u << 16);
+                L.rs[o] = x.rs;
+                L.re[o] = x.re;
+                L.rprev[o] = x.rs;
+                L.ref[o] = x.ref_rc;
+                placed = true;
+            }
+            ++next_seq;
+            ++n_open;
+        }
+        if (overflow) {
+            A.big_list[atomicAdd(&ctr->n_big, 1u)] = r;
+            continue;
+        }
+#pragma unroll
+        for (uint32_t o = 0; o < kLaneOpen; ++o)
+            if (L.seq(o) != LaneSlots::kFree) out[n_closed++] = L.get(o);
+        R.nam_off = lane_sort_nams(C, S, t, out, n_closed, H, noff);
+        R.n_nams = n_closed;
+    }
+}
+
 // Open NAM list of one warp in struct-of-arrays form (field f of NAM o at
 // b[f * stride + o]), so that 32 lanes reading one field of 32 NAMs touch 32
 // consecutive words.
@@ -1982,6 +2195,12 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
+    if (C.lane_variant == 3) {
+        const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSmR);
+        k_nams_lane_r<<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        GBSA_LAUNCHED();
+        return;
+    }
     const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSm);
     switch (C.lane_variant) {
         case 1: k_nams_lane<6><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr); break;

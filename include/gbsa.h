@@ -259,8 +259,9 @@ typedef struct gbsa_batch_config {
                                 heavier ones by a warp */
     int32_t  sort_variant;   /* block size of the sort of rescued reads with many NAMs: 0 256, 1 512 */
     uint32_t chunk_reads;    /* reads per batch of the host entry point (three batches in flight) */
-    int32_t  lane_variant;   /* register budget of the lane-per-read NAM merge: resident blocks it must fit,
-                                0 no bound (96 registers), 1 six (80), 2 eight (64) */
+    int32_t  lane_variant;   /* the lane-per-read NAM merge: open NAMs in shared memory with a register
+                                budget of 0 no bound (96 registers), 1 six blocks (80), 2 eight (64); or
+                                3 open NAMs in registers (168 registers, three blocks per SM) */
     int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
                                 1 six (80), 2 eight (64); fewer registers leave room for the rescued reads'
                                 sorts beside it */
