@@ -10,13 +10,13 @@ Sweeps, over the C-ABI (gbsa_batcher_*):
                  register budget of 96, 80 or 64, or open NAMs in registers
   warp_variant   the register budget of the warp-per-read NAM merge (96, 80 or 64)
 (the first three as a grid, then the two register budgets as a grid at the best of
-the first) on slices of the repeat-rich mid-size configuration (150 bp pairs), of the uneven length
-configuration (50-500 bp, single-end and pairs mixed) and of the human-scale one (repeat
+the first) on the repeat-rich mid-size configuration (150 bp pairs), the uneven length configuration
+(50-500 bp, single-end and pairs mixed) and a tenth of the human-scale one (repeat
 families, 150 bp pairs), timing each shape's graph
 launches with CUDA events and checking its output byte for byte against the plain
 form's; then the host entry point's chunk size on end-to-end reads/s over the whole
 mid-size configuration (100 Mbp, 1M pairs).  The fastest
-shape (sum of the slices' times relative to the best on each) is written to
+shape (sum of the workloads' times relative to the best on each) is written to
 tuned.json next to the library, which gbsa_batcher_create reads; the whole sweep is
 written as a table to the path given by --table.
 
@@ -43,21 +43,23 @@ CHUNKS = (1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 
 
 def _workloads(scale):
-    """(name, genome, reads, items) slices the sweep times."""
+    """(name, genome, reads, items) workloads the sweep times: the benchmark's mid-size
+    and uneven-length configurations whole, and a tenth of the human-scale one (kernel
+    shapes that differ by a few percent on small slices order differently at full size)."""
     out = []
-    gp = synth.genome_params("C2", scale=0.1 * scale, seed=201)
+    gp = synth.genome_params("C2", scale=scale, seed=201)
     g = synth.make_genome(gp)
-    rp = synth.read_params("C2", n_units=max(2000, int(150_000 * scale)), seed=202)
-    out.append(("C2 slice: 10 Mbp repeat-rich genome, 150 bp pairs", g, synth.make_reads(g, rp), synth.read_items(rp)))
-    gp = synth.genome_params("C3", scale=scale, seed=203)
+    rp = synth.read_params("C2", n_units=max(2000, int(1_000_000 * scale)), seed=202)
+    out.append(("C2: 100 Mbp repeat-rich genome, 1M pairs of 150 bp", g, synth.make_reads(g, rp), synth.read_items(rp)))
+    gp = synth.genome_params("C1", scale=scale, seed=203)
     g = synth.make_genome(gp)
-    rp = synth.read_params("C3", n_units=max(2000, int(200_000 * scale)), seed=204)
-    out.append(("C3 slice: 5 Mbp genome, 50-500 bp reads, half pairs", g, synth.make_reads(g, rp),
+    rp = synth.read_params("C3", n_units=max(2000, int(1_333_333 * scale)), seed=204)
+    out.append(("C3: 5 Mbp genome, 2M reads of 50-500 bp, half pairs", g, synth.make_reads(g, rp),
                 synth.read_items(rp)))
-    gp = synth.genome_params("C4", scale=0.05 * scale, seed=207)
+    gp = synth.genome_params("C4", scale=0.1 * scale, seed=207)
     g = synth.make_genome(gp)
-    rp = synth.read_params("C4", n_units=max(2000, int(150_000 * scale)), seed=208)
-    out.append(("C4 slice: 155 Mbp genome with 45% repeat families, 150 bp pairs", g, synth.make_reads(g, rp),
+    rp = synth.read_params("C4", n_units=max(2000, int(1_000_000 * scale)), seed=208)
+    out.append(("C4 tenth: 310 Mbp genome with 45% repeat families, 1M pairs of 150 bp", g, synth.make_reads(g, rp),
                 synth.read_items(rp)))
     return out
 
@@ -100,7 +102,7 @@ def _same(a, b):
     return all(np.array_equal(x, y) for x, y in zip(a, b))
 
 
-def sweep(scale=1.0, reps=5, log=print):
+def sweep(scale=1.0, reps=7, log=print):
     """Shapes are (seed_variant, lane_max_hits, sort_variant, lane_variant, warp_variant)."""
     grid = [(v, l, s, 0, 0) for v in range(abi.SEED_VARIANTS) for l in LANE_MAX_HITS for s in SORT_VARIANTS]
     pick, rows, exact, score, plain_ms = _sweep(grid, scale, reps, log)
