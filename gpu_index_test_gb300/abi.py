@@ -80,6 +80,8 @@ class BatchConfig(C.Structure):
         ("chunk_reads", C.c_uint32),
         ("lane_variant", C.c_int32),
         ("warp_variant", C.c_int32),
+        ("rescue_block_hits", C.c_uint32),
+        ("_reserved", C.c_uint32),
     ]
 
     def as_dict(self):
@@ -100,8 +102,9 @@ SEED_VARIANTS = 6   # shapes of the batched form's seeding + lookup kernel
 
 
 def batch_config(seed_variant=0, lane_max_hits=160, sort_variant=0, chunk_reads=1 << 19, lane_variant=0,
-                 warp_variant=0):
-    return BatchConfig(seed_variant, lane_max_hits, sort_variant, chunk_reads, lane_variant, warp_variant)
+                 warp_variant=0, rescue_block_hits=4000):
+    return BatchConfig(seed_variant, lane_max_hits, sort_variant, chunk_reads, lane_variant, warp_variant,
+                       rescue_block_hits, 0)
 
 
 REF_RANDSTROBE = np.dtype([("hash", "<u8"), ("position", "<u4"), ("packed", "<u4")])

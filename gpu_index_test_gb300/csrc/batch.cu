@@ -104,6 +104,7 @@ gbsa_batch_config builtin_config() {
     c.lane_max_hits = kLaneMaxHitsCap;
     c.sort_variant = 0;
     c.chunk_reads = 1u << 19;
+    c.rescue_block_hits = kRescueBlockHitsDefault;
     return c;
 }
 
@@ -142,6 +143,7 @@ gbsa_batch_config tuned_config(int* from_file) {
     // the merge kernels' register budgets (a file written before they were tuned lacks them)
     x.lane_variant = parse_flat_json(t, "lane_variant", &v) ? (int32_t)v : 0;
     x.warp_variant = parse_flat_json(t, "warp_variant", &v) ? (int32_t)v : 0;
+    x.rescue_block_hits = parse_flat_json(t, "rescue_block_hits", &v) ? (uint32_t)v : kRescueBlockHitsDefault;
     if (!ok) return c;
     try {
         check_config(x);
@@ -180,6 +182,7 @@ void lane_init(gbsa_batcher& b, Lane& L) {
     L.m->cfg.sort_variant = b.cfg.sort_variant;
     L.m->cfg.lane_variant = b.cfg.lane_variant;
     L.m->cfg.warp_variant = b.cfg.warp_variant;
+    L.m->cfg.rescue_block_hits = b.cfg.rescue_block_hits;
     L.desc.resize(sizeof(BatchDesc));
     L.h_desc.resize(sizeof(BatchDesc));
     for (cudaEvent_t* e : {&L.done, &L.in_ready, &L.out_free})

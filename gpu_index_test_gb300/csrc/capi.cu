@@ -901,11 +901,11 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
                 m->cfg.sort_variant = bc.sort_variant;
                 m->cfg.lane_variant = bc.lane_variant;
                 m->cfg.warp_variant = bc.warp_variant;
+                // heavy rescued reads of small batches merged a block each (10k-100k-read
+                // batches of 150 bp pairs: about 0.3 of the batch time less)
+                m->cfg.rescue_block_hits = bc.rescue_block_hits;
             }
         }
-        // heavy rescued reads of small batches merged a block each (10k-100k-read batches
-        // of 150 bp pairs: about 0.3 of the batch time less; large batches unchanged)
-        m->cfg.rescue_block_hits = kRescueBlockHitsDefault;
         l2_window_attach(*m, true);
         m->max_reads = std::max<uint32_t>(max_reads, 1);
         m->max_bases = std::max<uint64_t>(max_bases, 1);

@@ -265,6 +265,8 @@ typedef struct gbsa_batch_config {
     int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
                                 1 six (80), 2 eight (64); fewer registers leave room for the rescued reads'
                                 sorts beside it */
+    uint32_t rescue_block_hits;  /* as gbsa_mapper_set_rescue_block (0: every rescued read by one warp) */
+    uint32_t _reserved;          /* 0 */
 } gbsa_batch_config;
 
 typedef struct gbsa_batcher gbsa_batcher;

@@ -38,12 +38,12 @@ def test_params_and_errors_without_gpu():
 
 
 def test_batch_config_layout_and_default_without_gpu():
-    """gbsa_batch_config is six 32-bit fields; the default is the committed tuned file
+    """gbsa_batch_config is eight 32-bit fields; the default is the committed tuned file
     when it is present and well formed (no GPU needed to read it)."""
     import json
     import os
 
-    assert C.sizeof(abi.BatchConfig) == 24
+    assert C.sizeof(abi.BatchConfig) == 32
     cfg, from_file = native.batch_config_default()
     path = os.path.join(os.path.dirname(native.GBSA_SO), "tuned.json")
     if os.path.exists(path):
@@ -51,6 +51,7 @@ def test_batch_config_layout_and_default_without_gpu():
         want = json.load(open(path))
         for k in ("seed_variant", "lane_max_hits", "sort_variant", "chunk_reads", "lane_variant", "warp_variant"):
             assert getattr(cfg, k) == want.get(k, 0), k
+        assert cfg.rescue_block_hits == want.get("rescue_block_hits", 4000)
     else:
         assert not from_file
     assert 0 <= cfg.seed_variant < abi.SEED_VARIANTS and 1 <= cfg.lane_max_hits <= 160
