@@ -115,7 +115,7 @@ void check_config(const gbsa_batch_config& c) {
         throw Error(GBSA_ERR_PARAM, "lane_max_hits must be in [1, 160]");
     if (c.sort_variant < 0 || c.sort_variant > 1) throw Error(GBSA_ERR_PARAM, "sort_variant must be 0 or 1");
     if (c.chunk_reads < 1024) throw Error(GBSA_ERR_PARAM, "chunk_reads must be at least 1024");
-    if (c.lane_variant < 0 || c.lane_variant > 3) throw Error(GBSA_ERR_PARAM, "lane_variant must be 0 to 3");
+    if (c.lane_variant < 0 || c.lane_variant > 4) throw Error(GBSA_ERR_PARAM, "lane_variant must be 0 to 4");
     if (c.warp_variant < 0 || c.warp_variant > 2) throw Error(GBSA_ERR_PARAM, "warp_variant must be 0, 1 or 2");
 }
 
@@ -167,6 +167,7 @@ struct gbsa_batcher {
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t caller_ev = nullptr;
     uint64_t graph_launches = 0, captures = 0, eager_runs = 0;
+    bool profile = false;
 };
 
 namespace gbsa {
@@ -183,6 +184,7 @@ void lane_init(gbsa_batcher& b, Lane& L) {
     L.m->cfg.lane_variant = b.cfg.lane_variant;
     L.m->cfg.warp_variant = b.cfg.warp_variant;
     L.m->cfg.rescue_block_hits = b.cfg.rescue_block_hits;
+    if (b.profile && gbsa_mapper_set_profile(L.m, 1) != GBSA_OK) throw Error(GBSA_ERR_CUDA, gbsa_last_error());
     L.desc.resize(sizeof(BatchDesc));
     L.h_desc.resize(sizeof(BatchDesc));
     for (cudaEvent_t* e : {&L.done, &L.in_ready, &L.out_free})
@@ -484,6 +486,32 @@ int gbsa_batcher_stats(const gbsa_batcher* b, uint64_t* graph_launches, uint64_t
     if (graph_launches) *graph_launches = b->graph_launches;
     if (captures) *captures = b->captures;
     if (eager_runs) *eager_runs = b->eager_runs;
+    return GBSA_OK;
+}
+
+int gbsa_batcher_set_profile(gbsa_batcher* b, int on) {
+    try {
+        b->profile = on != 0;
+        for (Lane& L : b->lanes) {
+            if (!L.m) continue;
+            GBSA_CUDA(cudaStreamSynchronize(L.m->st));
+            GBSA_CUDA(cudaStreamSynchronize(L.m->side));
+            if (gbsa_mapper_set_profile(L.m, on) != GBSA_OK) throw Error(GBSA_ERR_CUDA, gbsa_last_error());
+            drop_graph(L);   // the graph is captured anew, with (or without) the stage events
+        }
+        return GBSA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
+}
+
+int gbsa_batcher_stage_ms(const gbsa_batcher* b, float* ms, int n) {
+    if (b->lanes[0].m) return gbsa_mapper_stage_ms(b->lanes[0].m, ms, n);
+    for (int i = 0; i < n; ++i) ms[i] = 0.0f;
     return GBSA_OK;
 }
 

@@ -122,8 +122,8 @@ struct MapConfig {
     uint32_t lane_max_hits;
     int sort_variant;
     // register budgets of the NAM merge kernels (resident blocks they must fit):
-    // lane_variant 0 none, 1 six blocks, 2 eight (3: the open NAMs in registers,
-    // k_nams_lane_r); warp_variant 0 five, 1 six, 2 eight
+    // lane_variant 0 none, 1 six blocks, 2 eight (3, 4: the open NAMs in registers,
+    // k_nams_lane_r, at 168 / 128 registers); warp_variant 0 five, 1 six, 2 eight
     int lane_variant;
     int warp_variant;
     // rescued reads whose estimated merge hits (their seeds' runs up to the count cap)

@@ -762,7 +762,6 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks) k_nams_lane(MapCo
 // kLaneOpen slots, so the lanes of a warp stay together through a hit whatever their
 // open lists hold; shared memory holds only the final sort's entries.
 constexpr uint32_t kLaneEntriesR = 20;   // NAMs of a read sorted in shared memory (more: in place, in HBM)
-constexpr int kLaneBlocksPerSmR = 3;
 
 struct LaneSlots {
     // query start | query end << 12 | creation number << 24 (query coordinates are below
@@ -854,7 +853,10 @@ __device__ __forceinline__ uint64_t lane_sort_nams(const MapConfig& C, Sort& S, 
     return noff;
 }
 
-__global__ void __launch_bounds__(32 * kLaneWarps, kLaneBlocksPerSmR)
+// kMinBlocks: the register budget (3: 168 registers, no spills; 4: 128 registers, which
+// leaves room beside two blocks per SM for the rescue kernel's block).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
     k_nams_lane_r(MapConfig C, uint32_t n, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
     __shared__ LaneSortR S;
     __shared__ uint32_t s_cnt[kLaneBuckets];
@@ -2195,9 +2197,14 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
-    if (C.lane_variant == 3) {
-        const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * kLaneBlocksPerSmR);
-        k_nams_lane_r<<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+    if (C.lane_variant >= 3) {
+        // 3: three blocks per SM at 168 registers (the SM's registers: the rescue kernel
+        // starts as they retire); 4: two blocks per SM at 128 registers, beside the
+        // rescue kernel's block
+        const bool beside = C.lane_variant == 4;
+        const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * (beside ? 2u : 3u));
+        if (beside) k_nams_lane_r<4><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        else k_nams_lane_r<3><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
         GBSA_LAUNCHED();
         return;
     }

@@ -103,6 +103,8 @@ def lib():
             "gbsa_batcher_free": (None, [vp]),
             "gbsa_batcher_get_config": (i32, [vp, C.POINTER(abi.BatchConfig)]),
             "gbsa_batcher_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+            "gbsa_batcher_set_profile": (i32, [vp, i32]),
+            "gbsa_batcher_stage_ms": (i32, [vp, vp, i32]),
             "gbsa_batcher_map_device": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, u64, vp, vp, vp, C.POINTER(u64),
                                               vp]),
             "gbsa_batcher_map": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, u64, vp, vp, vp]),
@@ -496,6 +498,16 @@ class Batcher:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().gbsa_batcher_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return {"graph_launches": a.value, "captures": b.value, "eager_runs": c.value}
+
+    def set_profile(self, on=True):
+        """Stage events inside the batch graph (the graph is captured anew)."""
+        _check(lib().gbsa_batcher_set_profile(self.h, 1 if on else 0))
+
+    def stage_ms(self):
+        """Stage times of the last device-entry batch (fused seeding + lookup names)."""
+        a = np.zeros(7, np.float32)
+        lib().gbsa_batcher_stage_ms(self.h, a.ctypes.data, 7)
+        return dict(zip(Mapper.STAGES, a.tolist()))
 
     def map_reads(self, reads, items=None, capacity=None):
         """Host entry point; items (n_items + 1 read starts) may be None."""

@@ -261,7 +261,8 @@ typedef struct gbsa_batch_config {
     uint32_t chunk_reads;    /* reads per batch of the host entry point (three batches in flight) */
     int32_t  lane_variant;   /* the lane-per-read NAM merge: open NAMs in shared memory with a register
                                 budget of 0 no bound (96 registers), 1 six blocks (80), 2 eight (64); or
-                                3 open NAMs in registers (168 registers, three blocks per SM) */
+                                3 open NAMs in registers (168 registers, three blocks per SM), 4 the same
+                                at 128 registers and two blocks per SM (room for the rescue kernel) */
     int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
                                 1 six (80), 2 eight (64); fewer registers leave room for the rescued reads'
                                 sorts beside it */
@@ -290,6 +291,11 @@ void gbsa_batcher_free(gbsa_batcher* b);
 int gbsa_batcher_get_config(const gbsa_batcher* b, gbsa_batch_config* out);
 /* Graph launches, graph captures and batches run without a graph, since creation. */
 int gbsa_batcher_stats(const gbsa_batcher* b, uint64_t* graph_launches, uint64_t* captures, uint64_t* eager_runs);
+/* Stage timing of the batches (events inside the graph, captured anew when this changes)
+ * and the stage times of the last batch of the device entry point, as
+ * gbsa_mapper_set_profile / gbsa_mapper_stage_ms.  No reference counterpart. */
+int gbsa_batcher_set_profile(gbsa_batcher* b, int on);
+int gbsa_batcher_stage_ms(const gbsa_batcher* b, float* ms, int n);
 /* Device buffers, as gbsa_map_reads_device; d_items (device, n_items + 1 entries, from 0
  * to n_reads, non-decreasing) may be NULL.  The batch runs after the work queued on
  * stream so far and the call returns once it has ended (the NAM total is read back);
