@@ -349,7 +349,8 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     MapConfig C = m.cfg;
     C.count_bytes = m.count_bytes;
     auto mark = [&](int i) {
-        if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[i], st));
+        // (external: inside a stream capture the record becomes a node of the graph)
+        if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[i], st, cudaEventRecordExternal));
     };
     // Seeding and lookup run as one kernel (a warp seeds a read, then looks it up:
     // hashing overlaps the gathers) unless the index's entries exceed fuse_index_bytes:
@@ -395,9 +396,9 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     As.slots = m.side_slots.as<uint8_t>();
     launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, side);
     GBSA_CUDA(cudaEventRecord(m.rescue_ev, side));
-    if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[6], side));
+    if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[6], side, cudaEventRecordExternal));
     if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, side);
-    if (m.profile) GBSA_CUDA(cudaEventRecord(m.ev[7], side));
+    if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[7], side, cudaEventRecordExternal));
     GBSA_CUDA(cudaEventRecord(m.join_ev, side));
     launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(4);
