@@ -313,6 +313,15 @@ static void grow(DeviceBuffer& b, uint64_t& cap, uint64_t used, size_t elem) {
 // device counters and the NAM total are copied to m.h_status (pinned).  Nothing waits
 // on the host.
 
+// Records a stage-timing event; inside a stream capture as an external event node, so
+// that the graph's launches record it.
+void record_stage(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    GBSA_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusActive) GBSA_CUDA(cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal));
+    else GBSA_CUDA(cudaEventRecord(ev, st));
+}
+
 // Batched form (bm != nullptr): n is bm->cap, the read capacity of the work areas; the
 // batch itself (reads, count, work items, outputs) is read from bm->desc in device
 // memory by the kernels, so that the sequence can be captured once as a CUDA graph and
@@ -349,8 +358,7 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     MapConfig C = m.cfg;
     C.count_bytes = m.count_bytes;
     auto mark = [&](int i) {
-        // (external: inside a stream capture the record becomes a node of the graph)
-        if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[i], st, cudaEventRecordExternal));
+        if (m.profile) record_stage(m.ev[i], st);
     };
     // Seeding and lookup run as one kernel (a warp seeds a read, then looks it up:
     // hashing overlaps the gathers) unless the index's entries exceed fuse_index_bytes:
@@ -396,9 +404,9 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     As.slots = m.side_slots.as<uint8_t>();
     launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, side);
     GBSA_CUDA(cudaEventRecord(m.rescue_ev, side));
-    if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[6], side, cudaEventRecordExternal));
+    if (m.profile) record_stage(m.ev[6], side);
     if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, side);
-    if (m.profile) GBSA_CUDA(cudaEventRecordWithFlags(m.ev[7], side, cudaEventRecordExternal));
+    if (m.profile) record_stage(m.ev[7], side);
     GBSA_CUDA(cudaEventRecord(m.join_ev, side));
     launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(4);
