@@ -2194,9 +2194,35 @@ void launch_lookup(const IndexView& I, const MapConfig& C, uint32_t n, ReadRec* 
     GBSA_LAUNCHED();
 }
 
+// The NAM phase's kernels (lane and warp merges, rescue, NAM gather) run beside each
+// other and need most of an SM's shared memory together (rescue 73 KB + lane merge
+// 3 x 40 KB): they ask for the largest shared-memory carveout, so that the SM keeps that
+// configuration through the phase instead of switching it as each kernel's blocks
+// arrive (left to the driver, the lane merge took 5.0 instead of 3.3 ms on the C2 batch
+// inside the batch graph).  The seeding + lookup kernels keep the default: they use the
+// rest of the unified L1 to cache index entries.  Set once per device.
+void nam_phase_carveout() {
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    GBSA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (done[dev]) return;
+    const void* fs[] = {(const void*)k_nams_lane<0>, (const void*)k_nams_lane<6>, (const void*)k_nams_lane<8>,
+                        (const void*)k_nams_lane_r<3>, (const void*)k_nams_lane_r<4>,
+                        (const void*)k_nams<kHeavyBlocksPerSm>, (const void*)k_nams<6>, (const void*)k_nams<8>,
+                        (const void*)k_rescue, (const void*)k_gather_nams};
+    for (const void* f : fs)
+        GBSA_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
+    done[dev] = 1;
+}
+
 void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr,
                  cudaStream_t st) {
     if (!n) return;
+    nam_phase_carveout();
     if (C.lane_variant >= 3) {
         // 3: three blocks per SM at 168 registers (the SM's registers: the rescue kernel
         // starts as they retire); 4: two blocks per SM at 128 registers, beside the
@@ -2242,6 +2268,7 @@ void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Co
 void launch_rescue(const IndexView& I, const MapConfig& C, uint32_t n_reads, ReadRec* rec, Arenas A, Counters* ctr,
                    cudaStream_t st) {
     if (!n_reads) return;
+    nam_phase_carveout();
     // persistent, kRescueBlocksPerSm per SM (at most one scratch slot per warp)
     const unsigned blocks =
         std::min<unsigned>(warp_grid(n_reads, kWarpsPerBlock), (unsigned)device_sm_count() * kRescueBlocksPerSm);
