@@ -15,8 +15,8 @@
 // 3.3 MB, held by every GPU that loads the library until the process exits.
 //
 // Set-up: the first call on a device (with that device current) looks up the
-// array's device address with cudaGetSymbolAddress and caches it; make that first
-// call before any stream capture.  All calls share the array and it keeps the last
+// array's device address with cudaGetSymbolAddress and caches it.  All calls share
+// the array and it keeps the last
 // call's contents: the status words are cleared at the start of every call, and
 // calls that overlap on the GPU (different streams or threads running at the same
 // time) race on it.  Every call waits for its stream twice (it reads the total and

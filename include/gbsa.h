@@ -189,8 +189,8 @@ int gbsa_randstrobes_query(const gbsa_params* p, const char* seqs, const uint64_
  * queued on `stream`; the call allocates nothing.  Its only scratch is a file-scope
  * device array of about 3.3 MB (64 warp slots for reads of up to GBSA_MAX_READ_LEN
  * bases), held by every GPU that loads the library until the process exits.  The
- * first call on a device looks up that array's address (make it before any stream
- * capture); calls that overlap on the GPU race on the array.  Each call waits for
+ * first call on a device looks up that array's address; calls that overlap on the
+ * GPU race on the array.  Each call waits for
  * its stream before it returns (it reads the total back).  d_out_offsets has
  * n_reads + 1 entries and is always filled; *out_total receives the total; reads
  * longer than GBSA_MAX_READ_LEN give GBSA_ERR_READ_TOO_LONG and a total above
