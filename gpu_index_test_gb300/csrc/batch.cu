@@ -315,17 +315,85 @@ void batcher_warm_up(gbsa_batcher& b, uint32_t max_reads, double nams_per_read) 
     batcher_run_requests(b, &r, 1, &st, &tot);
 }
 
+// Copies the reads of k requests to the mapper's device inputs, one region per request
+// in request order: a request whose reads lie in one span of its buffer (gaps of at most
+// an eighth: the usual case, a request's reads back to back) is copied from there in one
+// transfer;
+// the others are gathered into pinned staging first.  Offsets are rebased to the device
+// layout.  (One span over all requests would be a host gather whenever the requests'
+// buffers lie apart: at saturation that gather took 5 ms per batch.)
+void stage_requests(gbsa_mapper& m, const ServeRequest* rq, uint32_t k, const uint32_t* first, uint32_t n,
+                    cudaStream_t st) {
+    struct Part {
+        uint64_t lo = 0, span = 0, total = 0, dst = 0, gather_at = 0;
+        bool direct = true;
+    };
+    std::vector<Part> parts(k);
+    host_parallel_tasks(k, [&](size_t j) {
+        const ServeRequest& r = rq[j];
+        uint64_t lo = UINT64_MAX, hi = 0, tot = 0;
+        for (uint32_t i = 0; i < r.n_reads; ++i) {
+            lo = std::min<uint64_t>(lo, r.offsets[i]);
+            hi = std::max<uint64_t>(hi, r.offsets[i] + r.lengths[i]);
+            tot += r.lengths[i];
+        }
+        Part& P = parts[j];
+        P.lo = r.n_reads ? lo : 0;
+        P.span = r.n_reads ? hi - lo : 0;
+        P.total = tot;
+        P.direct = P.span <= tot + (tot >> 3) + 4096;   // gaps small enough to copy along
+    });
+    uint64_t dst = 0, gathered = 0;
+    for (Part& P : parts) {
+        P.dst = dst;
+        dst = (dst + (P.direct ? P.span : P.total) + 15) & ~15ull;
+        if (!P.direct) {
+            P.gather_at = gathered;
+            gathered += P.total;
+        }
+    }
+    mapper_reserve(m, n, dst);
+    m.seqs.resize(dst + 64);
+    m.offs.resize(8ull * (n + 1));
+    m.lens.resize(4ull * (n + 1));
+    m.h_meta.resize(12ull * (n + 1));
+    if (gathered) m.h_seqs.resize(gathered + 1);
+    uint64_t* ho = m.h_meta.as<uint64_t>();
+    uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
+    char* hs = gathered ? m.h_seqs.as<char>() : nullptr;
+    host_parallel_tasks(k, [&](size_t j) {
+        const ServeRequest& r = rq[j];
+        const Part& P = parts[j];
+        uint64_t acc = 0;
+        for (uint32_t i = 0; i < r.n_reads; ++i) {
+            const uint32_t x = first[j] + i;
+            hl[x] = r.lengths[i];
+            if (P.direct) {
+                ho[x] = P.dst + r.offsets[i] - P.lo;
+            } else {
+                std::memcpy(hs + P.gather_at + acc, r.seqs + r.offsets[i], r.lengths[i]);
+                ho[x] = P.dst + acc;
+                acc += r.lengths[i];
+            }
+        }
+    });
+    uint8_t* d = m.seqs.as<uint8_t>();
+    for (uint32_t j = 0; j < k; ++j) {
+        const Part& P = parts[j];
+        if (P.direct && P.span)
+            GBSA_CUDA(cudaMemcpyAsync(d + P.dst, rq[j].seqs + P.lo, P.span, cudaMemcpyHostToDevice, st));
+        else if (!P.direct && P.total)
+            GBSA_CUDA(cudaMemcpyAsync(d + P.dst, hs + P.gather_at, P.total, cudaMemcpyHostToDevice, st));
+    }
+    GBSA_CUDA(cudaMemcpyAsync(m.offs.as<void>(), ho, 8ull * n, cudaMemcpyHostToDevice, st));
+    GBSA_CUDA(cudaMemcpyAsync(m.lens.as<void>(), hl, 4ull * n, cudaMemcpyHostToDevice, st));
+}
+
 void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, int* status, uint64_t* totals) {
     Lane& L = b.lanes[0];
     lane_init(b, L);
-    // the batch's reads: offsets relative to the lowest read address of all requests
     uint32_t n = 0;
-    uintptr_t base = UINTPTR_MAX;
-    for (uint32_t j = 0; j < k; ++j) {
-        n += rq[j].n_reads;
-        for (uint32_t i = 0; i < rq[j].n_reads; ++i)
-            base = std::min(base, reinterpret_cast<uintptr_t>(rq[j].seqs) + rq[j].offsets[i]);
-    }
+    for (uint32_t j = 0; j < k; ++j) n += rq[j].n_reads;
     if (n == 0) {
         for (uint32_t j = 0; j < k; ++j) {
             rq[j].nam_offsets[0] = 0;
@@ -336,19 +404,9 @@ void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, i
     }
     GBSA_CUDA(cudaEventSynchronize(L.done));
     lane_reserve(b, L, n);
-    L.h_items.resize(12ull * (n + 1));   // the batch's offsets (u64) and lengths (u32)
-    uint64_t* offs = L.h_items.as<uint64_t>();
-    uint32_t* lens = reinterpret_cast<uint32_t*>(offs + n + 1);
     std::vector<uint32_t> first(k + 1, 0);
     for (uint32_t j = 0; j < k; ++j) first[j + 1] = first[j] + rq[j].n_reads;
-    host_parallel_tasks(k, [&](size_t j) {
-        const uintptr_t s0 = reinterpret_cast<uintptr_t>(rq[j].seqs);
-        for (uint32_t i = 0; i < rq[j].n_reads; ++i) {
-            offs[first[j] + i] = s0 + rq[j].offsets[i] - base;
-            lens[first[j] + i] = rq[j].lengths[i];
-        }
-    });
-    stage_reads(*L.m, reinterpret_cast<const char*>(base), offs, lens, n, b.copy_in);
+    stage_requests(*L.m, rq, k, first.data(), n, b.copy_in);
     GBSA_CUDA(cudaEventRecord(L.in_ready, b.copy_in));
     GBSA_CUDA(cudaStreamWaitEvent(L.m->st, L.in_ready, 0));
     const uint64_t want = (uint64_t)(L.nams_per_read * 1.25 * n) + 1024;

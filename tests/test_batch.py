@@ -116,11 +116,19 @@ def test_batched_form_grows_its_work_areas():
         assert same(b.map_reads(reads, synth.read_items(rp)), ref)
 
 
+def _rows(req):
+    """A request's reads in the pool: (start, n) for a run, or an index array."""
+    start, n = req
+    return np.arange(start, start + n) if n is not None else np.asarray(start)
+
+
 def _serve(srv, pool, reqs):
     bufs = {}
-    for tag, (start, n) in enumerate(reqs):
-        offs = np.ascontiguousarray(pool.offsets[start:start + n])
-        lens = np.ascontiguousarray(pool.lengths[start:start + n])
+    for tag, req in enumerate(reqs):
+        rows = _rows(req)
+        n = len(rows)
+        offs = np.ascontiguousarray(pool.offsets[rows])
+        lens = np.ascontiguousarray(pool.lengths[rows])
         cap = 64 * n + 64
         out = (np.zeros(cap, abi.NAM), np.zeros(n + 1, np.uint64), np.zeros(max(1, n), np.float32),
                np.zeros(max(1, n), np.uint8))
@@ -148,16 +156,21 @@ def test_server_batches_requests_and_each_equals_alone():
         n = int(rng.integers(1, 400)) * 2
         reqs.append((int(rng.integers(0, (pool.n - n) // 2)) * 2, n))
     reqs.append((0, 0))   # an empty request
+    # requests whose reads lie far apart in the caller's buffer (gathered into staging)
+    for k in range(6):
+        reqs.insert(10 * k + 3, (np.sort(rng.choice(pool.n, 300, replace=False)), None))
     srv = native.Server(idx, workers=2, max_reads=16384)
     bufs, done = _serve(srv, pool, reqs)
     info = srv.info()
     srv.free()
     assert info["slots"] == 2 and info["requests"] == len(reqs) and info["batches"] < len(reqs)
     m = native.Mapper(idx)
-    for tag, (start, n) in enumerate(reqs):
+    for tag, req in enumerate(reqs):
         st, tot = done[tag]
         assert st == 0
-        alone = m.map_reads(pool.subset(np.arange(start, start + n)))
+        rows = _rows(req)
+        n = len(rows)
+        alone = m.map_reads(pool.subset(rows))
         offs, lens, (nams, noff, frac, resc) = bufs[tag]
         assert tot == len(alone[0]) and (noff == alone[1]).all()
         assert nams_equal(nams[:tot], alone[0])
