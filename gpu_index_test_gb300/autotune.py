@@ -8,7 +8,8 @@ Sweeps, over the C-ABI (gbsa_batcher_*):
   sort_variant   the block size of the sort of rescued reads with many NAMs
   lane_variant   the lane-per-read NAM merge: open NAMs in shared memory with a
                  register budget of 96, 80 or 64, or open NAMs in registers
-  warp_variant   the register budget of the warp-per-read NAM merge (96, 80 or 64)
+  warp_variant   the register budget of the warp-per-read NAM merge (96, 80 or 64) and its
+                 blocks per SM (5, or 4 beside the sorts)
 (the first three as a grid, then the two register budgets as a grid at the best of
 the first) on the repeat-rich mid-size configuration (150 bp pairs), the uneven length configuration
 (50-500 bp, single-end and pairs mixed) and a tenth of the human-scale one (repeat
@@ -37,7 +38,7 @@ from ._build_paths import GBSA_SO
 
 LANE_MAX_HITS = (64, 96, 128, 160)
 SORT_VARIANTS = (0, 1)
-REG_VARIANTS = (0, 1, 2)
+REG_VARIANTS = (0, 1, 2, 3, 4)   # warp merge: 3, 4 launched four blocks per SM
 LANE_VARIANTS = (0, 1, 2, 3, 4)   # 3, 4: the open NAMs in registers
 CHUNKS = (1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 

@@ -124,6 +124,7 @@ struct MapConfig {
     // register budgets of the NAM merge kernels (resident blocks they must fit):
     // lane_variant 0 none, 1 six blocks, 2 eight (3, 4: the open NAMs in registers,
     // k_nams_lane_r, at 168 / 128 registers); warp_variant 0 five, 1 six, 2 eight
+    // (3, 4: 96 / 80 registers launched four blocks per SM)
     int lane_variant;
     int warp_variant;
     // rescued reads whose estimated merge hits (their seeds' runs up to the count cap)

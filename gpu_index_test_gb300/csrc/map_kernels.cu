@@ -2254,11 +2254,14 @@ void launch_bucket_reads(uint32_t n, uint32_t lane_max_hits, ReadRec* rec, Arena
 
 void launch_nams_warp(const MapConfig& C, uint32_t n, ReadRec* rec, Arenas A, Counters* ctr, cudaStream_t st) {
     if (!n) return;
-    // at most nam_kernel_warps(n) warps: one scratch slot each
-    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * kHeavyGridPerSm,
+    // at most nam_kernel_warps(n) warps: one scratch slot each.  Variants 3 and 4 launch
+    // 4 blocks per SM (96 / 80 registers), leaving registers for the rescued reads' sorts
+    // beside them.
+    const unsigned per_sm = C.warp_variant >= 3 ? 4u : (unsigned)kHeavyGridPerSm;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)device_sm_count() * per_sm,
                                                          (n + kHeavyWarps - 1) / kHeavyWarps);
     switch (C.warp_variant) {
-        case 1: k_nams<6><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
+        case 1: case 4: k_nams<6><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
         case 2: k_nams<8><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
         default: k_nams<kHeavyBlocksPerSm><<<blocks, 32 * kHeavyWarps, 0, st>>>(C, rec, A, ctr); break;
     }

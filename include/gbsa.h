@@ -264,8 +264,9 @@ typedef struct gbsa_batch_config {
                                 3 open NAMs in registers (168 registers, three blocks per SM), 4 the same
                                 at 128 registers and two blocks per SM (room for the rescue kernel) */
     int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
-                                1 six (80), 2 eight (64); fewer registers leave room for the rescued reads'
-                                sorts beside it */
+                                1 six (80), 2 eight (64), launched 5 blocks per SM; 3 (96) and 4 (80)
+                                launched 4 blocks per SM; fewer registers leave room for the rescued
+                                reads' sorts beside it */
     uint32_t rescue_block_hits;  /* as gbsa_mapper_set_rescue_block (0: every rescued read by one warp) */
     uint32_t _reserved;          /* 0 */
 } gbsa_batch_config;
