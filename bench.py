@@ -644,6 +644,13 @@ def batched_measure(idx, reads, items, d_seq, d_off, d_len, plain_out, plain_ms,
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    # stage times inside the batch graph (events as graph nodes; one batch after the timing)
+    b.set_profile(True)
+    step()
+    step()
+    torch.cuda.synchronize()
+    stage = {k: round(v, 3) for k, v in b.stage_ms().items()}
+    b.set_profile(False)
     # e2e: host entry point, pinned reads in, NAMs / offsets / fractions / flags out
     h_seq = torch.from_numpy(reads.seq).pin_memory()
     h_nams = torch.empty(cap * 44, dtype=torch.uint8).pin_memory()
@@ -694,7 +701,7 @@ def batched_measure(idx, reads, items, d_seq, d_off, d_len, plain_out, plain_ms,
                 "from a device queue; NAM phase kernels in the same graph",
         "config": cfg, "config_source": "tuned.json (autotuner)" if tuned else "built-in",
         "device_reads_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 3),
-        "vs_plain_device": round(plain_ms / ms, 3),
+        "vs_plain_device": round(plain_ms / ms, 3), "stage_ms": stage,
         "e2e_reads_per_s": round(n / e2e_s, 1), "vs_plain_e2e": round(plain_e2e_s / e2e_s, 3),
         "small_batches": {"reads": k, "plain_ms": round(lat["plain"] * 1e3, 3),
                           "batched_ms": round(lat["batched"] * 1e3, 3),
