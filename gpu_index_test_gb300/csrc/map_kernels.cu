@@ -615,6 +615,82 @@ __global__ void k_bucket_reads(uint32_t n, uint32_t lane_max, const ReadRec* __r
     }
 }
 
+// Sorts a lane's n_closed NAMs (out[0..n_closed), written as they closed) by the NAM
+// order, stably, and returns the arena offset of the sorted list: for at most
+// Sort::kEntries NAMs on (first key word, index) entries in shared memory (full keys only
+// on a tie of the first word), then one pass writes the NAMs in order behind the unsorted
+// ones (out + H); more NAMs are insertion-sorted in place.  keys_ready: the entries were
+// written as the NAMs closed (else they are computed here from out).  The NAM loads of
+// the key pass and of the ordered copy are issued four at a time: each is a round trip
+// to L2 (out was just written), and one at a time they made the sort the lane merges'
+// largest cost.
+template <class Sort>
+__device__ __forceinline__ uint64_t lane_sort_nams(const MapConfig& C, Sort& S, uint32_t t, NamState* out,
+                                                   uint32_t n_closed, uint32_t H, uint64_t noff, bool keys_ready) {
+    if (n_closed <= Sort::kEntries) {
+        if (!keys_ready) {
+            uint32_t i = 0;
+            for (; i + 4 <= n_closed; i += 4) {
+                const NamState a = out[i], b = out[i + 1], c = out[i + 2], d = out[i + 3];
+                S.set_entry(i, t, nam_key(a, 0, C.sort_mode).k1, i);
+                S.set_entry(i + 1, t, nam_key(b, 0, C.sort_mode).k1, i + 1);
+                S.set_entry(i + 2, t, nam_key(c, 0, C.sort_mode).k1, i + 2);
+                S.set_entry(i + 3, t, nam_key(d, 0, C.sort_mode).k1, i + 3);
+            }
+            for (; i < n_closed; ++i) S.set_entry(i, t, nam_key(out[i], 0, C.sort_mode).k1, i);
+        }
+        for (uint32_t i = 1; i < n_closed; ++i) {
+            const uint64_t kx = S.key(i, t);
+            if (kx > S.key(i - 1, t)) continue;   // already in place
+            const uint32_t ix = S.index(i, t);
+            NamKey fx;
+            bool have_fx = false;
+            uint32_t j = i;
+            while (j > 0) {
+                const uint64_t ky = S.key(j - 1, t);
+                const uint32_t iy = S.index(j - 1, t);
+                bool less = kx < ky;
+                if (kx == ky) {
+                    if (!have_fx) {
+                        fx = nam_key(out[ix], 0, C.sort_mode);
+                        have_fx = true;
+                    }
+                    less = nam_key3_less(fx, nam_key(out[iy], 0, C.sort_mode));
+                }
+                if (!less) break;
+                S.set_entry(j, t, ky, iy);
+                --j;
+            }
+            S.set_entry(j, t, kx, ix);
+        }
+        NamState* sorted = out + H;
+        uint32_t i = 0;
+        for (; i + 4 <= n_closed; i += 4) {
+            const NamState a = out[S.index(i, t)], b = out[S.index(i + 1, t)], c = out[S.index(i + 2, t)],
+                           d = out[S.index(i + 3, t)];
+            sorted[i] = a;
+            sorted[i + 1] = b;
+            sorted[i + 2] = c;
+            sorted[i + 3] = d;
+        }
+        for (; i < n_closed; ++i) sorted[i] = out[S.index(i, t)];
+        return noff + H;
+    }
+    for (uint32_t i = 1; i < n_closed; ++i) {
+        const NamState x = out[i];
+        const NamKey kx = nam_key(x, 0, C.sort_mode);
+        uint32_t j = i;
+        while (j > 0) {
+            const NamState y = out[j - 1];
+            if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
+            out[j] = y;
+            --j;
+        }
+        out[j] = x;
+    }
+    return noff;
+}
+
 // kMinBlocks: resident blocks the compiler must leave room for (0: no bound); a smaller
 // register budget leaves room on the SM for the rescued reads' sorts beside it.
 template <int kMinBlocks>
@@ -699,55 +775,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks) k_nams_lane(MapCo
             continue;
         }
         for (uint32_t o = 0; o < n_open; ++o) out[n_closed++] = S.get(o, t);
-        // stable insertion sort by the NAM order
-        uint64_t first = noff;
-        if (n_closed <= LaneOpen::kEntries) {
-            // on (first key word, index) entries in shared memory, full keys only on a
-            // tie of the first word; then one pass writes the NAMs in order behind the
-            // unsorted ones (no NAM moves through memory while sorting)
-            for (uint32_t i = 0; i < n_closed; ++i) S.set_entry(i, t, nam_key(out[i], 0, C.sort_mode).k1, i);
-            for (uint32_t i = 1; i < n_closed; ++i) {
-                const uint64_t kx = S.key(i, t);
-                if (kx > S.key(i - 1, t)) continue;   // already in place
-                const uint32_t ix = S.index(i, t);
-                NamKey fx;
-                bool have_fx = false;
-                uint32_t j = i;
-                while (j > 0) {
-                    const uint64_t ky = S.key(j - 1, t);
-                    const uint32_t iy = S.index(j - 1, t);
-                    bool less = kx < ky;
-                    if (kx == ky) {
-                        if (!have_fx) {
-                            fx = nam_key(out[ix], 0, C.sort_mode);
-                            have_fx = true;
-                        }
-                        less = nam_key3_less(fx, nam_key(out[iy], 0, C.sort_mode));
-                    }
-                    if (!less) break;
-                    S.set_entry(j, t, ky, iy);
-                    --j;
-                }
-                S.set_entry(j, t, kx, ix);
-            }
-            NamState* sorted = out + H;
-            for (uint32_t i = 0; i < n_closed; ++i) sorted[i] = out[S.index(i, t)];
-            first = noff + H;
-        } else {
-            for (uint32_t i = 1; i < n_closed; ++i) {
-                const NamState x = out[i];
-                const NamKey kx = nam_key(x, 0, C.sort_mode);
-                uint32_t j = i;
-                while (j > 0) {
-                    const NamState y = out[j - 1];
-                    if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
-                    out[j] = y;
-                    --j;
-                }
-                out[j] = x;
-            }
-        }
-        R.nam_off = first;
+        // the lane's open-list words are free now: they hold the sort entries
+        R.nam_off = lane_sort_nams(C, S, t, out, n_closed, H, noff, false);
         R.n_nams = n_closed;
     }
 }
@@ -804,53 +833,12 @@ struct LaneSortR {
     }
 };
 
-template <class Sort>
-__device__ __forceinline__ uint64_t lane_sort_nams(const MapConfig& C, Sort& S, uint32_t t, NamState* out,
-                                                   uint32_t n_closed, uint32_t H, uint64_t noff) {
-    // stable insertion sort by the NAM order (as k_nams_lane)
-    if (n_closed <= Sort::kEntries) {
-        for (uint32_t i = 0; i < n_closed; ++i) S.set_entry(i, t, nam_key(out[i], 0, C.sort_mode).k1, i);
-        for (uint32_t i = 1; i < n_closed; ++i) {
-            const uint64_t kx = S.key(i, t);
-            if (kx > S.key(i - 1, t)) continue;
-            const uint32_t ix = S.index(i, t);
-            NamKey fx;
-            bool have_fx = false;
-            uint32_t j = i;
-            while (j > 0) {
-                const uint64_t ky = S.key(j - 1, t);
-                const uint32_t iy = S.index(j - 1, t);
-                bool less = kx < ky;
-                if (kx == ky) {
-                    if (!have_fx) {
-                        fx = nam_key(out[ix], 0, C.sort_mode);
-                        have_fx = true;
-                    }
-                    less = nam_key3_less(fx, nam_key(out[iy], 0, C.sort_mode));
-                }
-                if (!less) break;
-                S.set_entry(j, t, ky, iy);
-                --j;
-            }
-            S.set_entry(j, t, kx, ix);
-        }
-        NamState* sorted = out + H;
-        for (uint32_t i = 0; i < n_closed; ++i) sorted[i] = out[S.index(i, t)];
-        return noff + H;
-    }
-    for (uint32_t i = 1; i < n_closed; ++i) {
-        const NamState x = out[i];
-        const NamKey kx = nam_key(x, 0, C.sort_mode);
-        uint32_t j = i;
-        while (j > 0) {
-            const NamState y = out[j - 1];
-            if (!nam_key3_less(kx, nam_key(y, 0, C.sort_mode))) break;
-            out[j] = y;
-            --j;
-        }
-        out[j] = x;
-    }
-    return noff;
+// Writes a closing NAM to the lane's list and, while the list fits the shared-memory
+// sort, its sort entry (its first key word, computed from registers).
+__device__ __forceinline__ void lane_close_r(const MapConfig& C, LaneSortR& S, uint32_t t, NamState* out,
+                                             uint32_t& n_closed, const NamState& m) {
+    if (n_closed < LaneSortR::kEntries) S.set_entry(n_closed, t, nam_key(m, 0, C.sort_mode).k1, n_closed);
+    out[n_closed++] = m;
 }
 
 // kMinBlocks: the register budget (3: 168 registers, no spills; 4: 128 registers, which
@@ -894,7 +882,7 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
 #pragma unroll
                 for (uint32_t o = 0; o < kLaneOpen; ++o)
                     if (L.seq(o) != LaneSlots::kFree) {
-                        out[n_closed++] = L.get(o);
+                        lane_close_r(C, S, t, out, n_closed, L.get(o));
                         L.free_slot(o);
                     }
                 n_open = 0;
@@ -931,7 +919,7 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
 #pragma unroll
                 for (uint32_t o = 0; o < kLaneOpen; ++o)
                     if (L.seq(o) != LaneSlots::kFree && L.qe(o) < x.qs) {
-                        out[n_closed++] = L.get(o);
+                        lane_close_r(C, S, t, out, n_closed, L.get(o));
                         L.free_slot(o);
                         --n_open;
                     }
@@ -961,8 +949,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
         }
 #pragma unroll
         for (uint32_t o = 0; o < kLaneOpen; ++o)
-            if (L.seq(o) != LaneSlots::kFree) out[n_closed++] = L.get(o);
-        R.nam_off = lane_sort_nams(C, S, t, out, n_closed, H, noff);
+            if (L.seq(o) != LaneSlots::kFree) lane_close_r(C, S, t, out, n_closed, L.get(o));
+        R.nam_off = lane_sort_nams(C, S, t, out, n_closed, H, noff, n_closed <= LaneSortR::kEntries);
         R.n_nams = n_closed;
     }
 }
