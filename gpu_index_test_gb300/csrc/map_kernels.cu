@@ -621,9 +621,8 @@ __global__ void k_bucket_reads(uint32_t n, uint32_t lane_max, const ReadRec* __r
 // on a tie of the first word), then one pass writes the NAMs in order behind the unsorted
 // ones (out + H); more NAMs are insertion-sorted in place.  keys_ready: the entries were
 // written as the NAMs closed (else they are computed here from out).  The NAM loads of
-// the key pass and of the ordered copy are issued four at a time: each is a round trip
-// to L2 (out was just written), and one at a time they made the sort the lane merges'
-// largest cost.
+// the key pass and of the ordered copy are issued four at a time (each is a round trip
+// to L2: out was just written).
 template <class Sort>
 __device__ __forceinline__ uint64_t lane_sort_nams(const MapConfig& C, Sort& S, uint32_t t, NamState* out,
                                                    uint32_t n_closed, uint32_t H, uint64_t noff, bool keys_ready) {
