@@ -39,7 +39,7 @@ from ._build_paths import GBSA_SO
 LANE_MAX_HITS = (64, 96, 128, 160)
 SORT_VARIANTS = (0, 1)
 REG_VARIANTS = (0, 1, 2, 3, 4)   # warp merge: 3, 4 launched four blocks per SM
-LANE_VARIANTS = (0, 1, 2, 3, 4)   # 3, 4: the open NAMs in registers
+LANE_VARIANTS = (0, 1, 2, 3, 4, 5, 6)   # 3-6: the open NAMs in registers
 CHUNKS = (1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20)
 
 

@@ -122,8 +122,9 @@ struct MapConfig {
     uint32_t lane_max_hits;
     int sort_variant;
     // register budgets of the NAM merge kernels (resident blocks they must fit):
-    // lane_variant 0 none, 1 six blocks, 2 eight (3, 4: the open NAMs in registers,
-    // k_nams_lane_r, at 168 / 128 registers); warp_variant 0 five, 1 six, 2 eight
+    // lane_variant 0 none, 1 six blocks, 2 eight (3-6: the open NAMs in registers,
+    // k_nams_lane_r: 10 slots at 168 / 128 registers, 6 slots at 96 / 124); warp_variant
+    // 0 five, 1 six, 2 eight
     // (3, 4: 96 / 80 registers launched four blocks per SM)
     int lane_variant;
     int warp_variant;

@@ -791,14 +791,15 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks) k_nams_lane(MapCo
 // open lists hold; shared memory holds only the final sort's entries.
 constexpr uint32_t kLaneEntriesR = 20;   // NAMs of a read sorted in shared memory (more: in place, in HBM)
 
+template <uint32_t kSlots>
 struct LaneSlots {
     // query start | query end << 12 | creation number << 24 (query coordinates are below
     // GBSA_MAX_READ_LEN = 4096, creation numbers below kLaneMaxHitsCap + 1); creation
     // number kFree: the slot is free
-    uint32_t qse[kLaneOpen];
-    uint32_t qpn[kLaneOpen];   // previous hit's query start | n_hits << 16
-    int32_t rs[kLaneOpen], re[kLaneOpen], rprev[kLaneOpen];
-    uint32_t ref[kLaneOpen];
+    uint32_t qse[kSlots];
+    uint32_t qpn[kSlots];   // previous hit's query start | n_hits << 16
+    int32_t rs[kSlots], re[kSlots], rprev[kSlots];
+    uint32_t ref[kSlots];
     static constexpr uint32_t kFree = 0xFFu;
     __device__ __forceinline__ uint32_t seq(uint32_t o) const { return qse[o] >> 24; }
     __device__ __forceinline__ int32_t qe(uint32_t o) const { return (int32_t)((qse[o] >> 12) & 0xFFFu); }
@@ -841,8 +842,10 @@ __device__ __forceinline__ void lane_close_r(const MapConfig& C, LaneSortR& S, u
 }
 
 // kMinBlocks: the register budget (3: 168 registers, no spills; 4: 128 registers, which
-// leaves room beside two blocks per SM for the rescue kernel's block).
-template <int kMinBlocks>
+// leaves room beside two blocks per SM for the rescue kernel's block; 5 with 6 slots: 96
+// registers, three blocks per SM beside the rescue kernel's block).  kSlots: open NAMs
+// per lane (reads that need more go to the warp kernel).
+template <int kMinBlocks, uint32_t kSlots>
 __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
     k_nams_lane_r(MapConfig C, uint32_t n, ReadRec* __restrict__ rec, Arenas A, Counters* ctr) {
     __shared__ LaneSortR S;
@@ -867,9 +870,9 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
         }
         const HitPacked* hits = A.hits + R.hit_off;
         NamState* out = A.nams + noff;
-        LaneSlots L;
+        LaneSlots<kSlots> L;
 #pragma unroll
-        for (uint32_t o = 0; o < kLaneOpen; ++o) L.qse[o] = LaneSlots::kFree << 24;
+        for (uint32_t o = 0; o < kSlots; ++o) L.qse[o] = LaneSlots<kSlots>::kFree << 24;
         uint32_t n_open = 0, n_closed = 0, cur_dir = 0, next_seq = 0;
         bool overflow = false;
         HitRec nx = load_hit(hits, 0, H);
@@ -879,8 +882,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
             const uint32_t dir = x.ref_rc >> 31;
             if (dir != cur_dir) {   // the other orientation's NAMs can take no more hits
 #pragma unroll
-                for (uint32_t o = 0; o < kLaneOpen; ++o)
-                    if (L.seq(o) != LaneSlots::kFree) {
+                for (uint32_t o = 0; o < kSlots; ++o)
+                    if (L.seq(o) != LaneSlots<kSlots>::kFree) {
                         lane_close_r(C, S, t, out, n_closed, L.get(o));
                         L.free_slot(o);
                     }
@@ -888,9 +891,9 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
                 cur_dir = dir;
             }
             // the accepting NAM created first (free slots have the largest number)
-            uint32_t best = kLaneOpen, bseq = LaneSlots::kFree;
+            uint32_t best = kSlots, bseq = LaneSlots<kSlots>::kFree;
 #pragma unroll
-            for (uint32_t o = 0; o < kLaneOpen; ++o) {
+            for (uint32_t o = 0; o < kSlots; ++o) {
                 const int32_t sqe = L.qe(o);
                 const int32_t sqp = (int32_t)(L.qpn[o] & 0xFFFFu);
                 bool ok = L.ref[o] == x.ref_rc && sqp < x.qs && x.qs <= sqe && L.rprev[o] < x.rs && x.rs <= L.re[o];
@@ -900,9 +903,9 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
                     best = o;
                 }
             }
-            if (best < kLaneOpen) {
+            if (best < kSlots) {
 #pragma unroll
-                for (uint32_t o = 0; o < kLaneOpen; ++o) {
+                for (uint32_t o = 0; o < kSlots; ++o) {
                     if (o != best) continue;
                     if (x.qe > L.qe(o) && x.re > L.re[o]) {
                         L.qse[o] = (L.qse[o] & 0xFF000FFFu) | ((uint32_t)x.qe << 12);
@@ -913,24 +916,24 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
                 }
                 continue;
             }
-            if (n_open == kLaneOpen) {
+            if (n_open == kSlots) {
                 // close NAMs the current query start has passed
 #pragma unroll
-                for (uint32_t o = 0; o < kLaneOpen; ++o)
-                    if (L.seq(o) != LaneSlots::kFree && L.qe(o) < x.qs) {
+                for (uint32_t o = 0; o < kSlots; ++o)
+                    if (L.seq(o) != LaneSlots<kSlots>::kFree && L.qe(o) < x.qs) {
                         lane_close_r(C, S, t, out, n_closed, L.get(o));
                         L.free_slot(o);
                         --n_open;
                     }
-                if (n_open == kLaneOpen) {
+                if (n_open == kSlots) {
                     overflow = true;
                     break;
                 }
             }
             bool placed = false;
 #pragma unroll
-            for (uint32_t o = 0; o < kLaneOpen; ++o) {
-                if (placed || L.seq(o) != LaneSlots::kFree) continue;
+            for (uint32_t o = 0; o < kSlots; ++o) {
+                if (placed || L.seq(o) != LaneSlots<kSlots>::kFree) continue;
                 L.qse[o] = (uint32_t)x.qs | ((uint32_t)x.qe << 12) | (next_seq << 24);
                 L.qpn[o] = (uint32_t)x.qs | (1u << 16);
                 L.rs[o] = x.rs;
@@ -947,8 +950,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, kMinBlocks)
             continue;
         }
 #pragma unroll
-        for (uint32_t o = 0; o < kLaneOpen; ++o)
-            if (L.seq(o) != LaneSlots::kFree) lane_close_r(C, S, t, out, n_closed, L.get(o));
+        for (uint32_t o = 0; o < kSlots; ++o)
+            if (L.seq(o) != LaneSlots<kSlots>::kFree) lane_close_r(C, S, t, out, n_closed, L.get(o));
         R.nam_off = lane_sort_nams(C, S, t, out, n_closed, H, noff, n_closed <= LaneSortR::kEntries);
         R.n_nams = n_closed;
     }
@@ -2197,7 +2200,8 @@ void nam_phase_carveout() {
     if ((int)done.size() <= dev) done.resize(dev + 1, 0);
     if (done[dev]) return;
     const void* fs[] = {(const void*)k_nams_lane<0>, (const void*)k_nams_lane<6>, (const void*)k_nams_lane<8>,
-                        (const void*)k_nams_lane_r<3>, (const void*)k_nams_lane_r<4>,
+                        (const void*)k_nams_lane_r<3, kLaneOpen>, (const void*)k_nams_lane_r<4, kLaneOpen>,
+                        (const void*)k_nams_lane_r<5, 6>, (const void*)k_nams_lane_r<3, 6>,
                         (const void*)k_nams<kHeavyBlocksPerSm>, (const void*)k_nams<6>, (const void*)k_nams<8>,
                         (const void*)k_rescue, (const void*)k_gather_nams};
     for (const void* f : fs)
@@ -2213,11 +2217,14 @@ void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec,
     if (C.lane_variant >= 3) {
         // 3: three blocks per SM at 168 registers (the SM's registers: the rescue kernel
         // starts as they retire); 4: two blocks per SM at 128 registers, beside the
-        // rescue kernel's block
-        const bool beside = C.lane_variant == 4;
-        const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * (beside ? 2u : 3u));
-        if (beside) k_nams_lane_r<4><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
-        else k_nams_lane_r<3><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        // rescue kernel's block; 5: six slots, three blocks per SM at 96 registers, beside it
+        // 6: six slots at 124 registers, two blocks per SM beside the rescue kernel's block
+        const unsigned per_sm = C.lane_variant == 4 || C.lane_variant == 6 ? 2u : 3u;
+        const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * per_sm);
+        if (C.lane_variant == 4) k_nams_lane_r<4, kLaneOpen><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        else if (C.lane_variant == 5) k_nams_lane_r<5, 6><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        else if (C.lane_variant == 6) k_nams_lane_r<3, 6><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
+        else k_nams_lane_r<3, kLaneOpen><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
         GBSA_LAUNCHED();
         return;
     }

@@ -262,7 +262,9 @@ typedef struct gbsa_batch_config {
     int32_t  lane_variant;   /* the lane-per-read NAM merge: open NAMs in shared memory with a register
                                 budget of 0 no bound (96 registers), 1 six blocks (80), 2 eight (64); or
                                 3 open NAMs in registers (168 registers, three blocks per SM), 4 the same
-                                at 128 registers and two blocks per SM (room for the rescue kernel) */
+                                at 128 registers and two blocks per SM (room for the rescue kernel);
+                                5, 6 six open NAMs per lane in registers (reads needing more go to the warp
+                                merge) at 96 registers and three blocks per SM, or 124 and two */
     int32_t  warp_variant;   /* register budget of the warp-per-read NAM merge: 0 five blocks (96 registers),
                                 1 six (80), 2 eight (64), launched 5 blocks per SM; 3 (96) and 4 (80)
                                 launched 4 blocks per SM; fewer registers leave room for the rescued

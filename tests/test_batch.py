@@ -53,9 +53,9 @@ def test_every_tuned_variant_is_bit_exact(c3, variant):
     form's output."""
     g, reads, items, idx, o = c3
     ref = native.Mapper(idx).map_reads(reads)
-    regs = ((0, 0), (1, 1), (2, 2), (3, 3), (4, 4), (0, 3))
+    regs = ((0, 0), (1, 1), (2, 2), (3, 3), (4, 4), (5, 3), (6, 0))
     for j, (lane_max, sort_variant) in enumerate(((160, 0), (64, 1), (96, 0), (128, 1))):
-        lv, wv = regs[(j + variant) % 6]
+        lv, wv = regs[(j + variant) % 7]
         cfg = abi.batch_config(variant, lane_max, sort_variant, 4096, lv, wv)
         b = native.Batcher(idx, config=cfg, max_reads=reads.n)
         assert same(b.map_reads(reads, items), ref)   # several chunks of ~4096 reads, three sets of work areas
