@@ -188,6 +188,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     pm.free()
     npr = max(24, int(np.ceil(len(plain[0]) / pool.n * 2.5)))
     srv = native.Server(idx, workers=slots, max_reads=batch_reads, max_bases=batch_reads * 250)
+    g0 = srv.stats()
     n_slots, slot_nams = 48, max_reads * npr
     plain_bytes = np.ascontiguousarray(plain[0]).view(np.uint8)
     plain_off = np.ascontiguousarray(plain[1]).astype(np.int64)
@@ -289,6 +290,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
             "bit_exact_vs_plain": bool(exact and failed == 0),
         })
     info = srv.info()
+    growth = srv.stats()
     srv.free()
     ok = [r for r in results if r["p99_ms"] is not None and r["p99_ms"] < 20.0 and r["bit_exact_vs_plain"]]
     sat = max(ok, key=lambda r: r["reads_per_s"]) if ok else None
@@ -298,6 +300,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     sat10 = max(ok10, key=lambda r: r["reads_per_s"]) if ok10 else None
     # the same requests' sizes, mapped one by one on 10k-read requests: p99 target is for them
     return {"index": index_name, "slots": info["slots"], "slot_bytes": info["slot_bytes"],
+            "graph_during_requests": {k: growth[k] - g0[k] for k in growth},
             "memory_budget_bytes": info["budget"], "batch_reads": batch_reads,
             "request_reads": "1k-100k log-uniform, 100-250 bp pairs", "rates": results,
             "saturation": ({"rate_req_s": sat["rate_req_s"], "reads_per_s": sat["reads_per_s"], "p99_ms": sat["p99_ms"]}

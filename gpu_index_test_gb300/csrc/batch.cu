@@ -295,6 +295,15 @@ void batcher_warm_up(gbsa_batcher& b, uint32_t max_reads, double nams_per_read) 
         L.out_nams.resize(sizeof(gbsa_nam) * want);
         L.out_cap = want;
     }
+    // rescue scratch for the heavy rescued reads of a full batch (repeat-rich genomes use
+    // about 1 KB per read of the batch; a batch that outgrows it grows it, which frees
+    // device memory and so waits for every other slot's work)
+    const uint64_t ovf_want = std::max<uint64_t>(64ull << 20, 4096ull * max_reads);
+    if (L.m->ovf_cap < ovf_want) {
+        L.m->ovf.release();
+        L.m->ovf.resize(ovf_want);
+        L.m->ovf_cap = ovf_want;
+    }
     // one batch of pseudo-random 150 bp reads runs eagerly and captures the graph
     const uint32_t n = std::min<uint32_t>(1024, max_reads), len = 150;
     std::vector<char> seq((size_t)n * len);

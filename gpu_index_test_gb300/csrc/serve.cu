@@ -201,6 +201,21 @@ int gbsa_server_info(const gbsa_server* s, uint32_t* slots, uint64_t* slot_bytes
     return GBSA_OK;
 }
 
+int gbsa_server_stats(const gbsa_server* s, uint64_t* graph_launches, uint64_t* captures, uint64_t* eager_runs) {
+    uint64_t g = 0, c = 0, e = 0;
+    for (gbsa_batcher* b : s->slots) {
+        uint64_t x = 0, y = 0, z = 0;
+        gbsa_batcher_stats(b, &x, &y, &z);
+        g += x;
+        c += y;
+        e += z;
+    }
+    if (graph_launches) *graph_launches = g;
+    if (captures) *captures = c;
+    if (eager_runs) *eager_runs = e;
+    return GBSA_OK;
+}
+
 int gbsa_server_submit(gbsa_server* s, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
                        uint32_t n_reads, gbsa_nam* nams, uint64_t nam_capacity, uint64_t* nam_offsets, float* frac,
                        uint8_t* rescued, uint64_t tag) {

@@ -74,6 +74,7 @@ def lib():
             "gbsa_server_create_ex": (i32, [vp, vp, C.POINTER(abi.ServerConfig), vp]),
             "gbsa_server_info": (i32, [vp, C.POINTER(u32), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64),
                                        C.POINTER(u64)]),
+            "gbsa_server_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
             "gbsa_server_free": (None, [vp]),
@@ -554,6 +555,12 @@ class Server:
         h = C.c_void_p()
         _check(lib().gbsa_server_create_ex(index.h, C.byref(self.opt), C.byref(cfg), C.byref(h)))
         self.h = h
+
+    def stats(self):
+        """Graph launches, captures and eager batches over all slots since creation."""
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().gbsa_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"graph_launches": a.value, "captures": b.value, "eager_runs": c.value}
 
     def info(self):
         a, b, c, d, e = C.c_uint32(), C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -369,6 +369,10 @@ int gbsa_server_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
 /* Slots created, device bytes of one slot, the budget, and batches / requests mapped. */
 int gbsa_server_info(const gbsa_server* s, uint32_t* slots, uint64_t* slot_bytes, uint64_t* budget,
                      uint64_t* batches, uint64_t* requests);
+/* Graph launches, graph captures and batches run without a graph (the first batch of a
+ * slot, and one that outgrew its work areas, which frees and allocates device memory)
+ * over all slots since creation.  No reference counterpart. */
+int gbsa_server_stats(const gbsa_server* s, uint64_t* graph_launches, uint64_t* captures, uint64_t* eager_runs);
 int gbsa_server_submit(gbsa_server* s, const char* seqs, const uint64_t* offsets,
                        const uint32_t* lengths, uint32_t n_reads, gbsa_nam* nams,
                        uint64_t nam_capacity, uint64_t* nam_offsets, float* frac,
