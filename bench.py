@@ -44,9 +44,10 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rates", default="1000,2000,3000,4000,5000,6000,8000",
+    ap.add_argument("--serve-rates", default="1000,2000,2500,3000,3500,4000,6000",
                     help="request rates (req/s) of the served-form measurement; empty to skip")
-    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="arrival window per rate (4 s: ~8-16k requests, enough for a stable p99)")
     ap.add_argument("--no-fastq", dest="fastq", action="store_false", help="skip the FASTQ staging measurement")
     ap.add_argument("--no-l2-window", dest="l2_window", action="store_false",
                     help="map without the L2 access-policy window on the bucket table (for comparison)")
