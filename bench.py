@@ -221,6 +221,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
         for i in range(n_slots):
             free.put(i)
         meta = {}
+        t_sub = {}
         info0 = srv.info()
         t0 = time.perf_counter() + 0.05
 
@@ -234,6 +235,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
                 lens = np.ascontiguousarray(pool.lengths[start:start + n])
                 meta[tag] = (slot, start, n, offs, lens)
                 b = bufs[slot]
+                t_sub[tag] = time.perf_counter()
                 srv.submit(seq_ptr, offs.ctypes.data, lens.ctypes.data, n, b[0].data_ptr(), slot_nams,
                            b[1].data_ptr(), b[2].data_ptr(), b[3].data_ptr(), tag)
 
@@ -251,7 +253,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
 
         th = threading.Thread(target=submitter)
         th.start()
-        lat, lat_n, reads_done, failed = [], [], 0, 0
+        lat, lat_n, lat_srv, reads_done, failed = [], [], [], 0, 0
         checks = []
         t_last = t0
         with ThreadPoolExecutor(max_workers=12) as ex:
@@ -264,6 +266,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
                         free.put(slot)
                         continue
                     lat.append(now - (t0 + arrivals[tag][0]))
+                    lat_srv.append(now - t_sub[tag])
                     lat_n.append(n)
                     reads_done += n
                     t_last = max(t_last, now)
@@ -281,6 +284,10 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
             "p50_ms": round(float(lat_ms[len(lat_ms) // 2]), 2) if len(lat_ms) else None,
             "p99_ms": round(float(lat_ms[min(len(lat_ms) - 1, int(len(lat_ms) * 0.99))]), 2) if len(lat_ms) else None,
             "max_ms": round(float(lat_ms[-1]), 2) if len(lat_ms) else None,
+            # from the client's submit call (the client's own delay behind the schedule left out)
+            "p99_ms_from_submit": round(float(np.percentile(np.array(lat_srv) * 1e3, 99)), 2) if lat_srv else None,
+            "p99_submit_delay_ms": round(float(np.percentile(
+                [(t_sub[i] - t0 - arrivals[i][0]) * 1e3 for i in t_sub], 99)), 2) if t_sub else None,
             "requests_le_10k_reads": int(len(small)),
             "p50_ms_le_10k_reads": round(float(small[len(small) // 2]), 2) if len(small) else None,
             "p99_ms_le_10k_reads": round(float(small[min(len(small) - 1, int(len(small) * 0.99))]), 2)
