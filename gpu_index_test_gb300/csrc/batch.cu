@@ -59,6 +59,7 @@ struct Lane {
     PinnedBuffer h_items;
     uint64_t out_cap = 0;
     cudaEvent_t done = nullptr, in_ready = nullptr, out_free = nullptr;
+    cudaEvent_t wait_ev = nullptr;   // blocking-sync event: the host thread sleeps while it waits
     double nams_per_read = 16.0;
     bool async = false;            // the last batch was launched as a graph and not yet checked
 };
@@ -189,6 +190,14 @@ void lane_init(gbsa_batcher& b, Lane& L) {
     L.h_desc.resize(sizeof(BatchDesc));
     for (cudaEvent_t* e : {&L.done, &L.in_ready, &L.out_free})
         GBSA_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    GBSA_CUDA(cudaEventCreateWithFlags(&L.wait_ev, cudaEventDisableTiming | cudaEventBlockingSync));
+}
+
+// Waits for the work queued on st so far without spinning: a server runs a host thread per
+// slot, and threads spinning in cudaStreamSynchronize took the cores that submit requests.
+void wait_blocking(Lane& L, cudaStream_t st) {
+    GBSA_CUDA(cudaEventRecord(L.wait_ev, st));
+    GBSA_CUDA(cudaEventSynchronize(L.wait_ev));
 }
 
 void drop_graph(Lane& L) {
@@ -267,7 +276,7 @@ bool graph_ready(const Lane& L) { return L.exec && L.key == graph_key(*L.m); }
 uint64_t run_sync(gbsa_batcher& b, Lane& L, const BatchDesc& d) {
     if (graph_ready(L)) {
         launch_graph(b, L, d);
-        GBSA_CUDA(cudaStreamSynchronize(L.m->st));
+        wait_blocking(L, L.m->st);
         L.async = false;
         if (check_batch(*L.m, false)) return batch_total(*L.m);
         drop_graph(L);
@@ -337,8 +346,10 @@ void stage_requests(gbsa_mapper& m, const ServeRequest* rq, uint32_t k, const ui
         uint64_t lo = 0, span = 0, total = 0, dst = 0, gather_at = 0;
         bool direct = true;
     };
+    // (on the slot's own thread: the host pool runs one job at a time, and slots would
+    // queue behind one another for work this small)
     std::vector<Part> parts(k);
-    host_parallel_tasks(k, [&](size_t j) {
+    for (uint32_t j = 0; j < k; ++j) {
         const ServeRequest& r = rq[j];
         uint64_t lo = UINT64_MAX, hi = 0, tot = 0;
         for (uint32_t i = 0; i < r.n_reads; ++i) {
@@ -351,7 +362,7 @@ void stage_requests(gbsa_mapper& m, const ServeRequest* rq, uint32_t k, const ui
         P.span = r.n_reads ? hi - lo : 0;
         P.total = tot;
         P.direct = P.span <= tot + (tot >> 3) + 4096;   // gaps small enough to copy along
-    });
+    }
     uint64_t dst = 0, gathered = 0;
     for (Part& P : parts) {
         P.dst = dst;
@@ -370,7 +381,7 @@ void stage_requests(gbsa_mapper& m, const ServeRequest* rq, uint32_t k, const ui
     uint64_t* ho = m.h_meta.as<uint64_t>();
     uint32_t* hl = reinterpret_cast<uint32_t*>(ho + n + 1);
     char* hs = gathered ? m.h_seqs.as<char>() : nullptr;
-    host_parallel_tasks(k, [&](size_t j) {
+    for (uint32_t j = 0; j < k; ++j) {
         const ServeRequest& r = rq[j];
         const Part& P = parts[j];
         uint64_t acc = 0;
@@ -385,7 +396,7 @@ void stage_requests(gbsa_mapper& m, const ServeRequest* rq, uint32_t k, const ui
                 acc += r.lengths[i];
             }
         }
-    });
+    }
     uint8_t* d = m.seqs.as<uint8_t>();
     for (uint32_t j = 0; j < k; ++j) {
         const Part& P = parts[j];
@@ -453,7 +464,7 @@ void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, i
     L.h_desc.resize(sizeof(BatchDesc) + 8ull * (n + 1));
     uint64_t* h_off = reinterpret_cast<uint64_t*>(L.h_desc.as<uint8_t>() + sizeof(BatchDesc));
     GBSA_CUDA(cudaMemcpyAsync(h_off, L.out_off.as<void>(), 8ull * (n + 1), cudaMemcpyDeviceToHost, st));
-    GBSA_CUDA(cudaStreamSynchronize(st));
+    wait_blocking(L, st);
     for (uint32_t j = 0; j < k; ++j) {
         const ServeRequest& r = rq[j];
         const uint64_t a = h_off[first[j]], e = h_off[first[j + 1]];
@@ -470,7 +481,7 @@ void batcher_run_requests(gbsa_batcher& b, const ServeRequest* rq, uint32_t k, i
             GBSA_CUDA(cudaMemcpyAsync(r.rescued, L.out_resc.as<uint8_t>() + first[j], r.n_reads,
                                       cudaMemcpyDeviceToHost, st));
     }
-    GBSA_CUDA(cudaStreamSynchronize(st));
+    wait_blocking(L, st);
     GBSA_CUDA(cudaEventRecord(L.done, st));
 }
 
@@ -530,7 +541,7 @@ void gbsa_batcher_free(gbsa_batcher* b) {
             cudaStreamSynchronize(L.m->side);
         }
         drop_graph(L);
-        for (cudaEvent_t e : {L.done, L.in_ready, L.out_free})
+        for (cudaEvent_t e : {L.done, L.in_ready, L.out_free, L.wait_ev})
             if (e) cudaEventDestroy(e);
         gbsa_mapper_free(L.m);
         L.m = nullptr;
