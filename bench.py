@@ -173,14 +173,11 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     slots; p50/p99 latency from each request's scheduled arrival to its completion;
     every request checked byte for byte against one plain-form map_reads of the whole
     request pool (a read's NAMs depend only on the read, so this is the request mapped
-    alone).  The rates sweep up to saturation; the highest rate with p99 < 20 ms is
-    reported."""
-    import queue
-    import threading
-    from concurrent.futures import ThreadPoolExecutor
-
+    alone).  The schedule runs through gbsa_server_replay (native submit, completion and
+    checker threads), so no interpreter delays sit between the schedule and the server.
+    The rates sweep up to saturation; the highest rate with p99 < 20 ms is reported."""
     import torch
-    from gpu_index_test_gb300 import native, synth
+    from gpu_index_test_gb300 import abi, native, synth
 
     pool = synth.make_reads(g, synth.ReadParams(seed=123, n_units=max(2000, int(1_000_000 * scale)), len_min=100,
                                                 len_max=250, paired_frac=1.0, insert_mean=400, insert_sd=50))
@@ -191,19 +188,17 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     srv = native.Server(idx, workers=slots, max_reads=batch_reads, max_bases=batch_reads * 250)
     g0 = srv.stats()
     n_slots, slot_nams = 48, max_reads * npr
-    plain_bytes = np.ascontiguousarray(plain[0]).view(np.uint8)
-    plain_off = np.ascontiguousarray(plain[1]).astype(np.int64)
-    libc = C.CDLL(None)
-    libc.memcmp.restype = C.c_int
-    libc.memcmp.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
-
-    def same_bytes(pa, pb, nbytes):
-        # memcmp through ctypes releases the GIL: the checker threads run in parallel
-        return nbytes == 0 or libc.memcmp(pa, pb, nbytes) == 0
+    plain_bytes = np.ascontiguousarray(plain[0])
+    plain_off_u = np.ascontiguousarray(plain[1], np.uint64)
+    plain_frac = np.ascontiguousarray(plain[2], np.float32)
+    plain_resc = np.ascontiguousarray(plain[3], np.uint8)
+    pool_offs = np.ascontiguousarray(pool.offsets, np.uint64)
+    pool_lens = np.ascontiguousarray(pool.lengths, np.uint32)
     bufs = [(torch.empty(slot_nams * 44, dtype=torch.uint8).pin_memory(),
              torch.empty(max_reads + 1, dtype=torch.int64).pin_memory(),
              torch.empty(max_reads, dtype=torch.float32).pin_memory(),
              torch.empty(max_reads, dtype=torch.uint8).pin_memory()) for _ in range(n_slots)]
+    buf_ptrs = [tuple(t.data_ptr() for t in b) for b in bufs]
     seq_ptr = pool.seq.ctypes.data
     results = []
     for rate in rates:
@@ -217,77 +212,42 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
             n = min(n, pool.n // 2 * 2)
             start = int(rng.integers(0, (pool.n - n) // 2 + 1)) * 2
             arrivals.append((t, start, n))
-        free = queue.Queue()
-        for i in range(n_slots):
-            free.put(i)
-        meta = {}
-        t_sub = {}
+        # the schedule is replayed by the library's native load replay: submit calls at their
+        # times from a native thread, completions collected and every request's results
+        # compared byte for byte with the pool's plain-form results on native checker threads
+        # before its buffers are reused (no interpreter between the schedule and the server)
+        reqs = np.zeros(len(arrivals), abi.REPLAY_REQUEST)
+        reqs["at_us"] = [a[0] * 1e6 for a in arrivals]
+        reqs["start"] = [a[1] for a in arrivals]
+        reqs["n_reads"] = [a[2] for a in arrivals]
         info0 = srv.info()
-        t0 = time.perf_counter() + 0.05
-
-        def submitter():
-            for tag, (ta, start, n) in enumerate(arrivals):
-                dt = t0 + ta - time.perf_counter()
-                if dt > 0:
-                    time.sleep(dt)
-                slot = free.get()
-                offs = np.ascontiguousarray(pool.offsets[start:start + n])
-                lens = np.ascontiguousarray(pool.lengths[start:start + n])
-                meta[tag] = (slot, start, n, offs, lens)
-                b = bufs[slot]
-                t_sub[tag] = time.perf_counter()
-                srv.submit(seq_ptr, offs.ctypes.data, lens.ctypes.data, n, b[0].data_ptr(), slot_nams,
-                           b[1].data_ptr(), b[2].data_ptr(), b[3].data_ptr(), tag)
-
-        def check(slot, start, n, tot):
-            # every byte of the request's NAMs, fractions and flags, and its offsets
-            b = bufs[slot]
-            a0, a1 = int(plain[1][start]), int(plain[1][start + n])
-            ok = tot == a1 - a0 and \
-                same_bytes(b[0].data_ptr(), plain_bytes.ctypes.data + a0 * 44, tot * 44) and \
-                same_bytes(b[2].data_ptr(), plain[2].ctypes.data + 4 * start, 4 * n) and \
-                same_bytes(b[3].data_ptr(), plain[3].ctypes.data + start, n) and \
-                np.array_equal(b[1][: n + 1].numpy(), plain_off[start:start + n + 1] - a0)
-            free.put(slot)
-            return ok
-
-        th = threading.Thread(target=submitter)
-        th.start()
-        lat, lat_n, lat_srv, reads_done, failed = [], [], [], 0, 0
-        checks = []
-        t_last = t0
-        with ThreadPoolExecutor(max_workers=12) as ex:
-            while len(lat) + failed < len(arrivals):
-                for tag, st, tot in srv.poll(wait_ms=20):
-                    now = time.perf_counter()
-                    slot, start, n, _, _ = meta[tag]
-                    if st != 0:
-                        failed += 1
-                        free.put(slot)
-                        continue
-                    lat.append(now - (t0 + arrivals[tag][0]))
-                    lat_srv.append(now - t_sub[tag])
-                    lat_n.append(n)
-                    reads_done += n
-                    t_last = max(t_last, now)
-                    checks.append(ex.submit(check, slot, start, n, tot))
-            exact = all(c.result() for c in checks)
-        th.join()
+        sub_us, done_us, status, mismatch = srv.replay(
+            seq_ptr, pool_offs, pool_lens, reqs, buf_ptrs, slot_nams, max_reads,
+            expected=(plain_bytes.ctypes.data, plain_off_u.ctypes.data, plain_frac.ctypes.data, plain_resc.ctypes.data))
         info1 = srv.info()
-        lat_ms = np.sort(np.array(lat)) * 1e3
-        small = np.sort(np.array([x for x, k in zip(lat, lat_n) if k <= 10_000])) * 1e3
+        ok_req = status == 0
+        failed = int((~ok_req).sum())
+        lat = (done_us - reqs["at_us"])[ok_req] / 1e3
+        lat_srv = (done_us - sub_us)[ok_req] / 1e3
+        lat_n = reqs["n_reads"][ok_req]
+        reads_done = int(lat_n.sum())
+        t_last = float(done_us[ok_req].max()) / 1e6 if ok_req.any() else 0.0
+        exact = bool(mismatch.sum() == 0)
+        lat_ms = np.sort(lat)
+        small = np.sort(lat[lat_n <= 10_000])
         n_req = len(arrivals)
+        delay = np.sort(sub_us - reqs["at_us"]) / 1e3
         results.append({
             "rate_req_s": rate, "requests": n_req, "failed": failed,
             "offered_reads_per_s": round(sum(a[2] for a in arrivals) / seconds, 1),
-            "reads_per_s": round(reads_done / max(1e-9, t_last - t0), 1),
+            "reads_per_s": round(reads_done / max(1e-9, t_last), 1),
             "p50_ms": round(float(lat_ms[len(lat_ms) // 2]), 2) if len(lat_ms) else None,
             "p99_ms": round(float(lat_ms[min(len(lat_ms) - 1, int(len(lat_ms) * 0.99))]), 2) if len(lat_ms) else None,
             "max_ms": round(float(lat_ms[-1]), 2) if len(lat_ms) else None,
-            # from the client's submit call (the client's own delay behind the schedule left out)
-            "p99_ms_from_submit": round(float(np.percentile(np.array(lat_srv) * 1e3, 99)), 2) if lat_srv else None,
-            "p99_submit_delay_ms": round(float(np.percentile(
-                [(t_sub[i] - t0 - arrivals[i][0]) * 1e3 for i in t_sub], 99)), 2) if t_sub else None,
+            # from the submit call, and how late the replay's submit calls were against the schedule
+            "p99_ms_from_submit": round(float(np.percentile(lat_srv, 99)), 2) if len(lat_srv) else None,
+            "p99_submit_delay_ms": round(float(delay[min(len(delay) - 1, int(len(delay) * 0.99))]), 2)
+            if len(delay) else None,
             "requests_le_10k_reads": int(len(small)),
             "p50_ms_le_10k_reads": round(float(small[len(small) // 2]), 2) if len(small) else None,
             "p99_ms_le_10k_reads": round(float(small[min(len(small) - 1, int(len(small) * 0.99))]), 2)
@@ -306,7 +266,6 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     ok10 = [r for r in results if r["p99_ms_le_10k_reads"] is not None and r["p99_ms_le_10k_reads"] < 20.0
             and r["bit_exact_vs_plain"]]
     sat10 = max(ok10, key=lambda r: r["reads_per_s"]) if ok10 else None
-    # the same requests' sizes, mapped one by one on 10k-read requests: p99 target is for them
     return {"index": index_name, "slots": info["slots"], "slot_bytes": info["slot_bytes"],
             "graph_during_requests": {k: growth[k] - g0[k] for k in growth},
             "memory_budget_bytes": info["budget"], "batch_reads": batch_reads,

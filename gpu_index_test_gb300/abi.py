@@ -88,6 +88,14 @@ class BatchConfig(C.Structure):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
+class ReplayRequest(C.Structure):
+    """gbsa_replay_request: reads [start, start + n_reads) of the pool at at_us."""
+    _fields_ = [("at_us", C.c_double), ("start", C.c_uint64), ("n_reads", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+REPLAY_REQUEST = np.dtype([("at_us", "<f8"), ("start", "<u8"), ("n_reads", "<u4"), ("_pad", "<u4")])
+
+
 class ServerConfig(C.Structure):
     """gbsa_server_config."""
     _fields_ = [

@@ -14,7 +14,9 @@
 // and requests overlap on the device; each request's results equal gbsa_map_reads'
 // for its reads alone (a read's NAMs depend only on the read).  No reference
 // counterpart: the reference maps one file per process (step2/main.cu:4100-4760).
+#include <atomic>
 #include <chrono>
+#include <cstring>
 #include <condition_variable>
 #include <deque>
 #include <memory>
@@ -257,6 +259,130 @@ uint32_t gbsa_server_poll(gbsa_server* s, uint64_t* tags, int* status, uint64_t*
         ++k;
     }
     return k;
+}
+
+int gbsa_server_replay(gbsa_server* s, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
+                       const gbsa_replay_request* reqs, uint32_t n_req, uint32_t n_bufs, gbsa_nam* const* nams,
+                       uint64_t nam_cap, uint64_t* const* nam_offsets, float* const* frac, uint8_t* const* rescued,
+                       uint32_t max_reads, const gbsa_nam* exp_nams, const uint64_t* exp_nam_offsets,
+                       const float* exp_frac, const uint8_t* exp_rescued, double* submit_us, double* done_us,
+                       int* status, uint8_t* mismatch) {
+    try {
+        if (n_bufs == 0) throw Error(GBSA_ERR_PARAM, "no output buffers");
+        for (uint32_t i = 0; i < n_req; ++i)
+            if (reqs[i].n_reads > max_reads) throw Error(GBSA_ERR_CAPACITY, "request larger than the buffers");
+        using clk = std::chrono::steady_clock;
+        std::mutex mu;
+        std::condition_variable cv_free, cv_check;
+        std::deque<uint32_t> free_bufs, to_check;   // buffer sets; requests whose results wait for a check
+        for (uint32_t b = 0; b < n_bufs; ++b) free_bufs.push_back(b);
+        std::vector<uint32_t> buf_of(n_req, 0);
+        bool done_all = false;
+        const clk::time_point t0 = clk::now() + std::chrono::milliseconds(20);
+        auto us_since = [&](clk::time_point t) { return std::chrono::duration<double, std::micro>(t - t0).count(); };
+        std::vector<uint64_t> totals(n_req, 0);
+        // checkers: compare a finished request with the expected results, then free its buffers
+        auto checker = [&] {
+            for (;;) {
+                uint32_t i;
+                {
+                    std::unique_lock<std::mutex> g(mu);
+                    cv_check.wait(g, [&] { return done_all || !to_check.empty(); });
+                    if (to_check.empty()) return;
+                    i = to_check.front();
+                    to_check.pop_front();
+                }
+                const uint32_t b = buf_of[i];
+                bool bad = status[i] != GBSA_OK;
+                if (!bad && exp_nams) {
+                    const gbsa_replay_request& r = reqs[i];
+                    const uint64_t a = exp_nam_offsets[r.start], e = exp_nam_offsets[r.start + r.n_reads];
+                    bad = totals[i] != e - a ||
+                          std::memcmp(nams[b], exp_nams + a, sizeof(gbsa_nam) * (e - a)) != 0 ||
+                          std::memcmp(frac[b], exp_frac + r.start, 4ull * r.n_reads) != 0 ||
+                          std::memcmp(rescued[b], exp_rescued + r.start, r.n_reads) != 0;
+                    for (uint32_t j = 0; !bad && j <= r.n_reads; ++j)
+                        bad = nam_offsets[b][j] != exp_nam_offsets[r.start + j] - a;
+                }
+                mismatch[i] = bad ? 1 : 0;
+                {
+                    std::lock_guard<std::mutex> g(mu);
+                    free_bufs.push_back(b);
+                }
+                cv_free.notify_one();
+            }
+        };
+        // completions, as they arrive (poll returns at once while nothing is in flight:
+        // then the poller naps instead of spinning on the server's lock)
+        std::atomic<uint32_t> arrived{0};
+        std::thread poller([&] {
+            std::vector<uint64_t> tags(256), tot(256);
+            std::vector<int> st(256);
+            while (arrived.load() < n_req) {
+                const uint32_t k = gbsa_server_poll(s, tags.data(), st.data(), tot.data(), 256, 50);
+                const clk::time_point now = clk::now();
+                if (k == 0) {
+                    std::this_thread::sleep_for(std::chrono::microseconds(50));
+                    continue;
+                }
+                std::lock_guard<std::mutex> g(mu);
+                for (uint32_t j = 0; j < k; ++j) {
+                    const uint32_t i = (uint32_t)tags[j];
+                    done_us[i] = us_since(now);
+                    status[i] = st[j];
+                    totals[i] = tot[j];
+                    to_check.push_back(i);
+                    arrived.fetch_add(1);
+                }
+                cv_check.notify_all();
+            }
+        });
+        const unsigned n_check = std::max(2u, std::min(8u, std::thread::hardware_concurrency() / 4));
+        std::vector<std::thread> checkers;
+        for (unsigned c = 0; c < n_check; ++c) checkers.emplace_back(checker);
+        // submissions at their times
+        int rc = GBSA_OK;
+        for (uint32_t i = 0; i < n_req; ++i) {
+            std::this_thread::sleep_until(t0 + std::chrono::duration_cast<clk::duration>(
+                                                   std::chrono::duration<double, std::micro>(reqs[i].at_us)));
+            uint32_t b;
+            {
+                std::unique_lock<std::mutex> g(mu);
+                cv_free.wait(g, [&] { return !free_bufs.empty(); });
+                b = free_bufs.front();
+                free_bufs.pop_front();
+            }
+            buf_of[i] = b;
+            const gbsa_replay_request& r = reqs[i];
+            submit_us[i] = us_since(clk::now());
+            const int x = gbsa_server_submit(s, seqs, offsets + r.start, lengths + r.start, r.n_reads, nams[b], nam_cap,
+                                             nam_offsets[b], frac[b], rescued[b], i);
+            if (x != GBSA_OK) {   // not queued: record it as done at once
+                std::lock_guard<std::mutex> g(mu);
+                rc = x;
+                done_us[i] = submit_us[i];
+                status[i] = x;
+                to_check.push_back(i);
+                arrived.fetch_add(1);
+                cv_check.notify_all();
+            }
+        }
+        poller.join();
+        {
+            std::lock_guard<std::mutex> g(mu);
+            done_all = true;
+        }
+        cv_check.notify_all();
+        for (auto& t : checkers) t.join();
+        if (rc != GBSA_OK) set_last_error("a request was not accepted");
+        return rc;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return GBSA_ERR_CUDA;
+    }
 }
 
 void gbsa_server_free(gbsa_server* s) {

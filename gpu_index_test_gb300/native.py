@@ -75,6 +75,8 @@ def lib():
             "gbsa_server_info": (i32, [vp, C.POINTER(u32), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64),
                                        C.POINTER(u64)]),
             "gbsa_server_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+            "gbsa_server_replay": (i32, [vp, vp, vp, vp, vp, u32, u32, vp, u64, vp, vp, vp, u32, vp, vp, vp, vp, vp,
+                                         vp, vp, vp]),
             "gbsa_server_submit": (i32, [vp, vp, vp, vp, u32, vp, u64, vp, vp, vp, u64]),
             "gbsa_server_poll": (u32, [vp, vp, vp, vp, u32, i32]),
             "gbsa_server_free": (None, [vp]),
@@ -555,6 +557,23 @@ class Server:
         h = C.c_void_p()
         _check(lib().gbsa_server_create_ex(index.h, C.byref(self.opt), C.byref(cfg), C.byref(h)))
         self.h = h
+
+    def replay(self, seq_ptr, offsets, lengths, reqs, bufs, nam_cap, max_reads, expected=None):
+        """gbsa_server_replay: reqs is an abi.REPLAY_REQUEST array, bufs a list of
+        (nams, nam_offsets, frac, rescued) pointer tuples, expected None or pointers
+        (nams, nam_offsets, frac, rescued) of the pool's results.  Returns (submit_us,
+        done_us, status, mismatch) arrays."""
+        n = len(reqs)
+        P = C.c_void_p * len(bufs)
+        nb = [P(*[b[k] for b in bufs]) for k in range(4)]
+        sub, done = np.zeros(n), np.zeros(n)
+        st, mis = np.zeros(n, np.int32), np.zeros(n, np.uint8)
+        ex = expected or (None, None, None, None)
+        rc = lib().gbsa_server_replay(self.h, seq_ptr, offsets.ctypes.data, lengths.ctypes.data, reqs.ctypes.data, n,
+                                      len(bufs), nb[0], nam_cap, nb[1], nb[2], nb[3], max_reads, ex[0], ex[1], ex[2],
+                                      ex[3], sub.ctypes.data, done.ctypes.data, st.ctypes.data, mis.ctypes.data)
+        _check(rc)
+        return sub, done, st, mis
 
     def stats(self):
         """Graph launches, captures and eager batches over all slots since creation."""

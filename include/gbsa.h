@@ -381,6 +381,32 @@ uint32_t gbsa_server_poll(gbsa_server* s, uint64_t* tags, int* status, uint64_t*
                           uint32_t cap, int wait_ms);
 void gbsa_server_free(gbsa_server* s);
 
+/* A request of gbsa_server_replay: reads [start, start + n_reads) of the read pool,
+ * submitted at_us microseconds after the replay starts. */
+typedef struct gbsa_replay_request {
+    double   at_us;
+    uint64_t start;
+    uint32_t n_reads;
+    uint32_t _pad;
+} gbsa_replay_request;
+
+/* Load replay for measuring the served form: submits the requests at their times from a
+ * native thread (in order; a request waits for one of n_bufs output buffer sets to be
+ * free), collects completions on another, and, when exp_nams is not NULL, compares each
+ * request's NAMs, offsets, fractions and flags byte for byte with the expected results of
+ * the whole pool (exp_nam_offsets has n_pool + 1 entries; a request's offsets are relative
+ * to its first read) on checker threads before its buffers are reused.  Buffer set b is
+ * nams[b] (room for nam_cap NAMs), nam_offsets[b] (max_reads + 1), frac[b], rescued[b]
+ * (max_reads).  Per request: submit_us / done_us (microseconds after the start, of the
+ * submit call and of the completion's arrival), status (a GBSA_* code) and mismatch (1 when
+ * the results differ from the expected ones).  No reference counterpart. */
+int gbsa_server_replay(gbsa_server* s, const char* seqs, const uint64_t* offsets, const uint32_t* lengths,
+                       const gbsa_replay_request* reqs, uint32_t n_req, uint32_t n_bufs, gbsa_nam* const* nams,
+                       uint64_t nam_cap, uint64_t* const* nam_offsets, float* const* frac, uint8_t* const* rescued,
+                       uint32_t max_reads, const gbsa_nam* exp_nams, const uint64_t* exp_nam_offsets,
+                       const float* exp_frac, const uint8_t* exp_rescued, double* submit_us, double* done_us,
+                       int* status, uint8_t* mismatch);
+
 /* Read-pair classification after the NAM sort (gpu_pre_cal_type,
  * step2/main.cu:3552-3580): for each pair, 0 = no NAMs on either end, 1 = NAMs on
  * mate 1 only, 2 = mate 2 only, 3 = both ends' top_dropoff (main.cu:889-898) below

@@ -177,6 +177,49 @@ def test_server_batches_requests_and_each_equals_alone():
         assert (frac[:n] == alone[2]).all() and (resc[:n] == alone[3]).all()
 
 
+def test_server_replay_checks_every_request():
+    """gbsa_server_replay: requests submitted at their times from native threads, each
+    compared byte for byte with the pool's plain-form results; a request whose expected
+    results were altered (one NAM's score) is flagged, the others are not."""
+    import torch
+    g = synth.make_genome(synth.genome_params("C2", scale=0.01, seed=131))
+    pool = synth.make_reads(g, synth.ReadParams(seed=132, n_units=8000, len_min=100, len_max=250, paired_frac=1.0,
+                                                insert_mean=400, insert_sd=50))
+    idx = native.Index.build(native.params_from_read_length(150), g)
+    m = native.Mapper(idx)
+    exp = m.map_reads(pool)
+    rng = np.random.default_rng(133)
+    k = 60
+    reqs = np.zeros(k, abi.REPLAY_REQUEST)
+    reqs["at_us"] = np.sort(rng.uniform(0, 20_000, k))
+    reqs["n_reads"] = rng.integers(1, 300, k) * 2
+    reqs["start"] = [int(rng.integers(0, (pool.n - n) // 2)) * 2 for n in reqs["n_reads"]]
+    max_reads, cap = 1024, 64 * 1024
+    bufs = [(torch.empty(cap * 44, dtype=torch.uint8).pin_memory(), torch.empty(max_reads + 1, dtype=torch.int64).pin_memory(),
+             torch.empty(max_reads, dtype=torch.float32).pin_memory(), torch.empty(max_reads, dtype=torch.uint8).pin_memory())
+            for _ in range(4)]
+    ptrs = [tuple(t.data_ptr() for t in b) for b in bufs]
+    nams = np.ascontiguousarray(exp[0])
+    off = np.ascontiguousarray(exp[1], np.uint64)
+    frac, resc = np.ascontiguousarray(exp[2]), np.ascontiguousarray(exp[3])
+    # plant a mistake in the expected results of request 7 (its first read with NAMs)
+    s7, n7 = int(reqs["start"][7]), int(reqs["n_reads"][7])
+    j = int(off[s7])
+    assert off[s7 + n7] > off[s7]
+    nams["score"][j] += 1.0
+    srv = native.Server(idx, workers=2, max_reads=max_reads)
+    offs = np.ascontiguousarray(pool.offsets, np.uint64)
+    lens = np.ascontiguousarray(pool.lengths, np.uint32)
+    sub, done, st, mis = srv.replay(pool.seq.ctypes.data, offs, lens, reqs, ptrs, cap, max_reads,
+                                    expected=(nams.ctypes.data, off.ctypes.data, frac.ctypes.data, resc.ctypes.data))
+    srv.free()
+    assert (st == 0).all()
+    r_j = int(np.searchsorted(off, j, side="right")) - 1   # the read that holds NAM j
+    hit = (reqs["start"] <= r_j) & (r_j < reqs["start"] + reqs["n_reads"])
+    assert hit[7] and (mis == hit.astype(np.uint8)).all()
+    assert (done >= sub).all() and (sub >= reqs["at_us"] - 1.0).all()
+
+
 def test_server_memory_budget_limits_slots():
     """Slots are created against the device-memory budget: a budget below one slot's
     work areas leaves a single slot, which still serves every request."""
