@@ -163,28 +163,13 @@ __device__ __forceinline__ uint64_t lookup_sectors(const IndexView& I, uint64_t 
 
 constexpr uint32_t kRescueHeavyHits = 2000;   // estimated merge hits of a heavy rescued read
 
-// Drops the whole 128-byte L2 lines inside [p, p + bytes) without writing them back (the
-// warp's lanes one line each); partial lines at either end are kept (they hold other
-// reads' data).  The caller's warp must be done with the range.
-__device__ __forceinline__ void warp_discard_l2(const void* p, uint64_t bytes) {
-    const uint64_t a = (reinterpret_cast<uint64_t>(p) + 127) & ~127ull;
-    const uint64_t e = (reinterpret_cast<uint64_t>(p) + bytes) & ~127ull;
-    for (uint64_t x = a + 128ull * lane_id(); x < e; x += 128ull * 32)
-        asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
-}
-
 // kCount: also count the reference's algorithmic bytes and gather sectors (a
 // separate instance, so that the counting code costs the mapping kernel nothing).
 // find / is_filtered / walk for the queries of read r (warp): per-query index
 // positions and hit counts, the nonrepetitive fraction and rescue decision, and for a
 // read that is not rescued its hits (query order, then run order) in the hit arena.
 // The query loop of find_nams (step2/nam.cu:748-790).
-// kDiscard (the kernels that seed the read just before, so that a batch run again after
-// an overflow writes the queries anew): once a read's queries are spent — all of its
-// per-query hit counts, and for a read that is not rescued also its query records and
-// index positions — their whole 128-byte L2 lines are dropped without being written back
-// (discard.global.L2), so the intermediate arrays cost no DRAM writes.
-template <bool kCount, bool kDiscard = false>
+template <bool kCount>
 __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig& C, uint32_t r, ReadRec* __restrict__ rec,
                                             const Arenas& A, Counters* ctr) {
     const uint32_t lane = lane_id();
@@ -255,10 +240,6 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
             else A.rescue_list[atomicAdd(&ctr->n_rescue, 1u)] = r;
             R.n_hits = 0;
         }
-        if (kDiscard) {   // the rescue kernel reads the queries and positions, not the counts
-            __syncwarp();
-            warp_discard_l2(aux, 4ull * nq2);
-        }
         return;
     }
     // hit offsets in generation order (query order, then run order)
@@ -294,12 +275,6 @@ __device__ __forceinline__ void lookup_read(const IndexView& I, const MapConfig&
     if (lane == 0) {
         R.hit_off = hoff;
         R.n_hits = (uint32_t)H;
-    }
-    if (kDiscard) {
-        __syncwarp();
-        warp_discard_l2(Q, sizeof(Query) * (uint64_t)nq2);
-        warp_discard_l2(qp, 8ull * nq2);
-        warp_discard_l2(aux, 4ull * nq2);
     }
 }
 
@@ -366,7 +341,7 @@ __global__ void __launch_bounds__(32 * kSeedWarps, kFusedBlocksPerSm)
         }
         emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
         __syncwarp();
-        lookup_read<kCount, true>(I, C, r, rec, A, ctr);
+        lookup_read<kCount>(I, C, r, rec, A, ctr);
         __syncwarp();
     }
 }
@@ -421,7 +396,7 @@ __global__ void __launch_bounds__(32 * kWarps, kBlocks)
             emit_read_queries(P, s_sh[w], s_sp[w], ns, L, R, A, ctr);
             __syncwarp();
             if (kLookup) {
-                lookup_read<kCount, true>(I, C, r, rec, A, ctr);
+                lookup_read<kCount>(I, C, r, rec, A, ctr);
                 __syncwarp();
             }
         }
