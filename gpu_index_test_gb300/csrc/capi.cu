@@ -371,21 +371,7 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     m.fused = fused;
     mark(0);
     if (desc) launch_seed_lookup_queue(m.idx->dp, I, C, desc, m.rec.as<ReadRec>(), A, ctr, bm->variant, fused, st);
-    else if (fused) {
-        // the queue kernel in the tuned shape over pairs of consecutive reads (a warp seeds
-        // and looks up two reads per item: 2-3% less time than one per item)
-        BatchDesc pd{};
-        pd.seqs = d_seqs;
-        pd.offs = d_offs;
-        pd.lens = d_lens;
-        pd.n_reads = n;
-        pd.n_items = n;
-        pd.group = kPlainGroup;
-        m.plain_desc.resize(sizeof(BatchDesc));
-        launch_write_desc(pd, m.plain_desc.as<BatchDesc>(), st);
-        launch_seed_lookup_queue(m.idx->dp, I, C, m.plain_desc.as<BatchDesc>(), m.rec.as<ReadRec>(), A, ctr,
-                                 m.seed_variant, true, st);
-    }
+    else if (fused) launch_seed_lookup(m.idx->dp, I, C, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     else if (!seeded) launch_seed(m.idx->dp, d_seqs, d_offs, d_lens, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(1);
     if (!seeded)
@@ -924,7 +910,6 @@ int gbsa_mapper_create(const gbsa_index* idx, const gbsa_map_options* opt, uint3
                 m->cfg.sort_variant = bc.sort_variant;
                 m->cfg.lane_variant = bc.lane_variant;
                 m->cfg.warp_variant = bc.warp_variant;
-                m->seed_variant = bc.seed_variant;
                 // heavy rescued reads of small batches merged a block each (10k-100k-read
                 // batches of 150 bp pairs: about 0.3 of the batch time less)
                 m->cfg.rescue_block_hits = bc.rescue_block_hits;

@@ -65,8 +65,6 @@ struct BatchDesc {
     uint64_t* out_off;      // n_reads + 1 NAM offsets
     float* frac;            // may be null
     uint8_t* rescued;       // may be null
-    uint32_t group;         // with items == nullptr: reads per work item (0 or 1: one)
-    uint32_t pad;
 };
 
 constexpr uint32_t kLaneBuckets = 13;   // hit-count buckets of the lane NAM kernel (<= 16)
@@ -137,7 +135,6 @@ struct MapConfig {
 };
 constexpr uint32_t kLaneMaxHitsCap = 160;
 constexpr uint32_t kRescueBlockHitsDefault = 4000;   // a new mapper's rescue_block_hits
-constexpr uint32_t kPlainGroup = 2;   // reads per work item of the plain form's seeding + lookup
 
 // Reads shorter than this (and with at most kSmemSyncmers syncmers) are seeded
 // with shared-memory buffers; the rest by the scratch-memory kernel.
@@ -169,8 +166,6 @@ struct SeedVariant {
 };
 constexpr int kSeedVariants = 6;
 SeedVariant seed_variant(int v);
-// Writes d to device memory at out on st (a descriptor for the queue kernel, stream-ordered).
-void launch_write_desc(const BatchDesc& d, BatchDesc* out, cudaStream_t st);
 // lookup false: seeding alone (the lookup then runs as launch_lookup with desc).
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
                               ReadRec* rec, Arenas A, Counters* ctr, int variant, bool lookup, cudaStream_t st);

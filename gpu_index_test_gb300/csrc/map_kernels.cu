@@ -368,15 +368,14 @@ __global__ void __launch_bounds__(32 * kWarps, kBlocks)
     const uint64_t* __restrict__ offs = desc->offs;
     const uint32_t* __restrict__ lens = desc->lens;
     const uint32_t* __restrict__ items = desc->items;
-    const uint32_t group = items || desc->group < 2 ? 1u : desc->group;   // reads per item without items
-    const uint32_t n_items = items ? desc->n_items : (desc->n_reads + group - 1) / group;
+    const uint32_t n_items = items ? desc->n_items : desc->n_reads;
     for (;;) {
         const uint32_t it = warp_next(&ctr->queue_head);
         if (it >= n_items) break;
         // item bounds outside [0, n_reads] are clamped (reads no item covers stay empty)
         const uint32_t n_reads = desc->n_reads;
-        const uint32_t r0 = min(items ? items[it] : it * group, n_reads);
-        const uint32_t r1 = min(items ? items[it + 1] : it * group + group, n_reads);
+        const uint32_t r0 = min(items ? items[it] : it, n_reads);
+        const uint32_t r1 = min(items ? items[it + 1] : it + 1, n_reads);
         for (uint32_t r = r0; r < r1; ++r) {
             const uint32_t L = lens[r];
             ReadRec& R = rec[r];
@@ -2145,13 +2144,6 @@ static void launch_q_variant(int v, const DevParams& P, const IndexView& I, cons
         case 5: launch_q<kCount, kLookup, 8, 6, 256, 96>(P, I, C, desc, rec, A, ctr, st); break;
         default: launch_q<kCount, kLookup, 8, 6, 512, 160>(P, I, C, desc, rec, A, ctr, st); break;
     }
-}
-
-__global__ void k_write_desc(BatchDesc d, BatchDesc* out) { *out = d; }
-
-void launch_write_desc(const BatchDesc& d, BatchDesc* out, cudaStream_t st) {
-    k_write_desc<<<1, 1, 0, st>>>(d, out);
-    GBSA_LAUNCHED();
 }
 
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,

@@ -22,10 +22,6 @@ struct gbsa_mapper {
     uint64_t max_bases = 0;
     gbsa::DeviceBuffer seqs, offs, lens, rec, q, qaux, qpos, hits, nams, slots, ovf, lists, ctr, long_scratch, cnt,
         out_off, out_nams, out_frac, out_resc, resc_cycles, nam_notes, jobs, side_slots, lane_lists;
-    // the plain form's fused seeding + lookup runs the queue kernel (the tuned shape,
-    // kPlainGroup consecutive reads per work item) from this device descriptor
-    gbsa::DeviceBuffer plain_desc;
-    int seed_variant = 0;
     uint64_t q_cap = 0, hit_cap = 0, nam_cap = 0, ovf_cap = 0, slot_bytes = 0;
     uint32_t long_warps = 0;
     gbsa::PinnedBuffer h_seqs, h_meta, h_out;
