@@ -380,20 +380,6 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     mark(2);
     if (fused) launch_lookup_long(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
     else launch_lookup(I, C, n, m.rec.as<ReadRec>(), A, ctr, st, desc);
-    // The rescue chain works on the rescued reads only and the NAM kernels on the
-    // others: the rescue chain runs on the side stream (with its own scratch slots) so
-    // that its tail of reads with thousands of hits overlaps them.  It forks as soon as
-    // the rescue list is complete (after the lookup), beside the bucketing of the others.
-    // (at the NAM stream's priority: a caller's stream has the lowest)
-    cudaStream_t side = m.side;
-    if (main_st != m.st) {
-        int prio = 0, lo = 0, hi = 0;
-        GBSA_CUDA(cudaStreamGetPriority(main_st, &prio));
-        GBSA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        if (prio != hi) side = m.side_lo;
-    }
-    GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
-    GBSA_CUDA(cudaStreamWaitEvent(side, m.fork_ev, 0));
     launch_bucket_reads(n, C.lane_max_hits, m.rec.as<ReadRec>(), A, ctr, st, desc);
     if (early) {
         GBSA_CUDA(cudaEventRecord(m.early_ev, early));
@@ -401,6 +387,19 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
         st = main_st;
     }
     mark(3);
+    // The rescue chain works on the rescued reads only and the NAM kernels on the
+    // others: the rescue chain runs on the side stream (with its own scratch slots) so
+    // that its tail of reads with thousands of hits overlaps them.
+    // (at the main stream's priority: a caller's stream has the lowest)
+    cudaStream_t side = m.side;
+    if (st != m.st) {
+        int prio = 0, lo = 0, hi = 0;
+        GBSA_CUDA(cudaStreamGetPriority(st, &prio));
+        GBSA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        if (prio != hi) side = m.side_lo;
+    }
+    GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
+    GBSA_CUDA(cudaStreamWaitEvent(side, m.fork_ev, 0));
     Arenas As = A;
     As.slots = m.side_slots.as<uint8_t>();
     launch_rescue(I, C, n, m.rec.as<ReadRec>(), As, ctr, side);
