@@ -399,6 +399,11 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
         if (prio != hi) side = m.side_lo;
     }
     GBSA_CUDA(cudaEventRecord(m.fork_ev, st));
+    // the lane merge is submitted ahead of the rescue kernel: the first of two kernels that
+    // become ready together takes the SMs first, and the rescue kernel ahead of the lane
+    // merge slowed the lane stage by a third
+    launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
+    mark(4);
     GBSA_CUDA(cudaStreamWaitEvent(side, m.fork_ev, 0));
     Arenas As = A;
     As.slots = m.side_slots.as<uint8_t>();
@@ -408,8 +413,6 @@ void enqueue_batch(gbsa_mapper& m, const uint8_t* d_seqs, const uint64_t* d_offs
     if (n) launch_sort_jobs(C, m.rec.as<ReadRec>(), As, ctr, side);
     if (m.profile) record_stage(m.ev[7], side);
     GBSA_CUDA(cudaEventRecord(m.join_ev, side));
-    launch_nams(I, C, n, m.rec.as<ReadRec>(), A, ctr, st);
-    mark(4);
     launch_nams_warp(C, n, m.rec.as<ReadRec>(), A, ctr, st);
     mark(5);
     // Every read's NAM count is known once the rescue kernel has ended (the sorts after
