@@ -103,6 +103,22 @@ def test_batched_device_entry_point_and_graph_reuse(c3):
     assert b.stats()["graph_launches"] >= 3
 
 
+def test_batched_stage_times_inside_the_graph(c3):
+    """Stage events recorded inside the batch graph (external event nodes) time the graph's
+    launches; profiling on or off, the output is the same."""
+    g, reads, items, idx, o = c3
+    b = native.Batcher(idx, max_reads=reads.n)
+    ref = b.map_reads(reads, items)
+    b.set_profile(True)
+    got = b.map_reads(reads, items)
+    st = b.stage_ms()
+    b.set_profile(False)
+    again = b.map_reads(reads, items)
+    b.free()
+    assert same(got, ref) and same(again, ref)
+    assert st["seed_lookup"] > 0 and st["nams"] > 0 and st["rescue"] >= 0
+
+
 def test_batched_form_grows_its_work_areas():
     """Reads inside a tandem-repeat-rich genome outgrow small work areas: the batch runs
     again with larger ones and is captured anew; the results equal the plain form's."""
@@ -162,8 +178,10 @@ def test_server_batches_requests_and_each_equals_alone():
     srv = native.Server(idx, workers=2, max_reads=16384)
     bufs, done = _serve(srv, pool, reqs)
     info = srv.info()
+    stats = srv.stats()
     srv.free()
     assert info["slots"] == 2 and info["requests"] == len(reqs) and info["batches"] < len(reqs)
+    assert stats["graph_launches"] >= info["batches"] - stats["eager_runs"]
     m = native.Mapper(idx)
     for tag, req in enumerate(reqs):
         st, tot = done[tag]
