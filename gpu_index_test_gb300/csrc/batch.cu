@@ -200,30 +200,6 @@ void wait_blocking(Lane& L, cudaStream_t st) {
     GBSA_CUDA(cudaEventSynchronize(L.wait_ev));
 }
 
-// Node priorities of a batch graph: the seeding and lookup kernels at the lowest priority,
-// every other kernel at the highest.  Batches in flight side by side (the host entry
-// point's three sets of work areas, the server's slots) then let the older batch's NAM
-// phase take the SMs ahead of the younger one's seeding, as the plain form's streams do,
-// so that batches finish in order and their copies out start early.
-void set_node_priorities(cudaGraph_t g) {
-    int lo = 0, hi = 0;
-    GBSA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    size_t n = 0;
-    GBSA_CUDA(cudaGraphGetNodes(g, nullptr, &n));
-    std::vector<cudaGraphNode_t> nodes(n);
-    GBSA_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
-    for (cudaGraphNode_t node : nodes) {
-        cudaGraphNodeType t;
-        GBSA_CUDA(cudaGraphNodeGetType(node, &t));
-        if (t != cudaGraphNodeTypeKernel) continue;
-        cudaKernelNodeParams kp{};
-        GBSA_CUDA(cudaGraphKernelNodeGetParams(node, &kp));
-        cudaKernelNodeAttrValue v{};
-        v.priority = is_seeding_kernel(kp.func) ? lo : hi;
-        GBSA_CUDA(cudaGraphKernelNodeSetAttribute(node, cudaKernelNodeAttributePriority, &v));
-    }
-}
-
 void drop_graph(Lane& L) {
     if (L.exec) cudaGraphExecDestroy(L.exec);
     L.exec = nullptr;
@@ -272,8 +248,7 @@ uint64_t run_eager(gbsa_batcher& b, Lane& L, const BatchDesc& d) {
             throw;
         }
         GBSA_CUDA(cudaStreamEndCapture(m.st, &g));
-        set_node_priorities(g);
-        const cudaError_t e = cudaGraphInstantiate(&L.exec, g, cudaGraphInstantiateFlagUseNodePriority);
+        const cudaError_t e = cudaGraphInstantiate(&L.exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
             L.exec = nullptr;

@@ -166,8 +166,6 @@ struct SeedVariant {
 };
 constexpr int kSeedVariants = 6;
 SeedVariant seed_variant(int v);
-// Whether f is one of the batched form's seeding / lookup kernels (graph node priorities).
-bool is_seeding_kernel(const void* f);
 // lookup false: seeding alone (the lookup then runs as launch_lookup with desc).
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
                               ReadRec* rec, Arenas A, Counters* ctr, int variant, bool lookup, cudaStream_t st);

@@ -2146,30 +2146,6 @@ static void launch_q_variant(int v, const DevParams& P, const IndexView& I, cons
     }
 }
 
-template <bool kCount, bool kLookup>
-static void add_q_kernels(std::vector<const void*>& out) {
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 8, 6, 512, 160>);
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 8, 5, 512, 160>);
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 4, 12, 512, 160>);
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 8, 7, 256, 96>);
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 16, 3, 512, 160>);
-    out.push_back((const void*)k_seed_lookup_q<kCount, kLookup, 8, 6, 256, 96>);
-}
-
-bool is_seeding_kernel(const void* f) {
-    static const std::vector<const void*> fs = [] {
-        std::vector<const void*> v;
-        add_q_kernels<false, false>(v);
-        add_q_kernels<false, true>(v);
-        add_q_kernels<true, true>(v);
-        v.push_back((const void*)k_seed_long);
-        v.push_back((const void*)k_lookup<false>);   // the lookup of indexes over the fuse limit
-        v.push_back((const void*)k_lookup<true>);
-        return v;
-    }();
-    return std::find(fs.begin(), fs.end(), f) != fs.end();
-}
-
 void launch_seed_lookup_queue(const DevParams& P, const IndexView& I, const MapConfig& C, const BatchDesc* desc,
                               ReadRec* rec, Arenas A, Counters* ctr, int variant, bool lookup, cudaStream_t st) {
     if (!lookup) launch_q_variant<false, false>(variant, P, I, C, desc, rec, A, ctr, st);
