@@ -116,7 +116,7 @@ void check_config(const gbsa_batch_config& c) {
         throw Error(GBSA_ERR_PARAM, "lane_max_hits must be in [1, 160]");
     if (c.sort_variant < 0 || c.sort_variant > 1) throw Error(GBSA_ERR_PARAM, "sort_variant must be 0 or 1");
     if (c.chunk_reads < 1024) throw Error(GBSA_ERR_PARAM, "chunk_reads must be at least 1024");
-    if (c.lane_variant < 0 || c.lane_variant > 8) throw Error(GBSA_ERR_PARAM, "lane_variant must be 0 to 8");
+    if (c.lane_variant < 0 || c.lane_variant > 6) throw Error(GBSA_ERR_PARAM, "lane_variant must be 0 to 6");
     if (c.warp_variant < 0 || c.warp_variant > 4) throw Error(GBSA_ERR_PARAM, "warp_variant must be 0 to 4");
 }
 

@@ -2218,10 +2218,8 @@ void launch_nams(const IndexView&, const MapConfig& C, uint32_t n, ReadRec* rec,
         // 3: three blocks per SM at 168 registers (the SM's registers: the rescue kernel
         // starts as they retire); 4: two blocks per SM at 128 registers, beside the
         // rescue kernel's block; 5: six slots, three blocks per SM at 96 registers, beside it
-        // 6: six slots at 124 registers, two blocks per SM beside the rescue kernel's block;
-        // 7, 8: ten slots at 168 registers, one or two blocks per SM
-        const unsigned per_sm = C.lane_variant == 7 ? 1u
-                                : (C.lane_variant == 4 || C.lane_variant == 6 || C.lane_variant == 8) ? 2u : 3u;
+        // 6: six slots at 124 registers, two blocks per SM beside the rescue kernel's block
+        const unsigned per_sm = C.lane_variant == 4 || C.lane_variant == 6 ? 2u : 3u;
         const unsigned blocks = grid_for(n, 32 * kLaneWarps, (unsigned)device_sm_count() * per_sm);
         if (C.lane_variant == 4) k_nams_lane_r<4, kLaneOpen><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
         else if (C.lane_variant == 5) k_nams_lane_r<5, 6><<<blocks, 32 * kLaneWarps, 0, st>>>(C, n, rec, A, ctr);
