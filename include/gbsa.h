@@ -441,9 +441,9 @@ typedef struct gbsa_nam_pair {
  * id and strand, n_hits at least half the best) and mate-2 NAMs in no pair (through
  * the heap) as single-end entries; the list sorted by the reference's comparator and
  * cut to max_tries.  Mate 1's NAMs must be in GBSA_SORT_REF_MATE1 order and mate 2's
- * in GBSA_SORT_REF_MATE2 order (gpu_sort_nams, main.cu:3449-3466).  The reference
- * compares fields of an otherwise uninitialised Nam for an absent end; here that Nam
- * is all zero with ref_start -1.  d_pairs receives max_tries records per pair (pair p
+ * in GBSA_SORT_REF_MATE2 order (gpu_sort_nams, main.cu:3449-3466).  For an absent end
+ * the comparator reads a default Nam (all zero by Nam's member initialisers) with
+ * ref_start -1, as here.  d_pairs receives max_tries records per pair (pair p
  * from p * max_tries on), d_counts the number written (0 when an end has no NAMs).
  * Device pointers; the kernel runs on `stream` (0: the default stream). */
 int gbsa_nam_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs, int layout,
@@ -491,9 +491,10 @@ typedef struct gbsa_pair_plan {
  * makes a rescue of that read from the other end's NAM.  d_types from
  * gbsa_classify_pairs_device.  d_plans receives n_pairs records, d_steps the steps (pair
  * after pair); *n_steps the step count (GBSA_ERR_CAPACITY when above step_capacity, with
- * nothing but the count valid).  Device pointers; the call synchronizes stream.  The
- * reference's insert-size estimate update of type 3 (main.cu:2002-2022) depends on the
- * order in which its threads run, so it is not reproduced: mu and sigma stay fixed. */
+ * nothing but the count valid).  Device pointers; the call synchronizes stream.  mu and
+ * sigma stay fixed: the reference updates its insert-size estimate after a type-3 pair
+ * (main.cu:2002-2022), but every pair starts from a fresh estimate (gpu_align_PE3,
+ * main.cu:3777), so the update changes no result. */
 int gbsa_plan_pairs_device(const gbsa_nam* d_nams, const uint64_t* d_nam_offsets, uint32_t n_pairs, int layout,
                            const uint8_t* d_types, const gbsa_nam_pair* d_pairs, const uint32_t* d_pair_counts,
                            uint32_t max_tries, float dropoff, gbsa_pair_plan* d_plans, gbsa_align_step* d_steps,

@@ -40,6 +40,15 @@ for p in "${pids[@]}"; do wait "$p"; done
 g++ -pthread -o "$OUT/ref_driver" "$OUT"/ref_driver.o "$OUT"/nam.o "$OUT"/index.o \
   "$OUT"/randstrobes.o "$OUT"/indexparameters.o "$OUT"/io.o
 echo "built $OUT/ref_driver"
+# the reference's read-pair code after the NAM stage (main.cu's own lines, cut by
+# oracle/cut_ref_align.py into oracle/_ref, compiled as host C++ by oracle/ref_align.cpp);
+# only where main.cu is present (the staged copy carries the NAM path's sources alone)
+if [ -f "$SRC/main.cu" ]; then
+  python3 "$HERE/cut_ref_align.py" "$SRC/main.cu" "$OUT/main_align.inc"
+  g++ "${FLAGS[@]}" -I"$OUT" -I"$HERE/../include" -c "$HERE/ref_align.cpp" -o "$OUT/ref_align.o"
+  g++ -o "$OUT/ref_align" "$OUT"/ref_align.o "$OUT"/indexparameters.o "$OUT"/io.o
+  echo "built $OUT/ref_align"
+fi
 # the reference-side binding (include/gbsa_shim.hpp) checked against the reference's own
 # find_nams: needs the library built first
 GBSA_DIR="$(cd "$HERE/../gpu_index_test_gb300" && pwd)"

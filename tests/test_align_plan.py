@@ -1,16 +1,28 @@
-"""The alignment orchestration of align_PE_part0..4 (step2/main.cu:1857-2165) as step
-lists: the oracle's planner on hand-made pairs (CPU), and the GPU planner and step
-runner against the oracle on mapped read pairs (GB300).
+"""The read-pair rows after the NAM stage: pair classification (gpu_pre_cal_type), NAM-pair
+scoring (get_best_scoring_nam_pairs_sort3) and the alignment orchestration of
+align_PE_part0..4 (step2/main.cu:1857-2165) as step lists with their seed extensions and
+mate rescues.
 
-The reference's versions are device code of its main.cu, which does not build (the
-Gallatin allocator it needs is not vendored), so the planner is pinned to the
-restatement: the CPU tests below work the reference's rules through by hand.
+The oracle is pinned to the reference's own code of these rows: main.cu as a whole does
+not build, but these functions' lines compile as host C++ (oracle/cut_ref_align.py,
+oracle/ref_align.cpp), and tests/golden/align_ref.npz holds their outputs on 3,600 read
+pairs (all five pair types, k = 9, 20 and 32, two max_tries / dropoff settings).  The CPU
+tests check the oracle against those outputs and work the reference's rules through by
+hand on small pairs; the GPU tests check the device planner and step runner against the
+reference's outputs and against the oracle on mapped read pairs (GB300).
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
 from gpu_index_test_gb300 import abi, native, synth
 from oracle import oracle_py
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_cases import (ALIGN_VARIANTS, AlignRef, Case, align_inputs, check_align,  # noqa: E402
+                          oracle_pair_rows, oracle_sort_mismatches)
 
 
 def _nam(ref_id, qs, qe, rs, re, n_hits, score, is_rc=0):
@@ -99,6 +111,101 @@ def test_plan_type4_pairs_and_rescues():
     plans, steps = oracle_py.plan_pairs(nams, offs, 1, np.array([4], np.uint8), jp, np.array([4], np.uint32),
                                         max_tries=2, dropoff=0.1)
     assert plans[0]["type4_loop_size"] == 2 and len(steps) == 4
+
+
+@pytest.mark.parametrize("i", range(len(ALIGN_VARIANTS)))
+def test_pair_rows_match_the_reference_code(i):
+    """The oracle's mate sorts, pair types, joint NAM pairs, plans (type, mapq,
+    type4_loop_size) and step records (is_read1, extension or rescue, the NAM after
+    reverse_nam_if_needed, done_align, the GPUAlignment fields) against the reference's own
+    gpu_sort_nams, gpu_pre_cal_type, get_best_scoring_nam_pairs_sort3 and gpu_align_PE0..4
+    on the variant's read pairs."""
+    ref = AlignRef(i)
+    case = Case(ref.v["src"])
+    nams, offs, reads = align_inputs(case, ref.v)
+    assert oracle_sort_mismatches(ref, nams, offs) == []
+    s, types, jp, jc, plans, steps, ext, resc = oracle_pair_rows(ref, case, nams, offs, reads)
+    assert check_align(ref, s, offs, types, jp, jc, plans, steps, ext, resc) == []
+    assert set(np.unique(ref.types).tolist()) == {0, 1, 2, 3, 4}
+
+
+def test_reference_pair_check_catches_planted_differences():
+    """check_align reports a changed pair type, joint pair, mapq, is_read1 tag, extension
+    score and rescue edit distance (each planted in a copy of the oracle's output)."""
+    ref = AlignRef(0)
+    case = Case(ref.v["src"])
+    nams, offs, reads = align_inputs(case, ref.v)
+    s, types, jp, jc, plans, steps, ext, resc = oracle_pair_rows(ref, case, nams, offs, reads)
+    assert check_align(ref, s, offs, types, jp, jc, plans, steps, ext, resc) == []
+    t3 = int(np.nonzero(types == 3)[0][0])
+    t = types.copy()
+    t[t3] = 4
+    assert any("types" in b for b in check_align(ref, s, offs, t, jp, jc, plans, steps, ext, resc))
+    j = jp.copy()
+    j4 = int(np.nonzero(jc > 0)[0][0])
+    j[j4][0]["score"] += 1
+    assert any("joint" in b for b in check_align(ref, s, offs, types, j, jc, plans, steps, ext, resc))
+    pl = plans.copy()
+    pl[t3]["mapq1"] -= 1
+    assert any("mapq1" in b for b in check_align(ref, s, offs, types, jp, jc, pl, steps, ext, resc))
+    st = steps.copy()
+    st[0]["is_read1"] ^= 1
+    assert any("is_read1" in b for b in check_align(ref, s, offs, types, jp, jc, plans, st, ext, resc))
+    e = ext.copy()
+    d = int(np.nonzero((steps["kind"] == abi.GBSA_STEP_EXTEND) & (ext["done"] == 1))[0][0])
+    e[d]["score"] += 1
+    assert any("score" in b for b in check_align(ref, s, offs, types, jp, jc, plans, steps, e, resc))
+    r = resc.copy()
+    u = int(np.nonzero(resc["is_unaligned"] == 1)[0][0])
+    r[u]["edit_distance"] -= 1
+    assert any("edit_distance" in b for b in check_align(ref, s, offs, types, jp, jc, plans, steps, ext, r))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("i", range(len(ALIGN_VARIANTS)))
+def test_pair_rows_on_the_gpu_match_the_reference_code(i):
+    """gbsa_classify_pairs_device, gbsa_nam_pairs_device, gbsa_plan_pairs_device and
+    gbsa_run_align_steps_device on the reference-sorted NAM lists of the variant's read pairs
+    against the reference's own outputs, record by record."""
+    import torch
+
+    ref = AlignRef(i)
+    v = ref.v
+    P, tries = v["n_pairs"], v["max_tries"]
+    case = Case(v["src"])
+    nams, offs, reads = align_inputs(case, v)
+    s = ref.sorted_lists(nams, offs)
+    g = case.genome
+    dev = torch.device("cuda:0")
+    up = lambda x: torch.from_numpy(np.ascontiguousarray(x).view(np.uint8).copy()).to(dev)
+    d_n, d_o = up(s), up(offs.astype(np.uint64))
+    d_t = torch.zeros(P, dtype=torch.uint8, device=dev)
+    native.classify_pairs_device(d_n.data_ptr(), d_o.data_ptr(), P, d_t.data_ptr(), 0, v["dropoff"], 300.0, 100.0)
+    d_p = torch.zeros(P * tries * 3, dtype=torch.int32, device=dev)
+    d_c = torch.zeros(P, dtype=torch.int32, device=dev)
+    native.nam_pairs_device(d_n.data_ptr(), d_o.data_ptr(), P, d_p.data_ptr(), d_c.data_ptr(), 0, 300.0, 100.0, tries)
+    cap = P * (2 + 2 * tries)
+    d_plans = torch.zeros(P * abi.PAIR_PLAN.itemsize, dtype=torch.uint8, device=dev)
+    d_steps = torch.zeros(cap * abi.ALIGN_STEP.itemsize, dtype=torch.uint8, device=dev)
+    n = native.plan_pairs_device(d_n.data_ptr(), d_o.data_ptr(), P, d_t.data_ptr(), d_p.data_ptr(), d_c.data_ptr(),
+                                 d_plans.data_ptr(), d_steps.data_ptr(), cap, 0, tries, v["dropoff"])
+    d_ref = up(g.seq)
+    d_roff, d_rlen = up(g.offsets.astype(np.uint64)), up(g.lengths.astype(np.uint64))
+    d_seq, d_qoff, d_qlen = up(reads.seq), up(reads.offsets.astype(np.uint64)), up(reads.lengths.astype(np.uint32))
+    d_ext = torch.zeros(max(1, n) * abi.SEED_ALIGNMENT.itemsize, dtype=torch.uint8, device=dev)
+    d_res = torch.zeros(max(1, n) * abi.MATE_RESCUE.itemsize, dtype=torch.uint8, device=dev)
+    native.run_align_steps_device(d_ref.data_ptr(), d_roff.data_ptr(), d_rlen.data_ptr(), len(g.lengths),
+                                  d_seq.data_ptr(), d_qoff.data_ptr(), d_qlen.data_ptr(), reads.n, d_n.data_ptr(),
+                                  d_o.data_ptr(), d_steps.data_ptr(), n, v["k"], d_ext.data_ptr(), d_res.data_ptr())
+    torch.cuda.synchronize()
+    types = d_t.cpu().numpy()
+    jp = d_p.cpu().numpy().view(abi.NAM_PAIR).reshape(P, tries)
+    jc = d_c.cpu().numpy().astype(np.uint32)
+    plans = d_plans.cpu().numpy().view(abi.PAIR_PLAN)
+    steps = d_steps.cpu().numpy().view(abi.ALIGN_STEP)[:n]
+    ext = d_ext.cpu().numpy().view(abi.SEED_ALIGNMENT)[:n]
+    resc = d_res.cpu().numpy().view(abi.MATE_RESCUE)[:n]
+    assert check_align(ref, s, offs, types, jp, jc, plans, steps, ext, resc) == []
 
 
 @pytest.mark.gpu

@@ -6,7 +6,10 @@ of the reference on small cases, including the edge cases the reference's code h
 a NAM whose orientation is wrong (a false reverse hit), k-mers that match in neither
 orientation, a read overhanging its contig, the 5% Hamming limit on both sides, N and
 lower-case bases, and NAMs outside their read or contig.  The GPU tests compare
-gbsa_extend_seeds_device with the oracle on NAMs from the mapper and on altered ones."""
+gbsa_extend_seeds_device with the oracle on NAMs from the mapper and on altered ones.
+The oracle's extension and mate rescue are also checked against the reference's own
+functions, compiled from its main.cu, on the read pairs of tests/golden/align_ref.npz
+(tests/test_align_plan.py)."""
 import os
 import sys
 
