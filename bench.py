@@ -166,6 +166,28 @@ SERVE_SLOTS = 8
 SERVE_BATCH_READS = 100_000
 
 
+def lookup_roofline(alg_lookup, sectors, packed, nams, stage_ms, fused, ms, gather_gbs):
+    """The seeding + lookup stage against the measured HBM copy bandwidth and against the
+    random-gather ceiling of the index's own tables (32-byte sectors the reference's probes
+    touch), and the whole batch's algorithmic bytes over its time: the definitions of the
+    headline line's roofline, for another form or configuration."""
+    peak, peak_kind = peaks()
+    lk = "seed_lookup" if fused else "lookup"
+    t = stage_ms.get(lk, 0.0) / 1e3
+    alg = alg_lookup + (packed if fused else 0)
+    out = {"kernel": lk, "stage_ms": round(stage_ms.get(lk, 0.0), 3), "alg_bytes_per_launch": int(alg),
+           "achieved": round(alg / t / 1e9, 1) if t > 0 else None, "peak": peak, "unit": "GB/s",
+           "frac": round(alg / t / 1e9 / peak, 4) if t > 0 else None, "peak_source": peak_kind}
+    g = sectors * 32 / t / 1e9 if t > 0 else 0.0
+    out["gather"] = {"sectors_per_launch": int(sectors), "achieved": round(g, 1), "peak": round(gather_gbs, 1),
+                     "frac": round(g / gather_gbs, 4) if gather_gbs > 0 and t > 0 else None,
+                     "peak_source": "gbsa_bench_gather_index on this index"}
+    whole = packed + alg_lookup + 44 * nams
+    out["whole_batch"] = {"alg_bytes": int(whole), "ms": round(ms, 3), "achieved": round(whole / (ms / 1e3) / 1e9, 1),
+                          "frac": round(whole / (ms / 1e3) / 1e9 / peak, 4)}
+    return out
+
+
 def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, max_reads=100_000,
                   batch_reads=SERVE_BATCH_READS):
     """Served form: Poisson arrivals of requests of 1k-100k reads (log-uniform) of
@@ -183,7 +205,16 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
                                                 len_max=250, paired_frac=1.0, insert_mean=400, insert_sd=50))
     pm = native.Mapper(idx, max_reads=pool.n, max_bases=int(pool.lengths.sum()))
     plain = pm.map_reads(pool)
+    # algorithmic bytes and gather sectors per read of the request pool: the counting
+    # instance on the pool's first reads, mapped as one batch
+    sample = pool.subset(np.arange(min(pool.n, 200_000)))
+    pm.set_count_bytes(True)
+    pm.map_reads(sample)
+    s_alg, s_sec = pm.last_alg_bytes(), pm.last_alg_sectors()
+    pm.set_count_bytes(False)
     pm.free()
+    s_packed = int(((sample.lengths.astype(np.int64) + 3) // 4).sum())
+    s_nams = int(plain[1][sample.n])
     npr = max(24, int(np.ceil(len(plain[0]) / pool.n * 2.5)))
     srv = native.Server(idx, workers=slots, max_reads=batch_reads, max_bases=batch_reads * 250)
     g0 = srv.stats()
@@ -291,6 +322,31 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
     ok10 = [r for r in results if r["p99_ms_le_10k_reads"] is not None and r["p99_ms_le_10k_reads"] < 20.0
             and r["bit_exact_vs_plain"]]
     sat10 = max(ok10, key=lambda r: r["reads_per_s"]) if ok10 else None
+    # the served throughput against the random-gather ceiling of the index's own tables
+    # and the HBM copy bandwidth: the pool's sectors and algorithmic bytes per read times
+    # the reads served per second
+    roof = None
+    if results:
+        try:
+            _, _, g_gbs = native.bench_gather_index(idx)
+            peak, peak_kind = peaks()
+            sec_read = s_sec / sample.n
+            alg_read = (s_packed + s_alg + 44 * s_nams) / sample.n
+
+            def at(r):
+                rs = r["reads_per_s"]
+                return {"rate_req_s": r["rate_req_s"], "reads_per_s": rs,
+                        "gather_gbs": round(rs * sec_read * 32 / 1e9, 1),
+                        "gather_frac": round(rs * sec_read * 32 / 1e9 / g_gbs, 4) if g_gbs > 0 else None,
+                        "alg_gbs": round(rs * alg_read / 1e9, 1), "hbm_frac": round(rs * alg_read / 1e9 / peak, 4)}
+            roof = {"sectors_per_read": round(sec_read, 2), "alg_bytes_per_read": round(alg_read, 1),
+                    "sample": f"counting instance on the first {sample.n} reads of the request pool",
+                    "gather_peak_gbs": round(g_gbs, 1), "gather_peak_source": "gbsa_bench_gather_index on this index",
+                    "hbm_peak_gbs": peak, "hbm_peak_source": peak_kind,
+                    "at_saturation": at(sat) if sat else None,
+                    "at_peak": at(max(results, key=lambda r: r["reads_per_s"]))}
+        except Exception as e:   # recorded, not fatal
+            roof = {"error": f"{type(e).__name__}: {e}"}
     return {"index": index_name, "slots": info["slots"], "slot_bytes": info["slot_bytes"],
             "graph_during_requests": {k: growth[k] - g0[k] for k in growth},
             "memory_budget_bytes": info["budget"], "batch_reads": batch_reads,
@@ -300,7 +356,7 @@ def serve_measure(idx, g, rates, seconds, scale, index_name, slots=SERVE_SLOTS, 
             "saturation_le_10k_reads": ({"rate_req_s": sat10["rate_req_s"], "reads_per_s": sat10["reads_per_s"],
                                          "p99_ms_le_10k_reads": sat10["p99_ms_le_10k_reads"]} if sat10 else None),
             "peak_reads_per_s": round(max(r["reads_per_s"] for r in results), 1) if results else None,
-            "plain_one_request_at_a_time": one,
+            "plain_one_request_at_a_time": one, "roofline": roof,
             "vs_plain_one_at_a_time": (round(max(r["reads_per_s"] for r in results) / one["reads_per_s"], 2)
                                        if one else None)}
 
@@ -754,6 +810,24 @@ def other_config(name, scale, cpu_seconds, steps=3, serve=None):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     fused = bool(m.fused_lookup())
+    # the lookup against the HBM and gather ceilings, as for the headline line: the
+    # counting instance's bytes and sectors, the stage times of one profiled batch and
+    # the gather ceiling of this index's own tables
+    try:
+        m.set_count_bytes(True)
+        step()
+        c_alg, c_sec = m.last_alg_bytes(), m.last_alg_sectors()
+        m.set_count_bytes(False)
+        m.set_profile(True)
+        step()
+        c_stages = m.stage_ms()
+        m.set_profile(False)
+        _, _, c_gbs = native.bench_gather_index(idx)
+        c_packed = int(((reads.lengths.astype(np.int64) + 3) // 4).sum())
+        roof = lookup_roofline(c_alg, c_sec, c_packed, int(total), c_stages, fused, ms, c_gbs)
+        roof["stage_ms_all"] = {k: round(v, 3) for k, v in c_stages.items()}
+    except Exception as e:   # recorded, not fatal
+        roof = {"error": f"{type(e).__name__}: {e}"}
     noff = d_noff.cpu().numpy().view(np.uint64)
     # the batched form on the same reads (work items: single-end reads and pairs)
     items = synth.read_items(rp)
@@ -800,6 +874,7 @@ def other_config(name, scale, cpu_seconds, steps=3, serve=None):
             "index_entries": int(info.size), "index_bits": int(info.bits), "index_build_gpu_s": round(build_s, 3),
             "form": "seeding and lookup fused" if fused else "seeding and lookup as two kernels (index over 2 GiB)",
             "device_reads_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 3), "nams": int(total),
+            "roofline": roof,
             "batched": {"device_reads_per_s": round(n / (bms / 1e3), 1), "ms_per_batch": round(bms, 3),
                         "vs_plain_device": round(ms / bms, 3), "work_items": int(len(items) - 1),
                         "bit_exact_vs_plain": b_exact},
@@ -1082,7 +1157,9 @@ def main():
     fused = m.fused_lookup()
     main_stages = ("seed_lookup", "lookup_long", "nams", "nams_warp") if fused else ("seed", "lookup", "nams", "nams_warp")
     dom = max(main_stages, key=lambda k: stage_ms.get(k, 0.0))
-    q, hits, nams_n = counts["queries"], counts["hits"], counts["nams"]
+    # NAMs the step outputs (the NAM-state arena's slots, counts["nam_slots"], include the
+    # room the lane merge reserves: two per hit)
+    q, hits, nams_n = counts["queries"], counts["hits"], int(total_nams)
     packed = int(((reads.lengths.astype(np.int64) + 3) // 4).sum())
     # Algorithmic bytes as the measurement plan defines them per read: the 2-bit packed
     # read (ceil(L/4) B), the lookup's probes (bucket bound pair, entries examined,
@@ -1142,6 +1219,12 @@ def main():
         tot_plain = int(d_noff[n].item())
         batched = batched_measure(idx, reads, items, d_seq, d_off, d_len, (d_nams, d_noff, d_frac, d_resc, tot_plain),
                                   ms, e2e_s, max(3, args.steps))
+        if batched is not None and fused and batched.get("stage_ms"):
+            # the same reads and index as the plain line: the same algorithmic bytes and
+            # sectors, over the persistent queue kernel's stage time
+            batched["roofline"] = lookup_roofline(alg_lookup, sectors_lookup, packed, nams_n, batched["stage_ms"],
+                                                  True, batched["ms_per_batch"], g_gbs)
+            batched["roofline"]["kernel"] = "seed_lookup (persistent work-queue kernel)"
 
     staging = None
     if world == 1 and args.fastq and args.config == "C2":

@@ -358,7 +358,7 @@ class Mapper:
     def last_counts(self):
         a = np.zeros(7, np.uint64)
         lib().gbsa_mapper_last_counts(self.h, a.ctypes.data)
-        return dict(zip(("queries", "hits", "nams", "rescued", "long_reads", "ovf_bytes", "warp_nam_reads"),
+        return dict(zip(("queries", "hits", "nam_slots", "rescued", "long_reads", "ovf_bytes", "warp_nam_reads"),
                         (int(x) for x in a)))
 
     def retries(self):

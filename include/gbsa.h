@@ -628,7 +628,9 @@ int gbsa_bench_gather_index(const gbsa_index* idx, double* probes_per_s, double*
 int gbsa_mapper_set_profile(gbsa_mapper* m, int on);
 int gbsa_mapper_stage_ms(const gbsa_mapper* m, float* ms, int n);
 /* Work counts of the last batch: out[0] query randstrobes, [1] hits of the normal
- * path, [2] NAMs, [3] rescued reads, [4] reads seeded by the long-read kernel,
+ * path, [2] NAM-state arena slots taken by the merges (the room they reserve: two per hit
+ * of a lane-merged read; not the NAMs output, which the call returns), [3] rescued reads,
+ * [4] reads seeded by the long-read kernel,
  * [5] overflow scratch bytes, [6] reads merged by the warp-cooperative NAM kernel.
  * out must hold 7 values.  No reference counterpart. */
 int gbsa_mapper_last_counts(const gbsa_mapper* m, uint64_t* out);
