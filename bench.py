@@ -1214,6 +1214,11 @@ def main():
     }
 
     batched = None
+    staging_wanted = world == 1 and args.fastq and args.config == "C2"
+    if not staging_wanted:
+        # nothing below maps through the plain mapper: its work areas (two sets after the
+        # chunked e2e calls; about 240 GB for the 10M reads of C4) make room for the batched form's
+        m.free()
     if rank == 0:
         items = synth.read_items(rp)
         tot_plain = int(d_noff[n].item())
@@ -1227,7 +1232,7 @@ def main():
             batched["roofline"]["kernel"] = "seed_lookup (persistent work-queue kernel)"
 
     staging = None
-    if world == 1 and args.fastq and args.config == "C2":
+    if staging_wanted:
         staging = fastq_pipeline(m, reads, h_nams[: tot_nams_e2e * 44].numpy().view(abi.NAM),
                                  h_noff.numpy().view(np.uint64))
 
