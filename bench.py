@@ -705,6 +705,28 @@ def batched_measure(idx, reads, items, d_seq, d_off, d_len, plain_out, plain_ms,
     torch.cuda.synchronize()
     stage = {k: round(v, 3) for k, v in b.stage_ms().items()}
     b.set_profile(False)
+    # small batches: before the e2e calls, whose chunks take more sets of the batcher's work
+    # areas (for 10M reads most of the device)
+    # the first `small` reads (whole items) through both device entry points
+    k_items = int(np.searchsorted(items, small, side="right")) - 1
+    k = int(items[k_items])
+    pm = native.Mapper(idx, max_reads=k, max_bases=int(reads.lengths[:k].sum()))
+
+    def small_plain():
+        return pm.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), k, d_nams.data_ptr(), cap,
+                                   d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), stream.cuda_stream)
+
+    lat = {}
+    for name, fn in (("plain", small_plain), ("batched", lambda: step(k, k_items))):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(50):
+            fn()
+        torch.cuda.synchronize()
+        lat[name] = (time.perf_counter() - t0) / 50
+    pm.free()
     # e2e: host entry point, pinned reads in, NAMs / offsets / fractions / flags out
     h_seq = torch.from_numpy(reads.seq).pin_memory()
     h_nams = torch.empty(cap * 44, dtype=torch.uint8).pin_memory()
@@ -728,26 +750,6 @@ def batched_measure(idx, reads, items, d_seq, d_off, d_len, plain_out, plain_ms,
     e2e_s = (time.perf_counter() - t0) / steps
     e2e_exact = bool(int(h_noff[n]) == p_tot and torch.equal(h_noff, p_noff.cpu())
                      and torch.equal(h_nams[: p_tot * 44], p_nams[: p_tot * 44].cpu()))
-    # small batches: the first `small` reads (whole items) through both device entry points
-    k_items = int(np.searchsorted(items, small, side="right")) - 1
-    k = int(items[k_items])
-    pm = native.Mapper(idx, max_reads=k, max_bases=int(reads.lengths[:k].sum()))
-
-    def small_plain():
-        return pm.map_reads_device(d_seq.data_ptr(), d_off.data_ptr(), d_len.data_ptr(), k, d_nams.data_ptr(), cap,
-                                   d_noff.data_ptr(), d_frac.data_ptr(), d_resc.data_ptr(), stream.cuda_stream)
-
-    lat = {}
-    for name, fn in (("plain", small_plain), ("batched", lambda: step(k, k_items))):
-        for _ in range(5):
-            fn()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(50):
-            fn()
-        torch.cuda.synchronize()
-        lat[name] = (time.perf_counter() - t0) / 50
-    pm.free()
     stats = b.stats()
     b.free()
     return {
