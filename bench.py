@@ -152,11 +152,12 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+def ncu_traffic(config):
+    """Per-launch DRAM bytes of each stage's kernel on a configuration's full workload, from
+    the committed ncu summaries ({} when none was captured)."""
     try:
         with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
-            return json.load(f)
+            return json.load(f).get(config, {})
     except (OSError, ValueError):
         return {}
 
@@ -827,6 +828,7 @@ def other_config(name, scale, cpu_seconds, steps=3, serve=None):
         _, _, c_gbs = native.bench_gather_index(idx)
         c_packed = int(((reads.lengths.astype(np.int64) + 3) // 4).sum())
         roof = lookup_roofline(c_alg, c_sec, c_packed, int(total), c_stages, fused, ms, c_gbs)
+        roof["traffic"] = ncu_traffic(name).get(roof["kernel"])
         roof["stage_ms_all"] = {k: round(v, 3) for k, v in c_stages.items()}
     except Exception as e:   # recorded, not fatal
         roof = {"error": f"{type(e).__name__}: {e}"}
@@ -1184,7 +1186,7 @@ def main():
     }
     peak, peak_kind = peaks()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
-    tr = ncu_traffic().get(dom)
+    tr = ncu_traffic(args.config).get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": alg[dom],
