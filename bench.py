@@ -828,7 +828,7 @@ def other_config(name, scale, cpu_seconds, steps=3, serve=None):
         _, _, c_gbs = native.bench_gather_index(idx)
         c_packed = int(((reads.lengths.astype(np.int64) + 3) // 4).sum())
         roof = lookup_roofline(c_alg, c_sec, c_packed, int(total), c_stages, fused, ms, c_gbs)
-        roof["traffic"] = ncu_traffic(name).get(roof["kernel"])
+        roof["traffic"] = ncu_traffic(name).get(roof["kernel"]) if scale == 1.0 else None
         roof["stage_ms_all"] = {k: round(v, 3) for k, v in c_stages.items()}
     except Exception as e:   # recorded, not fatal
         roof = {"error": f"{type(e).__name__}: {e}"}
@@ -1186,7 +1186,8 @@ def main():
     }
     peak, peak_kind = peaks()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
-    tr = ncu_traffic(args.config).get(dom)
+    # the ncu figures are per launch of the full-size workload
+    tr = ncu_traffic(args.config).get(dom) if args.scale == 1.0 else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": alg[dom],
